@@ -1,0 +1,298 @@
+"""Benchmark: pattern-node updates/s of the Felsenstein-pruning likelihood engine.
+
+Workload (one step = one full log-likelihood evaluation from scratch: every
+internal partial recomputed, then the root-branch lnL): protein LG+G4,
+100 taxa x 50,000 sites simulated on a seeded Yule tree (mean branch 0.05,
+alpha 0.8, empirical frequencies), FP64 drop-in path.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU restatement of the reference kernels
+(the oracle, OpenMP over all host cores) on a bounded pattern sample of the
+same workload, since the reference itself cannot be built on this image.
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from iqtree2_gb300 import simulate  # noqa: E402
+
+WORKLOAD = dict(workload="protein LG+G4 100 taxa x 50000 sites, full lnL (98 partial updates + root lnL)",
+                model="LG+G4", taxa=100, sites=50000, seed=2, mean_bl=0.05, alpha=0.8)
+METRIC = "pattern-node updates/s"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FP64_PEAK_TFLOPS_MEASURED = 1.20  # FMA-chain probe on this machine's GB300 (all SMs)
+
+
+def dataset():
+    return simulate.protein_lg_dataset(WORKLOAD["taxa"], WORKLOAD["sites"], WORKLOAD["seed"],
+                                       mean_bl=WORKLOAD["mean_bl"], alpha=WORKLOAD["alpha"])
+
+
+def topology_ops(ds):
+    """Full traversal toward the root branch used by computeLikelihood."""
+    from iqtree2_gb300.topology import Topology
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    # computeLikelihood evaluates at the farthest leaf's branch; any leaf branch has the same work
+    leaf = 0
+    nb = topo.adj[leaf][0][0]
+    ops = topo.branch_ops(nb, leaf)
+    return topo, ops, topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+
+
+def algorithmic_cost(ops, ntaxa, n, C, nptn, elem=8):
+    """Bytes and flops one traversal+lnL launch must move/execute, per pattern x all ops."""
+    B = n * C
+    bytes_per_ptn = 0.0
+    flops_per_ptn = 0.0
+    for (_, c0, c1, _, _) in ops:
+        tips = (c0 < 0) + (c1 < 0)
+        if tips == 2:
+            bytes_per_ptn += 2 + B * elem + 1
+            flops_per_ptn += (2 * n * n + n) * C
+        elif tips == 1:
+            bytes_per_ptn += 1 + B * elem + 1 + B * elem + 1
+            flops_per_ptn += (4 * n * n + n) * C
+        else:
+            bytes_per_ptn += 2 * B * elem + 2 + B * elem + 1
+            flops_per_ptn += (6 * n * n + n) * C
+    # root lnL: read one partial + one tip state + freq, write pattern lnL
+    bytes_per_ptn += B * elem + 1 + 8 + 8
+    flops_per_ptn += 3 * B
+    return bytes_per_ptn * nptn, flops_per_ptn * nptn
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(ds, ops, a, b, length, sample_ptn=2000, min_seconds=10.0):
+    """The CPU restatement of the reference kernels (oracle) on a pattern sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    pats = np.ascontiguousarray(ds.patterns[:, :sample_ptn])
+    freq = ds.freq[:sample_ptn]
+    t = oracle.OracleTree(ds.model, pats, freq, ds.edges, ds.lengths, nthreads=cores)
+    lengths = ds.lengths.copy()
+    t.compute_likelihood()  # warm-up
+    upd0, t0, reps = t.num_updates(), time.perf_counter(), 0
+    while True:
+        t.set_lengths(lengths)  # invalidate every partial: full recomputation
+        t.compute_likelihood()
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= 200:
+            break
+    upd = t.num_updates() - upd0
+    return {"value": upd / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{pats.shape[1]} of {ds.nptn} patterns x {len(ops)} partial updates, {reps} full "
+                      f"evaluations in {el:.1f}s (oracle C restatement, OpenMP)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    ds = dataset()
+    _, ops, a, b, length = topology_ops(ds)
+    per_step = max(3.0, 30.0 / max(args.steps, 1))
+    for _ in range(args.warmup):
+        cpu_baseline(ds, ops, a, b, length, min_seconds=0.5)
+    vals = [cpu_baseline(ds, ops, a, b, length, min_seconds=per_step) for _ in range(args.steps)]
+    v = statistics.median([x["value"] for x in vals])
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": WORKLOAD, "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference kernels restated in C (the reference needs Eigen3/Boost/cmake and does not "
+                    "build on this image); timed on a bounded pattern sample, all host cores"}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    from iqtree2_gb300 import engine
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+
+    ds = dataset()
+    topo, ops, a, b, length = topology_ops(ds)
+    m = ds.model
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                        precision=engine.F64, device=local, max_ops=topo.nslots)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    ops_arr = engine.Engine.ops_array(ops)
+    updates_per_step = len(ops) * ds.nptn
+    alg_bytes, alg_flops = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn)
+
+    for _ in range(args.warmup):
+        lnl = eng.compute_likelihood(ops_arr, a, b, length)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    eng.set_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        lnl = eng.compute_likelihood(ops_arr, a, b, length)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = eng.timing()
+    eng.set_timing(False)
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    value = updates_per_step * args.steps * world / (elapsed_ms / 1e3)
+
+    # end to end through the C ABI from host buffers: inputs copied each step, lnL read back
+    e2e_steps = max(2, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.set_model(m)
+        eng.set_patterns(ds.freq)
+        eng.set_tip_states(ds.patterns)
+        lnl_e2e = eng.compute_likelihood(ops_arr, a, b, length)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = ds.patterns.nbytes + ds.freq.nbytes + sum(x.nbytes for x in (m.eval, m.evec, m.inv_evec, m.rates,
+                                                                        m.props, m.tip_lh)) + ops_arr.nbytes
+    assert lnl_e2e == lnl
+
+    peaks, peak_src = measured_peaks()
+    kern_avg_s = kern_ms / max(kern_n, 1) / 1e3
+    achieved_gbs = alg_bytes / kern_avg_s / 1e9
+    fp64_tflops = alg_flops / kern_avg_s / 1e12
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(WORKLOAD, path="FP64 drop-in (eigen-space partials, 2^-256 scaling)",
+                       nptn=ds.nptn, parallelism=f"replicas x{world}", l2="inputs larger than L2 "
+                       "(98 partials x 32 MB per step)", lnl=lnl),
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
+                     "kernel": "k_traverse_f64<20,NORM,LNL>",
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "fp64": {"achieved_tflops": fp64_tflops, "peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
+                              "frac": fp64_tflops / FP64_PEAK_TFLOPS_MEASURED,
+                              "flops_per_launch": alg_flops, "form": "eigen-space (6n^2+n)C"}},
+        "e2e": {"value": updates_per_step / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": 8 * 4},
+        "clocks": clk,
+        "gpu_launches": 2 * args.steps,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(ds, ops, a, b, length)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

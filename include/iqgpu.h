@@ -1,0 +1,174 @@
+/*
+ * iqgpu -- GB300 (sm_103a) Felsenstein-pruning likelihood engine, C ABI.
+ *
+ * This is the drop-in boundary for IQ-TREE 2's likelihood kernels. A
+ * PhyloTree shim binds these entry points in place of
+ * the function pointers that PhyloTree::setLikelihoodKernel installs
+ * (tree/phylotreesse.cpp:91-199):
+ *
+ *   computePartialLikelihoodPointer      -> iqgpu_compute_partials
+ *   computeLikelihoodBranchPointer       -> iqgpu_branch_lnl / iqgpu_compute_likelihood
+ *   computeLikelihoodDervPointer         -> iqgpu_likelihood_derv
+ *   computeLikelihoodFromBufferPointer   -> iqgpu_lnl_from_buffer
+ *
+ * and reads the model through the same arrays as ModelSubst
+ * (getEigenvalues/getEigenvectors/getInverseEigenvectors,
+ * model/modelsubst.h:360-372) and RateHeterogeneity (getRate/getProp,
+ * model/rategamma.h:106,120).
+ *
+ * Above the kernel level, iqgpu_tree_* is a C++ restatement of the PhyloTree
+ * drivers that call those pointers (computeLikelihood, optimizeOneBranch,
+ * optimizeAllBranches, computePatternLikelihood), so a caller that owns only
+ * a tree and a model can use the engine without IQ-TREE's host code.
+ *
+ * Conventions. Plain pointers and sizes; every pointer argument is host
+ * memory unless its name ends in _dev. Every entry point returns an int
+ * status (IQGPU_OK or an IQGPU_ERR_* code); iqgpu_last_error() describes the
+ * last failure on the calling thread. One engine owns one CUDA stream and is
+ * used from one host thread at a time; different engines may be driven
+ * concurrently from different threads (PhyloSuperTree calls partitions from
+ * OpenMP threads, tree/phylosupertree.cpp:716-723).
+ *
+ * Partial references. A directed partial (the reference's PhyloNeighbor
+ * partial_lh: the subtree at `node` seen from `dad`) is named by an int32:
+ * r >= 0 is an HBM slot, r < 0 is tip taxon (-1 - r).
+ */
+#ifndef IQGPU_H
+#define IQGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define IQGPU_OK 0
+#define IQGPU_ERR_ARG 1        /* bad argument or size */
+#define IQGPU_ERR_OOM 2        /* device allocation or admission refused */
+#define IQGPU_ERR_CUDA 3       /* CUDA runtime error */
+#define IQGPU_ERR_NONFINITE 4  /* non-finite lnL/derivative (reference: outError "use -safe") */
+#define IQGPU_ERR_TIMEOUT 5    /* a bounded device wait gave up */
+#define IQGPU_ERR_STATE 6      /* call out of order (e.g. from-buffer before derivative) */
+#define IQGPU_ERR_NODEV 7      /* no CUDA device, or the device is not sm_103 */
+#define IQGPU_ERR_NEWTON 8     /* Newton-Raphson failed (reference: nrerror) */
+
+/* ---- precision of the stored partials ---------------------------------- */
+#define IQGPU_F64 0     /* FP64 eigen-space partials, uint8 2^-256 scale counts: the drop-in */
+#define IQGPU_F32 1     /* FP32 standard-basis partials, per-pattern power-of-two exponents */
+#define IQGPU_TF32X3 2  /* as F32, tensor-core contraction with split-TF32 (3 passes) */
+#define IQGPU_BF16 3    /* BF16 operands on tensor cores, FP32 accumulate and storage */
+
+typedef struct {
+    int32_t nptn;          /* patterns (aln->size()) */
+    int32_t nstates;       /* aln->num_states, <= 64 */
+    int32_t ncat;          /* site_rate->getNRate(), <= 16 */
+    int32_t ntaxa;         /* leaves */
+    int32_t state_unknown; /* aln->STATE_UNKNOWN, <= 255 */
+    int32_t nslots;        /* partial-likelihood slots to reserve in HBM */
+    int32_t safe;          /* 1 = SAFE (scale count per pattern x category), 0 = NORM */
+    int32_t precision;     /* IQGPU_F64 ... */
+    int32_t device;        /* CUDA device ordinal */
+    int32_t max_ops;       /* largest traversal the engine must accept (>= ntaxa) */
+} iqgpu_config;
+
+/* One TraversalInfo entry (tree/phylotree.h:320-333): compute the partial of
+ * dad_slot from two children with their branch lengths. */
+typedef struct {
+    int32_t dad_slot;
+    int32_t child[2];
+    int32_t reserved;
+    double len[2];
+} iqgpu_op;
+
+typedef struct iqgpu_engine iqgpu_engine;
+typedef struct iqgpu_tree iqgpu_tree;
+
+const char *iqgpu_last_error(void);
+/* Bytes of HBM an engine with this config would hold (PhyloTree::getMemoryRequired,
+ * tree/phylotree.cpp:967-1027). */
+int iqgpu_memory_required(const iqgpu_config *cfg, size_t *bytes);
+
+/* ---- engine lifetime and inputs ----------------------------------------- */
+/* replaces initializeAllPartialLh (tree/phylotree.cpp:893-940) */
+int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out);
+int iqgpu_destroy(iqgpu_engine *e);
+/* The configuration an engine was created with. */
+int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out);
+/* ModelSubst eigen arrays (model/modelsubst.h:360-372) + RateHeterogeneity
+ * rates/props (model/rategamma.h:106,120). eval[n], evec[n*n], inv_evec[n*n]
+ * row-major, rates[ncat], props[ncat]. A model change invalidates every slot
+ * on the caller's side (ModelFactory clears partials, model/modelfactory.cpp:1124-1127). */
+int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
+                    const double *rates, const double *props);
+/* Eigen-space tip vectors, (state_unknown+1) x nstates
+ * (computeTipPartialLikelihood, tree/phylotreesse.cpp:354-375). */
+int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh);
+/* Pattern weights and +I constant-site terms (computePtnFreq/computePtnInvar,
+ * tree/phylotreesse.cpp:537-612). ptn_invar may be NULL (all zero). */
+int iqgpu_set_patterns(iqgpu_engine *e, const double *ptn_freq, const double *ptn_invar);
+/* Tip states, ntaxa x nptn, one byte per state
+ * (getConvertedSequenceByNumber, tree/phylotree.cpp:3251). */
+int iqgpu_set_tip_states(iqgpu_engine *e, const uint8_t *states);
+
+/* ---- kernel-level entry points (the reference's function pointers) ----- */
+/* computePartialLikelihoodPointer over a traversal list, all patterns
+ * (computePartialLikelihoodGenericSIMD, tree/phylokernelnew.h:1289-2039). */
+int iqgpu_compute_partials(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops);
+/* computeLikelihoodBranchPointer (tree/phylokernelnew.h:2641-3223): lnL on the
+ * branch between partial a (dad_branch) and b (node_branch) of length len. */
+int iqgpu_branch_lnl(iqgpu_engine *e, int32_t a, int32_t b, double len, double *lnl);
+/* Fused traversal + branch lnL in one launch: the full computeLikelihood path. */
+int iqgpu_compute_likelihood(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops,
+                             int32_t a, int32_t b, double len, double *lnl);
+/* computeLikelihoodDervPointer (tree/phylokernelnew.h:2233-2633). When
+ * theta_computed is 0 the traversal runs first and theta (node o dad) is
+ * rebuilt (computeLikelihoodBufferGenericSIMD :2048-2231); df and ddf are the
+ * derivative sums of lnL in the length, not yet negated. */
+int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b,
+                          double len, int32_t theta_computed, double *df, double *ddf);
+/* computeLikelihoodFromBufferPointer (tree/phylokernelnew.h:3232-3428). */
+int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl);
+/* Per-pattern lnL of the last branch/from-buffer evaluation (_pattern_lh). */
+int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
+/* Copy a slot back in the reference layout: partial[ptn*B + c*n + x] in eigen
+ * space (F64) or standard basis (mixed), and scale counts (NORM: nptn bytes,
+ * SAFE: nptn*ncat bytes, pattern-major). Either output may be NULL. */
+int iqgpu_get_partial(iqgpu_engine *e, int32_t slot, double *partial, uint8_t *scale);
+/* Mixed precision: per-pattern power-of-two exponent of a slot (int32, nptn). */
+int iqgpu_get_exponent(iqgpu_engine *e, int32_t slot, int32_t *exponent);
+/* Wait for all work of this engine. */
+int iqgpu_sync(iqgpu_engine *e);
+/* Run this engine's work on the caller's CUDA stream (a cudaStream_t passed
+ * as void*); NULL returns to the engine's own stream. */
+int iqgpu_set_stream(iqgpu_engine *e, void *cuda_stream);
+/* Kernel timing with CUDA events on the engine's stream around every
+ * traversal launch (the dominant kernel): enable, read (total ms and number
+ * of timed launches since the last reset), reset. */
+int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
+int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
+
+/* ---- tree-level drivers (PhyloTree restatement) ------------------------ */
+/* edges[2*k], edges[2*k+1]: endpoints of branch k; leaves are 0..ntaxa-1,
+ * internal nodes ntaxa..2*ntaxa-3; a node's neighbour order is edge order. */
+int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out);
+int iqgpu_tree_destroy(iqgpu_tree *t);
+/* PhyloTree::computeLikelihood (tree/phylotree.cpp:1233-1280). pattern_lh may be NULL. */
+int iqgpu_tree_compute_likelihood(iqgpu_tree *t, double *lnl, double *pattern_lh);
+/* PhyloTree::optimizeOneBranch (tree/phylotree.cpp:2594-2644) */
+int iqgpu_tree_optimize_one_branch(iqgpu_tree *t, int32_t node1, int32_t node2, int32_t max_nr_step);
+/* PhyloTree::optimizeAllBranches (tree/phylotree.cpp:2698-2774) */
+int iqgpu_tree_optimize_all_branches(iqgpu_tree *t, int32_t iterations, double tolerance,
+                                     int32_t max_nr_step, double *lnl);
+int iqgpu_tree_get_lengths(iqgpu_tree *t, double *lengths);
+int iqgpu_tree_set_lengths(iqgpu_tree *t, const double *lengths);
+/* params->min_branch_length / max_branch_length (defaults 1e-6, 10) */
+int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl);
+/* Pattern-node updates executed so far (throughput accounting). */
+int iqgpu_tree_num_updates(iqgpu_tree *t, int64_t *updates);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

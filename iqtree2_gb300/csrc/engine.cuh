@@ -1,0 +1,114 @@
+// Internal definitions shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/iqgpu.h"
+
+namespace iqg {
+
+// 2^-256 scaling threshold and its log (tree/phylotree.h:74-80).
+constexpr int kScaleExp = 256;
+constexpr double kScaleThreshold = 8.636168555094444625386e-78;
+constexpr double kLogScaleThreshold = -177.4456782233459932741;
+constexpr double kTwoPow256 = 1.157920892373161954235709850086879078532699846656405640394575840079131296399e77;
+
+constexpr int kTPB = 128;        // threads (= patterns) per CTA in the pattern-tile kernels
+constexpr int kMaxStates = 64;
+constexpr int kMaxCat = 16;
+
+// Device copy of one traversal entry plus the offset of its per-op matrices.
+struct OpDev {
+    int32_t dad_slot;
+    int32_t child[2];
+    int32_t pad;
+    double len[2];
+    long long mat_off;  // doubles into Engine::d_opmats
+    long long pad2;
+};
+
+// Deterministic grid reduction: each CTA writes its partial sums, the last
+// CTA (by ticket) adds them in CTA order.
+struct Reduce {
+    double *partials;    // [gridDim.x][kRedSlots]
+    unsigned *ticket;    // zero between launches
+    double *out;         // [kRedSlots]
+};
+constexpr int kRedSlots = 4;
+
+struct TravParams {
+    int n, ncat, state_unknown, nops, nptn;
+    long long ldp;             // padded pattern count (row stride of a partial)
+    long long slot_stride;     // elements per slot
+    long long scale_stride;    // bytes per slot of scale counts
+    long long op_stride;       // doubles per op in opmats
+    const OpDev *ops;
+    const double *opmats;
+    const double *inv_evec;    // n*n
+    const double *eval, *rates, *props;
+    const double *tip_lh;      // (S+1)*n
+    const double *freq, *invar;
+    const uint8_t *states;     // ntaxa*ldp
+    double *partials;
+    uint8_t *scale;
+    // epilogue
+    int32_t a, b;              // branch partials (a internal)
+    double len;
+    double *pattern_lh;        // LNL
+    double *theta;             // THETA
+    double *buffer_scale;      // THETA
+    Reduce red;
+};
+
+enum Epilogue { EPI_NONE = 0, EPI_LNL = 1, EPI_THETA = 2 };
+
+}  // namespace iqg
+
+struct iqgpu_engine {
+    iqgpu_config cfg;
+    int n, C, B, S;
+    long long P, Ppad;
+    int nblk;
+    int dev;
+    cudaStream_t st;
+    // model
+    double *d_eval, *d_evec, *d_inv, *d_rates, *d_props, *d_tip;
+    double h_eval[iqg::kMaxStates], h_rates[iqg::kMaxCat], h_props[iqg::kMaxCat];
+    bool have_model, have_tips, have_patterns, have_states;
+    double *d_freq, *d_invar;
+    uint8_t *d_states;
+    // FP64 partials
+    double *d_part;
+    uint8_t *d_scale;
+    // ops
+    iqg::OpDev *d_ops, *h_ops;
+    double *d_opmats;
+    long long op_stride;
+    // theta / results
+    double *d_theta, *d_bscale, *d_plh;
+    double *d_red_partials;
+    unsigned *d_ticket;
+    double *d_red_out, *h_red_out;
+    bool theta_valid;
+    int32_t theta_a, theta_b;
+    // stream ownership and kernel timing
+    cudaStream_t own_st;
+    cudaEvent_t ev_t0, ev_t1;
+    bool timing, timing_pending;
+    double timing_ms;
+    long long timing_launches;
+};
+
+namespace iqg {
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+// FP64 kernel launchers (kernels_f64.cu)
+int launch_partial_info_f64(iqgpu_engine *e, int nops);
+int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
+int launch_derv_f64(iqgpu_engine *e, double len);
+int launch_from_buffer_f64(iqgpu_engine *e, double len);
+}  // namespace iqg

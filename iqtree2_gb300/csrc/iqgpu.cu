@@ -1,0 +1,497 @@
+// C ABI of the likelihood engine: lifetime, inputs and the kernel-level entry
+// points that stand in for PhyloTree's kernel function pointers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace iqg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return IQGPU_OK;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return IQGPU_ERR_CUDA;
+}
+
+static long long round_up(long long v, long long g) { return (v + g - 1) / g * g; }
+
+struct Sizes {
+    long long Ppad, part, scale, states, ops, opmats, theta, red, total, op_stride;
+};
+
+static int check_config(const iqgpu_config *c) {
+    if (!c) { set_error("null config"); return IQGPU_ERR_ARG; }
+    if (c->nptn <= 0 || c->nstates < 2 || c->nstates > kMaxStates || c->ncat < 1 || c->ncat > kMaxCat ||
+        c->ntaxa < 3 || c->state_unknown < c->nstates || c->state_unknown > 255 || c->nslots < 1 ||
+        c->max_ops < 1) {
+        set_error("config out of range (nptn>0, 2<=nstates<=64, 1<=ncat<=16, ntaxa>=3, "
+                  "nstates<=state_unknown<=255, nslots>=1, max_ops>=1)");
+        return IQGPU_ERR_ARG;
+    }
+    if (c->precision != IQGPU_F64) {
+        set_error("precision not supported by this build of the engine");
+        return IQGPU_ERR_ARG;
+    }
+    return IQGPU_OK;
+}
+
+static Sizes sizes(const iqgpu_config *c) {
+    Sizes s;
+    const long long n = c->nstates, C = c->ncat, B = n * C, S = c->state_unknown;
+    s.Ppad = round_up(c->nptn, kTPB);
+    s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
+    s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
+    s.states = (long long)c->ntaxa * s.Ppad;
+    s.op_stride = round_up(2 * C * n * n + 2 * (S + 1) * B, 4);
+    s.ops = (long long)c->max_ops * (long long)sizeof(OpDev);
+    s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
+    s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
+    s.red = (s.Ppad / kTPB) * kRedSlots * (long long)sizeof(double) + 64;
+    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + 2 * s.Ppad * 8 +
+              (n + 2 * n * n + 2 * C + (S + 1) * n) * 8;
+    return s;
+}
+
+}  // namespace iqg
+
+using namespace iqg;
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t err__ = (call);                           \
+        if (err__ != cudaSuccess) return cuda_fail(err__, #call); \
+    } while (0)
+
+extern "C" {
+
+const char *iqgpu_last_error(void) { return g_last_error.c_str(); }
+
+int iqgpu_memory_required(const iqgpu_config *cfg, size_t *bytes) {
+    int rc = check_config(cfg);
+    if (rc) return rc;
+    if (!bytes) { set_error("null output"); return IQGPU_ERR_ARG; }
+    *bytes = (size_t)sizes(cfg).total;
+    return IQGPU_OK;
+}
+
+static void free_engine(iqgpu_engine *e) {
+    if (!e) return;
+    cudaSetDevice(e->dev);
+    void *dev_ptrs[] = {e->d_eval, e->d_evec, e->d_inv, e->d_rates, e->d_props, e->d_tip, e->d_freq,
+                        e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
+                        e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out};
+    for (void *p : dev_ptrs)
+        if (p) cudaFree(p);
+    if (e->h_ops) cudaFreeHost(e->h_ops);
+    if (e->h_red_out) cudaFreeHost(e->h_red_out);
+    if (e->ev_t0) cudaEventDestroy(e->ev_t0);
+    if (e->ev_t1) cudaEventDestroy(e->ev_t1);
+    if (e->own_st) cudaStreamDestroy(e->own_st);
+    delete e;
+}
+
+int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
+    int rc = check_config(cfg);
+    if (rc) return rc;
+    if (!out) { set_error("null output"); return IQGPU_ERR_ARG; }
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
+        cudaGetLastError();
+        set_error("no CUDA device with that ordinal");
+        return IQGPU_ERR_NODEV;
+    }
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, cfg->device));
+    if (prop.major != 10 || prop.minor != 3) {
+        set_error("the engine is built for sm_103a (GB300); device is sm_" + std::to_string(prop.major) +
+                  std::to_string(prop.minor));
+        return IQGPU_ERR_NODEV;
+    }
+    CK(cudaSetDevice(cfg->device));
+    Sizes s = sizes(cfg);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if ((size_t)s.total > free_b) {
+        set_error("admission refused: engine needs " + std::to_string(s.total) + " bytes, " +
+                  std::to_string(free_b) + " free");
+        return IQGPU_ERR_OOM;
+    }
+    iqgpu_engine *e = new iqgpu_engine();
+    std::memset(e, 0, sizeof(*e));
+    e->cfg = *cfg;
+    e->dev = cfg->device;
+    e->n = cfg->nstates;
+    e->C = cfg->ncat;
+    e->B = e->n * e->C;
+    e->S = cfg->state_unknown;
+    e->P = cfg->nptn;
+    e->Ppad = s.Ppad;
+    e->nblk = (int)(s.Ppad / kTPB);
+    e->op_stride = s.op_stride;
+    auto fail = [&](cudaError_t err, const char *what) {
+        int r = cuda_fail(err, what);
+        if (err == cudaErrorMemoryAllocation) r = IQGPU_ERR_OOM;
+        free_engine(e);
+        return r;
+    };
+#define CKE(call)                                 \
+    do {                                          \
+        cudaError_t err__ = (call);               \
+        if (err__ != cudaSuccess) return fail(err__, #call); \
+    } while (0)
+    CKE(cudaStreamCreateWithFlags(&e->own_st, cudaStreamNonBlocking));
+    e->st = e->own_st;
+    CKE(cudaEventCreate(&e->ev_t0));
+    CKE(cudaEventCreate(&e->ev_t1));
+    const long long n = e->n, C = e->C, B = e->B, S = e->S;
+    CKE(cudaMalloc(&e->d_eval, n * 8));
+    CKE(cudaMalloc(&e->d_evec, n * n * 8));
+    CKE(cudaMalloc(&e->d_inv, n * n * 8));
+    CKE(cudaMalloc(&e->d_rates, C * 8));
+    CKE(cudaMalloc(&e->d_props, C * 8));
+    CKE(cudaMalloc(&e->d_tip, (S + 1) * n * 8));
+    CKE(cudaMalloc(&e->d_freq, e->Ppad * 8));
+    CKE(cudaMalloc(&e->d_invar, e->Ppad * 8));
+    CKE(cudaMalloc(&e->d_states, s.states));
+    CKE(cudaMalloc(&e->d_part, s.part));
+    CKE(cudaMalloc(&e->d_scale, s.scale));
+    CKE(cudaMalloc(&e->d_ops, s.ops));
+    CKE(cudaMalloc(&e->d_opmats, s.opmats));
+    CKE(cudaMalloc(&e->d_theta, B * e->Ppad * 8));
+    CKE(cudaMalloc(&e->d_bscale, e->Ppad * 8));
+    CKE(cudaMalloc(&e->d_plh, e->Ppad * 8));
+    CKE(cudaMalloc(&e->d_red_partials, (long long)e->nblk * kRedSlots * 8));
+    CKE(cudaMalloc(&e->d_ticket, 64));
+    CKE(cudaMalloc(&e->d_red_out, kRedSlots * 8));
+    CKE(cudaMallocHost(&e->h_ops, s.ops));
+    CKE(cudaMallocHost(&e->h_red_out, kRedSlots * 8));
+    CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
+    CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
+    CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
+    CKE(cudaMemsetAsync(e->d_scale, 0, s.scale, e->st));
+    CKE(cudaMemsetAsync(e->d_states, (int)S, s.states, e->st));
+    CKE(cudaStreamSynchronize(e->st));
+#undef CKE
+    *out = e;
+    return IQGPU_OK;
+}
+
+int iqgpu_destroy(iqgpu_engine *e) {
+    if (!e) return IQGPU_OK;
+    cudaSetDevice(e->dev);
+    cudaStreamSynchronize(e->st);
+    free_engine(e);
+    return IQGPU_OK;
+}
+
+int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out) {
+    if (!e || !out) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    *out = e->cfg;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
+                    const double *rates, const double *props) {
+    if (!e || !eval || !evec || !inv_evec || !rates || !props) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    const size_t n = e->n, C = e->C;
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy(e->d_eval, eval, n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_evec, evec, n * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_inv, inv_evec, n * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
+    std::memcpy(e->h_eval, eval, n * 8);
+    std::memcpy(e->h_rates, rates, C * 8);
+    std::memcpy(e->h_props, props, C * 8);
+    e->have_model = true;
+    e->theta_valid = false;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
+    if (!e || !tip_lh) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice));
+    e->have_tips = true;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_patterns(iqgpu_engine *e, const double *ptn_freq, const double *ptn_invar) {
+    if (!e || !ptn_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy(e->d_freq, ptn_freq, (size_t)e->P * 8, cudaMemcpyHostToDevice));
+    if (ptn_invar) CK(cudaMemcpy(e->d_invar, ptn_invar, (size_t)e->P * 8, cudaMemcpyHostToDevice));
+    else CK(cudaMemset(e->d_invar, 0, (size_t)e->Ppad * 8));
+    e->have_patterns = true;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_tip_states(iqgpu_engine *e, const uint8_t *states) {
+    if (!e || !states) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    for (long long i = 0; i < (long long)e->cfg.ntaxa * e->P; i++)
+        if (states[i] > e->S) {
+            set_error("tip state above STATE_UNKNOWN");
+            return IQGPU_ERR_ARG;
+        }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy2D(e->d_states, (size_t)e->Ppad, states, (size_t)e->P, (size_t)e->P, (size_t)e->cfg.ntaxa,
+                    cudaMemcpyHostToDevice));
+    e->have_states = true;
+    return IQGPU_OK;
+}
+
+static int ready(iqgpu_engine *e) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    if (!e->have_model || !e->have_tips || !e->have_patterns || !e->have_states) {
+        set_error("model, tip partials, patterns and tip states must be set first");
+        return IQGPU_ERR_STATE;
+    }
+    return IQGPU_OK;
+}
+
+static int check_ref(iqgpu_engine *e, int32_t r) {
+    if (r >= 0) return r < e->cfg.nslots ? IQGPU_OK : IQGPU_ERR_ARG;
+    return (-1 - r) < e->cfg.ntaxa ? IQGPU_OK : IQGPU_ERR_ARG;
+}
+
+// Validate a traversal, stage it in pinned memory and send it to the device.
+static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
+    if (nops < 0 || nops > e->cfg.max_ops || (nops > 0 && !ops)) {
+        set_error("traversal length out of range");
+        return IQGPU_ERR_ARG;
+    }
+    if (nops == 0) return IQGPU_OK;
+    // the previous upload must have left the staging buffer
+    CK(cudaStreamSynchronize(e->st));
+    for (int k = 0; k < nops; k++) {
+        const iqgpu_op &o = ops[k];
+        if (o.dad_slot < 0 || o.dad_slot >= e->cfg.nslots || check_ref(e, o.child[0]) || check_ref(e, o.child[1]) ||
+            o.child[0] == o.dad_slot || o.child[1] == o.dad_slot || !(o.len[0] >= 0.0) || !(o.len[1] >= 0.0)) {
+            set_error("bad traversal entry " + std::to_string(k));
+            return IQGPU_ERR_ARG;
+        }
+        OpDev &d = e->h_ops[k];
+        d.dad_slot = o.dad_slot;
+        d.child[0] = o.child[0];
+        d.child[1] = o.child[1];
+        d.pad = 0;
+        d.len[0] = o.len[0];
+        d.len[1] = o.len[1];
+        d.mat_off = (long long)k * e->op_stride;
+        d.pad2 = 0;
+    }
+    CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * nops, cudaMemcpyHostToDevice, e->st));
+    return launch_partial_info_f64(e, nops);
+}
+
+// Fold the last timed traversal into the running total.
+static int settle_timing(iqgpu_engine *e) {
+    if (!e->timing_pending) return IQGPU_OK;
+    CK(cudaEventSynchronize(e->ev_t1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e->ev_t0, e->ev_t1));
+    e->timing_ms += ms;
+    e->timing_launches++;
+    e->timing_pending = false;
+    return IQGPU_OK;
+}
+
+static int traverse(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
+    int rc;
+    if (e->timing) {
+        if ((rc = settle_timing(e))) return rc;
+        CK(cudaEventRecord(e->ev_t0, e->st));
+    }
+    if ((rc = launch_traverse_f64(e, nops, epi, a, b, len))) return rc;
+    if (e->timing) {
+        CK(cudaEventRecord(e->ev_t1, e->st));
+        e->timing_pending = true;
+    }
+    return IQGPU_OK;
+}
+
+static int fetch_result(iqgpu_engine *e) {
+    CK(cudaMemcpyAsync(e->h_red_out, e->d_red_out, kRedSlots * 8, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    return settle_timing(e);
+}
+
+int iqgpu_compute_partials(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
+    int rc = ready(e);
+    if (rc) return rc;
+    CK(cudaSetDevice(e->dev));
+    if ((rc = upload_ops(e, ops, nops))) return rc;
+    return traverse(e, nops, EPI_NONE, 0, 0, 0.0);
+}
+
+static int lnl_common(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b, double len,
+                      double *lnl) {
+    int rc = ready(e);
+    if (rc) return rc;
+    if (!lnl) { set_error("null output"); return IQGPU_ERR_ARG; }
+    if (a < 0) std::swap(a, b);
+    if (a < 0 || check_ref(e, a) || check_ref(e, b) || a == b || !(len >= 0.0)) {
+        set_error("bad branch: need an internal partial, distinct ends and len >= 0");
+        return IQGPU_ERR_ARG;
+    }
+    CK(cudaSetDevice(e->dev));
+    if ((rc = upload_ops(e, ops, nops))) return rc;
+    if ((rc = traverse(e, nops, EPI_LNL, a, b, len))) return rc;
+    if ((rc = fetch_result(e))) return rc;
+    const double *r = e->h_red_out;
+    *lnl = std::isfinite(r[0]) ? r[0] : r[1];
+    return IQGPU_OK;
+}
+
+int iqgpu_branch_lnl(iqgpu_engine *e, int32_t a, int32_t b, double len, double *lnl) {
+    return lnl_common(e, nullptr, 0, a, b, len, lnl);
+}
+
+int iqgpu_compute_likelihood(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b,
+                             double len, double *lnl) {
+    return lnl_common(e, ops, nops, a, b, len, lnl);
+}
+
+int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b, double len,
+                          int32_t theta_computed, double *df, double *ddf) {
+    int rc = ready(e);
+    if (rc) return rc;
+    if (!df || !ddf) { set_error("null output"); return IQGPU_ERR_ARG; }
+    if (a < 0) std::swap(a, b);
+    if (a < 0 || check_ref(e, a) || check_ref(e, b) || a == b || !(len >= 0.0)) {
+        set_error("bad branch");
+        return IQGPU_ERR_ARG;
+    }
+    CK(cudaSetDevice(e->dev));
+    if (!theta_computed || !e->theta_valid || e->theta_a != a || e->theta_b != b) {
+        if (theta_computed && (!e->theta_valid || e->theta_a != a || e->theta_b != b)) {
+            set_error("theta_computed set but the buffer holds another branch");
+            return IQGPU_ERR_STATE;
+        }
+        if ((rc = upload_ops(e, ops, nops))) return rc;
+        if ((rc = traverse(e, nops, EPI_THETA, a, b, len))) return rc;
+        e->theta_valid = true;
+        e->theta_a = a;
+        e->theta_b = b;
+    }
+    if ((rc = launch_derv_f64(e, len))) return rc;
+    if ((rc = fetch_result(e))) return rc;
+    *df = e->h_red_out[0];
+    *ddf = e->h_red_out[1];
+    if (!std::isfinite(*df)) {
+        if (!e->cfg.safe) {
+            set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this");
+            return IQGPU_ERR_NONFINITE;
+        }
+        *df = *ddf = 0.0;
+    }
+    return IQGPU_OK;
+}
+
+int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
+    int rc = ready(e);
+    if (rc) return rc;
+    if (!lnl) { set_error("null output"); return IQGPU_ERR_ARG; }
+    if (!e->theta_valid) { set_error("no theta buffer: call iqgpu_likelihood_derv first"); return IQGPU_ERR_STATE; }
+    CK(cudaSetDevice(e->dev));
+    if ((rc = launch_from_buffer_f64(e, len))) return rc;
+    if ((rc = fetch_result(e))) return rc;
+    const double *r = e->h_red_out;
+    if (!std::isfinite(r[0]) && !e->cfg.safe) {
+        set_error("Numerical underflow (lh-from-buffer); the SAFE kernel avoids this");
+        return IQGPU_ERR_NONFINITE;
+    }
+    *lnl = std::isfinite(r[0]) ? r[0] : r[1];
+    return IQGPU_OK;
+}
+
+int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out) {
+    if (!e || !out) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaMemcpyAsync(out, e->d_plh, (size_t)e->P * 8, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    return IQGPU_OK;
+}
+
+int iqgpu_get_partial(iqgpu_engine *e, int32_t slot, double *partial, uint8_t *scale) {
+    if (!e || slot < 0 || slot >= e->cfg.nslots) { set_error("bad slot"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    const long long B = e->B, P = e->P, Pp = e->Ppad;
+    if (partial) {
+        std::vector<double> tmp((size_t)(B * Pp));
+        CK(cudaMemcpy(tmp.data(), e->d_part + (size_t)slot * B * Pp, (size_t)(B * Pp) * 8, cudaMemcpyDeviceToHost));
+        for (long long p = 0; p < P; p++)
+            for (long long r = 0; r < B; r++) partial[p * B + r] = tmp[(size_t)(r * Pp + p)];
+    }
+    if (scale) {
+        const long long rows = e->cfg.safe ? e->C : 1;
+        std::vector<uint8_t> tmp((size_t)(rows * Pp));
+        CK(cudaMemcpy(tmp.data(), e->d_scale + (size_t)slot * rows * Pp, (size_t)(rows * Pp), cudaMemcpyDeviceToHost));
+        for (long long p = 0; p < P; p++)
+            for (long long c = 0; c < rows; c++) scale[p * rows + c] = tmp[(size_t)(c * Pp + p)];
+    }
+    return IQGPU_OK;
+}
+
+int iqgpu_get_exponent(iqgpu_engine *e, int32_t slot, int32_t *exponent) {
+    (void)slot;
+    (void)exponent;
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    set_error("the FP64 path keeps uint8 scale counts, not exponents");
+    return IQGPU_ERR_STATE;
+}
+
+int iqgpu_sync(iqgpu_engine *e) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    return settle_timing(e);
+}
+
+int iqgpu_set_stream(iqgpu_engine *e, void *cuda_stream) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    int rc = settle_timing(e);
+    if (rc) return rc;
+    e->st = cuda_stream ? (cudaStream_t)cuda_stream : e->own_st;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_timing(iqgpu_engine *e, int32_t enable) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    int rc = settle_timing(e);
+    if (rc) return rc;
+    e->timing = enable != 0;
+    e->timing_ms = 0.0;
+    e->timing_launches = 0;
+    return IQGPU_OK;
+}
+
+int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches) {
+    if (!e || !total_ms || !launches) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    int rc = settle_timing(e);
+    if (rc) return rc;
+    *total_ms = e->timing_ms;
+    *launches = e->timing_launches;
+    return IQGPU_OK;
+}
+
+}  // extern "C"

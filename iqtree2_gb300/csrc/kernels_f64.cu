@@ -1,0 +1,566 @@
+// FP64 drop-in path: eigen-space partials with the reference's 2^-256
+// scaling, one CUDA thread per pattern, the whole traversal in one launch.
+//
+// Layout in HBM: a partial slot is [B rows][ldp patterns] doubles with
+// row r = c*n + x (category-major, then state) and patterns contiguous, so a
+// warp reads 32 consecutive patterns of one row: 256-byte coalesced lines.
+// Scale counts are uint8 [ldp] (NORM) or [ncat][ldp] (SAFE).
+//
+// Every pattern is independent along the whole traversal, so a CTA walks the
+// full op list for its 128 patterns and no grid-wide synchronisation is
+// needed between ops (the reference does the same per OpenMP packet,
+// tree/phylokernelnew.h:2808-2823).
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+
+namespace iqg {
+
+// ---------------------------------------------------------------------------
+// per-op precompute: echild = U diag(exp(lambda r_c t)) and leaf lookup tables
+// (computePartialInfo, tree/phylokernelnew.h:895-1110)
+// ---------------------------------------------------------------------------
+__global__ void k_partial_info_f64(const OpDev *__restrict__ ops, double *__restrict__ opmats,
+                                   const double *__restrict__ evec, const double *__restrict__ eval,
+                                   const double *__restrict__ rates, const double *__restrict__ tip_lh,
+                                   int n, int C, int S) {
+    const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
+    const OpDev op = ops[k];
+    const int ref = op.child[ch];
+    const double len = op.len[ch];
+    const long long CNN = (long long)C * n * n;
+    const int B = n * C;
+    double *base = opmats + op.mat_off;
+    double *echild = base + ch * CNN;
+    __shared__ double sexp[kMaxCat * kMaxStates];
+    for (int t = threadIdx.x; t < C * n; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        sexp[t] = exp(eval[i] * (rates[c] * len));
+    }
+    __syncthreads();
+    if (z == 0) {
+        for (long long t = threadIdx.x; t < CNN; t += blockDim.x) {
+            const int c = (int)(t / (n * n)), x = (int)((t / n) % n), i = (int)(t % n);
+            echild[t] = evec[x * n + i] * sexp[c * n + i];
+        }
+    }
+    if (ref >= 0) return;
+    double *tab = base + 2 * CNN + (long long)ch * (S + 1) * B;
+    const long long rows = (long long)S * B;
+    for (long long t = (long long)z * blockDim.x + threadIdx.x; t < rows; t += (long long)Z * blockDim.x) {
+        const int s = (int)(t / B), r = (int)(t % B), c = r / n, x = r % n;
+        const double *T = tip_lh + (long long)s * n;
+        double acc = (evec[x * n] * sexp[c * n]) * T[0];
+        for (int i = 1; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], T[i], acc);
+        tab[t] = acc;
+    }
+    if (z == 0)
+        for (int t = threadIdx.x; t < B; t += blockDim.x) tab[rows + t] = 1.0;  // STATE_UNKNOWN row
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ double dot_reg(const double *__restrict__ row, const double (&v)[NT]) {
+    // 4 independent accumulators (the reference's unrolling, and FP64 FMA latency hiding)
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+    for (int i = 0; i + 3 < NT; i += 4) {
+        a0 = fma(__ldg(row + i), v[i], a0);
+        a1 = fma(__ldg(row + i + 1), v[i + 1], a1);
+        a2 = fma(__ldg(row + i + 2), v[i + 2], a2);
+        a3 = fma(__ldg(row + i + 3), v[i + 3], a3);
+    }
+#pragma unroll
+    for (int i = NT & ~3; i < NT; i++) a0 = fma(__ldg(row + i), v[i], a0);
+    return (a0 + a1) + (a2 + a3);
+}
+
+__device__ __forceinline__ void warp_reduce(double (&v)[kRedSlots]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < kRedSlots; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
+}
+
+// Block sums -> partials[blockIdx.x]; the last CTA adds all partials in CTA
+// order (deterministic) into red.out and re-arms the ticket.
+__device__ void grid_reduce(double (&v)[kRedSlots], const Reduce &red) {
+    __shared__ double sw[32][kRedSlots];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    warp_reduce(v);
+    if (lane == 0)
+        for (int k = 0; k < kRedSlots; k++) sw[wid][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s[kRedSlots];
+        for (int k = 0; k < kRedSlots; k++) s[k] = 0.0;
+        for (int w = 0; w < nw; w++)
+            for (int k = 0; k < kRedSlots; k++) s[k] += sw[w][k];
+        for (int k = 0; k < kRedSlots; k++) red.partials[(long long)blockIdx.x * kRedSlots + k] = s[k];
+        __threadfence();
+        const unsigned t = atomicAdd(red.ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s[kRedSlots];
+    for (int k = 0; k < kRedSlots; k++) s[k] = 0.0;
+    // fixed assignment of CTAs to threads, then a fixed-order tree: deterministic
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+        for (int k = 0; k < kRedSlots; k++) s[k] += __ldcg(red.partials + (long long)b * kRedSlots + k);
+    warp_reduce(s);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < kRedSlots; k++) sw[wid][k] = s[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kRedSlots; k++) {
+            double acc = 0.0;
+            for (int w = 0; w < nw; w++) acc += sw[w][k];
+            red.out[k] = acc;
+        }
+        *red.ticket = 0u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// traversal kernel
+// ---------------------------------------------------------------------------
+template <int NT, bool SAFE, int EPI>
+__global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
+    constexpr bool REG = (NT != 0 && NT <= 20);
+    constexpr int NR = REG ? NT : 1;  // register-array extent
+    constexpr int XC = 8;             // output chunk in the shared-memory path
+    const int n = NT ? NT : P.n;
+    const int C = P.ncat, B = n * C, S = P.state_unknown;
+    const int tid = threadIdx.x;
+    const long long p = (long long)blockIdx.x * kTPB + tid;
+    const long long ld = P.ldp;
+    extern __shared__ double smem[];
+    double *stmp = smem;                                     // !REG: [n][kTPB]
+    double *sval = smem + (REG ? 0 : (long long)kMaxStates * kTPB);  // EPI_LNL: [B]
+    const double invar = P.invar[p];
+    const long long CNN = (long long)C * n * n;
+    const long long SB = (long long)(S + 1) * B;
+    const double *__restrict__ Ui = P.inv_evec;
+
+    for (int k = 0; k < P.nops; ++k) {
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const double *eL = P.opmats + op.mat_off, *eR = eL + CNN;
+        const double *tL = eL + 2 * CNN, *tR = tL + SB;
+        if (lref >= 0 && rref < 0) {  // put the tip on the left (tree/phylokernelnew.h:1390-1400)
+            int t = lref; lref = rref; rref = t;
+            const double *q = eL; eL = eR; eR = q;
+            q = tL; tL = tR; tR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        double *dad = P.partials + (long long)op.dad_slot * P.slot_stride + p;
+        uint8_t *sdad = P.scale + (long long)op.dad_slot * P.scale_stride + p;
+        const double *Lp = lint ? P.partials + (long long)lref * P.slot_stride + p : nullptr;
+        const double *Rp = rint ? P.partials + (long long)rref * P.slot_stride + p : nullptr;
+        const double *tl = lint ? nullptr : tL + (long long)P.states[(long long)(-1 - lref) * ld + p] * B;
+        const double *tr = rint ? nullptr : tR + (long long)P.states[(long long)(-1 - rref) * ld + p] * B;
+        // scale counts of the dad: 0 (tip-tip), copy (tip-internal), sum (internal-internal)
+        if (SAFE) {
+            for (int c = 0; c < C; c++) {
+                unsigned s = 0;
+                if (lint) s += P.scale[(long long)lref * P.scale_stride + c * ld + p];
+                if (rint) s += P.scale[(long long)rref * P.scale_stride + c * ld + p];
+                sdad[c * ld] = (uint8_t)s;
+            }
+        } else {
+            unsigned s = 0;
+            if (lint) s += P.scale[(long long)lref * P.scale_stride + p];
+            if (rint) s += P.scale[(long long)rref * P.scale_stride + p];
+            sdad[0] = (uint8_t)s;
+        }
+        const bool check = (lint || rint) && invar == 0.0;  // tip-tip never scales
+        double lh_max = 0.0;
+        for (int c = 0; c < C; c++) {
+            double cmax = 0.0;
+            if constexpr (REG) {
+                double lv[NR], rv[NR], tmp[NR];
+                if (lint) {
+#pragma unroll
+                    for (int i = 0; i < NR; i++) lv[i] = Lp[(long long)(c * NR + i) * ld];
+                }
+                if (rint) {
+#pragma unroll
+                    for (int i = 0; i < NR; i++) rv[i] = Rp[(long long)(c * NR + i) * ld];
+                }
+#pragma unroll
+                for (int x = 0; x < NR; x++) {
+                    const double yl = lint ? dot_reg<NR>(eL + (long long)(c * NR + x) * NR, lv) : __ldg(tl + c * NR + x);
+                    const double yr = rint ? dot_reg<NR>(eR + (long long)(c * NR + x) * NR, rv) : __ldg(tr + c * NR + x);
+                    tmp[x] = yl * yr;
+                }
+                double out[NR];
+#pragma unroll
+                for (int x = 0; x < NR; x++) {
+                    out[x] = dot_reg<NR>(Ui + x * NR, tmp);
+                    cmax = fmax(cmax, fabs(out[x]));
+                }
+                if (SAFE && check && cmax < kScaleThreshold) {
+#pragma unroll
+                    for (int x = 0; x < NR; x++) out[x] *= kTwoPow256;
+                    sdad[c * ld] += 1;
+                }
+#pragma unroll
+                for (int x = 0; x < NR; x++) dad[(long long)(c * NR + x) * ld] = out[x];
+            } else {
+                // chunked matvecs with tmp staged in shared memory (large n)
+                for (int x0 = 0; x0 < n; x0 += XC) {
+                    double al[XC], ar[XC];
+#pragma unroll
+                    for (int xx = 0; xx < XC; xx++) { al[xx] = 0.0; ar[xx] = 0.0; }
+                    if (lint || rint) {
+                        for (int i = 0; i < n; i++) {
+                            const double l = lint ? Lp[(long long)(c * n + i) * ld] : 0.0;
+                            const double r = rint ? Rp[(long long)(c * n + i) * ld] : 0.0;
+#pragma unroll
+                            for (int xx = 0; xx < XC; xx++) {
+                                if (x0 + xx < n) {
+                                    if (lint) al[xx] = fma(__ldg(eL + (long long)(c * n + x0 + xx) * n + i), l, al[xx]);
+                                    if (rint) ar[xx] = fma(__ldg(eR + (long long)(c * n + x0 + xx) * n + i), r, ar[xx]);
+                                }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int xx = 0; xx < XC; xx++) {
+                        if (x0 + xx < n) {
+                            const double yl = lint ? al[xx] : __ldg(tl + c * n + x0 + xx);
+                            const double yr = rint ? ar[xx] : __ldg(tr + c * n + x0 + xx);
+                            stmp[(x0 + xx) * kTPB + tid] = yl * yr;
+                        }
+                    }
+                }
+                for (int x0 = 0; x0 < n; x0 += XC) {
+                    double acc[XC];
+#pragma unroll
+                    for (int xx = 0; xx < XC; xx++) acc[xx] = 0.0;
+                    for (int j = 0; j < n; j++) {
+                        const double t = stmp[j * kTPB + tid];
+#pragma unroll
+                        for (int xx = 0; xx < XC; xx++)
+                            if (x0 + xx < n) acc[xx] = fma(__ldg(Ui + (x0 + xx) * n + j), t, acc[xx]);
+                    }
+#pragma unroll
+                    for (int xx = 0; xx < XC; xx++) {
+                        if (x0 + xx < n) {
+                            dad[(long long)(c * n + x0 + xx) * ld] = acc[xx];
+                            cmax = fmax(cmax, fabs(acc[xx]));
+                        }
+                    }
+                }
+                if (SAFE && check && cmax < kScaleThreshold) {
+                    for (int x = 0; x < n; x++) dad[(long long)(c * n + x) * ld] *= kTwoPow256;
+                    sdad[c * ld] += 1;
+                }
+            }
+            lh_max = fmax(lh_max, cmax);
+        }
+        if (!SAFE && check && lh_max < kScaleThreshold) {
+            for (int r = 0; r < B; r++) dad[(long long)r * ld] *= kTwoPow256;
+            sdad[0] += 1;
+        }
+    }
+
+    if constexpr (EPI == EPI_NONE) return;
+
+    // ---- epilogue on the branch (a, b): a is internal (dad_branch), b is node_branch or a tip
+    const double *pa = P.partials + (long long)P.a * P.slot_stride + p;
+    const uint8_t *sa = P.scale + (long long)P.a * P.scale_stride + p;
+    const bool btip = P.b < 0;
+    const double *pb = btip ? nullptr : P.partials + (long long)P.b * P.slot_stride + p;
+    const uint8_t *sb = btip ? nullptr : P.scale + (long long)P.b * P.scale_stride + p;
+    const double *tipv = btip ? P.tip_lh + (long long)P.states[(long long)(-1 - P.b) * ld + p] * n : nullptr;
+    const bool valid = p < P.nptn;
+
+    if constexpr (EPI == EPI_THETA) {
+        // theta = node o dad and per-pattern scale offset (tree/phylokernelnew.h:2048-2231)
+        double *th = P.theta + p;
+        for (int c = 0; c < C; c++)
+            for (int x = 0; x < n; x++) {
+                const long long r = (long long)(c * n + x) * ld;
+                th[r] = (btip ? __ldg(tipv + x) : pb[r]) * pa[r];
+            }
+        double bs;
+        if (SAFE) {
+            unsigned sum[kMaxCat], mn = 1u << 30;
+            for (int c = 0; c < C; c++) {
+                sum[c] = (unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld]);
+                sum[c] &= 0xffu;  // UBYTE arithmetic
+                mn = min(mn, sum[c]);
+            }
+            for (int c = 0; c < C; c++) {
+                if (sum[c] == mn + 1) {
+                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] *= kScaleThreshold;
+                } else if (sum[c] > mn + 1) {
+                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] = 0.0;
+                }
+            }
+            bs = (double)mn;
+        } else {
+            bs = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+        }
+        P.buffer_scale[p] = bs * kLogScaleThreshold;
+        return;
+    } else {
+        // branch lnL (tree/phylokernelnew.h:2641-3223)
+        for (int t = tid; t < B; t += kTPB) {
+            const int c = t / n, i = t % n;
+            sval[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+        }
+        __syncthreads();
+        double lh_cat[kMaxCat];
+        double lh = 0.0;
+        for (int c = 0; c < C; c++) {
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) {
+                const long long r = (long long)(c * n + i) * ld;
+                const double w = btip ? sval[c * n + i] * __ldg(tipv + i) : sval[c * n + i] * pb[r];
+                acc = fma(w, pa[r], acc);
+            }
+            lh_cat[c] = acc;
+            if (!SAFE) lh += acc;
+        }
+        double scale_count;
+        if (SAFE) {
+            unsigned sum[kMaxCat], mn = 1u << 30;
+            for (int c = 0; c < C; c++) {
+                sum[c] = ((unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld])) & 0xffu;
+                mn = min(mn, sum[c]);
+            }
+            for (int c = 0; c < C; c++) {
+                if (sum[c] == mn + 1) lh_cat[c] *= kScaleThreshold;
+                else if (sum[c] > mn + 1) lh_cat[c] = 0.0;
+                lh += lh_cat[c];
+            }
+            scale_count = (double)mn;
+        } else {
+            scale_count = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+        }
+        lh = fabs(lh) + invar;
+        const double plh = log(lh) + scale_count * kLogScaleThreshold;
+        P.pattern_lh[p] = plh;
+        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        if (valid) {
+            const double f = P.freq[p];
+            v[0] = plh * f;
+            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;  // underflow fix-up sum
+            v[2] = isfinite(plh) ? 0.0 : 1.0;
+        }
+        grid_reduce(v, P.red);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// derivatives and lnL from the theta buffer
+// ---------------------------------------------------------------------------
+struct BufParams {
+    int n, ncat, nptn;
+    long long ldp;
+    const double *theta, *buffer_scale, *freq, *invar;
+    const double *eval, *rates, *props;
+    double len;
+    double *pattern_lh;
+    Reduce red;
+};
+
+// (tree/phylokernelnew.h:2233-2633): df = sum freq*d1/lh, ddf = sum freq*(d2/lh - (d1/lh)^2)
+__global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
+    __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
+    const int n = P.n, C = P.ncat, B = n * C;
+    for (int t = threadIdx.x; t < B; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        const double cof = P.eval[i] * P.rates[c];
+        const double val = exp(cof * P.len) * P.props[c];
+        const double val1 = cof * val;
+        v0[t] = val;
+        v1[t] = val1;
+        v2[t] = cof * val1;
+    }
+    __syncthreads();
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const double *th = P.theta + p;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
+        int k = 0;
+        for (; k + 1 < B; k += 2) {
+            const double t0 = th[(long long)k * P.ldp], t1 = th[(long long)(k + 1) * P.ldp];
+            a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
+            b0 = fma(v0[k + 1], t1, b0); b1 = fma(v1[k + 1], t1, b1); b2 = fma(v2[k + 1], t1, b2);
+        }
+        if (k < B) {
+            const double t0 = th[(long long)k * P.ldp];
+            a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
+        }
+        double lh = a0 + b0, d1 = a1 + b1, d2 = a2 + b2;
+        lh = fabs(lh) + P.invar[p];
+        const double inv = 1.0 / lh;
+        const double df_frac = d1 * inv, ddf_frac = d2 * inv;
+        const double f = P.freq[p];
+        const double tmp1 = df_frac * f, tmp2 = ddf_frac * f;
+        r[0] = tmp1;
+        r[1] = fma(-tmp1, df_frac, tmp2);
+        r[2] = (log(lh) + P.buffer_scale[p]) * f;  // lnL at this length, for free
+    }
+    grid_reduce(r, P.red);
+}
+
+// (tree/phylokernelnew.h:3232-3428)
+__global__ void __launch_bounds__(kTPB) k_from_buffer_f64(const BufParams P) {
+    __shared__ double v0[kMaxCat * kMaxStates];
+    const int n = P.n, C = P.ncat, B = n * C;
+    for (int t = threadIdx.x; t < B; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        v0[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+    }
+    __syncthreads();
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const double *th = P.theta + p;
+        double a0 = 0.0, a1 = 0.0;
+        int k = 0;
+        for (; k + 1 < B; k += 2) {
+            a0 = fma(v0[k], th[(long long)k * P.ldp], a0);
+            a1 = fma(v0[k + 1], th[(long long)(k + 1) * P.ldp], a1);
+        }
+        if (k < B) a0 = fma(v0[k], th[(long long)k * P.ldp], a0);
+        double lh = fabs(a0 + a1) + P.invar[p];
+        const double plh = log(fabs(lh)) + P.buffer_scale[p];
+        P.pattern_lh[p] = plh;
+        const double f = P.freq[p];
+        r[0] = plh * f;
+        r[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+        r[2] = isfinite(plh) ? 0.0 : 1.0;
+    }
+    grid_reduce(r, P.red);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static TravParams trav_params(iqgpu_engine *e, int nops) {
+    TravParams P;
+    P.n = e->n;
+    P.ncat = e->C;
+    P.state_unknown = e->S;
+    P.nops = nops;
+    P.nptn = (int)e->P;
+    P.ldp = e->Ppad;
+    P.slot_stride = (long long)e->B * e->Ppad;
+    P.scale_stride = (long long)(e->cfg.safe ? e->C : 1) * e->Ppad;
+    P.op_stride = e->op_stride;
+    P.ops = e->d_ops;
+    P.opmats = e->d_opmats;
+    P.inv_evec = e->d_inv;
+    P.eval = e->d_eval;
+    P.rates = e->d_rates;
+    P.props = e->d_props;
+    P.tip_lh = e->d_tip;
+    P.freq = e->d_freq;
+    P.invar = e->d_invar;
+    P.states = e->d_states;
+    P.partials = e->d_part;
+    P.scale = e->d_scale;
+    P.a = P.b = 0;
+    P.len = 0.0;
+    P.pattern_lh = e->d_plh;
+    P.theta = e->d_theta;
+    P.buffer_scale = e->d_bscale;
+    P.red.partials = e->d_red_partials;
+    P.red.ticket = e->d_ticket;
+    P.red.out = e->d_red_out;
+    return P;
+}
+
+int launch_partial_info_f64(iqgpu_engine *e, int nops) {
+    if (nops <= 0) return IQGPU_OK;
+    dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
+    k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
+                                                 e->d_tip, e->n, e->C, e->S);
+    return cuda_fail(cudaGetLastError(), "partial_info_f64");
+}
+
+template <int NT, bool SAFE, int EPI>
+static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
+    constexpr bool REG = (NT != 0 && NT <= 20);
+    size_t smem = (REG ? 0 : (size_t)kMaxStates * kTPB * sizeof(double)) +
+                  (EPI == EPI_LNL ? (size_t)kMaxCat * kMaxStates * sizeof(double) : 0);
+    auto kern = k_traverse_f64<NT, SAFE, EPI>;
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_f64 smem attribute");
+    }
+    kern<<<e->nblk, kTPB, smem, e->st>>>(P);
+    return cuda_fail(cudaGetLastError(), "traverse_f64");
+}
+
+template <bool SAFE, int EPI>
+static int dispatch_n(iqgpu_engine *e, const TravParams &P) {
+    switch (e->n) {
+    case 4: return launch_trav_t<4, SAFE, EPI>(e, P);
+    case 20: return launch_trav_t<20, SAFE, EPI>(e, P);
+    default: return launch_trav_t<0, SAFE, EPI>(e, P);
+    }
+}
+
+template <int EPI>
+static int dispatch_safe(iqgpu_engine *e, const TravParams &P) {
+    return e->cfg.safe ? dispatch_n<true, EPI>(e, P) : dispatch_n<false, EPI>(e, P);
+}
+
+int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
+    TravParams P = trav_params(e, nops);
+    P.a = a;
+    P.b = b;
+    P.len = len;
+    if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    switch (epi) {
+    case EPI_NONE: return dispatch_safe<EPI_NONE>(e, P);
+    case EPI_LNL: return dispatch_safe<EPI_LNL>(e, P);
+    default: return dispatch_safe<EPI_THETA>(e, P);
+    }
+}
+
+static BufParams buf_params(iqgpu_engine *e, double len) {
+    BufParams P;
+    P.n = e->n;
+    P.ncat = e->C;
+    P.nptn = (int)e->P;
+    P.ldp = e->Ppad;
+    P.theta = e->d_theta;
+    P.buffer_scale = e->d_bscale;
+    P.freq = e->d_freq;
+    P.invar = e->d_invar;
+    P.eval = e->d_eval;
+    P.rates = e->d_rates;
+    P.props = e->d_props;
+    P.len = len;
+    P.pattern_lh = e->d_plh;
+    P.red.partials = e->d_red_partials;
+    P.red.ticket = e->d_ticket;
+    P.red.out = e->d_red_out;
+    return P;
+}
+
+int launch_derv_f64(iqgpu_engine *e, double len) {
+    k_derv_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    return cuda_fail(cudaGetLastError(), "derv_f64");
+}
+
+int launch_from_buffer_f64(iqgpu_engine *e, double len) {
+    k_from_buffer_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    return cuda_fail(cudaGetLastError(), "from_buffer_f64");
+}
+
+}  // namespace iqg

@@ -1,0 +1,347 @@
+// PhyloTree drivers over the kernel-level C ABI.
+//
+// This is the host half of the drop-in: the same control flow as IQ-TREE 2's
+// PhyloTree around its kernel function pointers, restated in C++ on top of
+// iqgpu_compute_likelihood / iqgpu_likelihood_derv / iqgpu_lnl_from_buffer:
+//   traversal of stale partials   tree/phylotree.cpp:5918-6028 and
+//                                 tree/phylokernelnew.h:1145-1200
+//   computeLikelihood             tree/phylotree.cpp:1233-1280
+//   computeFuncDerv               tree/phylotree.cpp:2529-2536
+//   optimizeOneBranch             tree/phylotree.cpp:2594-2644
+//   optimizeAllBranches           tree/phylotree.cpp:2698-2774
+//   computeBestTraversal          tree/phylotree.cpp:2689 with
+//   findFarthestLeaf / getPreOrderBranches  tree/mtree.cpp:3040-3082
+//   minimizeNewton                utils/optimization.cpp:422-499
+//   clearReversePartialLh         tree/phylonode.cpp:22-33
+// Every directed partial of an internal subtree owns one HBM slot (three per
+// internal node), so a branch-length change only recomputes the partials it
+// invalidates, as with the reference's per-neighbour partial_lh buffers.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/iqgpu.h"
+
+namespace iqg {
+void set_error(const std::string &msg);
+}
+
+struct iqgpu_tree {
+    iqgpu_engine *e;
+    int64_t nptn;
+    int ntaxa, nnode, nedge;
+    std::vector<int> deg;
+    std::vector<int> nbr, edge, slot;  // [node*3 + j]
+    std::vector<uint8_t> computed;     // [node*3 + j]: partial of node->nbr valid
+    std::vector<double> len;
+    std::vector<int> height;
+    std::vector<iqgpu_op> ops;
+    int64_t nupdates = 0;
+    double min_bl = 1e-6, max_bl = 10.0;
+    int cur1 = -1, cur2 = -1;  // current_it: cur1 -> cur2
+    bool theta_computed = false;
+    int last_rc = IQGPU_OK;
+
+    bool leaf(int u) const { return u < ntaxa; }
+    int idx(int u, int v) const {
+        for (int j = 0; j < deg[u]; j++)
+            if (nbr[u * 3 + j] == v) return j;
+        return -1;
+    }
+    int ref(int dad, int node) const { return leaf(node) ? -1 - node : slot[dad * 3 + idx(dad, node)]; }
+    double &blen(int u, int v) { return len[edge[u * 3 + idx(u, v)]]; }
+
+    void traverse(int dad, int node) {
+        const int j = idx(dad, node);
+        if (leaf(node) || computed[dad * 3 + j]) return;
+        iqgpu_op op;
+        std::memset(&op, 0, sizeof(op));
+        int k = 0;
+        for (int q = 0; q < deg[node]; q++) {
+            const int ch = nbr[node * 3 + q];
+            if (ch == dad) continue;
+            traverse(node, ch);
+            op.child[k] = ref(node, ch);
+            op.len[k] = len[edge[node * 3 + q]];
+            k++;
+        }
+        op.dad_slot = slot[dad * 3 + j];
+        computed[dad * 3 + j] = 1;
+        ops.push_back(op);
+    }
+    void collect(int node, int dad) {
+        ops.clear();
+        traverse(dad, node);
+        traverse(node, dad);
+    }
+    int farthest_leaf(int node, int dad) {
+        if (dad >= 0 && leaf(node)) { height[node] = 0; return node; }
+        int res = -1;
+        height[node] = 0;
+        for (int q = 0; q < deg[node]; q++) {
+            const int ch = nbr[node * 3 + q];
+            if (ch == dad) continue;
+            const int lf = farthest_leaf(ch, node);
+            if (height[node] < height[ch] + 1) {
+                height[node] = height[ch] + 1;
+                res = lf;
+            }
+        }
+        return res;
+    }
+    void clear_reverse(int node, int dad) {
+        for (int q = 0; q < deg[node]; q++) {
+            const int x = nbr[node * 3 + q];
+            if (x == dad) continue;
+            computed[x * 3 + idx(x, node)] = 0;
+            clear_reverse(x, node);
+        }
+    }
+    void preorder(int node, int dad, std::vector<int> &n1, std::vector<int> &n2) {
+        if (dad >= 0) { n1.push_back(node); n2.push_back(dad); }
+        int order[3], d = deg[node];
+        for (int q = 0; q < d; q++) order[q] = nbr[node * 3 + q];
+        for (int i = 0; i < d; i++)
+            for (int k = i + 1; k < d; k++)
+                if (height[order[i]] > height[order[k]]) std::swap(order[i], order[k]);
+        for (int q = 0; q < d; q++)
+            if (order[q] != dad) preorder(order[q], node, n1, n2);
+    }
+};
+
+namespace {
+
+int64_t nptn_of(const iqgpu_tree *t) { return t->nptn; }
+
+// computeLikelihoodBranch(dad_branch = dad->node, dad)
+int lnl_branch(iqgpu_tree *t, int node, int dad, double *lnl) {
+    if (t->leaf(node)) std::swap(node, dad);
+    t->collect(node, dad);
+    const int rc = iqgpu_compute_likelihood(t->e, t->ops.data(), (int32_t)t->ops.size(), t->ref(dad, node),
+                                            t->ref(node, dad), t->blen(node, dad), lnl);
+    t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+    return rc;
+}
+
+// computeFuncDerv: f = -df, df = -ddf on the current branch
+int func_derv(iqgpu_tree *t, double value, double *f, double *df) {
+    const int n1 = t->cur1, n2 = t->cur2;
+    t->blen(n1, n2) = value;
+    int node = n2, dad = n1;
+    if (t->leaf(node)) std::swap(node, dad);
+    t->collect(node, dad);
+    double d1 = 0.0, d2 = 0.0;
+    const int rc = iqgpu_likelihood_derv(t->e, t->ops.data(), (int32_t)t->ops.size(), t->ref(dad, node),
+                                         t->ref(node, dad), value, t->theta_computed ? 1 : 0, &d1, &d2);
+    if (rc) return rc;
+    t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+    t->theta_computed = true;
+    *f = -d1;
+    *df = -d2;
+    return IQGPU_OK;
+}
+
+int from_buffer(iqgpu_tree *t, double *lnl) { return iqgpu_lnl_from_buffer(t->e, t->blen(t->cur1, t->cur2), lnl); }
+
+// Optimization::minimizeNewton (utils/optimization.cpp:422-499)
+int minimize_newton(iqgpu_tree *t, double x1, double xguess, double x2, double xacc, int max_nr_step, double *out) {
+    double f, df, dx, temp, xh, xl, rts, rts_old;
+    int rc;
+    rts = xguess;
+    if (rts < x1) rts = x1;
+    if (rts > x2) rts = x2;
+    if ((rc = func_derv(t, rts, &f, &df))) return rc;
+    if (!std::isfinite(f) || !std::isfinite(df)) { iqg::set_error("Wrong computeFuncDerv"); return IQGPU_ERR_NEWTON; }
+    if (df >= 0.0 && std::fabs(f) < xacc) { *out = rts; return IQGPU_OK; }
+    if (f < 0.0) { xl = rts; xh = x2; } else { xh = rts; xl = x1; }
+    dx = std::fabs(xh - xl);
+    for (int j = 1; j <= max_nr_step; j++) {
+        rts_old = rts;
+        if ((df <= 0.0) || (((rts - xh) * df - f) * ((rts - xl) * df - f) >= 0.0)) {
+            dx = 0.5 * (xh - xl);
+            rts = xl + dx;
+            if (xl == rts) { *out = rts; return IQGPU_OK; }
+        } else {
+            dx = f / df;
+            temp = rts;
+            rts -= dx;
+            if (temp == rts) { *out = rts; return IQGPU_OK; }
+        }
+        if (std::fabs(dx) < xacc || (j == max_nr_step)) { *out = rts_old; return IQGPU_OK; }
+        if ((rc = func_derv(t, rts, &f, &df))) return rc;
+        if (!std::isfinite(f) || !std::isfinite(df)) { iqg::set_error("Wrong computeFuncDerv"); return IQGPU_ERR_NEWTON; }
+        if (df > 0.0 && std::fabs(f) < xacc) { *out = rts; return IQGPU_OK; }
+        if (f < 0.0) xl = rts;
+        else if (f > 0.0) xh = rts;
+    }
+    iqg::set_error("Maximum number of iterations exceeded in minimizeNewton");
+    return IQGPU_ERR_NEWTON;
+}
+
+}  // namespace
+
+extern "C" {
+
+int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out) {
+    if (!e || !edges || !lengths || !out) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    *out = nullptr;
+    iqgpu_config cfgv;
+    int rc0 = iqgpu_get_config(e, &cfgv);
+    if (rc0) return rc0;
+    const iqgpu_config *cfg = &cfgv;
+    iqgpu_tree *t = new iqgpu_tree();
+    t->e = e;
+    t->nptn = cfg->nptn;
+    t->ntaxa = cfg->ntaxa;
+    t->nnode = 2 * t->ntaxa - 2;
+    t->nedge = 2 * t->ntaxa - 3;
+    if (cfg->nslots < 3 * (t->ntaxa - 2) || cfg->max_ops < 2 * t->ntaxa) {
+        delete t;
+        iqg::set_error("engine needs nslots >= 3*(ntaxa-2) and max_ops >= 2*ntaxa for a tree");
+        return IQGPU_ERR_ARG;
+    }
+    t->deg.assign(t->nnode, 0);
+    t->nbr.assign(t->nnode * 3, -1);
+    t->edge.assign(t->nnode * 3, -1);
+    t->slot.assign(t->nnode * 3, -1);
+    t->computed.assign(t->nnode * 3, 0);
+    t->height.assign(t->nnode, 0);
+    t->len.assign(lengths, lengths + t->nedge);
+    for (int k = 0; k < t->nedge; k++) {
+        const int u = edges[2 * k], v = edges[2 * k + 1];
+        if (u < 0 || v < 0 || u >= t->nnode || v >= t->nnode || u == v || t->deg[u] >= 3 || t->deg[v] >= 3 ||
+            !(lengths[k] >= 0.0)) {
+            delete t;
+            iqg::set_error("edge list is not an unrooted binary tree on 2*ntaxa-2 nodes");
+            return IQGPU_ERR_ARG;
+        }
+        t->nbr[u * 3 + t->deg[u]] = v;
+        t->edge[u * 3 + t->deg[u]++] = k;
+        t->nbr[v * 3 + t->deg[v]] = u;
+        t->edge[v * 3 + t->deg[v]++] = k;
+    }
+    for (int u = 0; u < t->nnode; u++) {
+        if ((t->leaf(u) && t->deg[u] != 1) || (!t->leaf(u) && t->deg[u] != 3)) {
+            delete t;
+            iqg::set_error("leaves need degree 1 and internal nodes degree 3");
+            return IQGPU_ERR_ARG;
+        }
+    }
+    int ns = 0;
+    for (int u = 0; u < t->nnode; u++)
+        for (int j = 0; j < t->deg[u]; j++)
+            if (!t->leaf(t->nbr[u * 3 + j])) t->slot[u * 3 + j] = ns++;
+    *out = t;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_destroy(iqgpu_tree *t) {
+    delete t;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_compute_likelihood(iqgpu_tree *t, double *lnl, double *pattern_lh) {
+    if (!t || !lnl) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    if (t->cur1 < 0) {
+        const int lf = t->farthest_leaf(0, -1);  // root is taxon 0, a leaf
+        t->cur1 = lf;
+        t->cur2 = t->nbr[lf * 3];
+    }
+    int rc = lnl_branch(t, t->cur2, t->cur1, lnl);
+    if (rc) return rc;
+    if (pattern_lh) rc = iqgpu_get_pattern_lh(t->e, pattern_lh);
+    return rc;
+}
+
+int iqgpu_tree_optimize_one_branch(iqgpu_tree *t, int32_t node1, int32_t node2, int32_t max_nr_step) {
+    if (!t || node1 < 0 || node2 < 0 || node1 >= t->nnode || node2 >= t->nnode || t->idx(node1, node2) < 0) {
+        iqg::set_error("not a branch");
+        return IQGPU_ERR_ARG;
+    }
+    t->cur1 = node1;
+    t->cur2 = node2;
+    const double current_len = t->blen(node1, node2);
+    t->theta_computed = false;
+    double optx = current_len;
+    int rc = minimize_newton(t, t->min_bl, current_len, t->max_bl, t->min_bl, max_nr_step, &optx);
+    if (rc) return rc;
+    if (optx > t->max_bl * 0.95) {
+        double opt_lh, orig_lh;
+        t->blen(node1, node2) = optx;
+        if ((rc = from_buffer(t, &opt_lh))) return rc;
+        t->blen(node1, node2) = current_len;
+        if ((rc = from_buffer(t, &orig_lh))) return rc;
+        if (orig_lh > opt_lh) optx = current_len;
+    }
+    t->blen(node1, node2) = optx;
+    if (current_len != optx) {
+        t->clear_reverse(node1, node2);
+        t->clear_reverse(node2, node1);
+    }
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_optimize_all_branches(iqgpu_tree *t, int32_t iterations, double tolerance, int32_t max_nr_step,
+                                     double *lnl) {
+    if (!t || !lnl) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    std::vector<int> n1, n2;
+    const int farleaf = t->farthest_leaf(0, -1);
+    t->farthest_leaf(farleaf, -1);
+    t->preorder(farleaf, -1, n1, n2);
+    double tree_lh;
+    int rc = lnl_branch(t, n2[0], n1[0], &tree_lh);
+    if (rc) return rc;
+    std::vector<double> saved;
+    for (int it = 0; it < iterations; it++) {
+        saved = t->len;
+        for (size_t j = 0; j < n1.size(); j++)
+            if ((rc = iqgpu_tree_optimize_one_branch(t, n1[j], n2[j], max_nr_step))) return rc;
+        double new_lh;
+        if ((rc = from_buffer(t, &new_lh))) return rc;
+        if (new_lh < tree_lh - tolerance * 0.1) {
+            // log-likelihood decreased: restore and stop
+            t->len = saved;
+            std::fill(t->computed.begin(), t->computed.end(), 0);
+            return iqgpu_tree_compute_likelihood(t, lnl, nullptr);
+        }
+        if (tree_lh <= new_lh && new_lh <= tree_lh + tolerance) {
+            *lnl = new_lh;
+            return IQGPU_OK;
+        }
+        tree_lh = new_lh;
+    }
+    *lnl = tree_lh;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_get_lengths(iqgpu_tree *t, double *lengths) {
+    if (!t || !lengths) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    std::memcpy(lengths, t->len.data(), sizeof(double) * t->nedge);
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_set_lengths(iqgpu_tree *t, const double *lengths) {
+    if (!t || !lengths) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    for (int k = 0; k < t->nedge; k++)
+        if (!(lengths[k] >= 0.0)) { iqg::set_error("negative branch length"); return IQGPU_ERR_ARG; }
+    t->len.assign(lengths, lengths + t->nedge);
+    std::fill(t->computed.begin(), t->computed.end(), 0);  // clearAllPartialLH
+    t->theta_computed = false;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl) {
+    if (!t || !(min_bl > 0.0) || !(max_bl > min_bl)) { iqg::set_error("bad bounds"); return IQGPU_ERR_ARG; }
+    t->min_bl = min_bl;
+    t->max_bl = max_bl;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_num_updates(iqgpu_tree *t, int64_t *updates) {
+    if (!t || !updates) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    *updates = t->nupdates;
+    return IQGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,301 @@
+"""Python binding of the GB300 likelihood engine (``libiqgpu.so``, C ABI).
+
+There is no CPU fallback: if the in-tree library cannot be loaded, or the
+device is not a GB300 (sm_103), every call raises.
+
+``Engine`` mirrors the reference's kernel function pointers
+(tree/phylotreesse.cpp:91-236) and ``GpuTree`` the PhyloTree drivers around
+them (computeLikelihood, optimizeOneBranch, optimizeAllBranches).
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+import numpy as np
+
+from . import build as _build
+
+F64, F32, TF32X3, BF16 = 0, 1, 2, 3
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"iqgpu error {code}: {msg}")
+        self.code = code
+
+
+class Config(ct.Structure):
+    _fields_ = [("nptn", ct.c_int32), ("nstates", ct.c_int32), ("ncat", ct.c_int32), ("ntaxa", ct.c_int32),
+                ("state_unknown", ct.c_int32), ("nslots", ct.c_int32), ("safe", ct.c_int32),
+                ("precision", ct.c_int32), ("device", ct.c_int32), ("max_ops", ct.c_int32)]
+
+
+class Op(ct.Structure):
+    _fields_ = [("dad_slot", ct.c_int32), ("child", ct.c_int32 * 2), ("reserved", ct.c_int32),
+                ("len", ct.c_double * 2)]
+
+
+OP_DTYPE = np.dtype([("dad_slot", np.int32), ("child", np.int32, (2,)), ("reserved", np.int32),
+                     ("len", np.float64, (2,))])
+assert OP_DTYPE.itemsize == ct.sizeof(Op) == 32
+
+_DP = ct.POINTER(ct.c_double)
+_U8P = ct.POINTER(ct.c_uint8)
+_I32P = ct.POINTER(ct.c_int32)
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load the in-tree engine library (built on demand if nvcc is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        _build.build()
+    L = ct.CDLL(path)
+    vp = ct.c_void_p
+    sig = {
+        "iqgpu_last_error": ([], ct.c_char_p),
+        "iqgpu_memory_required": ([ct.POINTER(Config), ct.POINTER(ct.c_size_t)], ct.c_int),
+        "iqgpu_create": ([ct.POINTER(Config), ct.POINTER(vp)], ct.c_int),
+        "iqgpu_destroy": ([vp], ct.c_int),
+        "iqgpu_get_config": ([vp, ct.POINTER(Config)], ct.c_int),
+        "iqgpu_set_model": ([vp, _DP, _DP, _DP, _DP, _DP], ct.c_int),
+        "iqgpu_set_tip_partials": ([vp, _DP], ct.c_int),
+        "iqgpu_set_patterns": ([vp, _DP, _DP], ct.c_int),
+        "iqgpu_set_tip_states": ([vp, _U8P], ct.c_int),
+        "iqgpu_compute_partials": ([vp, vp, ct.c_int32], ct.c_int),
+        "iqgpu_branch_lnl": ([vp, ct.c_int32, ct.c_int32, ct.c_double, _DP], ct.c_int),
+        "iqgpu_compute_likelihood": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, _DP], ct.c_int),
+        "iqgpu_likelihood_derv": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_int32, _DP, _DP],
+                                  ct.c_int),
+        "iqgpu_lnl_from_buffer": ([vp, ct.c_double, _DP], ct.c_int),
+        "iqgpu_get_pattern_lh": ([vp, _DP], ct.c_int),
+        "iqgpu_get_partial": ([vp, ct.c_int32, _DP, _U8P], ct.c_int),
+        "iqgpu_get_exponent": ([vp, ct.c_int32, _I32P], ct.c_int),
+        "iqgpu_sync": ([vp], ct.c_int),
+        "iqgpu_set_stream": ([vp, vp], ct.c_int),
+        "iqgpu_set_timing": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
+        "iqgpu_tree_create": ([vp, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
+        "iqgpu_tree_destroy": ([vp], ct.c_int),
+        "iqgpu_tree_compute_likelihood": ([vp, _DP, _DP], ct.c_int),
+        "iqgpu_tree_optimize_one_branch": ([vp, ct.c_int32, ct.c_int32, ct.c_int32], ct.c_int),
+        "iqgpu_tree_optimize_all_branches": ([vp, ct.c_int32, ct.c_double, ct.c_int32, _DP], ct.c_int),
+        "iqgpu_tree_get_lengths": ([vp, _DP], ct.c_int),
+        "iqgpu_tree_set_lengths": ([vp, _DP], ct.c_int),
+        "iqgpu_tree_set_bounds": ([vp, ct.c_double, ct.c_double], ct.c_int),
+        "iqgpu_tree_num_updates": ([vp, ct.POINTER(ct.c_int64)], ct.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names the header declares (checked by the CPU tests)."""
+    hdr = os.path.join(_build.ROOT, "include", "iqgpu.h")
+    import re
+    names = re.findall(r"^\s*(?:int|const char \*)\s*\*?\s*(iqgpu_\w+)\s*\(", open(hdr).read(), re.M)
+    return sorted(set(names))
+
+
+def _check(rc):
+    if rc != 0:
+        raise EngineError(rc, lib().iqgpu_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+class Engine:
+    """One engine = one HBM workspace and one CUDA stream (a PhyloTree's buffers)."""
+
+    def __init__(self, nptn, nstates, ncat, ntaxa, state_unknown, nslots, safe=False, precision=F64,
+                 device=0, max_ops=None):
+        self.cfg = Config(int(nptn), int(nstates), int(ncat), int(ntaxa), int(state_unknown), int(nslots),
+                          int(bool(safe)), int(precision), int(device),
+                          int(max_ops if max_ops is not None else max(2 * ntaxa, 8)))
+        h = ct.c_void_p()
+        _check(lib().iqgpu_create(ct.byref(self.cfg), ct.byref(h)))
+        self.h = h
+        self.nptn, self.nstates, self.ncat, self.ntaxa = int(nptn), int(nstates), int(ncat), int(ntaxa)
+        self.safe = bool(safe)
+
+    @staticmethod
+    def memory_required(**kw):
+        c = Config(kw["nptn"], kw["nstates"], kw["ncat"], kw["ntaxa"], kw["state_unknown"], kw["nslots"],
+                   int(kw.get("safe", 0)), int(kw.get("precision", F64)), 0,
+                   kw.get("max_ops", max(2 * kw["ntaxa"], 8)))
+        out = ct.c_size_t()
+        _check(lib().iqgpu_memory_required(ct.byref(c), ct.byref(out)))
+        return out.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().iqgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def block(self):
+        return self.nstates * self.ncat
+
+    def set_model(self, model):
+        a = [np.ascontiguousarray(x, np.float64) for x in (model.eval, model.evec, model.inv_evec,
+                                                            model.rates, model.props)]
+        _check(lib().iqgpu_set_model(self.h, *[_dp(x) for x in a]))
+        _check(lib().iqgpu_set_tip_partials(self.h, _dp(np.ascontiguousarray(model.tip_lh, np.float64))))
+
+    def set_patterns(self, freq, invar=None):
+        f = np.ascontiguousarray(freq, np.float64)
+        iv = None if invar is None else _dp(np.ascontiguousarray(invar, np.float64))
+        _check(lib().iqgpu_set_patterns(self.h, _dp(f), iv))
+
+    def set_tip_states(self, patterns):
+        s = np.ascontiguousarray(patterns, np.uint8)
+        _check(lib().iqgpu_set_tip_states(self.h, s.ctypes.data_as(_U8P)))
+
+    @staticmethod
+    def ops_array(ops):
+        arr = np.zeros(len(ops), OP_DTYPE)
+        for k, (dad, c0, c1, l0, l1) in enumerate(ops):
+            arr[k] = (dad, (c0, c1), 0, (l0, l1))
+        return arr
+
+    def compute_partials(self, ops):
+        arr = ops if isinstance(ops, np.ndarray) else self.ops_array(ops)
+        _check(lib().iqgpu_compute_partials(self.h, arr.ctypes.data, len(arr)))
+
+    def branch_lnl(self, a, b, length):
+        out = ct.c_double()
+        _check(lib().iqgpu_branch_lnl(self.h, a, b, length, ct.byref(out)))
+        return out.value
+
+    def compute_likelihood(self, ops, a, b, length):
+        arr = ops if isinstance(ops, np.ndarray) else self.ops_array(ops)
+        out = ct.c_double()
+        _check(lib().iqgpu_compute_likelihood(self.h, arr.ctypes.data, len(arr), a, b, length, ct.byref(out)))
+        return out.value
+
+    def likelihood_derv(self, ops, a, b, length, theta_computed=False):
+        arr = ops if isinstance(ops, np.ndarray) else self.ops_array(ops)
+        df, ddf = ct.c_double(), ct.c_double()
+        _check(lib().iqgpu_likelihood_derv(self.h, arr.ctypes.data, len(arr), a, b, length,
+                                           int(theta_computed), ct.byref(df), ct.byref(ddf)))
+        return df.value, ddf.value
+
+    def lnl_from_buffer(self, length):
+        out = ct.c_double()
+        _check(lib().iqgpu_lnl_from_buffer(self.h, length, ct.byref(out)))
+        return out.value
+
+    def pattern_lh(self):
+        out = np.zeros(self.nptn)
+        _check(lib().iqgpu_get_pattern_lh(self.h, _dp(out)))
+        return out
+
+    def partial(self, slot):
+        p = np.zeros((self.nptn, self.block))
+        s = np.zeros((self.nptn, self.ncat if self.safe else 1), np.uint8)
+        _check(lib().iqgpu_get_partial(self.h, slot, _dp(p), s.ctypes.data_as(_U8P)))
+        return p, s
+
+    def exponent(self, slot):
+        e = np.zeros(self.nptn, np.int32)
+        _check(lib().iqgpu_get_exponent(self.h, slot, e.ctypes.data_as(_I32P)))
+        return e
+
+    def sync(self):
+        _check(lib().iqgpu_sync(self.h))
+
+    def set_stream(self, cuda_stream_handle):
+        """Run on a caller stream (an int cudaStream_t, e.g. torch.cuda.Stream().cuda_stream)."""
+        _check(lib().iqgpu_set_stream(self.h, ct.c_void_p(cuda_stream_handle or None)))
+
+    def set_timing(self, enable=True):
+        _check(lib().iqgpu_set_timing(self.h, int(enable)))
+
+    def timing(self):
+        ms, n = ct.c_double(), ct.c_int64()
+        _check(lib().iqgpu_get_timing(self.h, ct.byref(ms), ct.byref(n)))
+        return ms.value, n.value
+
+
+class GpuTree:
+    """PhyloTree drivers on the GPU engine (one engine per tree)."""
+
+    def __init__(self, model, patterns, freq, edges, lengths, safe=False, precision=F64, device=0, invar=None):
+        ntaxa = patterns.shape[0]
+        self.ntaxa = ntaxa
+        self.nedge = 2 * ntaxa - 3
+        self.engine = Engine(patterns.shape[1], model.nstates, model.ncat, ntaxa, model.state_unknown,
+                             3 * (ntaxa - 2), safe=safe, precision=precision, device=device,
+                             max_ops=2 * ntaxa)
+        self.engine.set_model(model)
+        self.engine.set_patterns(freq, invar)
+        self.engine.set_tip_states(patterns)
+        self.edges = np.ascontiguousarray(edges, np.int32)
+        h = ct.c_void_p()
+        _check(lib().iqgpu_tree_create(self.engine.h, self.edges.ctypes.data_as(_I32P),
+                                       _dp(np.ascontiguousarray(lengths, np.float64)), ct.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().iqgpu_tree_destroy(self.h)
+            self.h = None
+        if getattr(self, "engine", None):
+            self.engine.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def compute_likelihood(self, want_pattern_lh=False):
+        out = ct.c_double()
+        plh = np.zeros(self.engine.nptn) if want_pattern_lh else None
+        _check(lib().iqgpu_tree_compute_likelihood(self.h, ct.byref(out), _dp(plh) if plh is not None else None))
+        return (out.value, plh) if want_pattern_lh else out.value
+
+    def optimize_one_branch(self, n1, n2, max_nr_step=100):
+        _check(lib().iqgpu_tree_optimize_one_branch(self.h, n1, n2, max_nr_step))
+
+    def optimize_all_branches(self, iterations=100, tolerance=1e-3, max_nr_step=100):
+        out = ct.c_double()
+        _check(lib().iqgpu_tree_optimize_all_branches(self.h, iterations, tolerance, max_nr_step, ct.byref(out)))
+        return out.value
+
+    def lengths(self):
+        out = np.zeros(self.nedge)
+        _check(lib().iqgpu_tree_get_lengths(self.h, _dp(out)))
+        return out
+
+    def set_lengths(self, lengths):
+        _check(lib().iqgpu_tree_set_lengths(self.h, _dp(np.ascontiguousarray(lengths, np.float64))))
+
+    def set_bounds(self, min_bl, max_bl):
+        _check(lib().iqgpu_tree_set_bounds(self.h, min_bl, max_bl))
+
+    def num_updates(self):
+        out = ct.c_int64()
+        _check(lib().iqgpu_tree_num_updates(self.h, ct.byref(out)))
+        return out.value

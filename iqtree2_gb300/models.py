@@ -1,0 +1,239 @@
+"""Host-side substitution-model inputs for the likelihood engine.
+
+The engine consumes a reversible model through the same three arrays IQ-TREE 2
+reads from ``ModelSubst`` (``getEigenvalues/getEigenvectors/
+getInverseEigenvectors``, model/modelsubst.h:360-372) plus the discrete rate
+categories of ``RateHeterogeneity`` (``getRate/getProp``,
+model/rategamma.h:106,120) and the eigen-space tip vectors built by
+``PhyloTree::computeTipPartialLikelihood`` (tree/phylotreesse.cpp:354-375).
+This module builds those arrays for the models the benchmarks use: GTR (DNA),
+LG (protein) and GY94 (codon), with +G discrete gamma rates.
+
+The eigen-decomposition follows the reversible path of
+``ModelMarkov::decomposeRateMatrix`` (model/modelmarkov.cpp:1450-1560):
+symmetrise Q with sqrt(pi), solve the symmetric eigenproblem (eigenvalues
+ascending), then U = diag(1/sqrt(pi)) V and U^-1 = V^T diag(sqrt(pi)).
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+from scipy import special
+
+# aln->STATE_UNKNOWN per alphabet (alignment/alignment.cpp:738-745).
+STATE_UNKNOWN = {4: 18, 20: 23, 61: 61}
+
+_DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+# Standard genetic code in TCAG order (first, second, third base).
+_CODE_TCAG = "FFLLSSSSYY**CC*WLLLLPPPPHHQQRRRRIIIMTTTTNNKKSSRRVVVVAAAADDEEGGGG"
+_TCAG_OF_ACGT = (2, 1, 3, 0)  # A C G T -> index in TCAG
+
+
+def _codon_aa(n1, n2, n3):
+    t = _TCAG_OF_ACGT
+    return _CODE_TCAG[t[n1] * 16 + t[n2] * 4 + t[n3]]
+
+
+def sense_codons():
+    """Sense codons in IQ-TREE's order (nt1*16+nt2*4+nt3, ACGT), stops removed."""
+    out = []
+    for c in range(64):
+        n1, n2, n3 = c // 16, (c // 4) % 4, c % 4
+        if _codon_aa(n1, n2, n3) != "*":
+            out.append((n1, n2, n3))
+    return out
+
+
+def normalize_rate_matrix(R, pi):
+    """Q = R diag(pi) with zero row sums, scaled to one substitution per unit time.
+
+    Mirrors the ``normalize_matrix`` branch of decomposeRateMatrix
+    (model/modelmarkov.cpp:1504-1512): the scale factor is computed from the
+    off-diagonal row sums before the diagonal is set.
+    """
+    R = np.array(R, dtype=np.float64)
+    pi = np.asarray(pi, dtype=np.float64)
+    Q = R * pi[None, :]
+    np.fill_diagonal(Q, 0.0)
+    row = Q.sum(axis=1)
+    Q -= np.diag(row)
+    Q *= 1.0 / float(row @ pi)
+    return Q
+
+
+def eigen_decompose(Q, pi):
+    """(eval, U, U^-1) of a reversible Q in the reference's storage convention."""
+    pi = np.asarray(pi, dtype=np.float64)
+    s = np.sqrt(pi)
+    S = (s[:, None] * Q) / s[None, :]
+    S = 0.5 * (S + S.T)
+    w, V = np.linalg.eigh(S)
+    U = V / s[:, None]
+    Uinv = V.T * s[None, :]
+    return (np.ascontiguousarray(w), np.ascontiguousarray(U), np.ascontiguousarray(Uinv))
+
+
+def gamma_rates_mean(alpha, ncat):
+    """Discrete-gamma category rates by the mean method (Yang 1994).
+
+    Restates ``RateGamma::computeRatesMean`` (model/rategamma.cpp:157-170):
+    cut points are Gamma(alpha, alpha) quantiles; each rate is ncat times the
+    Gamma(alpha+1) probability mass between consecutive cut points.
+    """
+    if ncat == 1:
+        return np.ones(1), np.ones(1)
+    k = np.arange(1, ncat)
+    cuts = special.gammaincinv(alpha, k / ncat) / alpha
+    mass = special.gammainc(alpha + 1.0, cuts * alpha)
+    rates = np.empty(ncat)
+    rates[0] = mass[0] * ncat
+    rates[-1] = (1.0 - mass[-1]) * ncat
+    rates[1:-1] = (mass[1:] - mass[:-1]) * ncat
+    rates *= ncat / rates.sum()
+    props = np.full(ncat, 1.0 / ncat)
+    return rates, props
+
+
+def tip_vectors(nstates):
+    """Standard-basis tip likelihood per alignment state, rows 0..STATE_UNKNOWN.
+
+    Single states are unit vectors and STATE_UNKNOWN is all ones
+    (ModelSubst::computeTipLikelihood, model/modelsubst.cpp:196-207). DNA
+    ambiguity states 4..17 use the bitmask ``state-3`` (ModelDNA,
+    model/modeldna.cpp:462-474); protein states 20..22 are B, Z and J
+    (ModelProtein, model/modelprotein.cpp:1149-1165).
+    """
+    su = STATE_UNKNOWN.get(nstates, nstates)
+    T = np.zeros((su + 1, nstates))
+    for s in range(su + 1):
+        if s < nstates:
+            T[s, s] = 1.0
+        elif nstates == 4 and s < 18:
+            mask = s - 3
+            for i in range(4):
+                if mask & (1 << i):
+                    T[s, i] = 1.0
+        elif nstates == 20 and s < 23:
+            pair = ((2, 3), (5, 6), (9, 10))[s - 20]
+            T[s, pair[0]] = T[s, pair[1]] = 1.0
+        else:
+            T[s, :] = 1.0
+    return T
+
+
+@dataclass
+class SubstModel:
+    """A reversible model plus +G categories, in the engine's input form."""
+
+    name: str
+    nstates: int
+    Q: np.ndarray
+    pi: np.ndarray
+    rates: np.ndarray
+    props: np.ndarray
+    eval: np.ndarray = field(init=False)
+    evec: np.ndarray = field(init=False)
+    inv_evec: np.ndarray = field(init=False)
+    tip_lh: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        self.eval, self.evec, self.inv_evec = eigen_decompose(self.Q, self.pi)
+        # eigen-space tip vectors: U^-1 . tipvec (ModelSubst::multiplyWithInvEigenvector)
+        self.tip_lh = np.ascontiguousarray(tip_vectors(self.nstates) @ self.inv_evec.T)
+
+    @property
+    def ncat(self):
+        return len(self.rates)
+
+    @property
+    def state_unknown(self):
+        return STATE_UNKNOWN.get(self.nstates, self.nstates)
+
+    def trans_matrix(self, t):
+        """P(t) = U exp(Lambda t) U^-1 (standard basis)."""
+        return (self.evec * np.exp(self.eval * t)[None, :]) @ self.inv_evec
+
+
+def gtr_model(exch, pi, alpha, ncat=4):
+    """GTR from 6 exchangeabilities (AC AG AT CG CT GT) and base frequencies."""
+    R = np.zeros((4, 4))
+    k = 0
+    for i in range(4):
+        for j in range(i + 1, 4):
+            R[i, j] = R[j, i] = exch[k]
+            k += 1
+    pi = np.asarray(pi, dtype=np.float64)
+    rates, props = gamma_rates_mean(alpha, ncat)
+    return SubstModel("GTR+G%d" % ncat, 4, normalize_rate_matrix(R, pi), pi, rates, props)
+
+
+def lg_exchangeabilities():
+    """LG exchangeabilities (symmetric 20x20) and frequencies from ``data/lg.dat``."""
+    vals = []
+    with open(os.path.join(_DATA_DIR, "lg.dat")) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            vals.extend(float(t) for t in line.split())
+    R = np.zeros((20, 20))
+    k = 0
+    for i in range(1, 20):
+        for j in range(i):
+            R[i, j] = R[j, i] = vals[k]
+            k += 1
+    freqs = np.array(vals[190:210])
+    return R, freqs / freqs.sum()
+
+
+def lg_model(pi, alpha, ncat=4):
+    R, _ = lg_exchangeabilities()
+    rates, props = gamma_rates_mean(alpha, ncat)
+    pi = np.asarray(pi, dtype=np.float64)
+    return SubstModel("LG+G%d" % ncat, 20, normalize_rate_matrix(R, pi), pi, rates, props)
+
+
+def f3x4_frequencies(nt_pos_freqs):
+    """F3x4 codon frequencies over the 61 sense codons (alignment/alignment.cpp:4924)."""
+    f = np.asarray(nt_pos_freqs, dtype=np.float64).reshape(3, 4)
+    pi = np.array([f[0, a] * f[1, b] * f[2, c] for (a, b, c) in sense_codons()])
+    return pi / pi.sum()
+
+
+def gy94_rate_matrix(kappa, omega):
+    """GY94 exchangeabilities between the 61 sense codons.
+
+    Non-zero only for codons that differ at one position; transitions carry
+    kappa and non-synonymous changes carry omega, as in
+    ``ModelCodon::computeCodonRateMatrix_1KAPPA`` (model/modelcodon.cpp:845-874).
+    """
+    cod = sense_codons()
+    n = len(cod)
+    R = np.zeros((n, n))
+    for i, a in enumerate(cod):
+        for j, b in enumerate(cod):
+            if i == j:
+                continue
+            diff = [p for p in range(3) if a[p] != b[p]]
+            if len(diff) != 1:
+                continue
+            p = diff[0]
+            x, y = a[p], b[p]
+            transition = {x, y} in ({0, 2}, {1, 3})
+            synonymous = _codon_aa(*a) == _codon_aa(*b)
+            r = 1.0
+            if transition:
+                r *= kappa
+            if not synonymous:
+                r *= omega
+            R[i, j] = r
+    return R
+
+
+def gy94_model(kappa, omega, pi, alpha, ncat=4):
+    R = gy94_rate_matrix(kappa, omega)
+    rates, props = gamma_rates_mean(alpha, ncat)
+    pi = np.asarray(pi, dtype=np.float64)
+    return SubstModel("GY94+G%d" % ncat, 61, normalize_rate_matrix(R, pi), pi, rates, props)

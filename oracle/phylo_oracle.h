@@ -1,0 +1,108 @@
+/*
+ * CPU FP64 oracle for the Felsenstein-pruning likelihood path.
+ *
+ * TEST INFRASTRUCTURE ONLY. Tests, the smoke check and the bench's CPU
+ * baseline legs use this to check and to time against; nothing in the
+ * product links it.
+ *
+ * It restates IQ-TREE 2's scalar kernel path (tree/phylokernelnew.h with a
+ * one-lane vector class, as the reference builds it when INSTRSET < 2,
+ * tree/phylotreesse.cpp:186-191) plus the host drivers around it
+ * (tree/phylotree.cpp, utils/optimization.cpp). Storage follows the
+ * reference: a partial is pattern-major, partial[ptn*B + c*n + x] with
+ * B = n*ncat, in eigen space; scale counts are uint8, one per pattern (NORM)
+ * or per pattern x category (SAFE).
+ *
+ * Parity status: the reference cannot be built here (it needs Eigen3,
+ * Boost and cmake-generated headers), and its test suite holds no golden
+ * vectors for this path, so this oracle is "parity unpinned" against the
+ * reference itself. It is pinned by analytic known-answer tests instead
+ * (closed-form two-taxon JC69, zero-length star trees, P(t) row sums) and by
+ * an independent standard-basis pruning written in numpy.
+ */
+#ifndef IQ_PHYLO_ORACLE_H
+#define IQ_PHYLO_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 2^-256 and its log: tree/phylotree.h:74-80 */
+#define ORC_SCALING_THRESHOLD_EXP 256
+#define ORC_SCALING_THRESHOLD 8.636168555094444625386e-78
+#define ORC_LOG_SCALING_THRESHOLD -177.4456782233459932741
+
+typedef struct {
+    int nptn, nstates, ncat, ntaxa, state_unknown, safe;
+    const double *eval;      /* n */
+    const double *evec;      /* n*n, U[x][i] */
+    const double *inv_evec;  /* n*n, Uinv[i][j] */
+    const double *rates;     /* ncat */
+    const double *props;     /* ncat */
+    const double *tip_lh;    /* (state_unknown+1)*n, eigen-space tip vectors */
+    const double *ptn_freq;  /* nptn */
+    const double *ptn_invar; /* nptn */
+    const uint8_t *tip_states; /* ntaxa*nptn */
+} orc_model;
+
+/* A reference to a directed partial: >= 0 is a slot, < 0 is tip taxon (-1-ref). */
+typedef struct {
+    int dad_slot;
+    int child[2];
+    double len[2];
+} orc_op;
+
+/* Partial update for a traversal list (computePartialLikelihoodGenericSIMD). */
+void orc_compute_partials(const orc_model *m, double *partials, uint8_t *scale,
+                          const orc_op *ops, int nops, int nthreads);
+
+/* Branch lnL (computeLikelihoodBranchGenericSIMD). `a` is the dad_branch
+ * partial, `b` the node_branch partial; either may be a tip. pattern_lh may
+ * be NULL. Returns lnL. */
+double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t *scale,
+                      int a, int b, double len, double *pattern_lh, int nthreads);
+
+/* theta = node o dad plus per-pattern scale offset (computeLikelihoodBufferGenericSIMD). */
+void orc_compute_theta(const orc_model *m, const double *partials, const uint8_t *scale,
+                       int a, int b, double *theta, double *buffer_scale, int nthreads);
+
+/* First and second derivative sums of lnL w.r.t. the branch length
+ * (computeLikelihoodDervGenericSIMD). */
+void orc_derv(const orc_model *m, const double *theta, double len,
+              double *df, double *ddf, int nthreads);
+
+/* lnL from the theta buffer (computeLikelihoodFromBufferGenericSIMD). */
+double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double *buffer_scale,
+                           double len, double *pattern_lh, int nthreads);
+
+/* ---- tree-level drivers (PhyloTree restatement) ---- */
+typedef struct orc_tree orc_tree;
+
+orc_tree *orc_tree_new(const orc_model *m, const int *edges, const double *lengths, int nthreads);
+void orc_tree_free(orc_tree *t);
+double orc_tree_compute_likelihood(orc_tree *t, double *pattern_lh);
+/* optimizeOneBranch on the branch between node1 and node2. Returns 0 or -1 on NR failure. */
+int orc_tree_optimize_one_branch(orc_tree *t, int node1, int node2, int max_nr_step);
+/* optimizeAllBranches; returns the final lnL. status (optional) gets 0 or -1. */
+double orc_tree_optimize_all_branches(orc_tree *t, int iterations, double tolerance,
+                                      int max_nr_step, int *status);
+void orc_tree_get_lengths(const orc_tree *t, double *lengths);
+void orc_tree_set_lengths(orc_tree *t, const double *lengths);
+void orc_tree_set_bounds(orc_tree *t, double min_bl, double max_bl);
+/* Number of partial updates (ops) executed so far, for throughput accounting. */
+long long orc_tree_num_updates(const orc_tree *t);
+/* Copy the partial of directed branch node->nbr (subtree at nbr seen from node)
+ * and its scale counts, computing it if needed. Returns 0, -1 if nbr is a leaf. */
+int orc_tree_get_partial(orc_tree *t, int node, int nbr, double *partial, uint8_t *scale);
+
+/* Derivative sums (df, ddf of lnL, not negated) on branch node1-node2 at length len;
+ * sets that branch's length and rebuilds theta. Returns 0 or -1 if not a branch. */
+int orc_tree_derv(orc_tree *t, int node1, int node2, double len, double *df, double *ddf);
+/* lnL on the branch node-dad (computeLikelihoodBranch with dad_branch = dad->node). */
+double orc_tree_lnl_branch(orc_tree *t, int node, int dad);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

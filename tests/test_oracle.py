@@ -1,0 +1,81 @@
+"""The CPU oracle against closed forms and an independent standard-basis pruning."""
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, jc_model, load_golden, rel
+import stdbasis
+
+
+@pytest.mark.parametrize("tag,alpha,ncat", [("g1", 1.0, 1), ("g4", 0.5, 4)])
+@pytest.mark.parametrize("safe", [False, True])
+def test_jc_pair_closed_form(oracle_mod, tag, alpha, ncat, safe):
+    d = np.load(f"{GOLDEN}/kat_jc.npz")
+    m = jc_model(ncat, alpha)
+    np.testing.assert_allclose(m.rates, d[f"rates_{tag}"], rtol=1e-12)
+    t = oracle_mod.OracleTree(m, d["patterns"], d["freq"], d["edges"], d["lengths"], safe=safe)
+    assert rel(t.compute_likelihood(), float(d[f"lnl_{tag}"])) < 1e-12
+
+
+def test_jc_ml_distance(oracle_mod):
+    d = np.load(f"{GOLDEN}/kat_jc.npz")
+    m = jc_model(1, 1.0)
+    t = oracle_mod.OracleTree(m, d["patterns"], d["freq"], d["edges"], d["lengths"])
+    t.optimize_all_branches(tolerance=1e-9)
+    L = t.lengths()
+    assert abs((L[0] + L[1]) - float(d["ml_distance_g1"])) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["dna16", "prot12", "codon8"])
+@pytest.mark.parametrize("safe", [False, True])
+def test_golden_standard_basis(oracle_mod, name, safe):
+    g = load_golden(name)
+    t = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe)
+    lnl, plh = t.compute_likelihood(want_pattern_lh=True)
+    assert rel(lnl, g.lnl_std) < 1e-12
+    np.testing.assert_allclose(plh, g.pattern_lnl_std, rtol=1e-11, atol=1e-11)
+
+
+def test_stationarity_rows_sum_to_one():
+    g = load_golden("prot12")
+    m = g.model
+    for t in (0.0, 0.01, 0.3, 5.0):
+        P = (m.evec * np.exp(m.eval * t)[None, :]) @ m.inv_evec
+        np.testing.assert_allclose(P.sum(axis=1), 1.0, atol=1e-12)
+
+
+def test_zero_length_star_tree(oracle_mod):
+    """All branches at length 0: every taxon shares one state, so
+    lnL = sum_ptn freq * log(pi[state])."""
+    m = jc_model(4, 0.5)
+    pi = np.array([0.1, 0.2, 0.3, 0.4])
+    from iqtree2_gb300 import models
+    m = models.gtr_model(np.array([1.0, 2.0, 0.5, 1.5, 3.0, 1.0]), pi, 0.5)
+    ntaxa = 5
+    from iqtree2_gb300 import simulate
+    edges, _ = simulate.yule_tree(ntaxa, 0.1, np.random.default_rng(3))
+    pats = np.repeat(np.arange(4, dtype=np.uint8)[None, :], ntaxa, axis=0)
+    freq = np.array([3.0, 5.0, 7.0, 11.0])
+    t = oracle_mod.OracleTree(m, pats, freq, edges, np.zeros(len(edges)))
+    assert rel(t.compute_likelihood(), float(np.sum(freq * np.log(pi)))) < 1e-12
+
+
+def test_scaling_triggers_and_matches_standard_basis(oracle_mod):
+    """A 150-taxon protein tree with long branches underflows 2^-256: scale
+    counts must appear and the scaled lnL must still equal the standard-basis
+    value."""
+    from iqtree2_gb300 import simulate
+    ds = simulate.protein_lg_dataset(150, 40, 11, mean_bl=0.5)
+    for safe in (False, True):
+        t = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe)
+        lnl = t.compute_likelihood()
+        ref, _ = stdbasis.tree_lnl(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
+        assert rel(lnl, ref) < 1e-11
+    # the root-adjacent partial carries a non-zero scale count somewhere
+    t = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths)
+    adj = {}
+    for (u, v) in ds.edges:
+        adj.setdefault(int(u), []).append(int(v))
+        adj.setdefault(int(v), []).append(int(u))
+    x = adj[0][0]
+    _, s = t.partial(0, x)
+    assert s.max() >= 1
