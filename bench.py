@@ -53,25 +53,37 @@ def topology_ops(ds):
     return topo, ops, topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
 
 
-def algorithmic_cost(ops, ntaxa, n, C, nptn, elem=8):
-    """Bytes and flops one traversal+lnL launch must move/execute, per pattern x all ops."""
-    B = n * C
+def algorithmic_cost(ops, ntaxa, n, C, nptn, mixed=False):
+    """Bytes and flops one traversal + root-lnL launch must move/execute.
+
+    FP64 path: 8-byte eigen-space partials, uint8 scale counts, eigen-space
+    flops (6n^2+n)C per internal-internal update. Mixed path: 4-byte
+    standard-basis partials padded to npad states, int32 exponents, standard
+    flops (4n^2+n)C per internal-internal update.
+    """
+    npad = (n + 3) // 4 * 4
+    if mixed:
+        blk, sc = C * npad * 4, 4
+        f_ii, f_ti, f_tt = (4 * n * n + n) * C, (2 * n * n + n) * C, n * C
+    else:
+        blk, sc = C * n * 8, 1
+        f_ii, f_ti, f_tt = (6 * n * n + n) * C, (4 * n * n + n) * C, (2 * n * n + n) * C
     bytes_per_ptn = 0.0
     flops_per_ptn = 0.0
     for (_, c0, c1, _, _) in ops:
         tips = (c0 < 0) + (c1 < 0)
         if tips == 2:
-            bytes_per_ptn += 2 + B * elem + 1
-            flops_per_ptn += (2 * n * n + n) * C
+            bytes_per_ptn += 2 + blk + sc
+            flops_per_ptn += f_tt
         elif tips == 1:
-            bytes_per_ptn += 1 + B * elem + 1 + B * elem + 1
-            flops_per_ptn += (4 * n * n + n) * C
+            bytes_per_ptn += 1 + blk + sc + blk + sc
+            flops_per_ptn += f_ti
         else:
-            bytes_per_ptn += 2 * B * elem + 2 + B * elem + 1
-            flops_per_ptn += (6 * n * n + n) * C
+            bytes_per_ptn += 2 * (blk + sc) + blk + sc
+            flops_per_ptn += f_ii
     # root lnL: read one partial + one tip state + freq, write pattern lnL
-    bytes_per_ptn += B * elem + 1 + 8 + 8
-    flops_per_ptn += 3 * B
+    bytes_per_ptn += blk + sc + 1 + 8 + 8
+    flops_per_ptn += 3 * n * C
     return bytes_per_ptn * nptn, flops_per_ptn * nptn
 
 
@@ -135,7 +147,7 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(ds, ops, a, b, length, sample_ptn=2000, min_seconds=10.0):
+def cpu_baseline(ds, ops, a, b, length, sample_ptn=8000, min_seconds=10.0):
     """The CPU restatement of the reference kernels (oracle) on a pattern sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -151,7 +163,7 @@ def cpu_baseline(ds, ops, a, b, length, sample_ptn=2000, min_seconds=10.0):
         t.compute_likelihood()
         reps += 1
         el = time.perf_counter() - t0
-        if el >= min_seconds or reps >= 200:
+        if el >= min_seconds or reps >= 5000:
             break
     upd = t.num_updates() - upd0
     return {"value": upd / el, "unit": METRIC, "cores": cores, "kind": "port",
@@ -182,6 +194,48 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def measure_path(eng, ops_arr, a, b, length, steps, warmup, stream, local, dist):
+    """Time `steps` full evaluations on device-resident inputs (CUDA events on the
+    engine's stream) and the dominant kernel per launch."""
+    import torch
+    for _ in range(warmup):
+        lnl = eng.compute_likelihood(ops_arr, a, b, length)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    eng.set_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        lnl = eng.compute_likelihood(ops_arr, a, b, length)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = eng.timing()
+    eng.set_timing(False)
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    return dict(lnl=lnl, elapsed_ms=elapsed_ms, kern_avg_s=kern_ms / max(kern_n, 1) / 1e3, clocks=clk)
+
+
+def make_engine(ds, topo, precision, local, stream):
+    from iqtree2_gb300 import engine
+    m = ds.model
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                        precision=precision, device=local, max_ops=topo.nslots)
+    eng.set_stream(stream.cuda_stream)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    return eng
+
+
 def run_ours(args):
     import torch
     from iqtree2_gb300 import engine
@@ -198,41 +252,24 @@ def run_ours(args):
     ds = dataset()
     topo, ops, a, b, length = topology_ops(ds)
     m = ds.model
-    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
-                        precision=engine.F64, device=local, max_ops=topo.nslots)
     stream = torch.cuda.Stream()
-    eng.set_stream(stream.cuda_stream)
-    eng.set_model(m)
-    eng.set_patterns(ds.freq)
-    eng.set_tip_states(ds.patterns)
     ops_arr = engine.Engine.ops_array(ops)
     updates_per_step = len(ops) * ds.nptn
-    alg_bytes, alg_flops = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn)
+    peaks, peak_src = measured_peaks()
 
-    for _ in range(args.warmup):
-        lnl = eng.compute_likelihood(ops_arr, a, b, length)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    eng.set_timing(True)
-    clocks = ClockSampler(local)
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        lnl = eng.compute_likelihood(ops_arr, a, b, length)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    elapsed_ms = ev0.elapsed_time(ev1)
-    kern_ms, kern_n = eng.timing()
-    eng.set_timing(False)
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    value = updates_per_step * args.steps * world / (elapsed_ms / 1e3)
+    # FP64 drop-in path, reported beside the headline
+    eng64 = make_engine(ds, topo, engine.F64, local, stream)
+    r64 = measure_path(eng64, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
+    eng64.close()
+    b64, f64 = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=False)
+
+    # headline: mixed-precision path, pattern tile picked by the autotuner
+    from iqtree2_gb300 import autotune
+    eng = make_engine(ds, topo, engine.F32, local, stream)
+    tile, tile_ms = autotune.tune(eng, ops_arr, a, b, length)
+    r = measure_path(eng, ops_arr, a, b, length, args.steps, args.warmup, stream, local, dist)
+    value = updates_per_step * args.steps * world / (r["elapsed_ms"] / 1e3)
+    bmx, fmx = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=True)
 
     # end to end through the C ABI from host buffers: inputs copied each step, lnL read back
     e2e_steps = max(2, min(args.steps, 10))
@@ -245,34 +282,39 @@ def run_ours(args):
         lnl_e2e = eng.compute_likelihood(ops_arr, a, b, length)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     h2d = ds.patterns.nbytes + ds.freq.nbytes + sum(x.nbytes for x in (m.eval, m.evec, m.inv_evec, m.rates,
-                                                                        m.props, m.tip_lh)) + ops_arr.nbytes
-    assert lnl_e2e == lnl
-
-    peaks, peak_src = measured_peaks()
-    kern_avg_s = kern_ms / max(kern_n, 1) / 1e3
-    achieved_gbs = alg_bytes / kern_avg_s / 1e9
-    fp64_tflops = alg_flops / kern_avg_s / 1e12
+                                                                        m.props, m.tip_lh, m.pi)) + ops_arr.nbytes
+    assert lnl_e2e == r["lnl"]
     if rank != 0:
         return
+    achieved = bmx / r["kern_avg_s"] / 1e9
+    a64 = b64 / r64["kern_avg_s"] / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(WORKLOAD, path="FP64 drop-in (eigen-space partials, 2^-256 scaling)",
-                       nptn=ds.nptn, parallelism=f"replicas x{world}", l2="inputs larger than L2 "
-                       "(98 partials x 32 MB per step)", lnl=lnl),
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
-                     "kernel": "k_traverse_f64<20,NORM,LNL>",
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "fp64": {"achieved_tflops": fp64_tflops, "peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
-                              "frac": fp64_tflops / FP64_PEAK_TFLOPS_MEASURED,
-                              "flops_per_launch": alg_flops, "form": "eigen-space (6n^2+n)C"}},
+        "warmup": args.warmup, "ms_per_step": r["elapsed_ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, path="mixed: FP32 standard-basis partials, per-pattern 2^k exponents, "
+                       "FP64 exp/log/sums", nptn=ds.nptn, parallelism=f"replicas x{world}",
+                       tile=tile, tile_ms={str(k): v for k, v in tile_ms.items()},
+                       l2="inputs larger than L2 (98 partials x 14 MB per step)"),
+        "full_lnl_evals_per_s": 1e3 * args.steps / r["elapsed_ms"],
+        "lnl": {"mixed": r["lnl"], "fp64": r64["lnl"], "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"])},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
+                     "kernel": "k_traverse_mixed<5,LNL>", "algorithmic_bytes_per_launch": bmx,
+                     "fp32_tflops": fmx / r["kern_avg_s"] / 1e12, "flops_per_launch": fmx,
+                     "kernel_ms": r["kern_avg_s"] * 1e3},
+        "fp64_path": {"value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
+                      "ms_per_step": r64["elapsed_ms"] / max(3, args.steps // 4),
+                      "kernel": "k_traverse_f64<20,NORM,LNL>",
+                      "hbm_frac": a64 / peaks["hbm_gbs"],
+                      "fp64_tflops": f64 / r64["kern_avg_s"] / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
+                      "fp64_frac": f64 / r64["kern_avg_s"] / 1e12 / FP64_PEAK_TFLOPS_MEASURED},
         "e2e": {"value": updates_per_step / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": 8 * 4},
-        "clocks": clk,
+        "clocks": r["clocks"],
         "gpu_launches": 2 * args.steps,
     }
+    line["speedup_vs_fp64_path"] = value / line["fp64_path"]["value"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(ds, ops, a, b, length)
     print(json.dumps(line))

@@ -71,7 +71,14 @@ typedef struct {
     int32_t precision;     /* IQGPU_F64 ... */
     int32_t device;        /* CUDA device ordinal */
     int32_t max_ops;       /* largest traversal the engine must accept (>= ntaxa) */
+    int32_t flags;         /* IQGPU_FLAG_* */
 } iqgpu_config;
+
+/* Reproduce the reference's derivative sum bit for bit: its dotProductTriple
+ * (tree/phylokernelnew.h:699-718), called with N = nstates*ncat, adds the last
+ * block entry twice when nstates is odd and N is even (codon +G4). Off by
+ * default: the engine then returns the exact derivative of lnL. */
+#define IQGPU_FLAG_REF_TRIPLE_TAIL 1
 
 /* One TraversalInfo entry (tree/phylotree.h:320-333): compute the partial of
  * dad_slot from two children with their branch lengths. */
@@ -102,6 +109,10 @@ int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out);
  * on the caller's side (ModelFactory clears partials, model/modelfactory.cpp:1124-1127). */
 int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
                     const double *rates, const double *props);
+/* State frequencies pi[n] (ModelSubst::getStateFrequency, model/modelsubst.h).
+ * The mixed-precision paths keep standard-basis partials and weight the root
+ * by pi; the FP64 eigen-space path ignores it (pi is folded into U^-1). */
+int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq);
 /* Eigen-space tip vectors, (state_unknown+1) x nstates
  * (computeTipPartialLikelihood, tree/phylotreesse.cpp:354-375). */
 int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh);
@@ -147,6 +158,10 @@ int iqgpu_set_stream(iqgpu_engine *e, void *cuda_stream);
  * traversal launch (the dominant kernel): enable, read (total ms and number
  * of timed launches since the last reset), reset. */
 int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
+/* Pattern tile (patterns per CTA, 32/64/128) of the mixed-precision traversal
+ * kernel; 0 restores the default. Chosen by the autotuner in
+ * iqtree2_gb300/autotune.py; results do not depend on it. */
+int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
 /* ---- tree-level drivers (PhyloTree restatement) ------------------------ */

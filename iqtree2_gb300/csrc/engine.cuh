@@ -94,6 +94,18 @@ struct iqgpu_engine {
     double *d_red_out, *h_red_out;
     bool theta_valid;
     int32_t theta_a, theta_b;
+    // mixed-precision (FP32 standard-basis) state
+    int npad;                 // n rounded up to 4
+    long long bp;             // floats per pattern block = C * npad
+    float *d_part32;          // [nslots][Ppad/8][C][npad/4][8][4]
+    int32_t *d_exp;           // [nslots][Ppad] power-of-two exponent per pattern
+    float *d_theta32;         // [B][Ppad] eigen-space theta
+    double *d_pi, *d_tipstd;  // state frequencies, standard-basis tip vectors
+    float *d_opmats32;
+    long long op_stride32;    // floats per op
+    double h_evec[iqg::kMaxStates * iqg::kMaxStates];
+    bool have_pi, tipstd_ready;
+    int tile;                 // patterns per CTA of the mixed traversal (0 = default)
     // stream ownership and kernel timing
     cudaStream_t own_st;
     cudaEvent_t ev_t0, ev_t1;
@@ -111,4 +123,16 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops);
 int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_f64(iqgpu_engine *e, double len);
 int launch_from_buffer_f64(iqgpu_engine *e, double len);
+
+// mixed-precision launchers (kernels_mixed.cu); op index nops holds the
+// transition matrices of the evaluated branch when epi != EPI_NONE
+int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch);
+int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
+int launch_derv_mixed(iqgpu_engine *e, double len);
+int launch_from_buffer_mixed(iqgpu_engine *e, double len);
+
+// element offset of (pattern p, category c, state y) in a mixed-precision slot
+__host__ __device__ inline long long mixed_index(long long p, int c, int y, int npad, int C) {
+    return (p >> 3) * (8LL * C * npad) + (long long)(c * (npad >> 2) + (y >> 2)) * 32 + (p & 7) * 4 + (y & 3);
+}
 }  // namespace iqg

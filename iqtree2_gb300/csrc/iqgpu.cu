@@ -37,25 +37,39 @@ static int check_config(const iqgpu_config *c) {
                   "nstates<=state_unknown<=255, nslots>=1, max_ops>=1)");
         return IQGPU_ERR_ARG;
     }
-    if (c->precision != IQGPU_F64) {
-        set_error("precision not supported by this build of the engine");
+    if (c->precision != IQGPU_F64 && c->precision != IQGPU_F32) {
+        set_error("precision not supported by this build of the engine (F64, F32)");
         return IQGPU_ERR_ARG;
     }
     return IQGPU_OK;
 }
 
+static bool is_mixed(const iqgpu_config *c) { return c->precision != IQGPU_F64; }
+
 static Sizes sizes(const iqgpu_config *c) {
     Sizes s;
     const long long n = c->nstates, C = c->ncat, B = n * C, S = c->state_unknown;
+    const long long npad = round_up(n, 4);
     s.Ppad = round_up(c->nptn, kTPB);
-    s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
-    s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
     s.states = (long long)c->ntaxa * s.Ppad;
-    s.op_stride = round_up(2 * C * n * n + 2 * (S + 1) * B, 4);
-    s.ops = (long long)c->max_ops * (long long)sizeof(OpDev);
-    s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
-    s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
-    s.red = (s.Ppad / kTPB) * kRedSlots * (long long)sizeof(double) + 64;
+    s.ops = (long long)(c->max_ops + 1) * (long long)sizeof(OpDev);
+    if (is_mixed(c)) {
+        // FP32 partials + int32 exponents; op blocks hold FP32 P(t) and leaf tables,
+        // plus one block for the evaluated branch and the FP32 copy of U^-1
+        s.part = (long long)c->nslots * s.Ppad * (C * npad * 4 + 4);
+        s.scale = 0;
+        s.op_stride = round_up(2 * C * n * npad + 2 * (S + 1) * C * npad, 4);
+        s.opmats = ((long long)(c->max_ops + 1) * s.op_stride + n * npad) * 4;
+        s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double);
+    } else {
+        s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
+        s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
+        s.op_stride = round_up(2 * C * n * n + 2 * (S + 1) * B, 4);
+        s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
+        s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
+    }
+    // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
+    s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
     s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + 2 * s.Ppad * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8;
     return s;
@@ -88,7 +102,8 @@ static void free_engine(iqgpu_engine *e) {
     cudaSetDevice(e->dev);
     void *dev_ptrs[] = {e->d_eval, e->d_evec, e->d_inv, e->d_rates, e->d_props, e->d_tip, e->d_freq,
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
-                        e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out};
+                        e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
+                        e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32};
     for (void *p : dev_ptrs)
         if (p) cudaFree(p);
     if (e->h_ops) cudaFreeHost(e->h_ops);
@@ -163,14 +178,30 @@ int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
     CKE(cudaMalloc(&e->d_freq, e->Ppad * 8));
     CKE(cudaMalloc(&e->d_invar, e->Ppad * 8));
     CKE(cudaMalloc(&e->d_states, s.states));
-    CKE(cudaMalloc(&e->d_part, s.part));
-    CKE(cudaMalloc(&e->d_scale, s.scale));
     CKE(cudaMalloc(&e->d_ops, s.ops));
-    CKE(cudaMalloc(&e->d_opmats, s.opmats));
-    CKE(cudaMalloc(&e->d_theta, B * e->Ppad * 8));
+    e->npad = (int)round_up(n, 4);
+    e->bp = C * e->npad;
+    if (is_mixed(cfg)) {
+        e->op_stride32 = s.op_stride;
+        CKE(cudaMalloc(&e->d_part32, (long long)cfg->nslots * e->Ppad * e->bp * 4));
+        CKE(cudaMalloc(&e->d_exp, (long long)cfg->nslots * e->Ppad * 4));
+        CKE(cudaMalloc(&e->d_opmats32, s.opmats));
+        CKE(cudaMalloc(&e->d_theta32, B * e->Ppad * 4));
+        CKE(cudaMalloc(&e->d_pi, n * 8));
+        // padding states of every slot stay zero: finite inputs for the float4 matvecs
+        CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
+        CKE(cudaMemsetAsync(e->d_exp, 0, (long long)cfg->nslots * e->Ppad * 4, e->st));
+        CKE(cudaMemsetAsync(e->d_opmats32, 0, s.opmats, e->st));
+    } else {
+        CKE(cudaMalloc(&e->d_part, s.part));
+        CKE(cudaMalloc(&e->d_scale, s.scale));
+        CKE(cudaMalloc(&e->d_opmats, s.opmats));
+        CKE(cudaMemsetAsync(e->d_scale, 0, s.scale, e->st));
+    }
+    CKE(cudaMalloc(&e->d_theta, is_mixed(cfg) ? 8 : B * e->Ppad * 8));
     CKE(cudaMalloc(&e->d_bscale, e->Ppad * 8));
     CKE(cudaMalloc(&e->d_plh, e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_red_partials, (long long)e->nblk * kRedSlots * 8));
+    CKE(cudaMalloc(&e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
     CKE(cudaMalloc(&e->d_ticket, 64));
     CKE(cudaMalloc(&e->d_red_out, kRedSlots * 8));
     CKE(cudaMallocHost(&e->h_ops, s.ops));
@@ -178,7 +209,6 @@ int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
     CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
     CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
     CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
-    CKE(cudaMemsetAsync(e->d_scale, 0, s.scale, e->st));
     CKE(cudaMemsetAsync(e->d_states, (int)S, s.states, e->st));
     CKE(cudaStreamSynchronize(e->st));
 #undef CKE
@@ -214,8 +244,27 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     std::memcpy(e->h_eval, eval, n * 8);
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
+    std::memcpy(e->h_evec, evec, n * n * 8);
+    if (is_mixed(&e->cfg)) {
+        // FP32 copy of U^-1, rows padded to npad, after the op matrix blocks
+        std::vector<float> inv32((size_t)n * e->npad, 0.f);
+        for (size_t i = 0; i < n; i++)
+            for (size_t j = 0; j < n; j++) inv32[i * e->npad + j] = (float)inv_evec[i * n + j];
+        float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
+        CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
+    }
     e->have_model = true;
     e->theta_valid = false;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq) {
+    if (!e || !state_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    if (!is_mixed(&e->cfg)) return IQGPU_OK;  // the eigen-space FP64 path folds pi into U^-1
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy(e->d_pi, state_freq, (size_t)e->n * 8, cudaMemcpyHostToDevice));
+    e->have_pi = true;
     return IQGPU_OK;
 }
 
@@ -260,6 +309,10 @@ static int ready(iqgpu_engine *e) {
         set_error("model, tip partials, patterns and tip states must be set first");
         return IQGPU_ERR_STATE;
     }
+    if (is_mixed(&e->cfg) && !e->have_pi) {
+        set_error("the mixed-precision path needs the state frequencies (iqgpu_set_state_freq)");
+        return IQGPU_ERR_STATE;
+    }
     return IQGPU_OK;
 }
 
@@ -269,12 +322,17 @@ static int check_ref(iqgpu_engine *e, int32_t r) {
 }
 
 // Validate a traversal, stage it in pinned memory and send it to the device.
-static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
+// The mixed path evaluates a branch with FP32 transition matrices, so a
+// branch evaluation appends one entry (index nops) whose child 0 is the far
+// end b of the branch with the branch length.
+static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch = false, int32_t b = 0,
+                      double len = 0.0) {
     if (nops < 0 || nops > e->cfg.max_ops || (nops > 0 && !ops)) {
         set_error("traversal length out of range");
         return IQGPU_ERR_ARG;
     }
-    if (nops == 0) return IQGPU_OK;
+    const bool extra = branch && is_mixed(&e->cfg);
+    if (nops == 0 && !extra) return IQGPU_OK;
     // the previous upload must have left the staging buffer
     CK(cudaStreamSynchronize(e->st));
     for (int k = 0; k < nops; k++) {
@@ -294,8 +352,19 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
         d.mat_off = (long long)k * e->op_stride;
         d.pad2 = 0;
     }
-    CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * nops, cudaMemcpyHostToDevice, e->st));
-    return launch_partial_info_f64(e, nops);
+    int total = nops;
+    if (extra) {
+        OpDev &d = e->h_ops[nops];
+        d.dad_slot = -1;
+        d.child[0] = d.child[1] = b;
+        d.pad = 0;
+        d.len[0] = d.len[1] = len;
+        d.mat_off = (long long)nops * e->op_stride;
+        d.pad2 = 0;
+        total++;
+    }
+    CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
+    return is_mixed(&e->cfg) ? launch_partial_info_mixed(e, total) : launch_partial_info_f64(e, total);
 }
 
 // Fold the last timed traversal into the running total.
@@ -316,7 +385,9 @@ static int traverse(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, do
         if ((rc = settle_timing(e))) return rc;
         CK(cudaEventRecord(e->ev_t0, e->st));
     }
-    if ((rc = launch_traverse_f64(e, nops, epi, a, b, len))) return rc;
+    rc = is_mixed(&e->cfg) ? launch_traverse_mixed(e, nops, epi, a, b, len)
+                           : launch_traverse_f64(e, nops, epi, a, b, len);
+    if (rc) return rc;
     if (e->timing) {
         CK(cudaEventRecord(e->ev_t1, e->st));
         e->timing_pending = true;
@@ -349,7 +420,7 @@ static int lnl_common(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_
         return IQGPU_ERR_ARG;
     }
     CK(cudaSetDevice(e->dev));
-    if ((rc = upload_ops(e, ops, nops))) return rc;
+    if ((rc = upload_ops(e, ops, nops, true, b, len))) return rc;
     if ((rc = traverse(e, nops, EPI_LNL, a, b, len))) return rc;
     if ((rc = fetch_result(e))) return rc;
     const double *r = e->h_red_out;
@@ -388,12 +459,13 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
         e->theta_a = a;
         e->theta_b = b;
     }
-    if ((rc = launch_derv_f64(e, len))) return rc;
+    rc = is_mixed(&e->cfg) ? launch_derv_mixed(e, len) : launch_derv_f64(e, len);
+    if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;
     *df = e->h_red_out[0];
     *ddf = e->h_red_out[1];
     if (!std::isfinite(*df)) {
-        if (!e->cfg.safe) {
+        if (!e->cfg.safe && !is_mixed(&e->cfg)) {
             set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this");
             return IQGPU_ERR_NONFINITE;
         }
@@ -408,10 +480,11 @@ int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
     if (!lnl) { set_error("null output"); return IQGPU_ERR_ARG; }
     if (!e->theta_valid) { set_error("no theta buffer: call iqgpu_likelihood_derv first"); return IQGPU_ERR_STATE; }
     CK(cudaSetDevice(e->dev));
-    if ((rc = launch_from_buffer_f64(e, len))) return rc;
+    rc = is_mixed(&e->cfg) ? launch_from_buffer_mixed(e, len) : launch_from_buffer_f64(e, len);
+    if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;
     const double *r = e->h_red_out;
-    if (!std::isfinite(r[0]) && !e->cfg.safe) {
+    if (!std::isfinite(r[0]) && !e->cfg.safe && !is_mixed(&e->cfg)) {
         set_error("Numerical underflow (lh-from-buffer); the SAFE kernel avoids this");
         return IQGPU_ERR_NONFINITE;
     }
@@ -432,6 +505,19 @@ int iqgpu_get_partial(iqgpu_engine *e, int32_t slot, double *partial, uint8_t *s
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
     const long long B = e->B, P = e->P, Pp = e->Ppad;
+    if (is_mixed(&e->cfg)) {
+        // standard-basis values as stored (true value = stored * 2^exponent)
+        if (partial) {
+            std::vector<float> tmp((size_t)(Pp * e->bp));
+            CK(cudaMemcpy(tmp.data(), e->d_part32 + (size_t)slot * Pp * e->bp, tmp.size() * 4, cudaMemcpyDeviceToHost));
+            for (long long p = 0; p < P; p++)
+                for (int c = 0; c < e->C; c++)
+                    for (int x = 0; x < e->n; x++)
+                        partial[p * B + c * e->n + x] = tmp[(size_t)mixed_index(p, c, x, e->npad, e->C)];
+        }
+        if (scale) std::memset(scale, 0, (size_t)P);
+        return IQGPU_OK;
+    }
     if (partial) {
         std::vector<double> tmp((size_t)(B * Pp));
         CK(cudaMemcpy(tmp.data(), e->d_part + (size_t)slot * B * Pp, (size_t)(B * Pp) * 8, cudaMemcpyDeviceToHost));
@@ -449,11 +535,15 @@ int iqgpu_get_partial(iqgpu_engine *e, int32_t slot, double *partial, uint8_t *s
 }
 
 int iqgpu_get_exponent(iqgpu_engine *e, int32_t slot, int32_t *exponent) {
-    (void)slot;
-    (void)exponent;
-    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
-    set_error("the FP64 path keeps uint8 scale counts, not exponents");
-    return IQGPU_ERR_STATE;
+    if (!e || !exponent || slot < 0 || slot >= e->cfg.nslots) { set_error("bad argument"); return IQGPU_ERR_ARG; }
+    if (!is_mixed(&e->cfg)) {
+        set_error("the FP64 path keeps uint8 scale counts, not exponents");
+        return IQGPU_ERR_STATE;
+    }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    CK(cudaMemcpy(exponent, e->d_exp + (size_t)slot * e->Ppad, (size_t)e->P * 4, cudaMemcpyDeviceToHost));
+    return IQGPU_OK;
 }
 
 int iqgpu_sync(iqgpu_engine *e) {
@@ -482,6 +572,16 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable) {
     e->timing = enable != 0;
     e->timing_ms = 0.0;
     e->timing_launches = 0;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
+    if (!e || !(patterns_per_cta == 0 || patterns_per_cta == 32 || patterns_per_cta == 64 ||
+                patterns_per_cta == 128)) {
+        set_error("tile must be 0, 32, 64 or 128 patterns");
+        return IQGPU_ERR_ARG;
+    }
+    e->tile = patterns_per_cta;
     return IQGPU_OK;
 }
 

@@ -365,6 +365,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
 // ---------------------------------------------------------------------------
 struct BufParams {
     int n, ncat, nptn;
+    int tail_dup;  // IQGPU_FLAG_REF_TRIPLE_TAIL with odd n and even n*ncat
     long long ldp;
     const double *theta, *buffer_scale, *freq, *invar;
     const double *eval, *rates, *props;
@@ -401,6 +402,10 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
         if (k < B) {
             const double t0 = th[(long long)k * P.ldp];
             a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
+        }
+        if (P.tail_dup) {  // the reference's odd-state tail, added a second time
+            const double t0 = th[(long long)(B - 1) * P.ldp];
+            a0 = fma(v0[B - 1], t0, a0); a1 = fma(v1[B - 1], t0, a1); a2 = fma(v2[B - 1], t0, a2);
         }
         double lh = a0 + b0, d1 = a1 + b1, d2 = a2 + b2;
         lh = fabs(lh) + P.invar[p];
@@ -537,6 +542,7 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
     P.n = e->n;
     P.ncat = e->C;
     P.nptn = (int)e->P;
+    P.tail_dup = (e->cfg.flags & IQGPU_FLAG_REF_TRIPLE_TAIL) && (e->n & 1) && ((e->n * e->C) % 2 == 0);
     P.ldp = e->Ppad;
     P.theta = e->d_theta;
     P.buffer_scale = e->d_bscale;

@@ -1,0 +1,213 @@
+// Mixed-precision path, part 1: per-op transition matrices and leaf tables,
+// derivative and from-buffer kernels, parameter plumbing. The traversal
+// kernel is in traverse_mixed.cu.
+//
+// Standard basis keeps every partial non-negative (no eigen-space
+// cancellation in FP32): dad[c][x] = (P_L,c L_c)[x] * (P_R,c R_c)[x]; a
+// pattern is rescaled by an exact power of two when its largest entry falls
+// below 2^-40 and the exponent is carried per pattern. FP64 stays in
+// exp(lambda r t), the products forming P(t), the per-pattern log, the
+// weighted lnL sum, the exponent correction and the derivative sums.
+#include <cuda_runtime.h>
+
+#include "mixed.cuh"
+
+namespace iqg {
+
+// ---------------------------------------------------------------------------
+// per-op transition matrices and leaf tables (FP64 exp and products, stored FP32)
+// (computePartialInfo, tree/phylokernelnew.h:895-1110, in the standard basis)
+// ---------------------------------------------------------------------------
+__global__ void k_partial_info_mixed(const OpDev *__restrict__ ops, float *__restrict__ opmats, long long op_stride,
+                                     const double *__restrict__ evec, const double *__restrict__ inv,
+                                     const double *__restrict__ eval, const double *__restrict__ rates,
+                                     const double *__restrict__ tip_lh, int n, int npad, int C, int S) {
+    const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
+    const OpDev op = ops[k];
+    const double len = op.len[ch];
+    __shared__ double sexp[kMaxCat * kMaxStates];
+    for (int t = threadIdx.x; t < C * n; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        sexp[t] = exp(eval[i] * (rates[c] * len));
+    }
+    __syncthreads();
+    float *base = opmats + (long long)k * op_stride;
+    const long long PM = (long long)C * n * npad;
+    float *Pm = base + ch * PM;
+    const long long TB = (long long)(S + 1) * C * npad;
+    float *tab = base + 2 * PM + ch * TB;
+    const long long nP = PM, nT = (op.child[ch] < 0) ? TB : 0;
+    const long long total = nP + nT;
+    for (long long t = (long long)z * blockDim.x + threadIdx.x; t < total; t += (long long)Z * blockDim.x) {
+        if (t < nP) {
+            // P_c[x][y] = sum_i U[x][i] exp(lambda_i r_c t) U^-1[i][y]
+            const int c = (int)(t / ((long long)n * npad)), r = (int)(t % ((long long)n * npad));
+            const int x = r / npad, y = r % npad;
+            double acc = 0.0;
+            if (y < n)
+                for (int i = 0; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], inv[i * n + y], acc);
+            Pm[t] = (float)acc;
+        } else {
+            // leaf table[s][c][x] = (P_c . tipvec_s)[x] = sum_i U[x][i] exp(.) tip_lh[s][i]
+            const long long u = t - nP;
+            const int s = (int)(u / ((long long)C * npad)), r = (int)(u % ((long long)C * npad));
+            const int c = r / npad, x = r % npad;
+            double acc = 0.0;
+            if (x < n) {
+                if (s == S) {
+                    acc = 1.0;  // unknown state: P . 1 = 1
+                } else {
+                    for (int i = 0; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], tip_lh[s * n + i], acc);
+                }
+            }
+            tab[u] = (float)acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// derivatives and lnL from the FP32 theta buffer, FP64 sums
+// (tree/phylokernelnew.h:2233-2633 and :3232-3428)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTPB) k_derv_mixed(const MixBufParams P) {
+    __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
+    const int n = P.n, C = P.ncat, B = n * C;
+    for (int t = threadIdx.x; t < B; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        const double cof = P.eval[i] * P.rates[c];
+        const double val = exp(cof * P.len) * P.props[c];
+        const double val1 = cof * val;
+        v0[t] = val;
+        v1[t] = val1;
+        v2[t] = cof * val1;
+    }
+    __syncthreads();
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const float *th = P.theta + p;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int k = 0; k < B; k++) {
+            const double t0 = (double)th[(long long)k * P.ldp];
+            a0 = fma(v0[k], t0, a0);
+            a1 = fma(v1[k], t0, a1);
+            a2 = fma(v2[k], t0, a2);
+        }
+        // the +I term is in true scale: bring it to the stored scale
+        const double lh = fabs(a0) + P.invar[p] * exp(-P.buffer_scale[p]);
+        const double inv = 1.0 / lh;
+        const double df_frac = a1 * inv, ddf_frac = a2 * inv;
+        const double f = P.freq[p];
+        const double tmp1 = df_frac * f, tmp2 = ddf_frac * f;
+        r[0] = tmp1;
+        r[1] = fma(-tmp1, df_frac, tmp2);
+        r[2] = (log(lh) + P.buffer_scale[p]) * f;
+    }
+    mix_grid_reduce(r, P.red);
+}
+
+__global__ void __launch_bounds__(kTPB) k_from_buffer_mixed(const MixBufParams P) {
+    __shared__ double v0[kMaxCat * kMaxStates];
+    const int n = P.n, C = P.ncat, B = n * C;
+    for (int t = threadIdx.x; t < B; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        v0[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+    }
+    __syncthreads();
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const float *th = P.theta + p;
+        double a0 = 0.0;
+        for (int k = 0; k < B; k++) a0 = fma(v0[k], (double)th[(long long)k * P.ldp], a0);
+        const double lh = fabs(a0) + P.invar[p] * exp(-P.buffer_scale[p]);
+        const double plh = log(lh) + P.buffer_scale[p];
+        P.pattern_lh[p] = plh;
+        const double f = P.freq[p];
+        r[0] = plh * f;
+        r[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+        r[2] = isfinite(plh) ? 0.0 : 1.0;
+    }
+    mix_grid_reduce(r, P.red);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+MixParams mix_params(iqgpu_engine *e, int nops) {
+    MixParams P;
+    P.n = e->n;
+    P.npad = e->npad;
+    P.ncat = e->C;
+    P.state_unknown = e->S;
+    P.nops = nops;
+    P.nptn = (int)e->P;
+    P.ldp = e->Ppad;
+    P.slot_floats = e->Ppad * e->bp;
+    P.op_stride = e->op_stride32;
+    P.ops = e->d_ops;
+    P.opmats = e->d_opmats32;
+    // the FP32 copy of U^-1 ([n][npad]) lives after max_ops+1 op matrix blocks
+    P.inv32 = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
+    P.pi = e->d_pi;
+    P.tip_lh = e->d_tip;
+    P.freq = e->d_freq;
+    P.invar = e->d_invar;
+    P.eval = e->d_eval;
+    P.rates = e->d_rates;
+    P.props = e->d_props;
+    P.states = e->d_states;
+    P.part = e->d_part32;
+    P.expo = e->d_exp;
+    P.a = P.b = 0;
+    P.len = 0.0;
+    P.pattern_lh = e->d_plh;
+    P.theta = e->d_theta32;
+    P.buffer_scale = e->d_bscale;
+    P.red.partials = e->d_red_partials;
+    P.red.ticket = e->d_ticket;
+    P.red.out = e->d_red_out;
+    return P;
+}
+
+int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
+    if (nops_with_branch <= 0) return IQGPU_OK;
+    const int Z = e->n > 20 ? 32 : 4;
+    dim3 grid(nops_with_branch, 2, Z);
+    k_partial_info_mixed<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv,
+                                                   e->d_eval, e->d_rates, e->d_tip, e->n, e->npad, e->C, e->S);
+    return cuda_fail(cudaGetLastError(), "partial_info_mixed");
+}
+
+static MixBufParams mixbuf_params(iqgpu_engine *e, double len) {
+    MixBufParams P;
+    P.n = e->n;
+    P.ncat = e->C;
+    P.nptn = (int)e->P;
+    P.ldp = e->Ppad;
+    P.theta = e->d_theta32;
+    P.buffer_scale = e->d_bscale;
+    P.freq = e->d_freq;
+    P.invar = e->d_invar;
+    P.eval = e->d_eval;
+    P.rates = e->d_rates;
+    P.props = e->d_props;
+    P.len = len;
+    P.pattern_lh = e->d_plh;
+    P.red.partials = e->d_red_partials;
+    P.red.ticket = e->d_ticket;
+    P.red.out = e->d_red_out;
+    return P;
+}
+
+int launch_derv_mixed(iqgpu_engine *e, double len) {
+    k_derv_mixed<<<e->nblk, kTPB, 0, e->st>>>(mixbuf_params(e, len));
+    return cuda_fail(cudaGetLastError(), "derv_mixed");
+}
+
+int launch_from_buffer_mixed(iqgpu_engine *e, double len) {
+    k_from_buffer_mixed<<<e->nblk, kTPB, 0, e->st>>>(mixbuf_params(e, len));
+    return cuda_fail(cudaGetLastError(), "from_buffer_mixed");
+}
+
+}  // namespace iqg

@@ -1,0 +1,107 @@
+// Shared definitions of the mixed-precision path (FP32 standard-basis
+// partials, per-pattern power-of-two exponents, FP64 exp/log/sums).
+//
+// Layout. A slot stores each pattern's block of C*npad floats (npad = n
+// rounded up to 4), interleaved by groups of 8 patterns so that every
+// (category, 4-state) chunk of 8 patterns is one contiguous 128-byte core
+// matrix: index(p, c, y) = (p/8)*8*C*npad + (c*npad/4 + y/4)*32 + (p%8)*4 + y%4.
+// A warp that handles 32 patterns of one category touches four whole
+// 128-byte lines per float4 load. The same bytes form K-major 8-row x 16-byte
+// core-matrix tiles, the tensor cores' operand layout.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+
+namespace iqg {
+
+constexpr float kMixThreshold = 9.094947017729282e-13f;  // 2^-40
+constexpr double kLn2 = 0.6931471805599453094172321;
+constexpr int kMixTile = 128;  // patterns per CTA; the CTA has kMixTile * ncat threads
+
+struct MixParams {
+    int n, npad, ncat, state_unknown, nops, nptn;
+    long long ldp;          // Ppad
+    long long slot_floats;  // Ppad * C * npad
+    long long op_stride;    // floats per op
+    const OpDev *ops;
+    const float *opmats;    // per op: P child0 [C][n][npad], P child1, table child0 [S+1][C][npad], table child1
+    const float *inv32;     // [n][npad] FP32 copy of U^-1
+    const double *pi;       // [n]
+    const double *tip_lh;   // eigen-space tip vectors (S+1)*n
+    const double *freq, *invar;
+    const double *eval, *rates, *props;
+    const uint8_t *states;
+    float *part;
+    int32_t *expo;
+    int32_t a, b;
+    double len;
+    double *pattern_lh;
+    float *theta;           // [B][ldp]
+    double *buffer_scale;
+    Reduce red;
+};
+
+struct MixBufParams {
+    int n, ncat, nptn;
+    long long ldp;
+    const float *theta;
+    const double *buffer_scale, *freq, *invar, *eval, *rates, *props;
+    double len;
+    double *pattern_lh;
+    Reduce red;
+};
+
+__device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+
+__device__ __forceinline__ void mix_warp_reduce(double (&v)[kRedSlots]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < kRedSlots; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
+}
+
+// Block sums -> partials[blockIdx.x]; the last CTA (by ticket) adds all
+// partials in CTA order, deterministically, and re-arms the ticket.
+__device__ __forceinline__ void mix_grid_reduce(double (&v)[kRedSlots], const Reduce &red) {
+    __shared__ double sw[32][kRedSlots];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    mix_warp_reduce(v);
+    if (lane == 0)
+        for (int k = 0; k < kRedSlots; k++) sw[wid][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        for (int w = 0; w < nw; w++)
+            for (int k = 0; k < kRedSlots; k++) s[k] += sw[w][k];
+        for (int k = 0; k < kRedSlots; k++) red.partials[(long long)blockIdx.x * kRedSlots + k] = s[k];
+        __threadfence();
+        const unsigned t = atomicAdd(red.ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+        for (int k = 0; k < kRedSlots; k++) s[k] += __ldcg(red.partials + (long long)b * kRedSlots + k);
+    mix_warp_reduce(s);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < kRedSlots; k++) sw[wid][k] = s[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kRedSlots; k++) {
+            double acc = 0.0;
+            for (int w = 0; w < nw; w++) acc += sw[w][k];
+            red.out[k] = acc;
+        }
+        *red.ticket = 0u;
+    }
+}
+
+MixParams mix_params(iqgpu_engine *e, int nops);
+
+}  // namespace iqg

@@ -1,0 +1,276 @@
+// Mixed-precision path, part 2: the traversal kernel on CUDA cores.
+//
+// A CTA owns TP consecutive patterns (128 for ncat <= 4) and runs TP*ncat
+// threads: warp w handles 32 patterns of one rate category, so the P(t)
+// matrix rows it reads are warp-uniform (L1 broadcast) and its float4 loads
+// of the children are four whole 128-byte lines. Each thread keeps its
+// category's outputs in registers until the pattern's largest entry over all
+// categories is known (one shared-memory max across the category warps, one
+// barrier per op), then applies the exact power-of-two rescale and stores once.
+// The whole post-order op list runs in one launch: a pattern's partials only
+// depend on the same pattern's children, computed earlier by the same threads.
+#include <cuda_runtime.h>
+
+#include "mixed.cuh"
+
+namespace iqg {
+
+template <int NQ>
+__device__ __forceinline__ float row_dot(const float *__restrict__ prow, const float4 (&v)[NQ]) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        const float4 m = ld4(prow + 4 * q);
+        a0 = fmaf(m.x, v[q].x, a0);
+        a1 = fmaf(m.y, v[q].y, a1);
+        a0 = fmaf(m.z, v[q].z, a0);
+        a1 = fmaf(m.w, v[q].w, a1);
+    }
+    return a0 + a1;
+}
+
+__device__ __forceinline__ float dot4(const float4 a, const float4 b, float acc) {
+    return fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc))));
+}
+
+// NQ = npad/4 float4 chunks per category held in registers (1 DNA, 5 protein);
+// NQ = 0 is the chunked path for larger n (codon).
+template <int NQ, int EPI>
+__global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const int TP) {
+    constexpr int XC = 16;
+    const int n = P.n, npad = P.npad, C = P.ncat, S = P.state_unknown;
+    const int nq = NQ ? NQ : npad >> 2;
+    const int c = threadIdx.x / TP;   // warp-uniform (TP is a multiple of 32)
+    const int pl = threadIdx.x % TP;
+    const long long p = (long long)blockIdx.x * TP + pl;
+    const long long ld = P.ldp;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * nq * 32;
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(S + 1) * C * npad;
+    __shared__ float s_max[2][512];
+    __shared__ float s_lc[512];
+
+    for (int k = 0; k < P.nops; ++k) {
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const float *base = P.opmats + (long long)k * P.op_stride;
+        const float *PL = base, *PR = base + PM, *TL = base + 2 * PM, *TR = TL + TB;
+        if (lref >= 0 && rref < 0) {
+            int t = lref; lref = rref; rref = t;
+            const float *q = PL; PL = PR; PR = q;
+            q = TL; TL = TR; TR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
+        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
+        const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad + c * npad;
+        const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad + c * npad;
+        const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
+        float cmax = 0.f;
+        float4 out[NQ ? NQ : 1];
+        if constexpr (NQ > 0) {
+            float4 lv[NQ], rv[NQ];
+            if (lint) {
+#pragma unroll
+                for (int q = 0; q < NQ; q++) lv[q] = *reinterpret_cast<const float4 *>(Lp + q * 32);
+            }
+            if (rint) {
+#pragma unroll
+                for (int q = 0; q < NQ; q++) rv[q] = *reinterpret_cast<const float4 *>(Rp + q * 32);
+            }
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                float o[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int x = 4 * q + j;
+                    float v = 0.f;
+                    if (x < n) {
+                        const float yl = lint ? row_dot<NQ>(PLc + (long long)x * npad, lv) : __ldg(tl + x);
+                        const float yr = rint ? row_dot<NQ>(PRc + (long long)x * npad, rv) : __ldg(tr + x);
+                        v = yl * yr;
+                    }
+                    o[j] = v;
+                    cmax = fmaxf(cmax, v);
+                }
+                out[q] = make_float4(o[0], o[1], o[2], o[3]);
+            }
+        } else {
+            for (int x0 = 0; x0 < npad; x0 += XC) {
+                float al[XC], ar[XC];
+#pragma unroll
+                for (int j = 0; j < XC; j++) { al[j] = 0.f; ar[j] = 0.f; }
+                for (int q = 0; q < nq; q++) {
+                    const float4 l4 = lint ? *reinterpret_cast<const float4 *>(Lp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 r4 = rint ? *reinterpret_cast<const float4 *>(Rp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int j = 0; j < XC; j++) {
+                        const int x = x0 + j;
+                        if (x < n) {
+                            if (lint) al[j] = dot4(ld4(PLc + (long long)x * npad + 4 * q), l4, al[j]);
+                            if (rint) ar[j] = dot4(ld4(PRc + (long long)x * npad + 4 * q), r4, ar[j]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < XC; j += 4) {
+                    float o[4];
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int x = x0 + j + jj;
+                        float v = 0.f;
+                        if (x < n) {
+                            const float yl = lint ? al[j + jj] : __ldg(tl + x);
+                            const float yr = rint ? ar[j + jj] : __ldg(tr + x);
+                            v = yl * yr;
+                        }
+                        o[jj] = v;
+                        cmax = fmaxf(cmax, v);
+                    }
+                    if (x0 + j < npad)
+                        *reinterpret_cast<float4 *>(dad + ((x0 + j) >> 2) * 32) = make_float4(o[0], o[1], o[2], o[3]);
+                }
+            }
+        }
+        // pattern maximum over the category warps
+        s_max[k & 1][threadIdx.x] = cmax;
+        __syncthreads();
+        float mx = 0.f;
+        for (int cc = 0; cc < C; cc++) mx = fmaxf(mx, s_max[k & 1][cc * TP + pl]);
+        int sh = 0;
+        float mul = 1.f;
+        if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
+            int ex;
+            frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
+            sh = 1 - ex;      // mx * 2^sh in [1, 2)
+            mul = __int_as_float((127 + sh) << 23);
+        }
+        if constexpr (NQ > 0) {
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                float4 v = out[q];
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(dad + q * 32) = v;
+            }
+        } else if (sh) {
+            for (int q = 0; q < nq; q++) {
+                float4 v = *reinterpret_cast<float4 *>(dad + q * 32);
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(dad + q * 32) = v;
+            }
+        }
+        if (c == 0) {
+            // exponents are read and written by the category-0 thread of the pattern only
+            const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+            P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+        }
+    }
+
+    if constexpr (EPI == EPI_NONE) return;
+
+    const float *pa = P.part + (long long)P.a * P.slot_floats + pbase;
+    const bool btip = P.b < 0;
+    const float *pb = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pbase;
+    const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+
+    if constexpr (EPI == EPI_THETA) {
+        // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i in eigen space (tree/phylokernelnew.h:2048-2231)
+        float *th = P.theta + p;
+        for (int i = 0; i < n; i++) {
+            const float *urow = P.inv32 + (long long)i * npad;
+            float ua = 0.f, ub = 0.f;
+            for (int q = 0; q < nq; q++) {
+                const float4 u = ld4(urow + 4 * q);
+                ua = dot4(u, *reinterpret_cast<const float4 *>(pa + q * 32), ua);
+                if (!btip) ub = dot4(u, *reinterpret_cast<const float4 *>(pb + q * 32), ub);
+            }
+            if (btip) ub = (float)__ldg(P.tip_lh + (long long)sb * n + i);
+            th[(long long)(c * n + i) * ld] = ua * ub;
+        }
+        if (c == 0) {
+            const int ea = P.expo[(long long)P.a * ld + p];
+            const int eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
+            P.buffer_scale[p] = (double)(ea + eb) * kLn2;
+        }
+        return;
+    } else {
+        // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
+        const float *base = P.opmats + (long long)P.nops * P.op_stride;  // branch matrices, child 0 = b
+        float lc = 0.f;
+        for (int x = 0; x < n; x++) {
+            float w;
+            if (btip) {
+                w = __ldg(base + 2 * PM + (long long)sb * C * npad + c * npad + x);
+            } else {
+                const float *prow = base + (long long)(c * n + x) * npad;
+                float s0 = 0.f;
+                for (int q = 0; q < nq; q++) s0 = dot4(ld4(prow + 4 * q), *reinterpret_cast<const float4 *>(pb + q * 32), s0);
+                w = s0;
+            }
+            const float av = pa[(x >> 2) * 32 + (x & 3)];
+            lc = fmaf((float)__ldg(P.pi + x) * av, w, lc);
+        }
+        s_lc[threadIdx.x] = lc;
+        __syncthreads();
+        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        if (c == 0) {
+            double lh = 0.0;
+            for (int cc = 0; cc < C; cc++) lh = fma((double)s_lc[cc * TP + pl], P.props[cc], lh);
+            const int ea = P.expo[(long long)P.a * ld + p];
+            const int eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
+            // the +I term is in true scale: bring it to the stored scale 2^-(ea+eb)
+            lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));
+            const double plh = log(lh) + (double)(ea + eb) * kLn2;
+            P.pattern_lh[p] = plh;
+            if (p < P.nptn) {
+                const double f = P.freq[p];
+                v[0] = plh * f;
+                v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+                v[2] = isfinite(plh) ? 0.0 : 1.0;
+            }
+        }
+        mix_grid_reduce(v, P.red);
+    }
+}
+
+// Patterns per CTA: the autotuned value when set (iqgpu_set_tile), else 32
+// (one warp per category; small CTAs let several CTAs per SM overlap one op's
+// loads with another's arithmetic around the per-op barrier). TP * ncat <= 512.
+static int mix_tile(const iqgpu_engine *e) {
+    int tp = e->tile > 0 ? e->tile : 32;
+    while (tp > 32 && tp * e->C > 512) tp >>= 1;
+    return tp;
+}
+
+template <int NQ, int EPI>
+static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
+    const int TP = mix_tile(e);
+    const int grid = (int)(e->Ppad / TP);
+    k_traverse_mixed<NQ, EPI><<<grid, TP * e->C, 0, e->st>>>(P, TP);
+    return cuda_fail(cudaGetLastError(), "traverse_mixed");
+}
+
+template <int EPI>
+static int dispatch_mix(iqgpu_engine *e, const MixParams &P) {
+    switch (e->npad) {
+    case 4: return launch_mix_t<1, EPI>(e, P);
+    case 20: return launch_mix_t<5, EPI>(e, P);
+    default: return launch_mix_t<0, EPI>(e, P);
+    }
+}
+
+int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
+    MixParams P = mix_params(e, nops);
+    P.a = a;
+    P.b = b;
+    P.len = len;
+    if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    switch (epi) {
+    case EPI_NONE: return dispatch_mix<EPI_NONE>(e, P);
+    case EPI_LNL: return dispatch_mix<EPI_LNL>(e, P);
+    default: return dispatch_mix<EPI_THETA>(e, P);
+    }
+}
+
+}  // namespace iqg

@@ -30,7 +30,11 @@ class EngineError(RuntimeError):
 class Config(ct.Structure):
     _fields_ = [("nptn", ct.c_int32), ("nstates", ct.c_int32), ("ncat", ct.c_int32), ("ntaxa", ct.c_int32),
                 ("state_unknown", ct.c_int32), ("nslots", ct.c_int32), ("safe", ct.c_int32),
-                ("precision", ct.c_int32), ("device", ct.c_int32), ("max_ops", ct.c_int32)]
+                ("precision", ct.c_int32), ("device", ct.c_int32), ("max_ops", ct.c_int32),
+                ("flags", ct.c_int32)]
+
+
+FLAG_REF_TRIPLE_TAIL = 1
 
 
 class Op(ct.Structure):
@@ -69,6 +73,7 @@ def lib():
         "iqgpu_get_config": ([vp, ct.POINTER(Config)], ct.c_int),
         "iqgpu_set_model": ([vp, _DP, _DP, _DP, _DP, _DP], ct.c_int),
         "iqgpu_set_tip_partials": ([vp, _DP], ct.c_int),
+        "iqgpu_set_state_freq": ([vp, _DP], ct.c_int),
         "iqgpu_set_patterns": ([vp, _DP, _DP], ct.c_int),
         "iqgpu_set_tip_states": ([vp, _U8P], ct.c_int),
         "iqgpu_compute_partials": ([vp, vp, ct.c_int32], ct.c_int),
@@ -84,6 +89,7 @@ def lib():
         "iqgpu_set_stream": ([vp, vp], ct.c_int),
         "iqgpu_set_timing": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
+        "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_tree_create": ([vp, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
         "iqgpu_tree_destroy": ([vp], ct.c_int),
         "iqgpu_tree_compute_likelihood": ([vp, _DP, _DP], ct.c_int),
@@ -123,10 +129,10 @@ class Engine:
     """One engine = one HBM workspace and one CUDA stream (a PhyloTree's buffers)."""
 
     def __init__(self, nptn, nstates, ncat, ntaxa, state_unknown, nslots, safe=False, precision=F64,
-                 device=0, max_ops=None):
+                 device=0, max_ops=None, flags=0):
         self.cfg = Config(int(nptn), int(nstates), int(ncat), int(ntaxa), int(state_unknown), int(nslots),
                           int(bool(safe)), int(precision), int(device),
-                          int(max_ops if max_ops is not None else max(2 * ntaxa, 8)))
+                          int(max_ops if max_ops is not None else max(2 * ntaxa, 8)), int(flags))
         h = ct.c_void_p()
         _check(lib().iqgpu_create(ct.byref(self.cfg), ct.byref(h)))
         self.h = h
@@ -137,7 +143,7 @@ class Engine:
     def memory_required(**kw):
         c = Config(kw["nptn"], kw["nstates"], kw["ncat"], kw["ntaxa"], kw["state_unknown"], kw["nslots"],
                    int(kw.get("safe", 0)), int(kw.get("precision", F64)), 0,
-                   kw.get("max_ops", max(2 * kw["ntaxa"], 8)))
+                   kw.get("max_ops", max(2 * kw["ntaxa"], 8)), int(kw.get("flags", 0)))
         out = ct.c_size_t()
         _check(lib().iqgpu_memory_required(ct.byref(c), ct.byref(out)))
         return out.value
@@ -161,6 +167,7 @@ class Engine:
         a = [np.ascontiguousarray(x, np.float64) for x in (model.eval, model.evec, model.inv_evec,
                                                             model.rates, model.props)]
         _check(lib().iqgpu_set_model(self.h, *[_dp(x) for x in a]))
+        _check(lib().iqgpu_set_state_freq(self.h, _dp(np.ascontiguousarray(model.pi, np.float64))))
         _check(lib().iqgpu_set_tip_partials(self.h, _dp(np.ascontiguousarray(model.tip_lh, np.float64))))
 
     def set_patterns(self, freq, invar=None):
@@ -237,17 +244,21 @@ class Engine:
         _check(lib().iqgpu_get_timing(self.h, ct.byref(ms), ct.byref(n)))
         return ms.value, n.value
 
+    def set_tile(self, patterns_per_cta):
+        _check(lib().iqgpu_set_tile(self.h, int(patterns_per_cta)))
+
 
 class GpuTree:
     """PhyloTree drivers on the GPU engine (one engine per tree)."""
 
-    def __init__(self, model, patterns, freq, edges, lengths, safe=False, precision=F64, device=0, invar=None):
+    def __init__(self, model, patterns, freq, edges, lengths, safe=False, precision=F64, device=0, invar=None,
+                 flags=0):
         ntaxa = patterns.shape[0]
         self.ntaxa = ntaxa
         self.nedge = 2 * ntaxa - 3
         self.engine = Engine(patterns.shape[1], model.nstates, model.ncat, ntaxa, model.state_unknown,
                              3 * (ntaxa - 2), safe=safe, precision=precision, device=device,
-                             max_ops=2 * ntaxa)
+                             max_ops=2 * ntaxa, flags=flags)
         self.engine.set_model(model)
         self.engine.set_patterns(freq, invar)
         self.engine.set_tip_states(patterns)

@@ -60,7 +60,8 @@ class _Model(ct.Structure):
                 ("state_unknown", ct.c_int), ("safe", ct.c_int),
                 ("eval", ct.c_void_p), ("evec", ct.c_void_p), ("inv_evec", ct.c_void_p),
                 ("rates", ct.c_void_p), ("props", ct.c_void_p), ("tip_lh", ct.c_void_p),
-                ("ptn_freq", ct.c_void_p), ("ptn_invar", ct.c_void_p), ("tip_states", ct.c_void_p)]
+                ("ptn_freq", ct.c_void_p), ("ptn_invar", ct.c_void_p), ("tip_states", ct.c_void_p),
+                ("ref_triple_tail", ct.c_int)]
 
 
 def _dp(a):
@@ -70,7 +71,7 @@ def _dp(a):
 class OracleModel:
     """Owns the arrays an ``orc_model`` points at."""
 
-    def __init__(self, model, patterns, freq, safe=False, invar=None):
+    def __init__(self, model, patterns, freq, safe=False, invar=None, ref_triple_tail=False):
         self.arrays = dict(
             eval=np.ascontiguousarray(model.eval, np.float64),
             evec=np.ascontiguousarray(model.evec, np.float64),
@@ -88,7 +89,8 @@ class OracleModel:
         self.safe = bool(safe)
         self.s = _Model(self.nptn, model.nstates, model.ncat, self.ntaxa, model.state_unknown, int(safe),
                         *[a[k].ctypes.data for k in ("eval", "evec", "inv_evec", "rates", "props",
-                                                     "tip_lh", "ptn_freq", "ptn_invar", "tip_states")])
+                                                     "tip_lh", "ptn_freq", "ptn_invar", "tip_states")],
+                        int(ref_triple_tail))
 
     @property
     def ptr(self):
@@ -102,8 +104,11 @@ class OracleModel:
 class OracleTree:
     """PhyloTree restatement: computeLikelihood / optimizeOneBranch / optimizeAllBranches."""
 
-    def __init__(self, model, patterns, freq, edges, lengths, safe=False, nthreads=0, invar=None):
-        self.m = OracleModel(model, patterns, freq, safe=safe, invar=invar)
+    def __init__(self, model, patterns, freq, edges, lengths, safe=False, nthreads=0, invar=None,
+                 ref_triple_tail=False):
+        """ref_triple_tail=True reproduces the reference's derivative sum exactly,
+        including its double-counted last entry for odd nstates (codon +G4)."""
+        self.m = OracleModel(model, patterns, freq, safe=safe, invar=invar, ref_triple_tail=ref_triple_tail)
         self.edges = np.ascontiguousarray(edges, np.int32)
         self.nedge = len(self.edges)
         L = lib()

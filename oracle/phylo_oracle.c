@@ -518,7 +518,9 @@ void orc_derv(const orc_model *m, const double *theta, double len, double *df, d
 #pragma omp for schedule(static)
         for (int ptn = 0; ptn < nptn; ptn++) {
             double lh, d1, d2;
-            dot_triple(val0, val1, val2, theta + (size_t)ptn * B, B, n, &lh, &d1, &d2);
+            /* the split follows nstates parity in the reference; following the
+             * parity of B itself gives the exact sum */
+            dot_triple(val0, val1, val2, theta + (size_t)ptn * B, B, m->ref_triple_tail ? n : B, &lh, &d1, &d2);
             lh = fabs(lh) + m->ptn_invar[ptn];
             lh = 1.0 / lh;
             double df_frac = d1 * lh, ddf_frac = d2 * lh;

@@ -44,6 +44,10 @@ typedef struct {
     const double *ptn_freq;  /* nptn */
     const double *ptn_invar; /* nptn */
     const uint8_t *tip_states; /* ntaxa*nptn */
+    /* 1: the reference's dotProductTriple, which adds the last block entry a
+     * second time when nstates is odd and nstates*ncat even
+     * (tree/phylokernelnew.h:699-718); 0: the exact derivative sum. */
+    int ref_triple_tail;
 } orc_model;
 
 /* A reference to a directed partial: >= 0 is a slot, < 0 is tip taxon (-1-ref). */

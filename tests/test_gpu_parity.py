@@ -82,11 +82,12 @@ def test_derivatives_and_from_buffer(oracle_mod, name, safe):
     eng.set_model(g.model)
     eng.set_patterns(g.freq)
     eng.set_tip_states(g.patterns)
-    orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe)
     internal = [tuple(map(int, e)) for e in g.edges if min(e) >= g.ntaxa]
     branches = [tuple(map(int, g.edges[0]))] + internal[:2]
     done = set()
     for (n1, n2) in branches:
+        # a fresh oracle per branch: its derivative hook moves that branch's length
+        orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe)
         node, dad = n2, n1
         if node < g.ntaxa:
             node, dad = n1, n2
@@ -201,3 +202,23 @@ def test_engine_errors_are_reported():
     with pytest.raises(engine.EngineError) as ei:
         eng.lnl_from_buffer(0.1)  # no theta yet
     assert ei.value.code == 6
+
+
+def test_reference_triple_tail_flag(oracle_mod):
+    """IQGPU_FLAG_REF_TRIPLE_TAIL reproduces the reference's codon derivative sum."""
+    g = load_golden("codon8")
+    topo = Topology(g.edges, g.lengths, g.ntaxa)
+    n1, n2 = map(int, g.edges[0])
+    node, dad = (n2, n1) if n2 >= g.ntaxa else (n1, n2)
+    for flag, quirk in ((0, False), (engine.FLAG_REF_TRIPLE_TAIL, True)):
+        eng = engine.Engine(g.patterns.shape[1], 61, g.model.ncat, g.ntaxa, 61, topo.nslots,
+                            max_ops=topo.nslots, flags=flag)
+        eng.set_model(g.model)
+        eng.set_patterns(g.freq)
+        eng.set_tip_states(g.patterns)
+        ops = topo.branch_ops(node, dad)
+        df, ddf = eng.likelihood_derv(ops, topo.ref(dad, node), topo.ref(node, dad), 0.02)
+        orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, ref_triple_tail=quirk)
+        odf, oddf = orc.derv(n1, n2, 0.02)
+        assert abs(df - odf) <= 1e-9 * max(1.0, abs(odf))
+        assert abs(ddf - oddf) <= 1e-9 * max(1.0, abs(oddf))

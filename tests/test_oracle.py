@@ -79,3 +79,31 @@ def test_scaling_triggers_and_matches_standard_basis(oracle_mod):
     x = adj[0][0]
     _, s = t.partial(0, x)
     assert s.max() >= 1
+
+
+def test_exact_derivative_matches_finite_difference_and_reference_quirk(oracle_mod):
+    """Codon +G4 (odd nstates, even block): the exact derivative sum equals the
+    finite difference of lnL; the reference's dotProductTriple tail (the last
+    block entry added twice) gives a different value, reproduced on request."""
+    g = load_golden("codon8")
+    n1, n2 = map(int, g.edges[0])
+    node, dad = (n2, n1) if n2 >= g.ntaxa else (n1, n2)
+    exact = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+    quirk = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, ref_triple_tail=True)
+    h, L = 1e-6, 0.02
+
+    def lnl(t, x):
+        t.derv(n1, n2, x)
+        return t.lnl_branch(node, dad)
+
+    fd = (lnl(exact, L + h) - lnl(exact, L - h)) / (2 * h)
+    df, _ = exact.derv(n1, n2, L)
+    assert abs(df - fd) < 1e-4 * abs(fd)
+    dq, _ = quirk.derv(n1, n2, L)
+    assert abs(dq - fd) > 1.0  # the reference's sum is off for this model
+    # DNA (even nstates) is unaffected by the flag
+    d = load_golden("dna16")
+    a = oracle_mod.OracleTree(d.model, d.patterns, d.freq, d.edges, d.lengths).derv(*map(int, d.edges[0]), 0.05)
+    b = oracle_mod.OracleTree(d.model, d.patterns, d.freq, d.edges, d.lengths,
+                              ref_triple_tail=True).derv(*map(int, d.edges[0]), 0.05)
+    assert a == b
