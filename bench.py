@@ -30,16 +30,33 @@ sys.path.insert(0, ROOT)
 
 from iqtree2_gb300 import simulate  # noqa: E402
 
-WORKLOAD = dict(workload="protein LG+G4 100 taxa x 50000 sites, full lnL (98 partial updates + root lnL)",
-                model="LG+G4", taxa=100, sites=50000, seed=2, mean_bl=0.05, alpha=0.8)
+WORKLOADS = {
+    # the headline: protein LG+G4, 100 taxa x 50,000 sites
+    "protein": dict(workload="protein LG+G4 100 taxa x 50000 sites, full lnL (98 partial updates + root lnL)",
+                    model="LG+G4", taxa=100, sites=50000, seed=2, mean_bl=0.05, alpha=0.8),
+    # the same model on 5,000 sites: the small case for ncu captures
+    "protein-small": dict(workload="protein LG+G4 100 taxa x 5000 sites, full lnL", model="LG+G4", taxa=100,
+                          sites=5000, seed=2, mean_bl=0.05, alpha=0.8),
+    "dna": dict(workload="DNA GTR+G4 16 taxa x 1000 sites, full lnL", model="GTR+G4", taxa=16, sites=1000,
+                seed=1, mean_bl=0.1, alpha=0.5),
+    "dna-large": dict(workload="DNA GTR+G4 200 taxa x 100000 sites, full lnL", model="GTR+G4", taxa=200,
+                      sites=100000, seed=4, mean_bl=0.1, alpha=0.5),
+    "codon": dict(workload="codon GY94+G4 40 taxa x 10000 codons, full lnL", model="GY94+G4", taxa=40,
+                  sites=10000, seed=3, mean_bl=0.1, alpha=0.5),
+}
+WORKLOAD = WORKLOADS["protein"]
 METRIC = "pattern-node updates/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_PEAK_TFLOPS_MEASURED = 1.20  # FMA-chain probe on this machine's GB300 (all SMs)
 
 
 def dataset():
-    return simulate.protein_lg_dataset(WORKLOAD["taxa"], WORKLOAD["sites"], WORKLOAD["seed"],
-                                       mean_bl=WORKLOAD["mean_bl"], alpha=WORKLOAD["alpha"])
+    w = WORKLOAD
+    if w["model"] == "LG+G4":
+        return simulate.protein_lg_dataset(w["taxa"], w["sites"], w["seed"], mean_bl=w["mean_bl"], alpha=w["alpha"])
+    if w["model"] == "GTR+G4":
+        return simulate.dna_gtr_dataset(w["taxa"], w["sites"], w["seed"], mean_bl=w["mean_bl"], alpha=w["alpha"])
+    return simulate.codon_gy94_dataset(w["taxa"], w["sites"], w["seed"], mean_bl=w["mean_bl"], alpha=w["alpha"])
 
 
 def topology_ops(ds):
@@ -329,7 +346,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="protein", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args)
     else:
