@@ -164,6 +164,28 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
+/* ---- derivative sums without device allocation ------------------------- */
+/* No counterpart in the reference. For callers that may not allocate device
+ * memory when they need a derivative (GPU memory owned by a pool they must
+ * not bypass, a pipeline that cannot afford the device synchronisation of
+ * cudaMalloc/cudaFree, or only borrowed device buffers at hand): the same
+ * FP64 derivative sums as iqgpu_likelihood_derv, from a theta buffer the
+ * caller owns. All pointers ending in _dev are device memory:
+ * theta_dev[B][ldp] (B = nstates*ncat, eigen space, row c*nstates+x),
+ * buffer_scale_dev/freq_dev/invar_dev[nptn]; eval/rates/props are host
+ * arrays. out_dev receives {df, ddf, lnl}. The kernel runs on cuda_stream
+ * (NULL = legacy default stream); nothing is allocated or freed. Its only
+ * scratch is a static device array sized for at most 524,288 patterns; larger
+ * nptn is rejected with IQGPU_ERR_ARG. Every call on a device shares that
+ * array, so calls whose kernels overlap on the GPU race: serialise them (one
+ * stream, or events). The first call on each device resolves the array's
+ * device address (set-up that must not happen inside a stream capture), so
+ * make one call on each device before capturing. */
+int iqgpu_derv_noalloc(const double *theta_dev, const double *buffer_scale_dev, const double *freq_dev,
+                       const double *invar_dev, int32_t nptn, int64_t ldp, int32_t nstates, int32_t ncat,
+                       const double *eval, const double *rates, const double *props, double len,
+                       double *out_dev, void *cuda_stream);
+
 /* ---- tree-level drivers (PhyloTree restatement) ------------------------ */
 /* edges[2*k], edges[2*k+1]: endpoints of branch k; leaves are 0..ntaxa-1,
  * internal nodes ntaxa..2*ntaxa-3; a node's neighbour order is edge order. */

@@ -90,6 +90,8 @@ def lib():
         "iqgpu_set_timing": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
+                                ct.c_double, vp, vp], ct.c_int),
         "iqgpu_tree_create": ([vp, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
         "iqgpu_tree_destroy": ([vp], ct.c_int),
         "iqgpu_tree_compute_likelihood": ([vp, _DP, _DP], ct.c_int),
