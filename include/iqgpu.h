@@ -164,6 +164,37 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
+/* ---- batched evaluation ------------------------------------------------- */
+/* One NNI candidate around a central branch node1-node2 (getBestNNIForBran,
+ * tree/phylotree.cpp:4069-4320): after the swap, sub[0] and sub[1] hang off
+ * node1 and sub[2], sub[3] off node2 (partial references: slot or tip),
+ * len[] are their branch lengths; scratch[] are two slots the engine may
+ * overwrite with the candidate's node1/node2 partials (the reference's
+ * nni_partial_lh); central is the starting central-branch length. */
+typedef struct {
+    int32_t sub[4];
+    int32_t scratch[2];
+    double len[4];
+    double central;
+} iqgpu_nni_candidate;
+
+/* Evaluate a batch of NNI candidates with one optimised branch each (-nni1):
+ * both new partials of every candidate in one traversal launch, then theta,
+ * Newton-Raphson on every central branch (minimizeNewton with max_nr_step,
+ * xacc = min_bl) and the final lnL in one CUDA graph. lnl[k] and
+ * central_len[k] receive each candidate's result. Mixed-precision engines;
+ * 2*ncand <= max_ops. */
+int iqgpu_nni_batch(iqgpu_engine *e, const iqgpu_nni_candidate *cand, int32_t ncand, int32_t max_nr_step,
+                    double min_bl, double max_bl, double *lnl, double *central_len);
+
+/* UFBoot resampled pattern weights, nreps x nptn, kept resident in HBM
+ * (Alignment::createBootstrapAlignment, alignment/alignment.cpp:3795-3830). */
+int iqgpu_set_boot_weights(iqgpu_engine *e, const float *weights, int32_t nreps);
+/* RELL scores of ntrees trees: out[t*nreps + r] = sum_ptn pattern_lh[t*nptn + ptn]
+ * * weight[r][ptn] (saveCurrentTree, tree/iqtree.cpp:3551-3630); FP32 products
+ * like the reference's float dot product, FP64 accumulation every 256 patterns. */
+int iqgpu_rell(iqgpu_engine *e, const double *pattern_lh, int32_t ntrees, double *out);
+
 /* ---- derivative sums without device allocation ------------------------- */
 /* No counterpart in the reference. For callers that may not allocate device
  * memory when they need a derivative (GPU memory owned by a pool they must

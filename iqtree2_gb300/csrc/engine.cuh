@@ -106,6 +106,7 @@ struct iqgpu_engine {
     double h_evec[iqg::kMaxStates * iqg::kMaxStates];
     bool have_pi, tipstd_ready;
     int tile;                 // patterns per CTA of the mixed traversal (0 = default)
+    int *d_status;            // device status word (bounded waits that gave up)
     // stream ownership and kernel timing
     cudaStream_t own_st;
     cudaEvent_t ev_t0, ev_t1;
@@ -130,6 +131,10 @@ int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch);
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_mixed(iqgpu_engine *e, double len);
 int launch_from_buffer_mixed(iqgpu_engine *e, double len);
+
+// side buffers of the batched entry points, released with the engine
+void nni_release(iqgpu_engine *e);
+void rell_release(iqgpu_engine *e);
 
 // element offset of (pattern p, category c, state y) in a mixed-precision slot
 __host__ __device__ inline long long mixed_index(long long p, int c, int y, int npad, int C) {

@@ -202,10 +202,11 @@ int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
     CKE(cudaMalloc(&e->d_bscale, e->Ppad * 8));
     CKE(cudaMalloc(&e->d_plh, e->Ppad * 8));
     CKE(cudaMalloc(&e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
-    CKE(cudaMalloc(&e->d_ticket, 64));
+    CKE(cudaMalloc(&e->d_ticket, 64));  // ticket at byte 0, status word at byte 32
+    e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
     CKE(cudaMalloc(&e->d_red_out, kRedSlots * 8));
     CKE(cudaMallocHost(&e->h_ops, s.ops));
-    CKE(cudaMallocHost(&e->h_red_out, kRedSlots * 8));
+    CKE(cudaMallocHost(&e->h_red_out, kRedSlots * 8 + 16));
     CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
     CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
     CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
@@ -220,6 +221,8 @@ int iqgpu_destroy(iqgpu_engine *e) {
     if (!e) return IQGPU_OK;
     cudaSetDevice(e->dev);
     cudaStreamSynchronize(e->st);
+    nni_release(e);
+    rell_release(e);
     free_engine(e);
     return IQGPU_OK;
 }
@@ -395,10 +398,25 @@ static int traverse(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, do
     return IQGPU_OK;
 }
 
+// A kernel that gave up a bounded wait leaves a nonzero status word.
+static int check_status(iqgpu_engine *e) {
+    int *h_status = reinterpret_cast<int *>(e->h_red_out + kRedSlots);
+    CK(cudaMemcpyAsync(h_status, e->d_status, 4, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    if (*h_status != 0) {
+        CK(cudaMemsetAsync(e->d_status, 0, 4, e->st));
+        set_error("a device-side wait gave up (TMA copy not completed); results of that launch are invalid");
+        return IQGPU_ERR_TIMEOUT;
+    }
+    return IQGPU_OK;
+}
+
 static int fetch_result(iqgpu_engine *e) {
     CK(cudaMemcpyAsync(e->h_red_out, e->d_red_out, kRedSlots * 8, cudaMemcpyDeviceToHost, e->st));
     CK(cudaStreamSynchronize(e->st));
-    return settle_timing(e);
+    int rc = settle_timing(e);
+    if (rc) return rc;
+    return is_mixed(&e->cfg) ? check_status(e) : IQGPU_OK;
 }
 
 int iqgpu_compute_partials(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
@@ -550,7 +568,9 @@ int iqgpu_sync(iqgpu_engine *e) {
     if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
-    return settle_timing(e);
+    int rc = settle_timing(e);
+    if (rc) return rc;
+    return is_mixed(&e->cfg) ? check_status(e) : IQGPU_OK;
 }
 
 int iqgpu_set_stream(iqgpu_engine *e, void *cuda_stream) {

@@ -167,6 +167,7 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
     P.red.partials = e->d_red_partials;
     P.red.ticket = e->d_ticket;
     P.red.out = e->d_red_out;
+    P.status = e->d_status;
     return P;
 }
 

@@ -41,7 +41,48 @@ struct MixParams {
     float *theta;           // [B][ldp]
     double *buffer_scale;
     Reduce red;
+    int *status;            // set to a nonzero code when a bounded wait gives up
 };
+
+// ---- TMA bulk copies and mbarriers (inline PTX, sm_90+ forms used on sm_103a) ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> shared, completion counted on the mbarrier (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// Wait for the mbarrier phase with the given parity; gives up after `limit`
+// polls and returns false (the caller reports a timeout instead of hanging).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, unsigned limit) {
+    const unsigned a = smem_u32(bar);
+    for (unsigned i = 0; i < limit; i++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+constexpr unsigned kWaitPolls = 1u << 26;  // ~ seconds of polling before a wait is declared lost
+constexpr int kStatusTimeout = 1;
 
 struct MixBufParams {
     int n, ncat, nptn;

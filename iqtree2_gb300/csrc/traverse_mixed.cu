@@ -1,14 +1,16 @@
 // Mixed-precision path, part 2: the traversal kernel on CUDA cores.
 //
-// A CTA owns TP consecutive patterns (128 for ncat <= 4) and runs TP*ncat
-// threads: warp w handles 32 patterns of one rate category, so the P(t)
-// matrix rows it reads are warp-uniform (L1 broadcast) and its float4 loads
-// of the children are four whole 128-byte lines. Each thread keeps its
-// category's outputs in registers until the pattern's largest entry over all
-// categories is known (one shared-memory max across the category warps, one
-// barrier per op), then applies the exact power-of-two rescale and stores once.
-// The whole post-order op list runs in one launch: a pattern's partials only
-// depend on the same pattern's children, computed earlier by the same threads.
+// A CTA owns TP consecutive patterns and runs TP*ncat threads: warp w handles
+// 32 patterns of one rate category, so the transition-matrix rows it reads
+// are warp-uniform (shared-memory broadcast) and its float4 loads of the
+// children are whole 128-byte lines. Each op's two P(t) blocks are staged in
+// shared memory by a 1-D TMA bulk copy; with two buffers the copy for op k+1
+// is in flight while op k computes. Each thread keeps its category's outputs
+// in registers until the pattern's largest entry over all categories is
+// known (one shared-memory max across the category warps), then applies the
+// exact power-of-two rescale and stores once. The whole post-order op list
+// runs in one launch: a pattern's partials only depend on the same pattern's
+// children, computed earlier by the same threads.
 #include <cuda_runtime.h>
 
 #include "mixed.cuh"
@@ -16,11 +18,11 @@
 namespace iqg {
 
 template <int NQ>
-__device__ __forceinline__ float row_dot(const float *__restrict__ prow, const float4 (&v)[NQ]) {
+__device__ __forceinline__ float row_dot_s(const float *prow, const float4 (&v)[NQ]) {
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
-        const float4 m = ld4(prow + 4 * q);
+        const float4 m = *reinterpret_cast<const float4 *>(prow + 4 * q);
         a0 = fmaf(m.x, v[q].x, a0);
         a1 = fmaf(m.y, v[q].y, a1);
         a0 = fmaf(m.z, v[q].z, a0);
@@ -36,7 +38,7 @@ __device__ __forceinline__ float dot4(const float4 a, const float4 b, float acc)
 // NQ = npad/4 float4 chunks per category held in registers (1 DNA, 5 protein);
 // NQ = 0 is the chunked path for larger n (codon).
 template <int NQ, int EPI>
-__global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const int TP) {
+__global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const int TP, const int nbuf) {
     constexpr int XC = 16;
     const int n = P.n, npad = P.npad, C = P.ncat, S = P.state_unknown;
     const int nq = NQ ? NQ : npad >> 2;
@@ -47,14 +49,48 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
     const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * nq * 32;
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(S + 1) * C * npad;
+    const unsigned pbytes = (unsigned)(2 * PM * 4);  // both children's P blocks of one op
+    extern __shared__ __align__(128) float smem[];   // [nbuf][2*PM] P(t) staging
+    __shared__ unsigned long long bars[2];
     __shared__ float s_max[2][512];
     __shared__ float s_lc[512];
 
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        if (P.nops > 0) {
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(smem, P.opmats, pbytes, &bars[0]);
+        }
+    }
+    __syncthreads();
+
     for (int k = 0; k < P.nops; ++k) {
+        const int buf = nbuf == 2 ? (k & 1) : 0;
+        const unsigned parity = nbuf == 2 ? ((k >> 1) & 1) : (k & 1);
+        // every thread observes the copy's completion itself; the vote makes the
+        // give-up decision uniform across the CTA  -- barrier (A)
+        const bool lost = !mbar_wait(&bars[buf], parity, kWaitPolls);
+        if (__syncthreads_or(lost)) {
+            if (threadIdx.x == 0) {
+                atomicExch(P.status, kStatusTimeout);
+                mbar_wait(&bars[buf], parity, kWaitPolls);  // last bounded wait for the copy in flight
+            }
+            return;
+        }
+        if (nbuf == 2 && threadIdx.x == 0 && k + 1 < P.nops) {
+            // buffer (k+1)&1 was last read in op k-1, before barrier (A)
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[(k + 1) & 1], pbytes);
+            tma_load_1d(smem + ((k + 1) & 1) * 2 * PM, P.opmats + (long long)(k + 1) * P.op_stride, pbytes,
+                        &bars[(k + 1) & 1]);
+        }
         const OpDev op = P.ops[k];
         int lref = op.child[0], rref = op.child[1];
-        const float *base = P.opmats + (long long)k * P.op_stride;
-        const float *PL = base, *PR = base + PM, *TL = base + 2 * PM, *TR = TL + TB;
+        const float *gbase = P.opmats + (long long)k * P.op_stride;
+        const float *sP = smem + buf * 2 * PM;
+        const float *PL = sP, *PR = sP + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
         if (lref >= 0 && rref < 0) {
             int t = lref; lref = rref; rref = t;
             const float *q = PL; PL = PR; PR = q;
@@ -87,8 +123,8 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
                     const int x = 4 * q + j;
                     float v = 0.f;
                     if (x < n) {
-                        const float yl = lint ? row_dot<NQ>(PLc + (long long)x * npad, lv) : __ldg(tl + x);
-                        const float yr = rint ? row_dot<NQ>(PRc + (long long)x * npad, rv) : __ldg(tr + x);
+                        const float yl = lint ? row_dot_s<NQ>(PLc + x * npad, lv) : __ldg(tl + x);
+                        const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : __ldg(tr + x);
                         v = yl * yr;
                     }
                     o[j] = v;
@@ -108,8 +144,8 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
                     for (int j = 0; j < XC; j++) {
                         const int x = x0 + j;
                         if (x < n) {
-                            if (lint) al[j] = dot4(ld4(PLc + (long long)x * npad + 4 * q), l4, al[j]);
-                            if (rint) ar[j] = dot4(ld4(PRc + (long long)x * npad + 4 * q), r4, ar[j]);
+                            if (lint) al[j] = dot4(*reinterpret_cast<const float4 *>(PLc + x * npad + 4 * q), l4, al[j]);
+                            if (rint) ar[j] = dot4(*reinterpret_cast<const float4 *>(PRc + x * npad + 4 * q), r4, ar[j]);
                         }
                     }
                 }
@@ -135,7 +171,12 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
         }
         // pattern maximum over the category warps
         s_max[k & 1][threadIdx.x] = cmax;
-        __syncthreads();
+        __syncthreads();  // (B) every thread is done with this op's P(t)
+        if (nbuf == 1 && threadIdx.x == 0 && k + 1 < P.nops) {
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(smem, P.opmats + (long long)(k + 1) * P.op_stride, pbytes, &bars[0]);
+        }
         float mx = 0.f;
         for (int cc = 0; cc < C; cc++) mx = fmaxf(mx, s_max[k & 1][cc * TP + pl]);
         int sh = 0;
@@ -236,7 +277,7 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
 
 // Patterns per CTA: the autotuned value when set (iqgpu_set_tile), else 32
 // (one warp per category; small CTAs let several CTAs per SM overlap one op's
-// loads with another's arithmetic around the per-op barrier). TP * ncat <= 512.
+// loads with another's arithmetic around the per-op barriers). TP * ncat <= 512.
 static int mix_tile(const iqgpu_engine *e) {
     int tp = e->tile > 0 ? e->tile : 32;
     while (tp > 32 && tp * e->C > 512) tp >>= 1;
@@ -247,7 +288,15 @@ template <int NQ, int EPI>
 static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     const int TP = mix_tile(e);
     const int grid = (int)(e->Ppad / TP);
-    k_traverse_mixed<NQ, EPI><<<grid, TP * e->C, 0, e->st>>>(P, TP);
+    const size_t pm_bytes = (size_t)2 * e->C * e->n * e->npad * 4;  // one op's two P(t) blocks
+    const int nbuf = pm_bytes * 2 <= 96 * 1024 ? 2 : 1;
+    const size_t smem = nbuf * pm_bytes;
+    auto kern = k_traverse_mixed<NQ, EPI>;
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_mixed smem attribute");
+    }
+    kern<<<grid, TP * e->C, smem, e->st>>>(P, TP, nbuf);
     return cuda_fail(cudaGetLastError(), "traverse_mixed");
 }
 

@@ -45,6 +45,9 @@ class Op(ct.Structure):
 OP_DTYPE = np.dtype([("dad_slot", np.int32), ("child", np.int32, (2,)), ("reserved", np.int32),
                      ("len", np.float64, (2,))])
 assert OP_DTYPE.itemsize == ct.sizeof(Op) == 32
+NNI_DTYPE = np.dtype([("sub", np.int32, (4,)), ("scratch", np.int32, (2,)), ("len", np.float64, (4,)),
+                      ("central", np.float64)])
+assert NNI_DTYPE.itemsize == 64
 
 _DP = ct.POINTER(ct.c_double)
 _U8P = ct.POINTER(ct.c_uint8)
@@ -92,6 +95,9 @@ def lib():
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
+        "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
+        "iqgpu_set_boot_weights": ([vp, ct.POINTER(ct.c_float), ct.c_int32], ct.c_int),
+        "iqgpu_rell": ([vp, _DP, ct.c_int32, _DP], ct.c_int),
         "iqgpu_tree_create": ([vp, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
         "iqgpu_tree_destroy": ([vp], ct.c_int),
         "iqgpu_tree_compute_likelihood": ([vp, _DP, _DP], ct.c_int),
@@ -248,6 +254,28 @@ class Engine:
 
     def set_tile(self, patterns_per_cta):
         _check(lib().iqgpu_set_tile(self.h, int(patterns_per_cta)))
+
+    def nni_batch(self, cands, max_nr_step=10, min_bl=1e-6, max_bl=10.0):
+        """cands: iterable of ((sub0..sub3), (scratch0, scratch1), (len0..len3), central)."""
+        cands = list(cands)
+        arr = np.zeros(len(cands), NNI_DTYPE)
+        for k, (sub, scr, lens, central) in enumerate(cands):
+            arr[k] = (sub, scr, lens, central)
+        lnl, blen = np.zeros(len(cands)), np.zeros(len(cands))
+        _check(lib().iqgpu_nni_batch(self.h, arr.ctypes.data, len(cands), int(max_nr_step), float(min_bl),
+                                     float(max_bl), _dp(lnl), _dp(blen)))
+        return lnl, blen
+
+    def set_boot_weights(self, weights):
+        w = np.ascontiguousarray(weights, np.float32)
+        _check(lib().iqgpu_set_boot_weights(self.h, w.ctypes.data_as(ct.POINTER(ct.c_float)), w.shape[0]))
+        self._nreps = w.shape[0]
+
+    def rell(self, pattern_lh):
+        plh = np.ascontiguousarray(pattern_lh, np.float64)
+        out = np.zeros((plh.shape[0], self._nreps))
+        _check(lib().iqgpu_rell(self.h, _dp(plh), plh.shape[0], _dp(out)))
+        return out
 
 
 class GpuTree:

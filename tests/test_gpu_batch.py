@@ -1,0 +1,105 @@
+"""Batched evaluation: NNI candidates in one graph-captured launch sequence and
+UFBoot RELL scores, against the FP64 oracle and numpy.
+
+Tolerances: NNI candidate lnL relative <= 1e-6 and optimised central branch
+within 1e-4 of the oracle's optimizeOneBranch (mixed-precision path); RELL
+scores relative <= 1e-6 of an FP64 numpy product.
+"""
+import numpy as np
+import pytest
+
+from helpers import rel
+from iqtree2_gb300 import engine, simulate
+from iqtree2_gb300.topology import Topology
+
+pytestmark = pytest.mark.gpu
+
+
+def nni_candidates(topo, nmax):
+    """Both swaps of every internal branch, as (u, v, subs, lens, swap tuple)."""
+    out = []
+    for (u, v) in sorted(topo.slot):
+        if u < topo.ntaxa or v < topo.ntaxa or u > v:
+            continue
+        a_, b_ = [w for (w, _) in topo.adj[u] if w != v]
+        c_, d_ = [w for (w, _) in topo.adj[v] if w != u]
+        for (x, y) in ((b_, c_), (b_, d_)):  # x leaves u for v, y leaves v for u
+            keep_u = a_ if x == b_ else b_
+            keep_v = d_ if y == c_ else c_
+            out.append(dict(u=u, v=v, n1=(keep_u, y), n2=(x, keep_v)))
+            if len(out) == nmax:
+                return out
+    return out
+
+
+def swapped_edges(ds, u, v, x, y):
+    """Edge list after moving subtree x from u to v and subtree y from v to u."""
+    edges = ds.edges.copy()
+    for k, (p, q) in enumerate(edges):
+        if {int(p), int(q)} == {u, x}:
+            edges[k] = (v, x)
+        elif {int(p), int(q)} == {v, y}:
+            edges[k] = (u, y)
+    return edges
+
+
+def test_nni_batch_matches_oracle(oracle_mod):
+    ds = simulate.dna_gtr_dataset(24, 3000, 41)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    cands = nni_candidates(topo, 16)
+    ncand = len(cands)
+    nslots = topo.nslots + 2 * ncand
+    eng = engine.Engine(ds.nptn, 4, 4, ds.ntaxa, 18, nslots, precision=engine.F32, max_ops=max(nslots, 2 * ncand))
+    eng.set_model(ds.model)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    done, ops = set(), []
+    for (u, w) in sorted(topo.slot):
+        ops += topo.ops_for(u, w, done)
+    eng.compute_partials(ops)
+    arr = []
+    for k, c in enumerate(cands):
+        u, v = c["u"], c["v"]
+        (s0, s1), (s2, s3) = c["n1"], c["n2"]
+        # subtrees hanging off u after the swap keep their own branch lengths
+        def side(sub, old):
+            return topo.ref(old, sub), topo.edge_len(old, sub)
+        old_of = {}
+        for w, _ in topo.adj[u]:
+            old_of[w] = u
+        for w, _ in topo.adj[v]:
+            old_of[w] = v
+        r0, l0 = side(s0, old_of[s0])
+        r1, l1 = side(s1, old_of[s1])
+        r2, l2 = side(s2, old_of[s2])
+        r3, l3 = side(s3, old_of[s3])
+        arr.append(((r0, r1, r2, r3), (topo.nslots + 2 * k, topo.nslots + 2 * k + 1), (l0, l1, l2, l3),
+                    topo.edge_len(u, v)))
+    lnl, blen = eng.nni_batch(arr, max_nr_step=10, min_bl=1e-6, max_bl=10.0)
+    for k, c in enumerate(cands):
+        u, v = c["u"], c["v"]
+        x = c["n2"][0]  # moved from u to v
+        y = c["n1"][1]  # moved from v to u
+        edges = swapped_edges(ds, u, v, x, y)
+        o = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, edges, ds.lengths)
+        assert o.optimize_one_branch(u, v, 10) == 0
+        ol = o.compute_likelihood()
+        ob = o.lengths()[[i for i, (p, q) in enumerate(edges) if {int(p), int(q)} == {u, v}][0]]
+        assert rel(lnl[k], ol) < 1e-6, (k, lnl[k], ol)
+        assert abs(blen[k] - ob) < 1e-4, (k, blen[k], ob)
+
+
+def test_rell_matches_numpy():
+    ds = simulate.dna_gtr_dataset(10, 5000, 43)
+    rng = np.random.default_rng(3)
+    w = simulate.bootstrap_weights(ds.freq, 200, rng)
+    eng = engine.Engine(ds.nptn, 4, 4, ds.ntaxa, 18, 24, precision=engine.F32, max_ops=24)
+    eng.set_model(ds.model)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    plh = -rng.uniform(2.0, 30.0, size=(70, ds.nptn))
+    eng.set_boot_weights(w)
+    got = eng.rell(plh)
+    want = plh @ w.astype(np.float64).T
+    assert got.shape == (70, 200)
+    assert np.max(np.abs(got - want) / np.abs(want)) < 1e-6
