@@ -339,6 +339,49 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_serve(args):
+    """Serving: seeded Poisson stream (mean --rate req/s) of lnL + one round of
+    branch optimisation; 70% DNA GTR+G4 / 30% protein LG+G4, taxa log-U[8, max],
+    sites log-U[500, max]; inputs simulated on the device, generation untimed.
+    Reports p50/p99 latency (completion - arrival) and throughput per precision."""
+    from iqtree2_gb300 import engine, serving
+    rng = np.random.default_rng(args.seed)
+    jobs = []
+    for k in range(args.requests):
+        kind = "dna" if rng.random() < 0.7 else "protein"
+        taxa = int(round(np.exp(rng.uniform(np.log(8), np.log(args.max_taxa)))))
+        sites = int(round(np.exp(rng.uniform(np.log(500), np.log(args.max_sites)))))
+        jobs.append(simulate.serving_dataset(kind, max(taxa, 4), sites, int(rng.integers(1 << 30))))
+    out = {"metric": "serve latency (completion - arrival)", "unit": "s", "requests": len(jobs),
+           "rate_per_s": args.rate, "data": "synthetic (device-simulated, seeded)",
+           "config": {"workload": f"Poisson {args.rate}/s, 70% DNA GTR+G4 / 30% LG+G4, taxa log-U[8,{args.max_taxa}], "
+                                  f"sites log-U[500,{args.max_sites}], lnL + 1 round of branch NR",
+                      "max_active": args.max_active}}
+    lnl = {}
+    for name, prec in (("mixed_f32", engine.F32), ("fp64", engine.F64)):
+        if name == "fp64" and args.no_fp64_serve:
+            continue
+        srv = serving.Server(max_active=args.max_active)
+        res, wall = serving.poisson_stream(srv, jobs, args.rate, args.seed, precision=prec)
+        st = srv.stats()
+        srv.close()
+        ok = [r for r in res if r["status"] == 0]
+        lat = np.array([r["latency"] for r in ok])
+        upd = sum((r["ntaxa"] - 2) * r["nptn"] for r in ok)
+        lnl[name] = {r["id"]: r["lnl_initial"] for r in ok}
+        out[name] = {"p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                     "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                     "throughput_jobs_per_s": len(ok) / wall, "wall_s": wall, "completed": len(ok),
+                     "refused": st["refused"], "peak_active": st["peak_active"],
+                     "peak_hbm_gb": st["peak_bytes"] / 1e9, "arena_gb": st["arena_bytes"] / 1e9,
+                     "full_traversal_updates": upd}
+    if "fp64" in lnl:
+        common = set(lnl["fp64"]) & set(lnl["mixed_f32"])
+        out["lnl_max_rel_err_mixed_vs_fp64"] = max(
+            (abs(lnl["mixed_f32"][k] - lnl["fp64"][k]) / abs(lnl["fp64"][k]) for k in common), default=None)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,10 +390,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="protein", choices=sorted(WORKLOADS))
+    ap.add_argument("--mode", default="headline", choices=["headline", "serve"])
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--max-taxa", type=int, default=2000)
+    ap.add_argument("--max-sites", type=int, default=500000)
+    ap.add_argument("--max-active", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--no-fp64-serve", action="store_true")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = WORKLOADS[args.workload]
-    if args.impl == "reference":
+    if args.mode == "serve":
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -100,6 +100,11 @@ int iqgpu_memory_required(const iqgpu_config *cfg, size_t *bytes);
 /* ---- engine lifetime and inputs ----------------------------------------- */
 /* replaces initializeAllPartialLh (tree/phylotree.cpp:893-940) */
 int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out);
+/* The same, with every device buffer carved from the caller's 256-byte
+ * aligned region of at least iqgpu_memory_required() bytes; the engine then
+ * calls no cudaMalloc/cudaFree (its side buffers for the NNI batch and RELL
+ * excepted). Used by the serving loop to admit jobs into one HBM arena. */
+int iqgpu_create_in(const iqgpu_config *cfg, void *dev_mem, size_t bytes, iqgpu_engine **out);
 int iqgpu_destroy(iqgpu_engine *e);
 /* The configuration an engine was created with. */
 int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out);
@@ -194,6 +199,64 @@ int iqgpu_set_boot_weights(iqgpu_engine *e, const float *weights, int32_t nreps)
  * * weight[r][ptn] (saveCurrentTree, tree/iqtree.cpp:3551-3630); FP32 products
  * like the reference's float dot product, FP64 accumulation every 256 patterns. */
 int iqgpu_rell(iqgpu_engine *e, const double *pattern_lh, int32_t ntrees, double *out);
+
+/* ---- serving: continuous batching of jobs ------------------------------ */
+/* A job is one likelihood + branch-optimisation request on its own tree and
+ * alignment (computeLikelihood, then optimizeAllBranches with opt_iterations
+ * rounds; 0 = lnL only). The server copies every input at submission. */
+typedef struct {
+    int32_t ntaxa, nptn, nstates, ncat, state_unknown, opt_iterations;
+    const double *eval, *evec, *inv_evec, *rates, *props, *state_freq, *tip_lh;
+    const double *ptn_freq;
+    const uint8_t *tip_states;  /* ntaxa x nptn */
+    const int32_t *edges;       /* 2 x (2*ntaxa-3) */
+    const double *lengths;      /* 2*ntaxa-3 */
+    double tolerance;           /* optimizeAllBranches tolerance (0 = 1e-3) */
+} iqgpu_job;
+
+typedef struct {
+    int64_t id;
+    int32_t status;             /* IQGPU_OK, IQGPU_ERR_OOM if refused, ... */
+    int32_t pad;
+    double lnl_initial, lnl;    /* before and after branch optimisation */
+    double t_submit, t_start, t_end;  /* seconds since the server started */
+    int64_t bytes;              /* HBM the job's engine held */
+    char error[128];
+} iqgpu_job_result;
+
+typedef struct {
+    int32_t device, precision_unused, max_active, pad;
+    uint64_t memory_budget;     /* arena bytes; 0 = 90% of free HBM */
+} iqgpu_server_config;
+
+typedef struct {
+    int64_t submitted, admitted, refused, completed, peak_active;
+    uint64_t peak_bytes, arena_bytes;
+} iqgpu_server_stats;
+
+typedef struct iqgpu_server iqgpu_server;
+
+/* Reserve the arena and start the scheduler. Jobs are admitted in arrival
+ * order when a worker slot (max_active) is free and their engine fits in the
+ * arena's free space; a job larger than the arena is refused (IQGPU_ERR_OOM).
+ * Admitted jobs run concurrently, each on its own stream. */
+int iqgpu_server_create(const iqgpu_server_config *cfg, iqgpu_server **out);
+/* Queue a job (precision IQGPU_F64 or IQGPU_F32); returns its id at once. */
+int iqgpu_server_submit(iqgpu_server *s, const iqgpu_job *job, int32_t precision, int64_t *id);
+/* Block until the job finishes; lengths (optional, 2*ntaxa-3) get the optimised branch lengths. */
+int iqgpu_server_wait(iqgpu_server *s, int64_t id, iqgpu_job_result *out, double *lengths);
+int iqgpu_server_get_stats(iqgpu_server *s, iqgpu_server_stats *out);
+/* Finish queued and running jobs, then release the arena. */
+int iqgpu_server_destroy(iqgpu_server *s);
+
+/* Seeded sequence simulation on the device (benchmark inputs; no counterpart
+ * on the reference's likelihood path). Edges in preorder: edge_parent[0] is
+ * the root and every parent appears as a child (or the root) before its own
+ * edges; cum_trans[edge][cat][x][y] are cumulative rows of P(r_cat t_edge),
+ * cum_freq the cumulative root frequencies. Writes ntaxa x nsites states. */
+int iqgpu_simulate(int32_t ntaxa, int64_t nsites, int32_t nstates, int32_t ncat, const int32_t *edge_parent,
+                   const int32_t *edge_child, const float *cum_trans, const float *cum_freq, uint64_t seed,
+                   int32_t device, uint8_t *states_out);
 
 /* ---- derivative sums without device allocation ------------------------- */
 /* No counterpart in the reference. For callers that may not allocate device

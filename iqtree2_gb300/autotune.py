@@ -27,7 +27,8 @@ def tune(eng, ops_arr, a, b, length, reps=3):
         eng.set_tile(_cache[key][0])
         return _cache[key]
     times = {}
-    for tile in CANDIDATES:
+    # tile 1 selects the one-thread-per-pattern kernel of 4-state models
+    for tile in ((1,) if eng.nstates == 4 else ()) + CANDIDATES:
         if tile * eng.ncat > 512 and tile > 32:
             continue
         eng.set_tile(tile)

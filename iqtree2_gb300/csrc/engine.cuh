@@ -107,6 +107,9 @@ struct iqgpu_engine {
     bool have_pi, tipstd_ready;
     int tile;                 // patterns per CTA of the mixed traversal (0 = default)
     int *d_status;            // device status word (bounded waits that gave up)
+    // caller-provided device memory (iqgpu_create_in): buffers are carved from it
+    char *arena_base;
+    size_t arena_size, arena_used;
     // stream ownership and kernel timing
     cudaStream_t own_st;
     cudaEvent_t ev_t0, ev_t1;

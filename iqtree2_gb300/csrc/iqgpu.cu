@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -71,7 +72,7 @@ static Sizes sizes(const iqgpu_config *c) {
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
     s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + 2 * s.Ppad * 8 +
-              (n + 2 * n * n + 2 * C + (S + 1) * n) * 8;
+              (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
     return s;
 }
 
@@ -97,6 +98,31 @@ int iqgpu_memory_required(const iqgpu_config *cfg, size_t *bytes) {
     return IQGPU_OK;
 }
 
+}  // extern "C"
+
+// Device buffers come from cudaMalloc, or are carved (256-byte aligned) from
+// the caller's region when the engine was made with iqgpu_create_in.
+template <class T>
+static cudaError_t dalloc(iqgpu_engine *e, T **p, long long bytes) {
+    if (!e->arena_base) return cudaMalloc(p, (size_t)bytes);
+    const size_t off = (e->arena_used + 255) & ~(size_t)255;
+    if (off + (size_t)bytes > e->arena_size) return cudaErrorMemoryAllocation;
+    *p = reinterpret_cast<T *>(e->arena_base + off);
+    e->arena_used = off + (size_t)bytes;
+    return cudaSuccess;
+}
+
+// Host staging: pinned memory, or plain heap memory in a caller-provided
+// region engine (no cudaMallocHost/cudaFreeHost per engine on a serving path)
+template <class T>
+static cudaError_t halloc(iqgpu_engine *e, T **p, long long bytes) {
+    if (!e->arena_base) return cudaMallocHost(p, (size_t)bytes);
+    *p = static_cast<T *>(std::malloc((size_t)bytes));
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+
+extern "C" {
+
 static void free_engine(iqgpu_engine *e) {
     if (!e) return;
     cudaSetDevice(e->dev);
@@ -104,17 +130,34 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32};
-    for (void *p : dev_ptrs)
-        if (p) cudaFree(p);
-    if (e->h_ops) cudaFreeHost(e->h_ops);
-    if (e->h_red_out) cudaFreeHost(e->h_red_out);
+    if (!e->arena_base) {
+        for (void *p : dev_ptrs)
+            if (p) cudaFree(p);
+        if (e->h_ops) cudaFreeHost(e->h_ops);
+        if (e->h_red_out) cudaFreeHost(e->h_red_out);
+    } else {
+        std::free(e->h_ops);
+        std::free(e->h_red_out);
+    }
     if (e->ev_t0) cudaEventDestroy(e->ev_t0);
     if (e->ev_t1) cudaEventDestroy(e->ev_t1);
     if (e->own_st) cudaStreamDestroy(e->own_st);
     delete e;
 }
 
-int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
+static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_bytes, iqgpu_engine **out);
+
+int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) { return create_engine(cfg, nullptr, 0, out); }
+
+int iqgpu_create_in(const iqgpu_config *cfg, void *dev_mem, size_t bytes, iqgpu_engine **out) {
+    if (!dev_mem || (reinterpret_cast<uintptr_t>(dev_mem) & 255)) {
+        set_error("iqgpu_create_in needs a 256-byte aligned device region");
+        return IQGPU_ERR_ARG;
+    }
+    return create_engine(cfg, dev_mem, bytes, out);
+}
+
+static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_bytes, iqgpu_engine **out) {
     int rc = check_config(cfg);
     if (rc) return rc;
     if (!out) { set_error("null output"); return IQGPU_ERR_ARG; }
@@ -134,15 +177,26 @@ int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
     }
     CK(cudaSetDevice(cfg->device));
     Sizes s = sizes(cfg);
-    size_t free_b = 0, total_b = 0;
-    CK(cudaMemGetInfo(&free_b, &total_b));
-    if ((size_t)s.total > free_b) {
-        set_error("admission refused: engine needs " + std::to_string(s.total) + " bytes, " +
-                  std::to_string(free_b) + " free");
-        return IQGPU_ERR_OOM;
+    if (dev_mem) {
+        if ((size_t)s.total > dev_bytes) {
+            set_error("admission refused: engine needs " + std::to_string(s.total) + " bytes, region holds " +
+                      std::to_string(dev_bytes));
+            return IQGPU_ERR_OOM;
+        }
+    } else {
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        if ((size_t)s.total > free_b) {
+            set_error("admission refused: engine needs " + std::to_string(s.total) + " bytes, " +
+                      std::to_string(free_b) + " free");
+            return IQGPU_ERR_OOM;
+        }
     }
     iqgpu_engine *e = new iqgpu_engine();
     std::memset(e, 0, sizeof(*e));
+    e->arena_base = static_cast<char *>(dev_mem);
+    e->arena_size = dev_bytes;
+    e->arena_used = 0;
     e->cfg = *cfg;
     e->dev = cfg->device;
     e->n = cfg->nstates;
@@ -169,44 +223,44 @@ int iqgpu_create(const iqgpu_config *cfg, iqgpu_engine **out) {
     CKE(cudaEventCreate(&e->ev_t0));
     CKE(cudaEventCreate(&e->ev_t1));
     const long long n = e->n, C = e->C, B = e->B, S = e->S;
-    CKE(cudaMalloc(&e->d_eval, n * 8));
-    CKE(cudaMalloc(&e->d_evec, n * n * 8));
-    CKE(cudaMalloc(&e->d_inv, n * n * 8));
-    CKE(cudaMalloc(&e->d_rates, C * 8));
-    CKE(cudaMalloc(&e->d_props, C * 8));
-    CKE(cudaMalloc(&e->d_tip, (S + 1) * n * 8));
-    CKE(cudaMalloc(&e->d_freq, e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_invar, e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_states, s.states));
-    CKE(cudaMalloc(&e->d_ops, s.ops));
+    CKE(dalloc(e, &e->d_eval, n * 8));
+    CKE(dalloc(e, &e->d_evec, n * n * 8));
+    CKE(dalloc(e, &e->d_inv, n * n * 8));
+    CKE(dalloc(e, &e->d_rates, C * 8));
+    CKE(dalloc(e, &e->d_props, C * 8));
+    CKE(dalloc(e, &e->d_tip, (S + 1) * n * 8));
+    CKE(dalloc(e, &e->d_freq, e->Ppad * 8));
+    CKE(dalloc(e, &e->d_invar, e->Ppad * 8));
+    CKE(dalloc(e, &e->d_states, s.states));
+    CKE(dalloc(e, &e->d_ops, s.ops));
     e->npad = (int)round_up(n, 4);
     e->bp = C * e->npad;
     if (is_mixed(cfg)) {
         e->op_stride32 = s.op_stride;
-        CKE(cudaMalloc(&e->d_part32, (long long)cfg->nslots * e->Ppad * e->bp * 4));
-        CKE(cudaMalloc(&e->d_exp, (long long)cfg->nslots * e->Ppad * 4));
-        CKE(cudaMalloc(&e->d_opmats32, s.opmats));
-        CKE(cudaMalloc(&e->d_theta32, B * e->Ppad * 4));
-        CKE(cudaMalloc(&e->d_pi, n * 8));
+        CKE(dalloc(e, &e->d_part32, (long long)cfg->nslots * e->Ppad * e->bp * 4));
+        CKE(dalloc(e, &e->d_exp, (long long)cfg->nslots * e->Ppad * 4));
+        CKE(dalloc(e, &e->d_opmats32, s.opmats));
+        CKE(dalloc(e, &e->d_theta32, B * e->Ppad * 4));
+        CKE(dalloc(e, &e->d_pi, n * 8));
         // padding states of every slot stay zero: finite inputs for the float4 matvecs
         CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
         CKE(cudaMemsetAsync(e->d_exp, 0, (long long)cfg->nslots * e->Ppad * 4, e->st));
         CKE(cudaMemsetAsync(e->d_opmats32, 0, s.opmats, e->st));
     } else {
-        CKE(cudaMalloc(&e->d_part, s.part));
-        CKE(cudaMalloc(&e->d_scale, s.scale));
-        CKE(cudaMalloc(&e->d_opmats, s.opmats));
+        CKE(dalloc(e, &e->d_part, s.part));
+        CKE(dalloc(e, &e->d_scale, s.scale));
+        CKE(dalloc(e, &e->d_opmats, s.opmats));
         CKE(cudaMemsetAsync(e->d_scale, 0, s.scale, e->st));
     }
-    CKE(cudaMalloc(&e->d_theta, is_mixed(cfg) ? 8 : B * e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_bscale, e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_plh, e->Ppad * 8));
-    CKE(cudaMalloc(&e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
-    CKE(cudaMalloc(&e->d_ticket, 64));  // ticket at byte 0, status word at byte 32
+    CKE(dalloc(e, &e->d_theta, is_mixed(cfg) ? 8 : B * e->Ppad * 8));
+    CKE(dalloc(e, &e->d_bscale, e->Ppad * 8));
+    CKE(dalloc(e, &e->d_plh, e->Ppad * 8));
+    CKE(dalloc(e, &e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
+    CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at byte 32
     e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
-    CKE(cudaMalloc(&e->d_red_out, kRedSlots * 8));
-    CKE(cudaMallocHost(&e->h_ops, s.ops));
-    CKE(cudaMallocHost(&e->h_red_out, kRedSlots * 8 + 16));
+    CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
+    CKE(halloc(e, &e->h_ops, s.ops));
+    CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
     CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
     CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
     CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
@@ -597,8 +651,8 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable) {
 
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
     if (!e || !(patterns_per_cta == 0 || patterns_per_cta == 32 || patterns_per_cta == 64 ||
-                patterns_per_cta == 128)) {
-        set_error("tile must be 0, 32, 64 or 128 patterns");
+                patterns_per_cta == 128 || (patterns_per_cta == 1 && e->n == 4))) {
+        set_error("tile must be 0, 32, 64 or 128 patterns (1 = one thread per pattern, 4-state models)");
         return IQGPU_ERR_ARG;
     }
     e->tile = patterns_per_cta;

@@ -1,0 +1,201 @@
+// Mixed-precision traversal specialised for 4-state (DNA) models.
+//
+// With n = 4 a category's update is 32 multiply-adds, so the kernel is bound
+// by memory latency, not arithmetic: one thread owns one pattern and all of
+// its rate categories. A thread then issues every child load of an op at once
+// (ncat float4 per child, each warp touching whole 128-byte lines), finds the
+// pattern's maximum without any cross-thread exchange, and rescales and
+// stores its block in registers; the only barrier per op is the one that
+// publishes the op's TMA-staged P(t) matrices (double-buffered, so op k+1's
+// copy is in flight while op k computes).
+#include <cuda_runtime.h>
+
+#include "mixed.cuh"
+
+namespace iqg {
+
+constexpr int kDnaTile = 128;  // patterns (= threads) per CTA
+constexpr int kDnaMaxCat = 4;  // register-resident categories (ncat <= 4 uses this kernel)
+
+template <int EPI>
+__global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
+    constexpr int n = 4, npad = 4;
+    const int C = P.ncat, S = P.state_unknown;
+    const long long p = (long long)blockIdx.x * kDnaTile + threadIdx.x;
+    const long long ld = P.ldp;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;  // + c*32
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(S + 1) * C * npad;
+    const unsigned pbytes = (unsigned)(2 * PM * 4);
+    __shared__ __align__(128) float sP[2][2 * kDnaMaxCat * 16];
+    __shared__ unsigned long long bars[2];
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        if (P.nops > 0) {
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(sP[0], P.opmats, pbytes, &bars[0]);
+        }
+    }
+    __syncthreads();
+
+    for (int k = 0; k < P.nops; ++k) {
+        const int buf = k & 1;
+        const bool lost = !mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
+        if (__syncthreads_or(lost)) {
+            if (threadIdx.x == 0) {
+                atomicExch(P.status, kStatusTimeout);
+                mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
+            }
+            return;
+        }
+        if (threadIdx.x == 0 && k + 1 < P.nops) {
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[buf ^ 1], pbytes);
+            tma_load_1d(sP[buf ^ 1], P.opmats + (long long)(k + 1) * P.op_stride, pbytes, &bars[buf ^ 1]);
+        }
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const float *gbase = P.opmats + (long long)k * P.op_stride;
+        const float *PL = sP[buf], *PR = sP[buf] + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
+        if (lref >= 0 && rref < 0) {
+            int t = lref; lref = rref; rref = t;
+            const float *q = PL; PL = PR; PR = q;
+            q = TL; TL = TR; TR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
+        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
+        const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
+        const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
+        float4 out[kDnaMaxCat];
+        float mx = 0.f;
+        // issue every load of the op first: ncat float4 per child
+        float4 lv[kDnaMaxCat], rv[kDnaMaxCat];
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                lv[c] = lint ? *reinterpret_cast<const float4 *>(Lp + c * 32) : ld4(tl + c * npad);
+                rv[c] = rint ? *reinterpret_cast<const float4 *>(Rp + c * 32) : ld4(tr + c * npad);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                float yl[4], yr[4];
+                const float *pl = PL + c * 16, *pr = PR + c * 16;
+#pragma unroll
+                for (int x = 0; x < 4; x++) {
+                    if (lint) {
+                        const float4 m = *reinterpret_cast<const float4 *>(pl + x * 4);
+                        yl[x] = fmaf(m.x, lv[c].x, fmaf(m.y, lv[c].y, fmaf(m.z, lv[c].z, m.w * lv[c].w)));
+                    } else {
+                        yl[x] = x == 0 ? lv[c].x : x == 1 ? lv[c].y : x == 2 ? lv[c].z : lv[c].w;
+                    }
+                    if (rint) {
+                        const float4 m = *reinterpret_cast<const float4 *>(pr + x * 4);
+                        yr[x] = fmaf(m.x, rv[c].x, fmaf(m.y, rv[c].y, fmaf(m.z, rv[c].z, m.w * rv[c].w)));
+                    } else {
+                        yr[x] = x == 0 ? rv[c].x : x == 1 ? rv[c].y : x == 2 ? rv[c].z : rv[c].w;
+                    }
+                }
+                out[c] = make_float4(yl[0] * yr[0], yl[1] * yr[1], yl[2] * yr[2], yl[3] * yr[3]);
+                mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
+            }
+        }
+        int sh = 0;
+        float mul = 1.f;
+        if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
+            int ex;
+            frexpf(mx, &ex);
+            sh = 1 - ex;
+            mul = __int_as_float((127 + sh) << 23);
+        }
+        float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                float4 v = out[c];
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(dad + c * 32) = v;
+            }
+        }
+        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+        P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+    }
+
+    if constexpr (EPI == EPI_NONE) return;
+
+    const float *pa = P.part + (long long)P.a * P.slot_floats + pbase;
+    const bool btip = P.b < 0;
+    const float *pb = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pbase;
+    const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+    const int ea = P.expo[(long long)P.a * ld + p];
+    const int eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
+
+    if constexpr (EPI == EPI_THETA) {
+        float *th = P.theta + p;
+        for (int c = 0; c < C; c++) {
+            const float4 av = *reinterpret_cast<const float4 *>(pa + c * 32);
+            const float4 bv = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + c * 32);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float4 u = ld4(P.inv32 + i * npad);
+                const float ua = fmaf(u.x, av.x, fmaf(u.y, av.y, fmaf(u.z, av.z, u.w * av.w)));
+                const float ub = btip ? (float)__ldg(P.tip_lh + (long long)sb * n + i)
+                                      : fmaf(u.x, bv.x, fmaf(u.y, bv.y, fmaf(u.z, bv.z, u.w * bv.w)));
+                th[(long long)(c * n + i) * ld] = ua * ub;
+            }
+        }
+        P.buffer_scale[p] = (double)(ea + eb) * kLn2;
+        return;
+    } else {
+        const float *base = P.opmats + (long long)P.nops * P.op_stride;  // branch matrices, child 0 = b
+        double lh = 0.0;
+        for (int c = 0; c < C; c++) {
+            const float4 av = *reinterpret_cast<const float4 *>(pa + c * 32);
+            float w[4];
+            if (btip) {
+                const float4 t = ld4(base + 2 * PM + (long long)sb * C * npad + c * npad);
+                w[0] = t.x; w[1] = t.y; w[2] = t.z; w[3] = t.w;
+            } else {
+                const float4 bv = *reinterpret_cast<const float4 *>(pb + c * 32);
+#pragma unroll
+                for (int x = 0; x < 4; x++) {
+                    const float4 m = ld4(base + (c * n + x) * npad);
+                    w[x] = fmaf(m.x, bv.x, fmaf(m.y, bv.y, fmaf(m.z, bv.z, m.w * bv.w)));
+                }
+            }
+            float lc = (float)__ldg(P.pi) * av.x * w[0];
+            lc = fmaf((float)__ldg(P.pi + 1) * av.y, w[1], lc);
+            lc = fmaf((float)__ldg(P.pi + 2) * av.z, w[2], lc);
+            lc = fmaf((float)__ldg(P.pi + 3) * av.w, w[3], lc);
+            lh = fma((double)lc, P.props[c], lh);
+        }
+        lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));
+        const double plh = log(lh) + (double)(ea + eb) * kLn2;
+        P.pattern_lh[p] = plh;
+        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        if (p < P.nptn) {
+            const double f = P.freq[p];
+            v[0] = plh * f;
+            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+            v[2] = isfinite(plh) ? 0.0 : 1.0;
+        }
+        mix_grid_reduce(v, P.red);
+    }
+}
+
+int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi) {
+    const int grid = (int)(e->Ppad / kDnaTile);
+    switch (epi) {
+    case EPI_NONE: k_traverse_dna<EPI_NONE><<<grid, kDnaTile, 0, e->st>>>(P); break;
+    case EPI_LNL: k_traverse_dna<EPI_LNL><<<grid, kDnaTile, 0, e->st>>>(P); break;
+    default: k_traverse_dna<EPI_THETA><<<grid, kDnaTile, 0, e->st>>>(P); break;
+    }
+    return cuda_fail(cudaGetLastError(), "traverse_dna");
+}
+
+}  // namespace iqg

@@ -309,12 +309,17 @@ static int dispatch_mix(iqgpu_engine *e, const MixParams &P) {
     }
 }
 
+int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
+
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
     MixParams P = mix_params(e, nops);
     P.a = a;
     P.b = b;
     P.len = len;
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    // 4-state models: one thread per pattern and all its categories, unless a
+    // per-category tile was chosen explicitly
+    if (e->n == 4 && e->C <= 4 && (e->tile == 0 || e->tile == 1)) return launch_traverse_dna(e, P, epi);
     switch (epi) {
     case EPI_NONE: return dispatch_mix<EPI_NONE>(e, P);
     case EPI_LNL: return dispatch_mix<EPI_LNL>(e, P);

@@ -176,3 +176,70 @@ def bootstrap_weights(freq, nreps, rng):
     nsites = int(round(freq.sum()))
     p = freq / freq.sum()
     return rng.multinomial(nsites, p, size=nreps).astype(np.float32)
+
+
+def _preorder_edges(ntaxa, edges):
+    """Edges oriented away from the first internal node, in preorder."""
+    adj = adjacency(ntaxa, edges)
+    root = ntaxa
+    par, ch, order = [], [], []
+    stack = [(root, -1)]
+    while stack:
+        node, dad = stack.pop()
+        for (nb, k) in adj[node]:
+            if nb == dad:
+                continue
+            par.append(node)
+            ch.append(nb)
+            order.append(k)
+            stack.append((nb, node))
+    return np.array(par, np.int32), np.array(ch, np.int32), np.array(order)
+
+
+def device_alignment(ntaxa, edges, lengths, model, nsites, seed, device=0):
+    """Simulate on the GPU (iqgpu_simulate); returns uint8 states (ntaxa, nsites)."""
+    import ctypes as ct
+
+    from . import engine
+    par, ch, order = _preorder_edges(ntaxa, edges)
+    n, C = model.nstates, model.ncat
+    cum = np.empty((len(order), C, n, n), np.float32)
+    for j, k in enumerate(order):
+        for c in range(C):
+            P = np.clip(model.trans_matrix(model.rates[c] * lengths[k]), 0.0, None)
+            P /= P.sum(axis=1, keepdims=True)
+            cp = np.cumsum(P, axis=1)
+            cp[:, -1] = 1.0
+            cum[j, c] = cp
+    cpi = np.cumsum(model.pi).astype(np.float32)
+    cpi[-1] = 1.0
+    out = np.empty((ntaxa, nsites), np.uint8)
+    L = engine.lib()
+    f = L.iqgpu_simulate
+    f.argtypes = [ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                  ct.c_void_p, ct.c_uint64, ct.c_int32, ct.c_void_p]
+    f.restype = ct.c_int
+    engine._check(f(ntaxa, nsites, n, C, par.ctypes.data, ch.ctypes.data, cum.ctypes.data, cpi.ctypes.data,
+                    int(seed) & 0xFFFFFFFFFFFFFFFF, device, out.ctypes.data))
+    return out
+
+
+def serving_dataset(kind, ntaxa, nsites, seed, compress_below=20000):
+    """A serving request: DNA GTR+G4 or protein LG+G4 simulated on the device.
+    Alignments up to ``compress_below`` sites are compressed into patterns;
+    larger ones keep one pattern per site (weight 1), the same likelihood."""
+    rng = np.random.default_rng(seed)
+    if kind == "dna":
+        model = models.gtr_model(rng.uniform(0.5, 3.0, size=6), rng.dirichlet([5.0] * 4), 0.5)
+        mean_bl = 0.1
+    else:
+        _, lg_pi = models.lg_exchangeabilities()
+        model = models.lg_model(lg_pi, 0.8)
+        mean_bl = 0.05
+    edges, lengths = yule_tree(ntaxa, mean_bl, rng)
+    aln = device_alignment(ntaxa, edges, lengths, model, nsites, int(rng.integers(1 << 62)))
+    if nsites <= compress_below:
+        pats, freq = compress_patterns(aln)
+    else:
+        pats, freq = aln, np.ones(nsites)
+    return Dataset(f"{kind}{ntaxa}x{nsites}", ntaxa, nsites, edges, lengths, model, pats, freq)
