@@ -167,6 +167,10 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
  * kernel; 0 restores the default. Chosen by the autotuner in
  * iqtree2_gb300/autotune.py; results do not depend on it. */
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
+/* Schedule of the mixed-precision traversal: 0 = one fused launch walking the
+ * whole op list per pattern tile; 1 = one launch per tree level, all of the
+ * level's (op, tile) pairs in flight together. Results do not depend on it. */
+int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
 /* ---- batched evaluation ------------------------------------------------- */

@@ -106,6 +106,9 @@ struct iqgpu_engine {
     double h_evec[iqg::kMaxStates * iqg::kMaxStates];
     bool have_pi, tipstd_ready;
     int tile;                 // patterns per CTA of the mixed traversal (0 = default)
+    bool level_sync;          // mixed traversal schedule: one launch per tree level
+    int *level_off;           // [max_ops + 2] first op of each level (ops are uploaded level-sorted)
+    int nlevels;
     int *d_status;            // device status word (bounded waits that gave up)
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;

@@ -2,6 +2,7 @@
 // points that stand in for PhyloTree's kernel function pointers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -139,6 +140,7 @@ static void free_engine(iqgpu_engine *e) {
         std::free(e->h_ops);
         std::free(e->h_red_out);
     }
+    std::free(e->level_off);
     if (e->ev_t0) cudaEventDestroy(e->ev_t0);
     if (e->ev_t1) cudaEventDestroy(e->ev_t1);
     if (e->own_st) cudaStreamDestroy(e->own_st);
@@ -207,6 +209,12 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     e->Ppad = s.Ppad;
     e->nblk = (int)(s.Ppad / kTPB);
     e->op_stride = s.op_stride;
+    e->level_off = static_cast<int *>(std::malloc(sizeof(int) * ((size_t)cfg->max_ops + 2)));
+    if (!e->level_off) {
+        delete e;
+        set_error("host allocation failed");
+        return IQGPU_ERR_OOM;
+    }
     auto fail = [&](cudaError_t err, const char *what) {
         int r = cuda_fail(err, what);
         if (err == cudaErrorMemoryAllocation) r = IQGPU_ERR_OOM;
@@ -399,14 +407,43 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
             set_error("bad traversal entry " + std::to_string(k));
             return IQGPU_ERR_ARG;
         }
-        OpDev &d = e->h_ops[k];
+    }
+    // Mixed engines take the ops in tree-level order (a valid post-order: every
+    // child is produced in a lower level), so that a level-synchronous launch
+    // can run each level's independent ops together.
+    std::vector<int> order(nops), level(nops, 1);
+    for (int k = 0; k < nops; k++) order[k] = k;
+    e->nlevels = 0;
+    if (is_mixed(&e->cfg) && nops > 0) {
+        std::vector<int> producer_level(e->cfg.nslots, 0);  // level of the op writing each slot in this list
+        int maxl = 0;
+        for (int k = 0; k < nops; k++) {
+            int l = 1;
+            for (int j = 0; j < 2; j++)
+                if (ops[k].child[j] >= 0) l = std::max(l, producer_level[ops[k].child[j]] + 1);
+            level[k] = l;
+            producer_level[ops[k].dad_slot] = l;
+            maxl = std::max(maxl, l);
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return level[x] < level[y]; });
+        int cur = 0;
+        for (int i = 0; i < nops; i++) {
+            while (cur < level[order[i]]) e->level_off[cur++] = i;
+        }
+        e->level_off[cur] = nops;
+        e->nlevels = maxl;  // level l (1-based) spans [level_off[l-1], level_off[l])
+    }
+    for (int i = 0; i < nops; i++) {
+        const int k = order[i];
+        const iqgpu_op &o = ops[k];
+        OpDev &d = e->h_ops[i];
         d.dad_slot = o.dad_slot;
         d.child[0] = o.child[0];
         d.child[1] = o.child[1];
         d.pad = 0;
         d.len[0] = o.len[0];
         d.len[1] = o.len[1];
-        d.mat_off = (long long)k * e->op_stride;
+        d.mat_off = (long long)i * e->op_stride;
         d.pad2 = 0;
     }
     int total = nops;
@@ -656,6 +693,12 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
         return IQGPU_ERR_ARG;
     }
     e->tile = patterns_per_cta;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    e->level_sync = level_sync != 0;
     return IQGPU_OK;
 }
 

@@ -42,6 +42,7 @@ struct MixParams {
     double *buffer_scale;
     Reduce red;
     int *status;            // set to a nonzero code when a bounded wait gives up
+    int branch_op;          // op block holding the evaluated branch's matrices (= total ops)
 };
 
 // ---- TMA bulk copies and mbarriers (inline PTX, sm_90+ forms used on sm_103a) ----

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
         P.buffer_scale[p] = (double)(ea + eb) * kLn2;
         return;
     } else {
-        const float *base = P.opmats + (long long)P.nops * P.op_stride;  // branch matrices, child 0 = b
+        const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
         double lh = 0.0;
         for (int c = 0; c < C; c++) {
             const float4 av = *reinterpret_cast<const float4 *>(pa + c * 32);

@@ -1,16 +1,23 @@
-// Mixed-precision path, part 2: the traversal kernel on CUDA cores.
+// Mixed-precision path, part 2: the traversal kernels on CUDA cores.
 //
-// A CTA owns TP consecutive patterns and runs TP*ncat threads: warp w handles
-// 32 patterns of one rate category, so the transition-matrix rows it reads
-// are warp-uniform (shared-memory broadcast) and its float4 loads of the
-// children are whole 128-byte lines. Each op's two P(t) blocks are staged in
-// shared memory by a 1-D TMA bulk copy; with two buffers the copy for op k+1
-// is in flight while op k computes. Each thread keeps its category's outputs
-// in registers until the pattern's largest entry over all categories is
-// known (one shared-memory max across the category warps), then applies the
-// exact power-of-two rescale and stores once. The whole post-order op list
-// runs in one launch: a pattern's partials only depend on the same pattern's
-// children, computed earlier by the same threads.
+// Thread mapping (both schedules): a CTA owns TP consecutive patterns and runs
+// TP*ncat threads; warp w handles 32 patterns of one rate category, so the
+// transition-matrix rows it reads are warp-uniform (shared-memory broadcast)
+// and its float4 loads of the children are whole 128-byte lines. Each thread
+// keeps its category's outputs in registers until the pattern's largest entry
+// over all categories is known (one shared-memory max across the category
+// warps), then applies the exact power-of-two rescale and stores once.
+//
+// Two schedules of the same per-op body:
+//  * fused: one CTA walks the whole post-order op list for its patterns (a
+//    pattern's partials depend only on the same pattern's children), with
+//    each op's P(t) blocks staged in shared memory by a TMA bulk copy that
+//    runs one op ahead (double buffer). One launch; children are usually still
+//    in L2 when their parent reads them; latency per op is exposed.
+//  * level-synchronous: ops are grouped by tree level (all ops of a level are
+//    independent); one launch per level runs every (op, pattern tile) pair of
+//    the level as its own CTA, so many independent ops are in flight per SM.
+// The autotuner picks the schedule and the tile per workload.
 #include <cuda_runtime.h>
 
 #include "mixed.cuh"
@@ -35,186 +42,147 @@ __device__ __forceinline__ float dot4(const float4 a, const float4 b, float acc)
     return fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc))));
 }
 
-// NQ = npad/4 float4 chunks per category held in registers (1 DNA, 5 protein);
-// NQ = 0 is the chunked path for larger n (codon).
-template <int NQ, int EPI>
-__global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const int TP, const int nbuf) {
+// One op for this thread's (pattern, category): sP holds the op's two P(t)
+// blocks; smax is this op's [ncat*TP] scratch for the cross-category maximum.
+// Contains one __syncthreads (all threads of the CTA must call it).
+template <int NQ>
+__device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float *sP, float *smax, int c, int pl,
+                                         long long p, long long pbase, int TP) {
     constexpr int XC = 16;
     const int n = P.n, npad = P.npad, C = P.ncat, S = P.state_unknown;
     const int nq = NQ ? NQ : npad >> 2;
-    const int c = threadIdx.x / TP;   // warp-uniform (TP is a multiple of 32)
-    const int pl = threadIdx.x % TP;
-    const long long p = (long long)blockIdx.x * TP + pl;
     const long long ld = P.ldp;
-    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * nq * 32;
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(S + 1) * C * npad;
-    const unsigned pbytes = (unsigned)(2 * PM * 4);  // both children's P blocks of one op
-    extern __shared__ __align__(128) float smem[];   // [nbuf][2*PM] P(t) staging
-    __shared__ unsigned long long bars[2];
-    __shared__ float s_max[2][512];
-    __shared__ float s_lc[512];
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_mbar_init();
-        if (P.nops > 0) {
-            mbar_expect_tx(&bars[0], pbytes);
-            tma_load_1d(smem, P.opmats, pbytes, &bars[0]);
-        }
+    const OpDev op = P.ops[k];
+    int lref = op.child[0], rref = op.child[1];
+    const float *gbase = P.opmats + (long long)k * P.op_stride;
+    const float *PL = sP, *PR = sP + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
+    if (lref >= 0 && rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+        int t = lref; lref = rref; rref = t;
+        const float *q = PL; PL = PR; PR = q;
+        q = TL; TL = TR; TR = q;
     }
-    __syncthreads();
-
-    for (int k = 0; k < P.nops; ++k) {
-        const int buf = nbuf == 2 ? (k & 1) : 0;
-        const unsigned parity = nbuf == 2 ? ((k >> 1) & 1) : (k & 1);
-        // every thread observes the copy's completion itself; the vote makes the
-        // give-up decision uniform across the CTA  -- barrier (A)
-        const bool lost = !mbar_wait(&bars[buf], parity, kWaitPolls);
-        if (__syncthreads_or(lost)) {
-            if (threadIdx.x == 0) {
-                atomicExch(P.status, kStatusTimeout);
-                mbar_wait(&bars[buf], parity, kWaitPolls);  // last bounded wait for the copy in flight
-            }
-            return;
-        }
-        if (nbuf == 2 && threadIdx.x == 0 && k + 1 < P.nops) {
-            // buffer (k+1)&1 was last read in op k-1, before barrier (A)
-            fence_proxy_async_smem();
-            mbar_expect_tx(&bars[(k + 1) & 1], pbytes);
-            tma_load_1d(smem + ((k + 1) & 1) * 2 * PM, P.opmats + (long long)(k + 1) * P.op_stride, pbytes,
-                        &bars[(k + 1) & 1]);
-        }
-        const OpDev op = P.ops[k];
-        int lref = op.child[0], rref = op.child[1];
-        const float *gbase = P.opmats + (long long)k * P.op_stride;
-        const float *sP = smem + buf * 2 * PM;
-        const float *PL = sP, *PR = sP + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
-        if (lref >= 0 && rref < 0) {
-            int t = lref; lref = rref; rref = t;
-            const float *q = PL; PL = PR; PR = q;
-            q = TL; TL = TR; TR = q;
-        }
-        const bool lint = lref >= 0, rint = rref >= 0;
-        float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
-        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
-        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
-        const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad + c * npad;
-        const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad + c * npad;
-        const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
-        float cmax = 0.f;
-        float4 out[NQ ? NQ : 1];
-        if constexpr (NQ > 0) {
-            float4 lv[NQ], rv[NQ];
-            if (lint) {
+    const bool lint = lref >= 0, rint = rref >= 0;
+    float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+    const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
+    const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
+    const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad + c * npad;
+    const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad + c * npad;
+    const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
+    float cmax = 0.f;
+    float4 out[NQ ? NQ : 1];
+    if constexpr (NQ > 0) {
+        float4 lv[NQ], rv[NQ];
+        if (lint) {
 #pragma unroll
-                for (int q = 0; q < NQ; q++) lv[q] = *reinterpret_cast<const float4 *>(Lp + q * 32);
-            }
-            if (rint) {
+            for (int q = 0; q < NQ; q++) lv[q] = *reinterpret_cast<const float4 *>(Lp + q * 32);
+        }
+        if (rint) {
 #pragma unroll
-                for (int q = 0; q < NQ; q++) rv[q] = *reinterpret_cast<const float4 *>(Rp + q * 32);
+            for (int q = 0; q < NQ; q++) rv[q] = *reinterpret_cast<const float4 *>(Rp + q * 32);
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            float o[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int x = 4 * q + j;
+                float v = 0.f;
+                if (x < n) {
+                    const float yl = lint ? row_dot_s<NQ>(PLc + x * npad, lv) : __ldg(tl + x);
+                    const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : __ldg(tr + x);
+                    v = yl * yr;
+                }
+                o[j] = v;
+                cmax = fmaxf(cmax, v);
+            }
+            out[q] = make_float4(o[0], o[1], o[2], o[3]);
+        }
+    } else {
+        for (int x0 = 0; x0 < npad; x0 += XC) {
+            float al[XC], ar[XC];
+#pragma unroll
+            for (int j = 0; j < XC; j++) { al[j] = 0.f; ar[j] = 0.f; }
+            for (int q = 0; q < nq; q++) {
+                const float4 l4 = lint ? *reinterpret_cast<const float4 *>(Lp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 r4 = rint ? *reinterpret_cast<const float4 *>(Rp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < XC; j++) {
+                    const int x = x0 + j;
+                    if (x < n) {
+                        if (lint) al[j] = dot4(*reinterpret_cast<const float4 *>(PLc + x * npad + 4 * q), l4, al[j]);
+                        if (rint) ar[j] = dot4(*reinterpret_cast<const float4 *>(PRc + x * npad + 4 * q), r4, ar[j]);
+                    }
+                }
             }
 #pragma unroll
-            for (int q = 0; q < NQ; q++) {
+            for (int j = 0; j < XC; j += 4) {
                 float o[4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int x = 4 * q + j;
+                for (int jj = 0; jj < 4; jj++) {
+                    const int x = x0 + j + jj;
                     float v = 0.f;
                     if (x < n) {
-                        const float yl = lint ? row_dot_s<NQ>(PLc + x * npad, lv) : __ldg(tl + x);
-                        const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : __ldg(tr + x);
+                        const float yl = lint ? al[j + jj] : __ldg(tl + x);
+                        const float yr = rint ? ar[j + jj] : __ldg(tr + x);
                         v = yl * yr;
                     }
-                    o[j] = v;
+                    o[jj] = v;
                     cmax = fmaxf(cmax, v);
                 }
-                out[q] = make_float4(o[0], o[1], o[2], o[3]);
+                if (x0 + j < npad)
+                    *reinterpret_cast<float4 *>(dad + ((x0 + j) >> 2) * 32) = make_float4(o[0], o[1], o[2], o[3]);
             }
-        } else {
-            for (int x0 = 0; x0 < npad; x0 += XC) {
-                float al[XC], ar[XC];
-#pragma unroll
-                for (int j = 0; j < XC; j++) { al[j] = 0.f; ar[j] = 0.f; }
-                for (int q = 0; q < nq; q++) {
-                    const float4 l4 = lint ? *reinterpret_cast<const float4 *>(Lp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    const float4 r4 = rint ? *reinterpret_cast<const float4 *>(Rp + q * 32) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                    for (int j = 0; j < XC; j++) {
-                        const int x = x0 + j;
-                        if (x < n) {
-                            if (lint) al[j] = dot4(*reinterpret_cast<const float4 *>(PLc + x * npad + 4 * q), l4, al[j]);
-                            if (rint) ar[j] = dot4(*reinterpret_cast<const float4 *>(PRc + x * npad + 4 * q), r4, ar[j]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < XC; j += 4) {
-                    float o[4];
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) {
-                        const int x = x0 + j + jj;
-                        float v = 0.f;
-                        if (x < n) {
-                            const float yl = lint ? al[j + jj] : __ldg(tl + x);
-                            const float yr = rint ? ar[j + jj] : __ldg(tr + x);
-                            v = yl * yr;
-                        }
-                        o[jj] = v;
-                        cmax = fmaxf(cmax, v);
-                    }
-                    if (x0 + j < npad)
-                        *reinterpret_cast<float4 *>(dad + ((x0 + j) >> 2) * 32) = make_float4(o[0], o[1], o[2], o[3]);
-                }
-            }
-        }
-        // pattern maximum over the category warps
-        s_max[k & 1][threadIdx.x] = cmax;
-        __syncthreads();  // (B) every thread is done with this op's P(t)
-        if (nbuf == 1 && threadIdx.x == 0 && k + 1 < P.nops) {
-            fence_proxy_async_smem();
-            mbar_expect_tx(&bars[0], pbytes);
-            tma_load_1d(smem, P.opmats + (long long)(k + 1) * P.op_stride, pbytes, &bars[0]);
-        }
-        float mx = 0.f;
-        for (int cc = 0; cc < C; cc++) mx = fmaxf(mx, s_max[k & 1][cc * TP + pl]);
-        int sh = 0;
-        float mul = 1.f;
-        if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
-            int ex;
-            frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
-            sh = 1 - ex;      // mx * 2^sh in [1, 2)
-            mul = __int_as_float((127 + sh) << 23);
-        }
-        if constexpr (NQ > 0) {
-#pragma unroll
-            for (int q = 0; q < NQ; q++) {
-                float4 v = out[q];
-                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-                *reinterpret_cast<float4 *>(dad + q * 32) = v;
-            }
-        } else if (sh) {
-            for (int q = 0; q < nq; q++) {
-                float4 v = *reinterpret_cast<float4 *>(dad + q * 32);
-                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-                *reinterpret_cast<float4 *>(dad + q * 32) = v;
-            }
-        }
-        if (c == 0) {
-            // exponents are read and written by the category-0 thread of the pattern only
-            const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
-            P.expo[(long long)op.dad_slot * ld + p] = e - sh;
         }
     }
+    // pattern maximum over the category warps
+    smax[c * TP + pl] = cmax;
+    __syncthreads();
+    float mx = 0.f;
+    for (int cc = 0; cc < C; cc++) mx = fmaxf(mx, smax[cc * TP + pl]);
+    int sh = 0;
+    float mul = 1.f;
+    if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
+        int ex;
+        frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
+        sh = 1 - ex;      // mx * 2^sh in [1, 2)
+        mul = __int_as_float((127 + sh) << 23);
+    }
+    if constexpr (NQ > 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            float4 v = out[q];
+            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+            *reinterpret_cast<float4 *>(dad + q * 32) = v;
+        }
+    } else if (sh) {
+        for (int q = 0; q < nq; q++) {
+            float4 v = *reinterpret_cast<float4 *>(dad + q * 32);
+            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+            *reinterpret_cast<float4 *>(dad + q * 32) = v;
+        }
+    }
+    if (c == 0) {
+        // exponents are read and written by the category-0 thread of the pattern only
+        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+        P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+    }
+}
 
-    if constexpr (EPI == EPI_NONE) return;
-
+// Branch epilogue (theta or lnL) for this thread's (pattern, category).
+template <int NQ, int EPI>
+__device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl, long long p, long long pbase, int TP,
+                                               float *s_lc) {
+    const int n = P.n, npad = P.npad, C = P.ncat, S = P.state_unknown;
+    const int nq = NQ ? NQ : npad >> 2;
+    const long long ld = P.ldp;
+    const long long PM = (long long)C * n * npad;
+    (void)S;
     const float *pa = P.part + (long long)P.a * P.slot_floats + pbase;
     const bool btip = P.b < 0;
     const float *pb = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pbase;
     const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
-
     if constexpr (EPI == EPI_THETA) {
         // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i in eigen space (tree/phylokernelnew.h:2048-2231)
         float *th = P.theta + p;
@@ -234,10 +202,9 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
             const int eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
             P.buffer_scale[p] = (double)(ea + eb) * kLn2;
         }
-        return;
     } else {
         // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
-        const float *base = P.opmats + (long long)P.nops * P.op_stride;  // branch matrices, child 0 = b
+        const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
         float lc = 0.f;
         for (int x = 0; x < n; x++) {
             float w;
@@ -275,11 +242,102 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
     }
 }
 
-// Patterns per CTA: the autotuned value when set (iqgpu_set_tile), else 32
-// (one warp per category; small CTAs let several CTAs per SM overlap one op's
-// loads with another's arithmetic around the per-op barriers). TP * ncat <= 512.
+// fused schedule: NQ = npad/4 float4 chunks per category held in registers
+// (1 DNA, 5 protein); NQ = 0 is the chunked path for larger n (codon)
+template <int NQ, int EPI>
+__global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const int TP, const int nbuf) {
+    const int C = P.ncat, npad = P.npad;
+    const int nq = NQ ? NQ : npad >> 2;
+    const int c = threadIdx.x / TP;   // warp-uniform (TP is a multiple of 32)
+    const int pl = threadIdx.x % TP;
+    const long long p = (long long)blockIdx.x * TP + pl;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * nq * 32;
+    const long long PM = (long long)C * P.n * npad;
+    const unsigned pbytes = (unsigned)(2 * PM * 4);  // both children's P blocks of one op
+    extern __shared__ __align__(128) float smem[];   // [nbuf][2*PM] P(t) staging
+    __shared__ unsigned long long bars[2];
+    __shared__ float s_max[2][512];
+    __shared__ float s_lc[512];
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        if (P.nops > 0) {
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(smem, P.opmats, pbytes, &bars[0]);
+        }
+    }
+    __syncthreads();
+
+    for (int k = 0; k < P.nops; ++k) {
+        const int buf = nbuf == 2 ? (k & 1) : 0;
+        const unsigned parity = nbuf == 2 ? ((k >> 1) & 1) : (k & 1);
+        // every thread observes the copy's completion itself; the vote makes the
+        // give-up decision uniform across the CTA -- barrier (A)
+        const bool lost = !mbar_wait(&bars[buf], parity, kWaitPolls);
+        if (__syncthreads_or(lost)) {
+            if (threadIdx.x == 0) {
+                atomicExch(P.status, kStatusTimeout);
+                mbar_wait(&bars[buf], parity, kWaitPolls);  // last bounded wait for the copy in flight
+            }
+            return;
+        }
+        if (nbuf == 2 && threadIdx.x == 0 && k + 1 < P.nops) {
+            // buffer (k+1)&1 was last read in op k-1, before barrier (A)
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[(k + 1) & 1], pbytes);
+            tma_load_1d(smem + ((k + 1) & 1) * 2 * PM, P.opmats + (long long)(k + 1) * P.op_stride, pbytes,
+                        &bars[(k + 1) & 1]);
+        }
+        mixed_op<NQ>(P, k, smem + buf * 2 * PM, s_max[k & 1], c, pl, p, pbase, TP);  // contains barrier (B)
+        if (nbuf == 1 && threadIdx.x == 0 && k + 1 < P.nops) {
+            // every thread passed (B): nobody reads this op's P(t) any more
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(smem, P.opmats + (long long)(k + 1) * P.op_stride, pbytes, &bars[0]);
+        }
+    }
+    if constexpr (EPI != EPI_NONE) mixed_epilogue<NQ, EPI>(P, c, pl, p, pbase, TP, s_lc);
+}
+
+// level-synchronous schedule: CTA (x, y) computes op op0+y for pattern tile x
+template <int NQ>
+__global__ void __launch_bounds__(512) k_level_mixed(const MixParams P, const int TP, const int op0) {
+    const int C = P.ncat, npad = P.npad;
+    const int nq = NQ ? NQ : npad >> 2;
+    const int c = threadIdx.x / TP;
+    const int pl = threadIdx.x % TP;
+    const long long p = (long long)blockIdx.x * TP + pl;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * nq * 32;
+    const long long PM = (long long)C * P.n * npad;
+    const unsigned pbytes = (unsigned)(2 * PM * 4);
+    const int k = op0 + blockIdx.y;
+    extern __shared__ __align__(128) float smem[];
+    __shared__ unsigned long long bar;
+    __shared__ float s_max[512];
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(&bar, pbytes);
+        tma_load_1d(smem, P.opmats + (long long)k * P.op_stride, pbytes, &bar);
+    }
+    __syncthreads();
+    const bool lost = !mbar_wait(&bar, 0, kWaitPolls);
+    if (__syncthreads_or(lost)) {
+        if (threadIdx.x == 0) {
+            atomicExch(P.status, kStatusTimeout);
+            mbar_wait(&bar, 0, kWaitPolls);
+        }
+        return;
+    }
+    mixed_op<NQ>(P, k, smem, s_max, c, pl, p, pbase, TP);
+}
+
+// Patterns per CTA: the autotuned value when set (iqgpu_set_tile), else 32.
+// TP * ncat <= 512.
 static int mix_tile(const iqgpu_engine *e) {
-    int tp = e->tile > 0 ? e->tile : 32;
+    int tp = e->tile >= 32 ? e->tile : 32;
     while (tp > 32 && tp * e->C > 512) tp >>= 1;
     return tp;
 }
@@ -289,8 +347,9 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     const int TP = mix_tile(e);
     const int grid = (int)(e->Ppad / TP);
     const size_t pm_bytes = (size_t)2 * e->C * e->n * e->npad * 4;  // one op's two P(t) blocks
+    if (e->level_sync && EPI == EPI_NONE) return IQGPU_OK;  // ops ran level by level already
     const int nbuf = pm_bytes * 2 <= 96 * 1024 ? 2 : 1;
-    const size_t smem = nbuf * pm_bytes;
+    const size_t smem = (P.nops > 0 ? nbuf : 1) * pm_bytes;
     auto kern = k_traverse_mixed<NQ, EPI>;
     if (smem > 48 * 1024) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -300,8 +359,38 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     return cuda_fail(cudaGetLastError(), "traverse_mixed");
 }
 
+template <int NQ>
+static int launch_levels_t(iqgpu_engine *e, const MixParams &P) {
+    const int TP = mix_tile(e);
+    const int grid = (int)(e->Ppad / TP);
+    const size_t smem = (size_t)2 * e->C * e->n * e->npad * 4;
+    auto kern = k_level_mixed<NQ>;
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "level_mixed smem attribute");
+    }
+    for (int l = 0; l < e->nlevels; l++) {
+        const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+        if (nl <= 0) continue;
+        kern<<<dim3(grid, nl), TP * e->C, smem, e->st>>>(P, TP, op0);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "level_mixed");
+    }
+    return IQGPU_OK;
+}
+
 template <int EPI>
-static int dispatch_mix(iqgpu_engine *e, const MixParams &P) {
+static int dispatch_mix(iqgpu_engine *e, MixParams P) {
+    int rc = IQGPU_OK;
+    if (e->level_sync && P.nops > 0) {
+        switch (e->npad) {
+        case 4: rc = launch_levels_t<1>(e, P); break;
+        case 20: rc = launch_levels_t<5>(e, P); break;
+        default: rc = launch_levels_t<0>(e, P); break;
+        }
+        if (rc || EPI == EPI_NONE) return rc;
+        P.nops = 0;  // the epilogue runs alone; branch matrices stay at P.branch_op
+    }
     switch (e->npad) {
     case 4: return launch_mix_t<1, EPI>(e, P);
     case 20: return launch_mix_t<5, EPI>(e, P);
@@ -319,7 +408,7 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
     // 4-state models: one thread per pattern and all its categories, unless a
     // per-category tile was chosen explicitly
-    if (e->n == 4 && e->C <= 4 && (e->tile == 0 || e->tile == 1)) return launch_traverse_dna(e, P, epi);
+    if (e->n == 4 && e->C <= 4 && e->tile <= 1 && !e->level_sync) return launch_traverse_dna(e, P, epi);
     switch (epi) {
     case EPI_NONE: return dispatch_mix<EPI_NONE>(e, P);
     case EPI_LNL: return dispatch_mix<EPI_LNL>(e, P);

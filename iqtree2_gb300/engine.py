@@ -93,6 +93,7 @@ def lib():
         "iqgpu_set_timing": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
         "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
@@ -254,6 +255,9 @@ class Engine:
 
     def set_tile(self, patterns_per_cta):
         _check(lib().iqgpu_set_tile(self.h, int(patterns_per_cta)))
+
+    def set_schedule(self, level_sync):
+        _check(lib().iqgpu_set_schedule(self.h, int(bool(level_sync))))
 
     def nni_batch(self, cands, max_nr_step=10, min_bl=1e-6, max_bl=10.0):
         """cands: iterable of ((sub0..sub3), (scratch0, scratch1), (len0..len3), central)."""
