@@ -70,6 +70,37 @@ def topology_ops(ds):
     return topo, ops, topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
 
 
+def op_levels(ops):
+    """Tree levels of a post-order op list (every child produced in a lower level)."""
+    lev, top = {}, 0
+    for (dad, c0, c1, _, _) in ops:
+        l = 1 + max([lev.get(c, 0) for c in (c0, c1) if c >= 0] + [0])
+        lev[dad] = l
+        top = max(top, l)
+    return top
+
+
+def kernel_name(use_tc, n, tile):
+    if use_tc:
+        return "k_traverse_tc<64,2>" if n > 32 else ("k_traverse_tc<32,2>" if tile.endswith("/s2") else
+                                                      "k_traverse_tc<32,4>")
+    if tile.startswith("1/"):
+        return "k_traverse_dna<LNL>"
+    nq = {4: 1, 20: 5}.get((n + 3) // 4 * 4, 0)
+    return f"k_level_mixed<{nq}>" if "/level" in tile else f"k_traverse_mixed<{nq},LNL>"
+
+
+def tc_mma_flops(ops, n, C, nptn):
+    """MMA flops the split-TF32 kernel executes: per internal child, category
+    and 128-pattern tile, 3 passes of M=128 x N x K (N, K padded)."""
+    npad = (n + 3) // 4 * 4
+    N = 32 if npad <= 32 else 64
+    K = (npad + 7) // 8 * 8
+    tiles = (nptn + 127) // 128
+    children = sum((c0 >= 0) + (c1 >= 0) for (_, c0, c1, _, _) in ops)
+    return 3 * 2 * 128 * N * K * C * children * tiles
+
+
 def algorithmic_cost(ops, ntaxa, n, C, nptn, mixed=False):
     """Bytes and flops one traversal + root-lnL launch must move/execute.
 
@@ -280,13 +311,29 @@ def run_ours(args):
     eng64.close()
     b64, f64 = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=False)
 
-    # headline: mixed-precision path, pattern tile picked by the autotuner
+    # headline: mixed-precision path (split-TF32 tensor cores for 16..64 states,
+    # FP32 CUDA cores otherwise); schedule / pattern tile picked by the autotuner
     from iqtree2_gb300 import autotune
-    eng = make_engine(ds, topo, engine.F32, local, stream)
+    use_tc = args.precision == "tf32x3" or (args.precision == "auto" and 16 <= m.nstates <= 64)
+    prec = engine.TF32X3 if use_tc else engine.F32
+    beside = None
+    if use_tc:  # the FP32 CUDA-core kernel, reported beside the tensor-core headline
+        engc = make_engine(ds, topo, engine.F32, local, stream)
+        ctile, ctile_ms = autotune.tune(engc, ops_arr, a, b, length)
+        rc_ = measure_path(engc, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
+        beside = dict(kernel_ms=rc_["kern_avg_s"] * 1e3, lnl=rc_["lnl"], tile=ctile,
+                      value=updates_per_step * max(3, args.steps // 4) / (rc_["elapsed_ms"] / 1e3))
+        engc.close()
+    eng = make_engine(ds, topo, prec, local, stream)
     tile, tile_ms = autotune.tune(eng, ops_arr, a, b, length)
     r = measure_path(eng, ops_arr, a, b, length, args.steps, args.warmup, stream, local, dist)
     value = updates_per_step * args.steps * world / (r["elapsed_ms"] / 1e3)
     bmx, fmx = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=True)
+    level_sched = "/level" in tile
+    nlev = op_levels(ops)
+    # launches per step: P(t) preparation, [B-operand prep], traversal (one per level
+    # on the level schedule), [separate branch epilogue]
+    launches = 1 + (nlev if level_sched else 1) + (2 if use_tc else (1 if level_sched else 0))
 
     # end to end through the C ABI from host buffers: inputs copied each step, lnL read back
     e2e_steps = max(2, min(args.steps, 10))
@@ -308,16 +355,18 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["elapsed_ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, path="mixed: FP32 standard-basis partials, per-pattern 2^k exponents, "
-                       "FP64 exp/log/sums", nptn=ds.nptn, parallelism=f"replicas x{world}",
+        "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3" if use_tc else "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, path=("mixed: split-TF32 (3-pass) tcgen05 contraction, " if use_tc else
+                                       "mixed: FP32 CUDA-core contraction, ") +
+                       "FP32 standard-basis partials, per-pattern 2^k exponents, FP64 exp/log/sums",
+                       nptn=ds.nptn, parallelism=f"replicas x{world}",
                        tile=tile, tile_ms={str(k): v for k, v in tile_ms.items()},
                        l2="inputs larger than L2 (98 partials x 14 MB per step)"),
         "full_lnl_evals_per_s": 1e3 * args.steps / r["elapsed_ms"],
         "lnl": {"mixed": r["lnl"], "fp64": r64["lnl"], "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"])},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
-                     "kernel": "k_traverse_mixed<5,LNL>", "algorithmic_bytes_per_launch": bmx,
+                     "kernel": kernel_name(use_tc, m.nstates, tile), "algorithmic_bytes_per_launch": bmx,
                      "fp32_tflops": fmx / r["kern_avg_s"] / 1e12, "flops_per_launch": fmx,
                      "kernel_ms": r["kern_avg_s"] * 1e3},
         "fp64_path": {"value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
@@ -329,8 +378,13 @@ def run_ours(args):
         "e2e": {"value": updates_per_step / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": 8 * 4},
         "clocks": r["clocks"],
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches * args.steps,
     }
+    if use_tc:
+        mma = tc_mma_flops(ops, m.nstates, m.ncat, ds.nptn)
+        line["roofline"]["tensor"] = {"mma_flops_per_launch": mma, "mma_tflops": mma / r["kern_avg_s"] / 1e12,
+                                      "note": "executed split-TF32 MMA flops (3 passes, padded N/K)"}
+        line["cuda_core_f32"] = beside
     line["speedup_vs_fp64_path"] = value / line["fp64_path"]["value"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(ds, ops, a, b, length)
@@ -398,6 +452,8 @@ def main():
     ap.add_argument("--max-active", type=int, default=16)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--no-fp64-serve", action="store_true")
+    ap.add_argument("--precision", default="auto", choices=["auto", "f32", "tf32x3"],
+                    help="headline contraction: auto = split-TF32 tensor cores for 16..64 states")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = WORKLOADS[args.workload]

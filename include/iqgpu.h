@@ -171,6 +171,11 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * whole op list per pattern tile; 1 = one launch per tree level, all of the
  * level's (op, tile) pairs in flight together. Results do not depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync);
+/* Shared-memory ring depth (stages in flight per CTA) of the tensor-core
+ * traversal (precision IQGPU_TF32X3): 0 = default, 2 or 4 for models of up to
+ * 32 padded states (2 fits four CTAs per SM, 4 fits two); 61-state models
+ * always use 2. Chosen by the autotuner; results do not depend on it. */
+int iqgpu_set_stages(iqgpu_engine *e, int32_t stages);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
 /* ---- batched evaluation ------------------------------------------------- */

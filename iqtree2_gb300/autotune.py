@@ -3,7 +3,8 @@
 Candidates: the fused schedule (one launch walks the op list per pattern
 tile) and the level-synchronous schedule (one launch per tree level), each
 with 32/64/128 patterns per CTA, plus the one-thread-per-pattern kernel for
-4-state models. The best choice depends on the state count (registers per
+4-state models; on the tensor-core path (split TF32) the tile is the MMA's
+128 rows and only the schedule is tuned. The best choice depends on the state count (registers per
 thread), the category count, the number of patterns (how many CTAs fill the
 152 SMs) and the tree's depth. The tuner times each candidate with the
 engine's CUDA-event kernel timer on the real op list and keeps the fastest;
@@ -19,27 +20,41 @@ _cache: dict = {}
 
 
 def candidates(eng):
-    out = [(1, 0)] if eng.nstates == 4 and eng.ncat <= 4 else []
+    """(tile, schedule, stages) triples; stages only matter on the tensor-core path."""
+    if getattr(eng, "tensor_cores", False):  # one CTA = 128 patterns (the MMA's M)
+        depths = (2, 4) if eng.nstates <= 32 else (2,)
+        return [(0, sched, st) for sched in (0, 1) for st in depths]
+    out = [(1, 0, 0)] if eng.nstates == 4 and eng.ncat <= 4 else []
     for sched in (0, 1):
         for tile in TILES:
             if tile > 32 and tile * eng.ncat > 512:
                 continue
-            out.append((tile, sched))
+            out.append((tile, sched, 0))
     return out
 
 
+def label(cand):
+    tile, sched, stages = cand
+    return f"{tile}/{'level' if sched else 'fused'}" + (f"/s{stages}" if stages else "")
+
+
+def apply(eng, cand):
+    tile, sched, stages = cand
+    eng.set_tile(tile)
+    eng.set_schedule(sched)
+    eng.set_stages(stages)
+
+
 def tune(eng, ops_arr, a, b, length, reps=3):
-    """Pick and set the fastest (tile, schedule); returns (label, {label: ms})."""
-    key = (eng.nstates, eng.ncat, int(math.log2(max(eng.nptn, 1))), len(ops_arr))
+    """Pick and set the fastest candidate; returns (label, {label: ms})."""
+    key = (eng.nstates, eng.ncat, int(math.log2(max(eng.nptn, 1))), len(ops_arr), getattr(eng, "precision", 1))
     if key in _cache:
-        (tile, sched), times = _cache[key]
-        eng.set_tile(tile)
-        eng.set_schedule(sched)
-        return f"{tile}/{'level' if sched else 'fused'}", times
+        best, times = _cache[key]
+        apply(eng, best)
+        return label(best), times
     times, best, best_ms = {}, None, float("inf")
-    for tile, sched in candidates(eng):
-        eng.set_tile(tile)
-        eng.set_schedule(sched)
+    for cand in candidates(eng):
+        apply(eng, cand)
         eng.compute_likelihood(ops_arr, a, b, length)  # warm-up
         eng.set_timing(True)
         for _ in range(reps):
@@ -47,10 +62,9 @@ def tune(eng, ops_arr, a, b, length, reps=3):
         ms, n = eng.timing()
         eng.set_timing(False)
         ms /= max(n, 1)
-        times[f"{tile}/{'level' if sched else 'fused'}"] = ms
+        times[label(cand)] = ms
         if ms < best_ms:
-            best, best_ms = (tile, sched), ms
-    eng.set_tile(best[0])
-    eng.set_schedule(best[1])
+            best, best_ms = cand, ms
+    apply(eng, best)
     _cache[key] = (best, times)
-    return f"{best[0]}/{'level' if best[1] else 'fused'}", times
+    return label(best), times

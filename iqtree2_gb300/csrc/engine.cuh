@@ -110,6 +110,13 @@ struct iqgpu_engine {
     int *level_off;           // [max_ops + 2] first op of each level (ops are uploaded level-sorted)
     int nlevels;
     int *d_status;            // device status word (bounded waits that gave up)
+    // tensor-core contraction (precision IQGPU_TF32X3, 16 <= n <= 64)
+    bool tc;
+    float *d_tcb;             // per op: [child 2][C][hi, lo][NP*KP] P(t) in core-matrix order
+    long long tcb_stride;     // floats per op
+    alignas(64) unsigned char tc_tmap[128];  // CUtensorMap over the partial slots (operand A tiles)
+    bool tc_tmap_ready;
+    int tc_stages;            // shared-memory ring depth of the tensor-core kernel (0 = default)
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;
@@ -137,6 +144,11 @@ int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch);
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_mixed(iqgpu_engine *e, double len);
 int launch_from_buffer_mixed(iqgpu_engine *e, double len);
+
+// tensor-core pattern-node update (traverse_tc.cu)
+int tc_np(int npad);  // N of the MMA: npad padded to 32 or 64
+int tc_kp(int npad);  // K of the MMA: npad padded to the TF32 K step
+int launch_tc_prep(iqgpu_engine *e, int nops);
 
 // side buffers of the batched entry points, released with the engine
 void nni_release(iqgpu_engine *e);

@@ -27,7 +27,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 static long long round_up(long long v, long long g) { return (v + g - 1) / g * g; }
 
 struct Sizes {
-    long long Ppad, part, scale, states, ops, opmats, theta, red, total, op_stride;
+    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, total, op_stride;
 };
 
 static int check_config(const iqgpu_config *c) {
@@ -39,14 +39,23 @@ static int check_config(const iqgpu_config *c) {
                   "nstates<=state_unknown<=255, nslots>=1, max_ops>=1)");
         return IQGPU_ERR_ARG;
     }
-    if (c->precision != IQGPU_F64 && c->precision != IQGPU_F32) {
-        set_error("precision not supported by this build of the engine (F64, F32)");
+    if (c->precision != IQGPU_F64 && c->precision != IQGPU_F32 && c->precision != IQGPU_TF32X3) {
+        set_error("precision not supported by this build of the engine (F64, F32, TF32X3)");
         return IQGPU_ERR_ARG;
     }
     return IQGPU_OK;
 }
 
 static bool is_mixed(const iqgpu_config *c) { return c->precision != IQGPU_F64; }
+// split-TF32 tensor-core contraction: 20- and 61-state models (any 16 <= n <= 64);
+// smaller state spaces stay on the FP32 CUDA-core kernels
+static bool uses_tc(const iqgpu_config *c) {
+    return c->precision == IQGPU_TF32X3 && c->nstates >= 16 && c->nstates <= 64;
+}
+static long long tcb_stride(const iqgpu_config *c) {
+    const int npad = (c->nstates + 3) / 4 * 4;
+    return 2LL * c->ncat * 2 * tc_np(npad) * tc_kp(npad);
+}
 
 static Sizes sizes(const iqgpu_config *c) {
     Sizes s;
@@ -70,9 +79,10 @@ static Sizes sizes(const iqgpu_config *c) {
         s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
         s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
     }
+    s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
-    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + 2 * s.Ppad * 8 +
+    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + 2 * s.Ppad * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
     return s;
 }
@@ -130,7 +140,7 @@ static void free_engine(iqgpu_engine *e) {
     void *dev_ptrs[] = {e->d_eval, e->d_evec, e->d_inv, e->d_rates, e->d_props, e->d_tip, e->d_freq,
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
-                        e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32};
+                        e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -254,6 +264,11 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
         CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
         CKE(cudaMemsetAsync(e->d_exp, 0, (long long)cfg->nslots * e->Ppad * 4, e->st));
         CKE(cudaMemsetAsync(e->d_opmats32, 0, s.opmats, e->st));
+        if (uses_tc(cfg)) {
+            e->tc = true;
+            e->tcb_stride = tcb_stride(cfg);
+            CKE(dalloc(e, &e->d_tcb, s.tcb));
+        }
     } else {
         CKE(dalloc(e, &e->d_part, s.part));
         CKE(dalloc(e, &e->d_scale, s.scale));
@@ -458,7 +473,10 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         total++;
     }
     CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
-    return is_mixed(&e->cfg) ? launch_partial_info_mixed(e, total) : launch_partial_info_f64(e, total);
+    if (!is_mixed(&e->cfg)) return launch_partial_info_f64(e, total);
+    int rc = launch_partial_info_mixed(e, total);
+    if (rc == IQGPU_OK && e->tc) rc = launch_tc_prep(e, nops);
+    return rc;
 }
 
 // Fold the last timed traversal into the running total.
@@ -699,6 +717,15 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync) {
     if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
     e->level_sync = level_sync != 0;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_stages(iqgpu_engine *e, int32_t stages) {
+    if (!e || !(stages == 0 || stages == 2 || stages == 4)) {
+        set_error("stages must be 0, 2 or 4");
+        return IQGPU_ERR_ARG;
+    }
+    e->tc_stages = stages;
     return IQGPU_OK;
 }
 

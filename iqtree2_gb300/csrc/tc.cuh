@@ -1,0 +1,147 @@
+// Tensor-core (tcgen05) building blocks for sm_103a, written as inline PTX.
+//
+// Operands are K-major, no swizzle: a "core matrix" is 8 rows x 16 bytes
+// stored contiguously (128 B, row r at byte 16 r). An operand tile is a grid
+// of core matrices described by two byte strides: LBO between core matrices
+// that are neighbours along K, SBO between neighbours along M (or N). The
+// mixed-precision partial layout stores every (8 patterns x 4 states) block as
+// exactly such a core matrix, so a child's partials are an A operand as they
+// lie in memory.
+//
+// Accumulators live in tensor memory (TMEM): for M = 128 and cta_group::1,
+// row i of D is TMEM lane i and column j is TMEM column (base + j); warp w of
+// the CTA reads lanes 32 (w % 4) .. 32 (w % 4) + 31.
+#pragma once
+
+#include <cstdint>
+
+namespace iqg {
+
+// ---- TMEM allocation (executed by one whole warp) ----
+__device__ __forceinline__ void tmem_alloc(unsigned smem_dst, unsigned ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_dst), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- ordering of tcgen05 operations across a thread barrier ----
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ---- descriptors ----
+// Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte
+// units (14 bits each), descriptor version 1 at bits 46-48, base offset 0,
+// relative LBO mode, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
+// (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// Instruction descriptor, kind::f16 with BF16 inputs (A = B = 1) and F32 D.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// ---- MMA issue (one thread) ----
+__device__ __forceinline__ void mma_tf32(unsigned d_taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         bool accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_bf16(unsigned d_taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         bool accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)accumulate)
+        : "memory");
+}
+// Arrive once on the mbarrier when every tcgen05 operation this thread has
+// issued so far is complete.
+__device__ __forceinline__ void mma_commit(unsigned long long *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(bar))
+                 : "memory");
+}
+
+// ---- TMEM -> registers ----
+// Each helper issues the loads and waits for them inside one asm block, so
+// no use of the destination registers can be scheduled before the wait.
+// 32x32b shape: this thread's lane, N consecutive 32-bit columns from taddr.
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float (&v)[4]) {
+    unsigned r[4];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld4x2(unsigned ta, unsigned tb, float (&a)[4], float (&b)[4]) {
+    unsigned r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%8];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4, %5, %6, %7}, [%9];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(ta), "r"(tb)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[4 + i]);
+    }
+}
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// TF32 split: hi = x rounded to the nearest TF32 value (10 explicit mantissa
+// bits; ties away from zero), formed on the bit pattern so that hi is exactly
+// representable whatever the tensor core does with low bits; lo = x - hi is
+// exact in FP32 and |lo| <= 2^-11 |x|. Rounding (not truncation) makes lo
+// zero-mean, so the dropped lo*lo term and the tensor core's handling of lo's
+// own low bits leave no systematic bias.
+__device__ __forceinline__ float tf32_hi(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// ---- TMA tiled load (tensor map), completion counted on an mbarrier ----
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
+                                            unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z),
+        "r"((unsigned)__cvta_generic_to_shared(bar))
+        : "memory");
+}
+
+}  // namespace iqg

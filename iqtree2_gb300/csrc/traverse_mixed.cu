@@ -399,6 +399,18 @@ static int dispatch_mix(iqgpu_engine *e, MixParams P) {
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
+int launch_traverse_tc(iqgpu_engine *e, const MixParams &M);
+
+// epilogue alone after the ops ran elsewhere (tensor cores)
+template <int EPI>
+static int epilogue_only(iqgpu_engine *e, MixParams P) {
+    P.nops = 0;
+    switch (e->npad) {
+    case 4: return launch_mix_t<1, EPI>(e, P);
+    case 20: return launch_mix_t<5, EPI>(e, P);
+    default: return launch_mix_t<0, EPI>(e, P);
+    }
+}
 
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
     MixParams P = mix_params(e, nops);
@@ -406,6 +418,11 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     P.b = b;
     P.len = len;
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    if (e->tc) {
+        int rc = launch_traverse_tc(e, P);
+        if (rc || epi == EPI_NONE) return rc;
+        return epi == EPI_LNL ? epilogue_only<EPI_LNL>(e, P) : epilogue_only<EPI_THETA>(e, P);
+    }
     // 4-state models: one thread per pattern and all its categories, unless a
     // per-category tile was chosen explicitly
     if (e->n == 4 && e->C <= 4 && e->tile <= 1 && !e->level_sync) return launch_traverse_dna(e, P, epi);

@@ -1,0 +1,494 @@
+// Mixed-precision path, part 3: the pattern-node update on the tensor cores
+// (tcgen05, split-TF32 in three passes) for 20- and 61-state models.
+//
+// For one op, one rate category c and one internal child, the update is a
+// small GEMM over a tile of 128 patterns:
+//     D[p][x] = sum_y A[p][y] * P_c[x][y]        (M = 128, N = NP, K = KP)
+// A is the child's partial block of category c. In the partial layout every
+// (8 patterns x 4 states) block is one contiguous 128-byte core matrix, so a
+// tile's category-c slice is 16 row groups of npad/4 core matrices: the K-major
+// operand the MMA reads, with LBO = 128 B and SBO = npad * 32 B. When npad is
+// not a multiple of the K step (npad = 20, K padded to 24), the last K step
+// reads one core matrix past the category: the next row group's first chunk
+// (or a zeroed pad after the last group), multiplied by the zero columns
+// 20..23 of B. B = P_c(t) is prepared once per op in core-matrix order
+// (k_tc_prep_b), N padded to 32 or 64 (columns >= n of D are never read).
+//
+// Split TF32: x = hi + lo with hi = x rounded to TF32 (exact) and lo = x - hi
+// (exact in FP32); D = A_lo B_hi + A_hi B_lo + A_hi B_hi, accumulated in FP32
+// in tensor memory, which carries the product to about FP32 accuracy (the
+// dropped A_lo B_lo term is below 2^-22 of it and has zero mean).
+//
+// Pipeline per CTA (128 threads, one pattern row per thread): the child slices
+// are "stages" (item, category, side). Thread 0 keeps up to NSTAGE stages in
+// flight, each one tiled TMA copy of the A slice (tensor map over all slots)
+// and one bulk copy of B, into a ring of shared-memory slots; every thread
+// converts its own row of a landed stage into hi/lo, thread 0 issues the MMAs
+// and commits them to the slot's mbarrier (slot reuse) and, after the last
+// side of a category, to the category parity's mbarrier. While the MMAs of
+// category c run, each thread reads its row of category c-1 (tcgen05.ld),
+// multiplies the children, stores the outputs and keeps the running maximum;
+// after the last category it applies the exact power-of-two rescale and
+// writes the pattern's exponent. Accumulators are double-buffered by
+// category parity (4 * NP TMEM columns).
+//
+// Two schedules, as on the CUDA cores: fused (a CTA walks the level-ordered op
+// list for its pattern tile; a stage whose child is written by an op of the
+// same CTA that has not finished yet waits until it has) and level-synchronous
+// (one launch per tree level; a grid of resident CTAs strides over the level's
+// (tile, op) pairs, so copies for the next pair overlap the current one).
+//
+// Every wait is bounded: a copy or an MMA that does not complete sets the
+// engine's status word; the CTA then waits (bounded) for what it has in
+// flight, releases its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "mixed.cuh"
+#include "tc.cuh"
+
+namespace iqg {
+
+constexpr int kTcRows = 128;  // patterns per tile = MMA M
+
+struct TcParams {
+    MixParams M;
+    const float *tcb;      // per op: [child 2][cat C][hi, lo][NP*KP] core-matrix order
+    long long tcb_stride;  // floats per op
+    int kq;                // npad / 4 core matrices per category
+    int ksteps;            // KP / 8
+    int kp;                // K padded to the TF32 K step (8)
+    int a_bytes;           // one A buffer: 16 * kq * 128 + 128 (pad)
+    int b_bytes;           // one B buffer: NP * KP * 4
+    int ntiles;            // Ppad / 128
+    int groups_per_slot;   // Ppad / 8 (third coordinate of the partial tensor map)
+};
+
+struct TcItem {
+    int k, tile, dad, lref, rref, lch;  // lch: original child index of the left side (after the tip-left swap)
+    bool lint, rint;
+};
+
+constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged in shared memory
+
+// Item j of this CTA. Fused: every op of the (level-ordered) list for pattern
+// tile blockIdx.x. Level: (tile, op) pairs of one level, strided over the
+// grid, tiles of the same op adjacent (their B operands share L2 lines).
+__device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc) {
+    const MixParams &P = T.M;
+    TcItem it;
+    if (fused) {
+        it.k = j;
+        it.tile = blockIdx.x;
+    } else {
+        const int i = blockIdx.x + j * gridDim.x;
+        it.tile = i % T.ntiles;
+        it.k = op0 + i / T.ntiles;
+    }
+    const int ci = it.k - (fused ? 0 : op0);
+    if (ci < kTcOpCache) {
+        const int4 o = opc[ci];
+        it.dad = o.x;
+        it.lref = o.y;
+        it.rref = o.z;
+    } else {
+        const OpDev op = P.ops[it.k];
+        it.dad = op.dad_slot;
+        it.lref = op.child[0];
+        it.rref = op.child[1];
+    }
+    it.lch = 0;
+    if (it.lref >= 0 && it.rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+        int t = it.lref; it.lref = it.rref; it.rref = t;
+        it.lch = 1;
+    }
+    it.lint = it.lref >= 0;
+    it.rint = it.rref >= 0;
+    return it;
+}
+
+// stages of an item: for each category, the internal sides in order L, R
+__device__ __forceinline__ int tc_nstages(const TcItem &it, int C) { return C * ((int)it.lint + (int)it.rint); }
+__device__ __forceinline__ void tc_stage(const TcItem &it, int st, int &c, int &side) {
+    const int per = (int)it.lint + (int)it.rint;
+    c = st / per;
+    side = per == 2 ? (st & 1) : (it.lint ? 0 : 1);
+}
+
+template <int NP, int NSTAGE>
+__global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constant__ CUtensorMap tmA, const TcParams T,
+                                                         const int op0, const int nl, const int fused_nops) {
+    const MixParams &P = T.M;
+    const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
+    const int r = threadIdx.x, warp = r >> 5;
+    const long long ld = P.ldp;
+    const bool fused = fused_nops > 0;
+    int nitems;
+    if (fused) {
+        nitems = fused_nops;
+    } else {
+        const int total = T.ntiles * nl;
+        nitems = (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    }
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(P.state_unknown + 1) * C * npad;
+    const int slot_bytes = 2 * T.a_bytes + 2 * T.b_bytes;
+    const unsigned stage_tx = (unsigned)(16 * kq * 128 + 2 * T.b_bytes);
+
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    __shared__ unsigned long long full[NSTAGE], mmab[NSTAGE], ebar[2];
+    __shared__ unsigned tmem_base_s;
+    __shared__ int4 opc[kTcOpCache];
+    // tiled TMA destinations want 128-byte alignment: round the dynamic base up (128 B spare requested)
+    unsigned char *const tc_smem = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+
+    // pads after each slot's A buffers must hold finite values (zero)
+    for (int i = r; i < NSTAGE * 2 * 32; i += kTcRows) {
+        const int s = i / 64, h = (i / 32) & 1;
+        float *pad = (float *)(tc_smem + s * slot_bytes + h * T.a_bytes + 16 * kq * 128);
+        pad[i & 31] = 0.f;
+    }
+    {
+        const int base = fused ? 0 : op0, cnt = fused ? fused_nops : nl;
+        for (int i = r; i < cnt && i < kTcOpCache; i += kTcRows) {
+            const OpDev op = P.ops[base + i];
+            opc[i] = make_int4(op.dad_slot, op.child[0], op.child[1], 0);
+        }
+    }
+    if (r == 0) {
+        for (int s = 0; s < NSTAGE; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&mmab[s], 1);
+        }
+        mbar_init(&ebar[0], 1);
+        mbar_init(&ebar[1], 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&tmem_base_s), 4 * NP);
+        tmem_relinquish();
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = tmem_base_s;
+    const unsigned lane_off = (unsigned)(warp * 32) << 16;
+
+    // ---- issue side (thread 0 only) ----
+    int iss_item = 0, iss_st = 0;  // next stage to issue
+    int issued = 0, consumed = 0, finalized = 0;
+    bool failed = false;
+    TcItem iss_it;
+    if (r == 0 && nitems > 0) iss_it = tc_item(T, 0, fused, op0, opc);
+
+    auto next_issue_item = [&]() {
+        iss_item++;
+        iss_st = 0;
+        if (iss_item < nitems) iss_it = tc_item(T, iss_item, fused, op0, opc);
+    };
+    // Issue stages while ring slots are free. `ahead` bounds the stages in
+    // flight beyond the consumed ones: NSTAGE - 1 right after an MMA commit (so
+    // the slot to refill is the one whose MMAs were committed a stage earlier),
+    // NSTAGE when every committed MMA is known to be complete.
+    auto try_issue = [&](int ahead) {
+        if (r != 0 || failed) return;
+        while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C)) next_issue_item();
+        while (iss_item < nitems && issued < consumed + ahead) {
+            int c, side;
+            tc_stage(iss_it, iss_st, c, side);
+            const int child = side == 0 ? iss_it.lref : iss_it.rref;
+            if (fused) {  // a child written by an op of this CTA that has not finished yet
+                for (int j = finalized; j < iss_item; j++)
+                    if ((j < kTcOpCache ? opc[j].x : P.ops[j].dad_slot) == child) return;
+            }
+            const int s = issued % NSTAGE;
+            if (issued >= NSTAGE) {  // the slot's previous stage must be out of the tensor cores
+                if (!mbar_wait(&mmab[s], (unsigned)((issued / NSTAGE - 1) & 1), kWaitPolls)) {
+                    failed = true;
+                    return;
+                }
+            }
+            unsigned char *slot = tc_smem + s * slot_bytes;
+            mbar_expect_tx(&full[s], stage_tx);
+            // A: 16 row groups x kq core matrices of category c (one tiled copy)
+            tma_load_3d(slot, &tmA, 0, c * kq, child * T.groups_per_slot + iss_it.tile * 16, &full[s]);
+            const int ch = side == 0 ? iss_it.lch : 1 - iss_it.lch;
+            const float *bsrc =
+                T.tcb + (long long)iss_it.k * T.tcb_stride + (long long)((ch * C + c) * 2) * NP * T.kp;
+            tma_load_1d(slot + 2 * T.a_bytes, bsrc, (unsigned)(2 * T.b_bytes), &full[s]);
+            issued++;
+            iss_st++;
+            while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C)) next_issue_item();
+        }
+    };
+
+    const uint32_t idesc = idesc_tf32(kTcRows, NP);
+    const unsigned a_sbo = (unsigned)(kq * 128), b_sbo = (unsigned)(T.kp / 4 * 128);
+    int ecount0 = 0, ecount1 = 0;  // commits made to ebar[0], ebar[1]
+    bool abort = false;
+    try_issue(NSTAGE);
+
+    // products of category c for this thread's pattern; running maximum in cmax
+    auto epilogue = [&](const TcItem &it, int c, float *dad, long long p, const float *TL, int sl, int sr,
+                        float &cmax) -> bool {
+        const int per = (int)it.lint + (int)it.rint;
+        const float *tl = it.lint ? nullptr : TL + (long long)sl * C * npad + c * npad;
+        const float *tr = it.rint ? nullptr : TL + (it.lch ? -TB : TB) + (long long)sr * C * npad + c * npad;
+        if (per > 0) {
+            const int ec = (c & 1) ? ecount1 : ecount0;
+            const bool ok = mbar_wait(&ebar[c & 1], (unsigned)((ec - 1) & 1), kWaitPolls);
+            if (__syncthreads_or(!ok)) return false;
+            tc_fence_after();
+        }
+        const unsigned dL = tmem + lane_off + (unsigned)((c & 1) * 2 * NP), dR = dL + NP;
+        float *out = dad + (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * kq * 32;
+        for (int q = 0; q < kq; q++) {
+            float lv[4], rv[4];
+            if (it.lint && it.rint) {
+                tmem_ld4x2(dL + 4 * q, dR + 4 * q, lv, rv);
+            } else if (it.rint) {
+                tmem_ld4(dR + 4 * q, rv);
+                const float4 t4 = ld4(tl + 4 * q);
+                lv[0] = t4.x; lv[1] = t4.y; lv[2] = t4.z; lv[3] = t4.w;
+            } else {
+                const float4 a4 = ld4(tl + 4 * q), b4 = ld4(tr + 4 * q);
+                lv[0] = a4.x; lv[1] = a4.y; lv[2] = a4.z; lv[3] = a4.w;
+                rv[0] = b4.x; rv[1] = b4.y; rv[2] = b4.z; rv[3] = b4.w;
+            }
+            float o[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                o[i] = (4 * q + i < n) ? lv[i] * rv[i] : 0.f;
+                cmax = fmaxf(cmax, o[i]);
+            }
+            *reinterpret_cast<float4 *>(out + q * 32) = make_float4(o[0], o[1], o[2], o[3]);
+        }
+        tc_fence_before();
+        return true;
+    };
+
+    for (int j = 0; j < nitems && !abort; j++) {
+        const TcItem it = tc_item(T, j, fused, op0, opc);
+        const long long p = (long long)it.tile * kTcRows + r;
+        // per-pattern inputs of the item, loaded up front so their latency overlaps the stages
+        const int sl = it.lint ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
+        const int sr = it.rint ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
+        const int e_in = (it.lint ? P.expo[(long long)it.lref * ld + p] : 0) +
+                         (it.rint ? P.expo[(long long)it.rref * ld + p] : 0);
+        const int per = (int)it.lint + (int)it.rint;
+        const float *TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
+        float *dad = P.part + (long long)it.dad * P.slot_floats;
+        float cmax = 0.f;
+        for (int c = 0; c < C && !abort; c++) {
+            // ---- this category's stages: convert to hi/lo, MMAs ----
+            for (int sd = 0; sd < per; sd++) {
+                const int side = per == 2 ? sd : (it.lint ? 0 : 1);
+                const int s = consumed % NSTAGE;
+                const bool ok = mbar_wait(&full[s], (unsigned)((consumed / NSTAGE) & 1), kWaitPolls);
+                float *ah = (float *)(tc_smem + s * slot_bytes);
+                float *al = (float *)(tc_smem + s * slot_bytes + T.a_bytes);
+                if (ok) {
+                    const int base = (r >> 3) * kq * 32 + (r & 7) * 4;
+                    for (int q = 0; q < kq; q++) {
+                        const float4 v = *reinterpret_cast<float4 *>(ah + base + q * 32);
+                        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+                        *reinterpret_cast<float4 *>(ah + base + q * 32) = h;
+                        *reinterpret_cast<float4 *>(al + base + q * 32) =
+                            make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                    }
+                }
+                fence_proxy_async_smem();
+                if (__syncthreads_or(!ok || (r == 0 && failed))) { abort = true; break; }
+                if (r == 0) {
+                    tc_fence_after();
+                    const unsigned d = tmem + (unsigned)((c & 1) * 2 * NP + side * NP);
+                    const unsigned uah = smem_u32(ah), ual = smem_u32(al);
+                    const unsigned ubh = smem_u32(tc_smem + s * slot_bytes + 2 * T.a_bytes);
+                    const unsigned ubl = ubh + (unsigned)T.b_bytes;
+                    for (int ks = 0; ks < T.ksteps; ks++) {
+                        const uint64_t dah = smem_desc(uah + ks * 256, 128, a_sbo);
+                        const uint64_t dal = smem_desc(ual + ks * 256, 128, a_sbo);
+                        const uint64_t dbh = smem_desc(ubh + ks * 256, 128, b_sbo);
+                        const uint64_t dbl = smem_desc(ubl + ks * 256, 128, b_sbo);
+                        mma_tf32(d, dal, dbh, idesc, ks > 0);
+                        mma_tf32(d, dah, dbl, idesc, true);
+                        mma_tf32(d, dah, dbh, idesc, true);
+                    }
+                    mma_commit(&mmab[s]);
+                    if (sd == per - 1) mma_commit(&ebar[c & 1]);
+                }
+                if (sd == per - 1) {
+                    if (c & 1) ecount1++;
+                    else ecount0++;
+                }
+                consumed++;
+                try_issue(NSTAGE - 1);
+            }
+            if (abort) break;
+            // ---- the previous category's outputs, while this one's MMAs run ----
+            if (c > 0 && !epilogue(it, c - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+        }
+        if (abort) break;
+        if (!epilogue(it, C - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+        // ---- rescale (exact power of two) and exponent ----
+        int sh = 0;
+        if (cmax < kMixThreshold && cmax > 0.f) {
+            int ex;
+            frexpf(cmax, &ex);
+            sh = 1 - ex;
+            const float mul = __int_as_float((127 + sh) << 23);
+            float *row = dad + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+            for (int q = 0; q < C * kq; q++) {
+                float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(row + q * 32) = v;
+            }
+        }
+        P.expo[(long long)it.dad * ld + p] = e_in - sh;
+        if (fused) {
+            // the outputs may be read next by this CTA's TMA copies (async proxy)
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            __syncthreads();
+            finalized = j + 1;
+        }
+        try_issue(NSTAGE);
+    }
+
+    if (r == 0 && (abort || failed)) {
+        atomicExch(P.status, kStatusTimeout);
+        // bounded waits for the copies and MMAs still in flight before the memory is released
+        for (int i = consumed; i < issued; i++) mbar_wait(&full[i % NSTAGE], (unsigned)((i / NSTAGE) & 1), kWaitPolls);
+        if (consumed > 0)
+            mbar_wait(&mmab[(consumed - 1) % NSTAGE], (unsigned)(((consumed - 1) / NSTAGE) & 1), kWaitPolls);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 4 * NP);
+}
+
+// B operands: per op, child, category: hi and lo of P_c(t)[x][y] in
+// [x/8][y/4][x%8][y%4] order, zero outside x < n, y < n.
+__global__ void k_tc_prep_b(const float *opmats, long long op_stride, float *tcb, long long tcb_stride, int n,
+                            int npad, int C, int NP, int KP) {
+    const int k = blockIdx.x, ch = blockIdx.y / C, c = blockIdx.y % C;
+    const float *Pm = opmats + (long long)k * op_stride + (long long)ch * C * n * npad + (long long)c * n * npad;
+    float *hi = tcb + (long long)k * tcb_stride + (long long)((ch * C + c) * 2) * NP * KP;
+    float *lo = hi + NP * KP;
+    for (int i = threadIdx.x; i < NP * KP; i += blockDim.x) {
+        const int x = i / KP, y = i % KP;
+        const float v = (x < n && y < n) ? Pm[x * npad + y] : 0.f;
+        const float h = tf32_hi(v);
+        const int off = (x >> 3) * (KP / 4) * 32 + (y >> 2) * 32 + (x & 7) * 4 + (y & 3);
+        hi[off] = h;
+        lo[off] = v - h;
+    }
+}
+
+int tc_np(int npad) { return npad <= 32 ? 32 : 64; }
+int tc_kp(int npad) { return (npad + 7) / 8 * 8; }
+
+int launch_tc_prep(iqgpu_engine *e, int nops) {
+    if (nops <= 0) return IQGPU_OK;
+    const int NP = tc_np(e->npad), KP = tc_kp(e->npad);
+    k_tc_prep_b<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32, e->d_tcb, e->tcb_stride,
+                                                           e->n, e->npad, e->C, NP, KP);
+    return cuda_fail(cudaGetLastError(), "tc_prep_b");
+}
+
+// Tensor map over all partial slots, viewed as [slot * Ppad/8 + group][C*kq core
+// matrices][32 floats]; a box of {32, kq, 16} is one category of a 128-pattern
+// tile in the operand layout. Built once per engine (the slots do not move).
+static int tc_tensor_map(iqgpu_engine *e) {
+    if (e->tc_tmap_ready) return IQGPU_OK;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (err != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return IQGPU_ERR_CUDA;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const int kq = e->npad / 4;
+    const cuuint64_t dims[3] = {32, (cuuint64_t)e->C * kq, (cuuint64_t)e->cfg.nslots * (cuuint64_t)(e->Ppad / 8)};
+    const cuuint64_t strides[2] = {128, (cuuint64_t)e->C * kq * 128};
+    const cuuint32_t box[3] = {32, (cuuint32_t)kq, 16};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult res = encode(reinterpret_cast<CUtensorMap *>(e->tc_tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, e->d_part32,
+                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (res != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed for the partial slots");
+        return IQGPU_ERR_CUDA;
+    }
+    e->tc_tmap_ready = true;
+    return IQGPU_OK;
+}
+
+template <int NP, int NSTAGE>
+static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
+    int rc = tc_tensor_map(e);
+    if (rc) return rc;
+    TcParams T;
+    T.M = M;
+    T.tcb = e->d_tcb;
+    T.tcb_stride = e->tcb_stride;
+    T.kq = e->npad / 4;
+    T.kp = tc_kp(e->npad);
+    T.ksteps = T.kp / 8;
+    T.a_bytes = 16 * T.kq * 128 + 128;
+    T.b_bytes = NP * T.kp * 4;
+    T.ntiles = (int)(e->Ppad / kTcRows);
+    T.groups_per_slot = (int)(e->Ppad / 8);
+    const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
+    const size_t smem = (size_t)NSTAGE * (2 * T.a_bytes + 2 * T.b_bytes) + 128;  // + alignment spare
+    auto kern = k_traverse_tc<NP, NSTAGE>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
+    if (!e->level_sync) {
+        kern<<<T.ntiles, kTcRows, smem, e->st>>>(tm, T, 0, 0, M.nops);
+        return cuda_fail(cudaGetLastError(), "traverse_tc");
+    }
+    // level schedule: a persistent grid of resident CTAs walks each level's (tile, op) pairs.
+    // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA reserve)
+    // and by tensor memory (512 columns, 4 * NP per CTA).
+    int sms = 1, smem_sm = 0, reserve = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->dev);
+    cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, e->dev);
+    cudaFuncAttributes fa;
+    size_t stat = 0;
+    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess) stat = fa.sharedSizeBytes;
+    const size_t per_cta = smem + stat + (size_t)reserve;
+    int per_sm = (int)std::min<size_t>(512 / (4 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
+    if (per_sm < 1) per_sm = 1;
+    for (int l = 0; l < e->nlevels; l++) {
+        const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+        if (nl <= 0) continue;
+        const long long items = (long long)T.ntiles * nl;
+        const int grid = (int)std::min<long long>(items, (long long)per_sm * std::max(sms, 1));
+        kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
+    }
+    return IQGPU_OK;
+}
+
+// The ops of a traversal on the tensor cores (the branch epilogue stays on
+// the CUDA-core kernel). Stage ring (iqgpu_set_stages): for <= 32 padded
+// states 4 slots (two CTAs per SM, 128 TMEM columns each) or 2 slots (four
+// CTAs per SM); for 64 padded states 2 slots (one CTA per SM, 256 columns).
+int launch_traverse_tc(iqgpu_engine *e, const MixParams &M) {
+    if (M.nops <= 0) return IQGPU_OK;
+    if (tc_np(e->npad) == 64) return launch_tc_t<64, 2>(e, M);
+    return e->tc_stages == 2 ? launch_tc_t<32, 2>(e, M) : launch_tc_t<32, 4>(e, M);
+}
+
+}  // namespace iqg

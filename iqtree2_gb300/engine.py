@@ -94,6 +94,7 @@ def lib():
         "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
         "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
@@ -147,6 +148,12 @@ class Engine:
         self.h = h
         self.nptn, self.nstates, self.ncat, self.ntaxa = int(nptn), int(nstates), int(ncat), int(ntaxa)
         self.safe = bool(safe)
+        self.precision = int(precision)
+
+    @property
+    def tensor_cores(self):
+        """True when the pattern-node update runs on the tensor cores (split TF32, 16..64 states)."""
+        return self.precision == TF32X3 and 16 <= self.nstates <= 64
 
     @staticmethod
     def memory_required(**kw):
@@ -258,6 +265,10 @@ class Engine:
 
     def set_schedule(self, level_sync):
         _check(lib().iqgpu_set_schedule(self.h, int(bool(level_sync))))
+
+    def set_stages(self, stages):
+        """Ring depth of the tensor-core traversal (0 = default, 2 or 4)."""
+        _check(lib().iqgpu_set_stages(self.h, int(stages)))
 
     def nni_batch(self, cands, max_nr_step=10, min_bl=1e-6, max_bl=10.0):
         """cands: iterable of ((sub0..sub3), (scratch0, scratch1), (len0..len3), central)."""

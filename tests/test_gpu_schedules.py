@@ -25,9 +25,9 @@ def test_all_schedules_agree(oracle_mod, name):
     a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
     want = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths).lnl_branch(nb, leaf)
     got = {}
-    for tile, sched in autotune.candidates(eng):
-        eng.set_tile(tile)
-        eng.set_schedule(sched)
+    for cand in autotune.candidates(eng):
+        tile, sched, _ = cand
+        autotune.apply(eng, cand)
         got[(tile, sched)] = eng.compute_likelihood(ops, a, b, length)
         assert rel(got[(tile, sched)], want) < 1e-6, (tile, sched)
     for tile in autotune.TILES:

@@ -1,0 +1,150 @@
+"""Tensor-core path (tcgen05, split TF32 in three passes) for 20- and 61-state
+models against the FP64 oracle and against the FP32 CUDA-core kernels.
+
+Tolerances, as for the FP32 path: lnL |dlnL| <= 1e-6 |lnL|; pattern lnL
+absolute <= 1e-4; partials relative to each pattern's largest entry <= 1e-5;
+first derivative relative <= 1e-4, second <= 1e-3 (+1e-3 absolute floor);
+optimised branch lengths within 1e-4. The two schedules of the tensor-core
+kernel run the same per-op arithmetic and agree bit for bit.
+"""
+import numpy as np
+import pytest
+
+from helpers import load_golden, rel
+from iqtree2_gb300 import autotune, engine, simulate
+from iqtree2_gb300.topology import Topology
+
+pytestmark = pytest.mark.gpu
+
+LNL_RTOL = 1e-6
+
+
+def _engine(g, topo, precision=engine.TF32X3):
+    eng = engine.Engine(g.patterns.shape[1], g.model.nstates, g.model.ncat, g.patterns.shape[0], g.model.state_unknown,
+                        topo.nslots, precision=precision, max_ops=topo.nslots)
+    eng.set_model(g.model)
+    eng.set_patterns(g.freq)
+    eng.set_tip_states(g.patterns)
+    return eng
+
+
+@pytest.mark.parametrize("name", ["prot12", "codon8"])
+def test_tc_golden_lnl(oracle_mod, name):
+    g = load_golden(name)
+    t = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, precision=engine.TF32X3)
+    lnl, plh = t.compute_likelihood(want_pattern_lh=True)
+    assert rel(lnl, g.lnl_std) < LNL_RTOL
+    np.testing.assert_allclose(plh, g.pattern_lnl_std, atol=1e-4)
+
+
+@pytest.mark.parametrize("name", ["prot12", "codon8"])
+def test_tc_partials_match_oracle(oracle_mod, name):
+    g = load_golden(name)
+    topo = Topology(g.edges, g.lengths, g.ntaxa)
+    eng = _engine(g, topo)
+    assert eng.tensor_cores
+    done, ops = set(), []
+    for (u, v) in sorted(topo.slot):
+        ops += topo.ops_for(u, v, done)
+    eng.compute_partials(ops)
+    orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+    n, C = g.model.nstates, g.model.ncat
+    U = g.model.evec
+    for (u, v), s in list(topo.slot.items())[:12]:
+        gp, _ = eng.partial(s)
+        op, _ = orc.partial(u, v)
+        std = np.einsum("xi,pci->pcx", U, op.reshape(-1, C, n)).reshape(op.shape)
+        gn = gp / np.abs(gp).max(axis=1, keepdims=True)
+        on = std / np.abs(std).max(axis=1, keepdims=True)
+        assert np.max(np.abs(gn - on)) < 1e-5, (u, v)
+
+
+@pytest.mark.parametrize("name", ["prot12", "codon8"])
+def test_tc_derivatives(oracle_mod, name):
+    g = load_golden(name)
+    topo = Topology(g.edges, g.lengths, g.ntaxa)
+    eng = _engine(g, topo)
+    internal = [tuple(map(int, e)) for e in g.edges if min(e) >= g.ntaxa]
+    done = set()
+    for (n1, n2) in [tuple(map(int, g.edges[0]))] + internal[:2]:
+        node, dad = n2, n1
+        if node < g.ntaxa:
+            node, dad = n1, n2
+        ops = topo.ops_for(dad, node, done) + topo.ops_for(node, dad, done)
+        a, b = topo.ref(dad, node), topo.ref(node, dad)
+        orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+        first = True
+        for length in (0.02, 0.1, 0.7):
+            df, ddf = eng.likelihood_derv(ops if first else [], a, b, length, theta_computed=not first)
+            first = False
+            odf, oddf = orc.derv(n1, n2, length)
+            assert abs(df - odf) <= 1e-4 * abs(odf) + 1e-3
+            assert abs(ddf - oddf) <= 1e-3 * abs(oddf) + 1e-3
+            assert rel(eng.lnl_from_buffer(length), orc.lnl_branch(node, dad)) < LNL_RTOL
+
+
+def test_tc_optimize_all_branches(oracle_mod):
+    g = load_golden("prot12")
+    t = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, precision=engine.TF32X3)
+    o = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+    lg, lo = t.optimize_all_branches(), o.optimize_all_branches()
+    assert rel(lg, lo) < LNL_RTOL
+    np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-4)
+
+
+@pytest.mark.parametrize("kind", ["protein", "codon"])
+def test_tc_schedules_agree_and_match_cuda_cores(oracle_mod, kind):
+    """Ragged pattern count (not a multiple of 128), tip-tip, tip-internal and
+    internal-internal ops; fused and level schedules bit-identical; the
+    CUDA-core FP32 kernel within the mixed tolerance."""
+    ds = (simulate.protein_lg_dataset(40, 1500, 31) if kind == "protein"
+          else simulate.codon_gy94_dataset(16, 700, 32))
+    topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    tc = _engine(ds, topo)
+    got = {}
+    for cand in autotune.candidates(tc):
+        autotune.apply(tc, cand)
+        got[cand] = tc.compute_likelihood(ops, a, b, length)
+        assert rel(got[cand], want) < LNL_RTOL, cand
+    vals = set(got.values())
+    assert len(vals) == 1, got  # same per-op arithmetic in every schedule and ring depth
+    cc = _engine(ds, topo, engine.F32)
+    assert rel(cc.compute_likelihood(ops, a, b, length), vals.pop()) < LNL_RTOL
+
+
+def test_tc_deep_tree_exponents(oracle_mod):
+    """200-taxon protein tree with long branches: the per-pattern exponents are
+    exercised on the tensor-core path."""
+    ds = simulate.protein_lg_dataset(200, 300, 33, mean_bl=0.3)
+    t = engine.GpuTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=engine.TF32X3)
+    o = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
+
+
+def test_tc_ambiguous_states(oracle_mod):
+    rng = np.random.default_rng(19)
+    ds = simulate.protein_lg_dataset(14, 500, 34)
+    pats = ds.patterns.copy()
+    mask = rng.random(pats.shape) < 0.15
+    pats[mask] = rng.integers(ds.model.nstates, ds.model.state_unknown + 1, size=mask.sum())
+    t = engine.GpuTree(ds.model, pats, ds.freq, ds.edges, ds.lengths, precision=engine.TF32X3)
+    o = oracle_mod.OracleTree(ds.model, pats, ds.freq, ds.edges, ds.lengths)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
+
+
+@pytest.mark.parametrize("kind", ["protein", "codon"])
+def test_tc_full_size_configs(oracle_mod, kind):
+    """Protein 100x50,000 and codon 40x10,000 on the tensor cores: lnL within
+    1e-6 of the FP64 oracle."""
+    ds = (simulate.protein_lg_dataset(100, 50000, 2) if kind == "protein"
+          else simulate.codon_gy94_dataset(40, 10000, 3))
+    t = engine.GpuTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=engine.TF32X3)
+    o = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths)
+    lg, lo = t.compute_likelihood(), o.compute_likelihood()
+    err = rel(lg, lo)
+    print(f"{kind}: split-TF32 lnL {lg:.6f} oracle {lo:.6f} rel err {err:.2e}")
+    assert err < LNL_RTOL
