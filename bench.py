@@ -80,25 +80,28 @@ def op_levels(ops):
     return top
 
 
-def kernel_name(use_tc, n, tile):
+def kernel_name(use_tc, n, tile, bf16=False):
+    """Dominant kernel of a path, from the autotuned label (tile/schedule[/sD][/kP])."""
     if use_tc:
-        return "k_traverse_tc<64,2>" if n > 32 else ("k_traverse_tc<32,2>" if tile.endswith("/s2") else
-                                                      "k_traverse_tc<32,4>")
+        depth = next((int(t[1:]) for t in tile.split("/") if t.startswith("s")), 2)
+        return f"k_traverse_tc<{64 if n > 32 else 32},{depth},{'true' if bf16 else 'false'}>"
     if tile.startswith("1/"):
-        return "k_traverse_dna<LNL>"
+        return "k_level_dna" if "/level" in tile else "k_traverse_dna<LNL>"
     nq = {4: 1, 20: 5}.get((n + 3) // 4 * 4, 0)
     return f"k_level_mixed<{nq}>" if "/level" in tile else f"k_traverse_mixed<{nq},LNL>"
 
 
-def tc_mma_flops(ops, n, C, nptn):
-    """MMA flops the split-TF32 kernel executes: per internal child, category
-    and 128-pattern tile, 3 passes of M=128 x N x K (N, K padded)."""
+def tc_mma_flops(ops, n, C, nptn, bf16=False):
+    """MMA flops the tensor-core kernel executes: per internal child, category
+    and 128-pattern tile, M=128 x N x K (N, K padded); split TF32 runs 3 passes,
+    BF16 one (K per stage padded to 16)."""
     npad = (n + 3) // 4 * 4
     N = 32 if npad <= 32 else 64
-    K = (npad + 7) // 8 * 8
+    ksplit = 2 if (npad > 32 and npad % 16 == 0) else 1
+    K = ((npad // ksplit + 15) // 16 * 16) * ksplit if bf16 else (npad + 7) // 8 * 8
     tiles = (nptn + 127) // 128
     children = sum((c0 >= 0) + (c1 >= 0) for (_, c0, c1, _, _) in ops)
-    return 3 * 2 * 128 * N * K * C * children * tiles
+    return (1 if bf16 else 3) * 2 * 128 * N * K * C * children * tiles
 
 
 def algorithmic_cost(ops, ntaxa, n, C, nptn, mixed=False):
@@ -348,6 +351,11 @@ def run_ours(args):
     h2d = ds.patterns.nbytes + ds.freq.nbytes + sum(x.nbytes for x in (m.eval, m.evec, m.inv_evec, m.rates,
                                                                         m.props, m.tip_lh, m.pi)) + ops_arr.nbytes
     assert lnl_e2e == r["lnl"]
+    if use_tc:  # BF16 operands (one MMA pass), reported beside: speed and lnL error
+        engb = make_engine(ds, topo, engine.BF16, local, stream)
+        btile, _ = autotune.tune(engb, ops_arr, a, b, length)
+        rb = measure_path(engb, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
+        engb.close()
     if rank != 0:
         return
     achieved = bmx / r["kern_avg_s"] / 1e9
@@ -381,6 +389,10 @@ def run_ours(args):
         "gpu_launches": launches * args.steps,
     }
     if use_tc:
+        line["bf16"] = dict(kernel_ms=rb["kern_avg_s"] * 1e3, tile=btile, kernel=kernel_name(True, m.nstates, btile, True),
+                            value=updates_per_step * max(3, args.steps // 4) / (rb["elapsed_ms"] / 1e3),
+                            lnl=rb["lnl"], rel_err_vs_fp64=abs(rb["lnl"] - r64["lnl"]) / abs(r64["lnl"]),
+                            mma_tflops=tc_mma_flops(ops, m.nstates, m.ncat, ds.nptn, bf16=True) / rb["kern_avg_s"] / 1e12)
         mma = tc_mma_flops(ops, m.nstates, m.ncat, ds.nptn)
         line["roofline"]["tensor"] = {"mma_flops_per_launch": mma, "mma_tflops": mma / r["kern_avg_s"] / 1e12,
                                       "note": "executed split-TF32 MMA flops (3 passes, padded N/K)"}

@@ -57,8 +57,11 @@ extern "C" {
 /* ---- precision of the stored partials ---------------------------------- */
 #define IQGPU_F64 0     /* FP64 eigen-space partials, uint8 2^-256 scale counts: the drop-in */
 #define IQGPU_F32 1     /* FP32 standard-basis partials, per-pattern power-of-two exponents */
-#define IQGPU_TF32X3 2  /* as F32, tensor-core contraction with split-TF32 (3 passes) */
-#define IQGPU_BF16 3    /* BF16 operands on tensor cores, FP32 accumulate and storage */
+#define IQGPU_TF32X3 2  /* as F32, tensor-core contraction with split-TF32 (3 passes) for
+                           16..64 states (fewer states: FP32 CUDA cores) */
+#define IQGPU_BF16 3    /* as F32, tensor-core contraction with BF16 operands (1 pass, FP32
+                           accumulate and storage) for 16..64 states; about 1e-3 relative
+                           per partial, error reported, not a drop-in */
 
 typedef struct {
     int32_t nptn;          /* patterns (aln->size()) */
@@ -171,11 +174,17 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * whole op list per pattern tile; 1 = one launch per tree level, all of the
  * level's (op, tile) pairs in flight together. Results do not depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync);
-/* Shared-memory ring depth (stages in flight per CTA) of the tensor-core
- * traversal (precision IQGPU_TF32X3): 0 = default, 2 or 4 for models of up to
- * 32 padded states (2 fits four CTAs per SM, 4 fits two); 61-state models
- * always use 2. Chosen by the autotuner; results do not depend on it. */
+/* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
+ * how many child slices per CTA may be in flight as TMA copies (landing slots
+ * of shared memory), 2, 3 or 4; 0 = default (3). A depth whose shared memory
+ * does not fit one CTA is lowered. Chosen by the autotuner; results do not
+ * depend on it. */
 int iqgpu_set_stages(iqgpu_engine *e, int32_t stages);
+/* K pieces per copied stage of the tensor-core traversal: 0/1 = a stage
+ * carries a category's whole K; 2 = halves (61-state models: half the shared
+ * memory per stage, two CTAs per SM instead of one). Ignored where K does not
+ * split evenly. Chosen by the autotuner; results do not depend on it. */
+int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 
 /* ---- batched evaluation ------------------------------------------------- */

@@ -20,29 +20,33 @@ _cache: dict = {}
 
 
 def candidates(eng):
-    """(tile, schedule, stages) triples; stages only matter on the tensor-core path."""
+    """(tile, schedule, stages, kpieces) tuples; stages and kpieces only matter
+    on the tensor-core path; schedule 0 = fused, 1 = level-synchronous."""
     if getattr(eng, "tensor_cores", False):  # one CTA = 128 patterns (the MMA's M)
-        depths = (2, 4) if eng.nstates <= 32 else (2,)
-        return [(0, sched, st) for sched in (0, 1) for st in depths]
-    out = [(1, 0, 0)] if eng.nstates == 4 and eng.ncat <= 4 else []
+        npad = (eng.nstates + 3) // 4 * 4
+        pieces = (1, 2) if (npad > 32 and npad % 16 == 0) else (1,)
+        return [(0, sched, st, kp) for sched in (0, 1) for st in (2, 3, 4) for kp in pieces]
+    out = [(1, 0, 0, 0), (1, 1, 0, 0)] if eng.nstates == 4 and eng.ncat <= 4 else []
     for sched in (0, 1):
         for tile in TILES:
             if tile > 32 and tile * eng.ncat > 512:
                 continue
-            out.append((tile, sched, 0))
+            out.append((tile, sched, 0, 0))
     return out
 
 
 def label(cand):
-    tile, sched, stages = cand
-    return f"{tile}/{'level' if sched else 'fused'}" + (f"/s{stages}" if stages else "")
+    tile, sched, stages, kp = cand
+    return (f"{tile}/{'level' if sched else 'fused'}" + (f"/s{stages}" if stages else "") +
+            (f"/k{kp}" if kp else ""))
 
 
 def apply(eng, cand):
-    tile, sched, stages = cand
+    tile, sched, stages, kp = cand
     eng.set_tile(tile)
     eng.set_schedule(sched)
     eng.set_stages(stages)
+    eng.set_kpieces(kp)
 
 
 def tune(eng, ops_arr, a, b, length, reps=3):

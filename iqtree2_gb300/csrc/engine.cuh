@@ -116,7 +116,9 @@ struct iqgpu_engine {
     long long tcb_stride;     // floats per op
     alignas(64) unsigned char tc_tmap[128];  // CUtensorMap over the partial slots (operand A tiles)
     bool tc_tmap_ready;
+    int tc_tmap_kqs;          // box height (core matrices) the tensor map was encoded with
     int tc_stages;            // shared-memory ring depth of the tensor-core kernel (0 = default)
+    int tc_kpieces;           // K pieces per stage (0/1 = whole K, 2 = halves)
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;
@@ -148,6 +150,7 @@ int launch_from_buffer_mixed(iqgpu_engine *e, double len);
 // tensor-core pattern-node update (traverse_tc.cu)
 int tc_np(int npad);  // N of the MMA: npad padded to 32 or 64
 int tc_kp(int npad);  // K of the MMA: npad padded to the TF32 K step
+int tc_ksplit(const iqgpu_engine *e);  // K pieces per (category, side) stage
 int launch_tc_prep(iqgpu_engine *e, int nops);
 
 // side buffers of the batched entry points, released with the engine

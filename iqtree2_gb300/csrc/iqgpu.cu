@@ -39,18 +39,19 @@ static int check_config(const iqgpu_config *c) {
                   "nstates<=state_unknown<=255, nslots>=1, max_ops>=1)");
         return IQGPU_ERR_ARG;
     }
-    if (c->precision != IQGPU_F64 && c->precision != IQGPU_F32 && c->precision != IQGPU_TF32X3) {
-        set_error("precision not supported by this build of the engine (F64, F32, TF32X3)");
+    if (c->precision != IQGPU_F64 && c->precision != IQGPU_F32 && c->precision != IQGPU_TF32X3 &&
+        c->precision != IQGPU_BF16) {
+        set_error("precision not supported by this build of the engine (F64, F32, TF32X3, BF16)");
         return IQGPU_ERR_ARG;
     }
     return IQGPU_OK;
 }
 
 static bool is_mixed(const iqgpu_config *c) { return c->precision != IQGPU_F64; }
-// split-TF32 tensor-core contraction: 20- and 61-state models (any 16 <= n <= 64);
-// smaller state spaces stay on the FP32 CUDA-core kernels
+// tensor-core contraction (split TF32 or BF16): 20- and 61-state models (any
+// 16 <= n <= 64); smaller state spaces stay on the FP32 CUDA-core kernels
 static bool uses_tc(const iqgpu_config *c) {
-    return c->precision == IQGPU_TF32X3 && c->nstates >= 16 && c->nstates <= 64;
+    return (c->precision == IQGPU_TF32X3 || c->precision == IQGPU_BF16) && c->nstates >= 16 && c->nstates <= 64;
 }
 static long long tcb_stride(const iqgpu_config *c) {
     const int npad = (c->nstates + 3) / 4 * 4;
@@ -721,11 +722,20 @@ int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync) {
 }
 
 int iqgpu_set_stages(iqgpu_engine *e, int32_t stages) {
-    if (!e || !(stages == 0 || stages == 2 || stages == 4)) {
-        set_error("stages must be 0, 2 or 4");
+    if (!e || !(stages == 0 || (stages >= 2 && stages <= 4))) {
+        set_error("stages must be 0, 2, 3 or 4");
         return IQGPU_ERR_ARG;
     }
     e->tc_stages = stages;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces) {
+    if (!e || pieces < 0 || pieces > 2) {
+        set_error("pieces must be 0, 1 or 2");
+        return IQGPU_ERR_ARG;
+    }
+    e->tc_kpieces = pieces;
     return IQGPU_OK;
 }
 

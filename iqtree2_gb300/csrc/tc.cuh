@@ -133,6 +133,13 @@ __device__ __forceinline__ float tf32_hi(float x) {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
+// Two floats rounded to BF16 (round to nearest even), packed low = a, high = b.
+__device__ __forceinline__ unsigned bf16x2(float a, float b) {
+    unsigned v;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(v) : "f"(b), "f"(a));
+    return v;
+}
+
 // ---- TMA tiled load (tensor map), completion counted on an mbarrier ----
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
                                             unsigned long long *bar) {

@@ -7,7 +7,8 @@
 // pattern's maximum without any cross-thread exchange, and rescales and
 // stores its block in registers; the only barrier per op is the one that
 // publishes the op's TMA-staged P(t) matrices (double-buffered, so op k+1's
-// copy is in flight while op k computes).
+// copy is in flight while op k computes). A level-synchronous form
+// (k_level_dna) runs each tree level as one launch.
 #include <cuda_runtime.h>
 
 #include "mixed.cuh"
@@ -186,6 +187,99 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
         }
         mix_grid_reduce(v, P.red);
     }
+}
+
+// Level-synchronous form: CTA (x, y) computes op op0 + y for patterns
+// 128 x .. 128 x + 127, one thread per pattern and all of its categories. All
+// (op, tile) pairs of a level are independent, so every child load of the
+// level can be in flight at once; the op's P(t) blocks (2 x ncat x 16 floats)
+// are read through the read-only cache (warp-uniform addresses).
+__global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0) {
+    constexpr int n = 4, npad = 4;
+    const int C = P.ncat, S = P.state_unknown;
+    const int k = op0 + blockIdx.y;
+    const long long p = (long long)blockIdx.x * kDnaTile + threadIdx.x;
+    const long long ld = P.ldp;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(S + 1) * C * npad;
+    const OpDev op = P.ops[k];
+    int lref = op.child[0], rref = op.child[1];
+    const float *gbase = P.opmats + (long long)k * P.op_stride;
+    const float *PL = gbase, *PR = gbase + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
+    if (lref >= 0 && rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+        int t = lref; lref = rref; rref = t;
+        const float *q = PL; PL = PR; PR = q;
+        q = TL; TL = TR; TR = q;
+    }
+    const bool lint = lref >= 0, rint = rref >= 0;
+    const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
+    const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
+    const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
+    const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
+    const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+    float4 lv[kDnaMaxCat], rv[kDnaMaxCat], out[kDnaMaxCat];
+#pragma unroll
+    for (int c = 0; c < kDnaMaxCat; c++) {
+        if (c < C) {
+            lv[c] = lint ? __ldcs(reinterpret_cast<const float4 *>(Lp + c * 32)) : ld4(tl + c * npad);
+            rv[c] = rint ? __ldcs(reinterpret_cast<const float4 *>(Rp + c * 32)) : ld4(tr + c * npad);
+        }
+    }
+    float mx = 0.f;
+#pragma unroll
+    for (int c = 0; c < kDnaMaxCat; c++) {
+        if (c < C) {
+            float yl[4], yr[4];
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+                if (lint) {
+                    const float4 m = ld4(PL + c * 16 + x * 4);
+                    yl[x] = fmaf(m.x, lv[c].x, fmaf(m.y, lv[c].y, fmaf(m.z, lv[c].z, m.w * lv[c].w)));
+                } else {
+                    yl[x] = x == 0 ? lv[c].x : x == 1 ? lv[c].y : x == 2 ? lv[c].z : lv[c].w;
+                }
+                if (rint) {
+                    const float4 m = ld4(PR + c * 16 + x * 4);
+                    yr[x] = fmaf(m.x, rv[c].x, fmaf(m.y, rv[c].y, fmaf(m.z, rv[c].z, m.w * rv[c].w)));
+                } else {
+                    yr[x] = x == 0 ? rv[c].x : x == 1 ? rv[c].y : x == 2 ? rv[c].z : rv[c].w;
+                }
+            }
+            out[c] = make_float4(yl[0] * yr[0], yl[1] * yr[1], yl[2] * yr[2], yl[3] * yr[3]);
+            mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
+        }
+    }
+    int sh = 0;
+    float mul = 1.f;
+    if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
+        int ex;
+        frexpf(mx, &ex);
+        sh = 1 - ex;
+        mul = __int_as_float((127 + sh) << 23);
+    }
+    float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+#pragma unroll
+    for (int c = 0; c < kDnaMaxCat; c++) {
+        if (c < C) {
+            float4 v = out[c];
+            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+            *reinterpret_cast<float4 *>(dad + c * 32) = v;
+        }
+    }
+    P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+}
+
+int launch_levels_dna(iqgpu_engine *e, const MixParams &P) {
+    const int grid = (int)(e->Ppad / kDnaTile);
+    for (int l = 0; l < e->nlevels; l++) {
+        const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+        if (nl <= 0) continue;
+        k_level_dna<<<dim3(grid, nl), kDnaTile, 0, e->st>>>(P, op0);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "level_dna");
+    }
+    return IQGPU_OK;
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi) {

@@ -399,6 +399,7 @@ static int dispatch_mix(iqgpu_engine *e, MixParams P) {
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
+int launch_levels_dna(iqgpu_engine *e, const MixParams &P);
 int launch_traverse_tc(iqgpu_engine *e, const MixParams &M);
 
 // epilogue alone after the ops ran elsewhere (tensor cores)
@@ -425,7 +426,14 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     }
     // 4-state models: one thread per pattern and all its categories, unless a
     // per-category tile was chosen explicitly
-    if (e->n == 4 && e->C <= 4 && e->tile <= 1 && !e->level_sync) return launch_traverse_dna(e, P, epi);
+    if (e->n == 4 && e->C <= 4 && e->tile == 1) {
+        if (!e->level_sync) return launch_traverse_dna(e, P, epi);
+        int rc = launch_levels_dna(e, P);
+        if (rc || epi == EPI_NONE) return rc;
+        P.nops = 0;  // the epilogue alone
+        return launch_traverse_dna(e, P, epi);
+    }
+    if (e->n == 4 && e->C <= 4 && e->tile == 0 && !e->level_sync) return launch_traverse_dna(e, P, epi);
     switch (epi) {
     case EPI_NONE: return dispatch_mix<EPI_NONE>(e, P);
     case EPI_LNL: return dispatch_mix<EPI_LNL>(e, P);

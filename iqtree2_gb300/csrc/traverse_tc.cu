@@ -59,10 +59,20 @@ struct TcParams {
     const float *tcb;      // per op: [child 2][cat C][hi, lo][NP*KP] core-matrix order
     long long tcb_stride;  // floats per op
     int kq;                // npad / 4 core matrices per category
-    int ksteps;            // KP / 8
     int kp;                // K padded to the TF32 K step (8)
-    int a_bytes;           // one A buffer: 16 * kq * 128 + 128 (pad)
-    int b_bytes;           // one B buffer: NP * KP * 4
+    int ksplit;            // stages per (category, side): K is split into ksplit pieces
+    int kqs;               // core matrices of A per stage = kq / ksplit
+    int kps;               // K per stage = kp / ksplit
+    int ksteps;            // MMA K steps per stage = kps / 8
+    int a_bytes;           // one FP32 A buffer: 16 * kqs * 128 + 128 (pad)
+    int b_bytes;           // one B buffer (TF32: hi or lo, NP * kps * 4; BF16: NP * kpb * 2)
+    int kpb;               // BF16: K per stage padded to 16
+    int a2_off;            // second A buffer in a slot: TF32 lo, or the BF16 operand
+    int b_off;             // B in a slot
+    int b_total;           // bytes of B per stage (TF32: hi + lo)
+    int slot_bytes;        // TF32 [A hi (copied, rounded in place)][A lo][B hi][B lo];
+                           // BF16 [A as copied][A bf16][B bf16]
+    long long b_stage;     // floats between consecutive stages' B blocks in tcb
     int ntiles;            // Ppad / 128
     int groups_per_slot;   // Ppad / 8 (third coordinate of the partial tensor map)
 };
@@ -110,15 +120,21 @@ __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, 
     return it;
 }
 
-// stages of an item: for each category, the internal sides in order L, R
-__device__ __forceinline__ int tc_nstages(const TcItem &it, int C) { return C * ((int)it.lint + (int)it.rint); }
-__device__ __forceinline__ void tc_stage(const TcItem &it, int st, int &c, int &side) {
+// stages of an item: for each category, the internal sides in order L, R,
+// each in ksplit pieces of K
+__device__ __forceinline__ int tc_nstages(const TcItem &it, int C, int ksplit) {
+    return C * ((int)it.lint + (int)it.rint) * ksplit;
+}
+__device__ __forceinline__ void tc_stage(const TcItem &it, int st, int ksplit, int &c, int &side, int &kh) {
     const int per = (int)it.lint + (int)it.rint;
-    c = st / per;
-    side = per == 2 ? (st & 1) : (it.lint ? 0 : 1);
+    c = st / (per * ksplit);
+    const int rem = st % (per * ksplit);
+    side = per == 2 ? rem / ksplit : (it.lint ? 0 : 1);
+    kh = rem % ksplit;
 }
 
-template <int NP, int NSTAGE>
+// BF: one BF16 pass (kind::f16, FP32 accumulate) instead of three TF32 passes.
+template <int NP, int NSTAGE, bool BF>
 __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constant__ CUtensorMap tmA, const TcParams T,
                                                          const int op0, const int nl, const int fused_nops) {
     const MixParams &P = T.M;
@@ -135,21 +151,26 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
     }
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(P.state_unknown + 1) * C * npad;
-    const int slot_bytes = 2 * T.a_bytes + 2 * T.b_bytes;
-    const unsigned stage_tx = (unsigned)(16 * kq * 128 + 2 * T.b_bytes);
+    const int kqs = T.kqs, ksplit = T.ksplit;
+    const int a_raw = 16 * kqs * 128;  // one stage's A slice as copied
+    const unsigned stage_tx = (unsigned)(a_raw + T.b_total);
 
     extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    // full: slot filled by TMA; mmab: the slot's MMAs complete; ebar: a
+    // category's MMAs complete (by category parity)
     __shared__ unsigned long long full[NSTAGE], mmab[NSTAGE], ebar[2];
     __shared__ unsigned tmem_base_s;
     __shared__ int4 opc[kTcOpCache];
     // tiled TMA destinations want 128-byte alignment: round the dynamic base up (128 B spare requested)
     unsigned char *const tc_smem = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+    auto slot_at = [&](int s) { return tc_smem + s * T.slot_bytes; };
 
-    // pads after each slot's A buffers must hold finite values (zero)
-    for (int i = r; i < NSTAGE * 2 * 32; i += kTcRows) {
-        const int s = i / 64, h = (i / 32) & 1;
-        float *pad = (float *)(tc_smem + s * slot_bytes + h * T.a_bytes + 16 * kq * 128);
-        pad[i & 31] = 0.f;
+    // pads after each slot's TF32 A buffers must hold finite values (zero)
+    if (!BF) {
+        for (int i = r; i < NSTAGE * 2 * 32; i += kTcRows) {
+            float *pad = (float *)(slot_at(i / 64) + ((i / 32) & 1) * T.a2_off + a_raw);
+            pad[i & 31] = 0.f;
+        }
     }
     {
         const int base = fused ? 0 : op0, cnt = fused ? fused_nops : nl;
@@ -196,10 +217,10 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
     // NSTAGE when every committed MMA is known to be complete.
     auto try_issue = [&](int ahead) {
         if (r != 0 || failed) return;
-        while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C)) next_issue_item();
+        while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C, ksplit)) next_issue_item();
         while (iss_item < nitems && issued < consumed + ahead) {
-            int c, side;
-            tc_stage(iss_it, iss_st, c, side);
+            int c, side, kh;
+            tc_stage(iss_it, iss_st, ksplit, c, side, kh);
             const int child = side == 0 ? iss_it.lref : iss_it.rref;
             if (fused) {  // a child written by an op of this CTA that has not finished yet
                 for (int j = finalized; j < iss_item; j++)
@@ -212,22 +233,22 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
                     return;
                 }
             }
-            unsigned char *slot = tc_smem + s * slot_bytes;
+            unsigned char *slot = slot_at(s);
             mbar_expect_tx(&full[s], stage_tx);
-            // A: 16 row groups x kq core matrices of category c (one tiled copy)
-            tma_load_3d(slot, &tmA, 0, c * kq, child * T.groups_per_slot + iss_it.tile * 16, &full[s]);
+            // A: 16 row groups x kqs core matrices of category c, K piece kh (one tiled copy)
+            tma_load_3d(slot, &tmA, 0, c * kq + kh * kqs, child * T.groups_per_slot + iss_it.tile * 16, &full[s]);
             const int ch = side == 0 ? iss_it.lch : 1 - iss_it.lch;
             const float *bsrc =
-                T.tcb + (long long)iss_it.k * T.tcb_stride + (long long)((ch * C + c) * 2) * NP * T.kp;
-            tma_load_1d(slot + 2 * T.a_bytes, bsrc, (unsigned)(2 * T.b_bytes), &full[s]);
+                T.tcb + (long long)iss_it.k * T.tcb_stride + (long long)((ch * C + c) * ksplit + kh) * T.b_stage;
+            tma_load_1d(slot + T.b_off, bsrc, (unsigned)T.b_total, &full[s]);
             issued++;
             iss_st++;
-            while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C)) next_issue_item();
+            while (iss_item < nitems && iss_st >= tc_nstages(iss_it, C, ksplit)) next_issue_item();
         }
     };
 
-    const uint32_t idesc = idesc_tf32(kTcRows, NP);
-    const unsigned a_sbo = (unsigned)(kq * 128), b_sbo = (unsigned)(T.kp / 4 * 128);
+    const uint32_t idesc = BF ? idesc_bf16(kTcRows, NP) : idesc_tf32(kTcRows, NP);
+    const unsigned a_sbo = (unsigned)(kqs * 128), b_sbo = (unsigned)(T.kps / 4 * 128);
     int ecount0 = 0, ecount1 = 0;  // commits made to ebar[0], ebar[1]
     bool abort = false;
     try_issue(NSTAGE);
@@ -285,20 +306,37 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
         float cmax = 0.f;
         for (int c = 0; c < C && !abort; c++) {
             // ---- this category's stages: convert to hi/lo, MMAs ----
-            for (int sd = 0; sd < per; sd++) {
+            for (int sk = 0; sk < per * ksplit; sk++) {
+                const int sd = sk / ksplit, kh = sk % ksplit;
+                const bool last = sk == per * ksplit - 1;
                 const int side = per == 2 ? sd : (it.lint ? 0 : 1);
                 const int s = consumed % NSTAGE;
                 const bool ok = mbar_wait(&full[s], (unsigned)((consumed / NSTAGE) & 1), kWaitPolls);
-                float *ah = (float *)(tc_smem + s * slot_bytes);
-                float *al = (float *)(tc_smem + s * slot_bytes + T.a_bytes);
+                float *ah = reinterpret_cast<float *>(slot_at(s));
+                unsigned char *a2 = slot_at(s) + T.a2_off;
                 if (ok) {
-                    const int base = (r >> 3) * kq * 32 + (r & 7) * 4;
-                    for (int q = 0; q < kq; q++) {
-                        const float4 v = *reinterpret_cast<float4 *>(ah + base + q * 32);
-                        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-                        *reinterpret_cast<float4 *>(ah + base + q * 32) = h;
-                        *reinterpret_cast<float4 *>(al + base + q * 32) =
-                            make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                    const int base = (r >> 3) * kqs * 32 + (r & 7) * 4;
+                    if constexpr (BF) {
+                        // this row's states, rounded to BF16, in [row group][8-state chunk][row][8] order
+                        const int nch = T.kpb / 8;
+                        uint4 *dst = reinterpret_cast<uint4 *>(a2 + (r >> 3) * nch * 128 + (r & 7) * 16);
+                        for (int j = 0; j < nch; j++) {
+                            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                            const float4 v0 = 2 * j < kqs ? *reinterpret_cast<const float4 *>(ah + base + 2 * j * 32) : z;
+                            const float4 v1 =
+                                2 * j + 1 < kqs ? *reinterpret_cast<const float4 *>(ah + base + (2 * j + 1) * 32) : z;
+                            dst[j * 8] = make_uint4(bf16x2(v0.x, v0.y), bf16x2(v0.z, v0.w), bf16x2(v1.x, v1.y),
+                                                    bf16x2(v1.z, v1.w));
+                        }
+                    } else {
+                        float *al = reinterpret_cast<float *>(a2);
+                        for (int q = 0; q < kqs; q++) {
+                            const float4 v = *reinterpret_cast<const float4 *>(ah + base + q * 32);
+                            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+                            *reinterpret_cast<float4 *>(ah + base + q * 32) = h;
+                            *reinterpret_cast<float4 *>(al + base + q * 32) =
+                                make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                        }
                     }
                 }
                 fence_proxy_async_smem();
@@ -306,22 +344,29 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
                 if (r == 0) {
                     tc_fence_after();
                     const unsigned d = tmem + (unsigned)((c & 1) * 2 * NP + side * NP);
-                    const unsigned uah = smem_u32(ah), ual = smem_u32(al);
-                    const unsigned ubh = smem_u32(tc_smem + s * slot_bytes + 2 * T.a_bytes);
-                    const unsigned ubl = ubh + (unsigned)T.b_bytes;
-                    for (int ks = 0; ks < T.ksteps; ks++) {
-                        const uint64_t dah = smem_desc(uah + ks * 256, 128, a_sbo);
-                        const uint64_t dal = smem_desc(ual + ks * 256, 128, a_sbo);
-                        const uint64_t dbh = smem_desc(ubh + ks * 256, 128, b_sbo);
-                        const uint64_t dbl = smem_desc(ubl + ks * 256, 128, b_sbo);
-                        mma_tf32(d, dal, dbh, idesc, ks > 0);
-                        mma_tf32(d, dah, dbl, idesc, true);
-                        mma_tf32(d, dah, dbh, idesc, true);
+                    const unsigned ub = smem_u32(slot_at(s) + T.b_off);
+                    if constexpr (BF) {
+                        const unsigned ua = smem_u32(a2), sbo = (unsigned)(T.kpb / 8 * 128);
+                        for (int ks = 0; ks < T.kpb / 16; ks++)
+                            mma_bf16(d, smem_desc(ua + ks * 256, 128, sbo), smem_desc(ub + ks * 256, 128, sbo), idesc,
+                                     ks > 0 || kh > 0);
+                    } else {
+                        const unsigned uah = smem_u32(ah), ual = smem_u32(a2);
+                        const unsigned ubl = ub + (unsigned)T.b_bytes;
+                        for (int ks = 0; ks < T.ksteps; ks++) {
+                            const uint64_t dah = smem_desc(uah + ks * 256, 128, a_sbo);
+                            const uint64_t dal = smem_desc(ual + ks * 256, 128, a_sbo);
+                            const uint64_t dbh = smem_desc(ub + ks * 256, 128, b_sbo);
+                            const uint64_t dbl = smem_desc(ubl + ks * 256, 128, b_sbo);
+                            mma_tf32(d, dal, dbh, idesc, ks > 0 || kh > 0);
+                            mma_tf32(d, dah, dbl, idesc, true);
+                            mma_tf32(d, dah, dbh, idesc, true);
+                        }
                     }
                     mma_commit(&mmab[s]);
-                    if (sd == per - 1) mma_commit(&ebar[c & 1]);
+                    if (last) mma_commit(&ebar[c & 1]);
                 }
-                if (sd == per - 1) {
+                if (last) {
                     if (c & 1) ecount1++;
                     else ecount0++;
                 }
@@ -373,30 +418,68 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 
 // B operands: per op, child, category: hi and lo of P_c(t)[x][y] in
 // [x/8][y/4][x%8][y%4] order, zero outside x < n, y < n.
+// B operands: per op, child, category and K piece kh: hi and lo of
+// P_c(t)[x][y] for y in piece kh, in [x/8][y'/4][x%8][y'%4] order (y' = y - kh
+// KS), zero outside x < n, y < n.
 __global__ void k_tc_prep_b(const float *opmats, long long op_stride, float *tcb, long long tcb_stride, int n,
-                            int npad, int C, int NP, int KP) {
+                            int npad, int C, int NP, int KP, int ksplit) {
     const int k = blockIdx.x, ch = blockIdx.y / C, c = blockIdx.y % C;
+    const int KS = KP / ksplit;
     const float *Pm = opmats + (long long)k * op_stride + (long long)ch * C * n * npad + (long long)c * n * npad;
-    float *hi = tcb + (long long)k * tcb_stride + (long long)((ch * C + c) * 2) * NP * KP;
-    float *lo = hi + NP * KP;
+    float *blk = tcb + (long long)k * tcb_stride + (long long)((ch * C + c) * ksplit) * 2 * NP * KS;
     for (int i = threadIdx.x; i < NP * KP; i += blockDim.x) {
         const int x = i / KP, y = i % KP;
+        const int kh = y / KS, yy = y % KS;
         const float v = (x < n && y < n) ? Pm[x * npad + y] : 0.f;
         const float h = tf32_hi(v);
-        const int off = (x >> 3) * (KP / 4) * 32 + (y >> 2) * 32 + (x & 7) * 4 + (y & 3);
+        float *hi = blk + (long long)kh * 2 * NP * KS;
+        const int off = (x >> 3) * (KS / 4) * 32 + (yy >> 2) * 32 + (x & 7) * 4 + (yy & 3);
         hi[off] = h;
-        lo[off] = v - h;
+        hi[NP * KS + off] = v - h;
+    }
+}
+
+// BF16 B operands: per op, child, category and K piece kh: P_c(t)[x][y] rounded
+// to BF16 for y = kh * KS + yy, in [x/8][yy/8][x%8][yy%8] order (KB = KS padded to
+// 16 columns), zero outside x < n, y < n.
+__global__ void k_tc_prep_b16(const float *opmats, long long op_stride, unsigned short *tcb, long long stride_h,
+                              int n, int npad, int C, int NP, int KS, int KB, int ksplit) {
+    const int k = blockIdx.x, ch = blockIdx.y / C, c = blockIdx.y % C;
+    const float *Pm = opmats + (long long)k * op_stride + (long long)ch * C * n * npad + (long long)c * n * npad;
+    for (int kh = 0; kh < ksplit; kh++) {
+        unsigned short *blk = tcb + (long long)k * stride_h + (long long)((ch * C + c) * ksplit + kh) * NP * KB;
+        for (int i = threadIdx.x; i < NP * KB; i += blockDim.x) {
+            const int x = i / KB, yy = i % KB, y = kh * KS + yy;
+            const float v = (x < n && yy < KS && y < n) ? Pm[x * npad + y] : 0.f;
+            const int off = (x >> 3) * (KB / 8) * 64 + (yy >> 3) * 64 + (x & 7) * 8 + (yy & 7);
+            blk[off] = (unsigned short)(bf16x2(v, 0.f) & 0xFFFFu);
+        }
     }
 }
 
 int tc_np(int npad) { return npad <= 32 ? 32 : 64; }
 int tc_kp(int npad) { return (npad + 7) / 8 * 8; }
+// 61-state models: each stage carries half of K (32 states), so a stage is half
+// the shared memory and two CTAs fit per SM; needs npad a multiple of 16
+// K pieces per stage (iqgpu_set_kpieces): 2 halves a stage's shared memory
+// (two 61-state CTAs per SM instead of one) at twice the stages per op; needs
+// npad > 32 and a multiple of 16.
+int tc_ksplit(const iqgpu_engine *e) {
+    return (e->tc_kpieces == 2 && e->npad > 32 && e->npad % 16 == 0) ? 2 : 1;
+}
 
 int launch_tc_prep(iqgpu_engine *e, int nops) {
     if (nops <= 0) return IQGPU_OK;
+    if (e->cfg.precision == IQGPU_BF16) {
+        const int NP = tc_np(e->npad), ks = tc_ksplit(e), KS = e->npad / ks, KB = (KS + 15) / 16 * 16;
+        k_tc_prep_b16<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32,
+                                                                 reinterpret_cast<unsigned short *>(e->d_tcb),
+                                                                 e->tcb_stride * 2, e->n, e->npad, e->C, NP, KS, KB, ks);
+        return cuda_fail(cudaGetLastError(), "tc_prep_b16");
+    }
     const int NP = tc_np(e->npad), KP = tc_kp(e->npad);
     k_tc_prep_b<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32, e->d_tcb, e->tcb_stride,
-                                                           e->n, e->npad, e->C, NP, KP);
+                                                           e->n, e->npad, e->C, NP, KP, tc_ksplit(e));
     return cuda_fail(cudaGetLastError(), "tc_prep_b");
 }
 
@@ -404,7 +487,6 @@ int launch_tc_prep(iqgpu_engine *e, int nops) {
 // matrices][32 floats]; a box of {32, kq, 16} is one category of a 128-pattern
 // tile in the operand layout. Built once per engine (the slots do not move).
 static int tc_tensor_map(iqgpu_engine *e) {
-    if (e->tc_tmap_ready) return IQGPU_OK;
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         void *fn = nullptr;
@@ -416,10 +498,11 @@ static int tc_tensor_map(iqgpu_engine *e) {
         }
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    const int kq = e->npad / 4;
+    const int kq = e->npad / 4, kqs = kq / tc_ksplit(e);
+    if (e->tc_tmap_ready && e->tc_tmap_kqs == kqs) return IQGPU_OK;
     const cuuint64_t dims[3] = {32, (cuuint64_t)e->C * kq, (cuuint64_t)e->cfg.nslots * (cuuint64_t)(e->Ppad / 8)};
     const cuuint64_t strides[2] = {128, (cuuint64_t)e->C * kq * 128};
-    const cuuint32_t box[3] = {32, (cuuint32_t)kq, 16};
+    const cuuint32_t box[3] = {32, (cuuint32_t)kqs, 16};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult res = encode(reinterpret_cast<CUtensorMap *>(e->tc_tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, e->d_part32,
                           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -429,27 +512,54 @@ static int tc_tensor_map(iqgpu_engine *e) {
         return IQGPU_ERR_CUDA;
     }
     e->tc_tmap_ready = true;
+    e->tc_tmap_kqs = kqs;
     return IQGPU_OK;
 }
 
-template <int NP, int NSTAGE>
-static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
-    int rc = tc_tensor_map(e);
-    if (rc) return rc;
+// Stage geometry of the tensor-core kernel for this engine.
+static TcParams tc_params(const iqgpu_engine *e, const MixParams &M, int NP, bool BF) {
     TcParams T;
     T.M = M;
     T.tcb = e->d_tcb;
     T.tcb_stride = e->tcb_stride;
     T.kq = e->npad / 4;
     T.kp = tc_kp(e->npad);
-    T.ksteps = T.kp / 8;
-    T.a_bytes = 16 * T.kq * 128 + 128;
-    T.b_bytes = NP * T.kp * 4;
+    T.ksplit = tc_ksplit(e);
+    T.kqs = T.kq / T.ksplit;
+    T.kps = T.kp / T.ksplit;
+    T.ksteps = T.kps / 8;
+    T.a_bytes = 16 * T.kqs * 128 + 128;
+    T.kpb = (T.kqs * 4 + 15) / 16 * 16;
+    T.a2_off = T.a_bytes;
+    if (BF) {  // [A as copied][A bf16][B bf16]
+        T.b_off = T.a_bytes + 16 * (T.kpb / 8) * 128;
+        T.b_bytes = NP * T.kpb * 2;
+        T.b_total = T.b_bytes;
+        T.b_stage = (long long)NP * T.kpb / 2;
+    } else {   // [A hi][A lo][B hi][B lo]
+        T.b_off = 2 * T.a_bytes;
+        T.b_bytes = NP * T.kps * 4;
+        T.b_total = 2 * T.b_bytes;
+        T.b_stage = 2LL * NP * T.kps;
+    }
+    T.slot_bytes = T.b_off + T.b_total;
     T.ntiles = (int)(e->Ppad / kTcRows);
     T.groups_per_slot = (int)(e->Ppad / 8);
+    return T;
+}
+
+static size_t tc_smem_bytes(const TcParams &T, int nstage) {
+    return (size_t)nstage * T.slot_bytes + 128;  // + alignment spare
+}
+
+template <int NP, int NSTAGE, bool BF>
+static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
+    int rc = tc_tensor_map(e);
+    if (rc) return rc;
+    const TcParams T = tc_params(e, M, NP, BF);
     const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
-    const size_t smem = (size_t)NSTAGE * (2 * T.a_bytes + 2 * T.b_bytes) + 128;  // + alignment spare
-    auto kern = k_traverse_tc<NP, NSTAGE>;
+    const size_t smem = tc_smem_bytes(T, NSTAGE);
+    auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     if (!e->level_sync) {
@@ -481,14 +591,37 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
     return IQGPU_OK;
 }
 
+template <int NP, bool BF>
+static int launch_tc_depth(iqgpu_engine *e, const MixParams &M, int depth) {
+    switch (depth) {
+    case 2: return launch_tc_t<NP, 2, BF>(e, M);
+    case 3: return launch_tc_t<NP, 3, BF>(e, M);
+    default: return launch_tc_t<NP, 4, BF>(e, M);
+    }
+}
+
+// Ring depth actually used: the requested one (iqgpu_set_stages; 0 = 2),
+// lowered until the CTA's shared memory fits the 227 KB a CTA may use.
+int tc_depth(const iqgpu_engine *e) {
+    const int NP = tc_np(e->npad);
+    const bool BF = e->cfg.precision == IQGPU_BF16;
+    MixParams M{};
+    const TcParams T = tc_params(e, M, NP, BF);
+    int depth = e->tc_stages ? e->tc_stages : 2;
+    while (depth > 2 && tc_smem_bytes(T, depth) + 4096 > 227u * 1024u) depth--;
+    return depth;
+}
+
 // The ops of a traversal on the tensor cores (the branch epilogue stays on
-// the CUDA-core kernel). Stage ring (iqgpu_set_stages): for <= 32 padded
-// states 4 slots (two CTAs per SM, 128 TMEM columns each) or 2 slots (four
-// CTAs per SM); for 64 padded states 2 slots (one CTA per SM, 256 columns).
+// the CUDA-core kernel). Per CTA: a ring of `depth` shared-memory slots; the
+// residency per SM follows from their size and from the 4 * NP tensor-memory
+// columns each CTA holds (depth 2: four CTAs per SM for 20 states, two for 61).
 int launch_traverse_tc(iqgpu_engine *e, const MixParams &M) {
     if (M.nops <= 0) return IQGPU_OK;
-    if (tc_np(e->npad) == 64) return launch_tc_t<64, 2>(e, M);
-    return e->tc_stages == 2 ? launch_tc_t<32, 2>(e, M) : launch_tc_t<32, 4>(e, M);
+    const int depth = tc_depth(e);
+    const bool BF = e->cfg.precision == IQGPU_BF16;
+    if (tc_np(e->npad) == 64) return BF ? launch_tc_depth<64, true>(e, M, depth) : launch_tc_depth<64, false>(e, M, depth);
+    return BF ? launch_tc_depth<32, true>(e, M, depth) : launch_tc_depth<32, false>(e, M, depth);
 }
 
 }  // namespace iqg

@@ -95,6 +95,7 @@ def lib():
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_set_kpieces": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
         "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
@@ -152,8 +153,8 @@ class Engine:
 
     @property
     def tensor_cores(self):
-        """True when the pattern-node update runs on the tensor cores (split TF32, 16..64 states)."""
-        return self.precision == TF32X3 and 16 <= self.nstates <= 64
+        """True when the pattern-node update runs on the tensor cores (split TF32 or BF16, 16..64 states)."""
+        return self.precision in (TF32X3, BF16) and 16 <= self.nstates <= 64
 
     @staticmethod
     def memory_required(**kw):
@@ -267,8 +268,12 @@ class Engine:
         _check(lib().iqgpu_set_schedule(self.h, int(bool(level_sync))))
 
     def set_stages(self, stages):
-        """Ring depth of the tensor-core traversal (0 = default, 2 or 4)."""
+        """Ring depth of the tensor-core traversal (0 = default, 2, 3 or 4)."""
         _check(lib().iqgpu_set_stages(self.h, int(stages)))
+
+    def set_kpieces(self, pieces):
+        """K pieces per stage of the tensor-core traversal (0/1 whole K, 2 halves)."""
+        _check(lib().iqgpu_set_kpieces(self.h, int(pieces)))
 
     def nni_batch(self, cands, max_nr_step=10, min_bl=1e-6, max_bl=10.0):
         """cands: iterable of ((sub0..sub3), (scratch0, scratch1), (len0..len3), central)."""

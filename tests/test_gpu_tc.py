@@ -148,3 +148,55 @@ def test_tc_full_size_configs(oracle_mod, kind):
     err = rel(lg, lo)
     print(f"{kind}: split-TF32 lnL {lg:.6f} oracle {lo:.6f} rel err {err:.2e}")
     assert err < LNL_RTOL
+
+
+# BF16 operands (one pass, FP32 accumulate): not a drop-in; the error is
+# measured and bounded loosely (stated here): lnL within 1e-3 relative of the
+# FP64 oracle, partials within 2e-2 of each pattern's largest entry.
+BF16_LNL_RTOL = 1e-3
+
+
+@pytest.mark.parametrize("name", ["prot12", "codon8"])
+def test_bf16_golden_lnl_and_partials(oracle_mod, name):
+    g = load_golden(name)
+    t = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, precision=engine.BF16)
+    lnl = t.compute_likelihood()
+    err = rel(lnl, g.lnl_std)
+    print(f"{name}: bf16 lnL rel err {err:.2e}")
+    assert err < BF16_LNL_RTOL
+    topo = Topology(g.edges, g.lengths, g.ntaxa)
+    eng = _engine(g, topo, engine.BF16)
+    assert eng.tensor_cores
+    done, ops = set(), []
+    for (u, v) in sorted(topo.slot):
+        ops += topo.ops_for(u, v, done)
+    eng.compute_partials(ops)
+    orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+    n, C = g.model.nstates, g.model.ncat
+    for (u, v), s in list(topo.slot.items())[:8]:
+        gp, _ = eng.partial(s)
+        op, _ = orc.partial(u, v)
+        std = np.einsum("xi,pci->pcx", g.model.evec, op.reshape(-1, C, n)).reshape(op.shape)
+        gn = gp / np.abs(gp).max(axis=1, keepdims=True)
+        on = std / np.abs(std).max(axis=1, keepdims=True)
+        assert np.max(np.abs(gn - on)) < 2e-2, (u, v)
+
+
+@pytest.mark.parametrize("kind", ["protein", "codon"])
+def test_bf16_schedules_agree(oracle_mod, kind):
+    ds = (simulate.protein_lg_dataset(30, 900, 41) if kind == "protein"
+          else simulate.codon_gy94_dataset(12, 500, 42))
+    topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    eng = _engine(ds, topo, engine.BF16)
+    got = {}
+    for cand in autotune.candidates(eng):
+        autotune.apply(eng, cand)
+        got[cand] = eng.compute_likelihood(ops, a, b, length)
+    assert len(set(got.values())) == 1, got
+    err = rel(next(iter(got.values())), want)
+    print(f"{kind}: bf16 lnL rel err {err:.2e}")
+    assert err < BF16_LNL_RTOL
