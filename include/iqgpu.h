@@ -172,8 +172,11 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
 /* Schedule of the mixed-precision traversal: 0 = one fused launch walking the
  * whole op list per pattern tile; 1 = one launch per tree level, all of the
- * level's (op, tile) pairs in flight together. Results do not depend on it. */
-int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync);
+ * level's (op, tile) pairs in flight together; 2 = dataflow: one persistent
+ * launch hands out (op, tile) pairs in level order and each waits (bounded)
+ * for its children's pairs (4-state one-thread-per-pattern kernel, tile 1;
+ * other kernels run fused). Results do not depend on it. */
+int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots
  * of shared memory), 2, 3 or 4; 0 = default (3). A depth whose shared memory

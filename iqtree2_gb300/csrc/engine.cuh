@@ -24,10 +24,10 @@ constexpr int kMaxCat = 16;
 struct OpDev {
     int32_t dad_slot;
     int32_t child[2];
-    int32_t pad;
+    int32_t prod0;      // mixed engines: index (in the uploaded list) of the op writing child 0, or -1
     double len[2];
     long long mat_off;  // doubles into Engine::d_opmats
-    long long pad2;
+    long long prod1;    // as prod0, for child 1
 };
 
 // Deterministic grid reduction: each CTA writes its partial sums, the last
@@ -110,6 +110,10 @@ struct iqgpu_engine {
     int *level_off;           // [max_ops + 2] first op of each level (ops are uploaded level-sorted)
     int nlevels;
     int *d_status;            // device status word (bounded waits that gave up)
+    bool flow;                // dataflow schedule (4-state one-thread-per-pattern kernel)
+    unsigned *d_flow_done;    // [max_ops][Ppad/128] epoch at which each (op, tile) item finished
+    unsigned *d_flow_ticket;  // next item to hand out
+    unsigned flow_epoch;
     // tensor-core contraction (precision IQGPU_TF32X3, 16 <= n <= 64)
     bool tc;
     float *d_tcb;             // per op: [child 2][C][hi, lo][NP*KP] P(t) in core-matrix order

@@ -27,7 +27,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 static long long round_up(long long v, long long g) { return (v + g - 1) / g * g; }
 
 struct Sizes {
-    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, total, op_stride;
+    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, flow, total, op_stride;
 };
 
 static int check_config(const iqgpu_config *c) {
@@ -81,9 +81,10 @@ static Sizes sizes(const iqgpu_config *c) {
         s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
     }
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
+    s.flow = is_mixed(c) ? (long long)(c->max_ops + 1) * (s.Ppad / 128) * 4 : 0;
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
-    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + 2 * s.Ppad * 8 +
+    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + 2 * s.Ppad * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
     return s;
 }
@@ -141,7 +142,8 @@ static void free_engine(iqgpu_engine *e) {
     void *dev_ptrs[] = {e->d_eval, e->d_evec, e->d_inv, e->d_rates, e->d_props, e->d_tip, e->d_freq,
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
-                        e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb};
+                        e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
+                        e->d_flow_done};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -265,6 +267,8 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
         CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
         CKE(cudaMemsetAsync(e->d_exp, 0, (long long)cfg->nslots * e->Ppad * 4, e->st));
         CKE(cudaMemsetAsync(e->d_opmats32, 0, s.opmats, e->st));
+        CKE(dalloc(e, &e->d_flow_done, s.flow));
+        CKE(cudaMemsetAsync(e->d_flow_done, 0, s.flow, e->st));
         if (uses_tc(cfg)) {
             e->tc = true;
             e->tcb_stride = tcb_stride(cfg);
@@ -280,8 +284,9 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     CKE(dalloc(e, &e->d_bscale, e->Ppad * 8));
     CKE(dalloc(e, &e->d_plh, e->Ppad * 8));
     CKE(dalloc(e, &e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
-    CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at byte 32
+    CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at byte 32, flow ticket at 48
     e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
+    e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
     CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
     CKE(halloc(e, &e->h_ops, s.ops));
     CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
@@ -449,6 +454,8 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         e->level_off[cur] = nops;
         e->nlevels = maxl;  // level l (1-based) spans [level_off[l-1], level_off[l])
     }
+    // producer of each child within the uploaded list (dataflow schedule)
+    std::vector<int> writer(is_mixed(&e->cfg) ? e->cfg.nslots : 0, -1);
     for (int i = 0; i < nops; i++) {
         const int k = order[i];
         const iqgpu_op &o = ops[k];
@@ -456,21 +463,22 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         d.dad_slot = o.dad_slot;
         d.child[0] = o.child[0];
         d.child[1] = o.child[1];
-        d.pad = 0;
+        d.prod0 = (!writer.empty() && o.child[0] >= 0) ? writer[o.child[0]] : -1;
         d.len[0] = o.len[0];
         d.len[1] = o.len[1];
         d.mat_off = (long long)i * e->op_stride;
-        d.pad2 = 0;
+        d.prod1 = (!writer.empty() && o.child[1] >= 0) ? writer[o.child[1]] : -1;
+        if (!writer.empty()) writer[o.dad_slot] = i;
     }
     int total = nops;
     if (extra) {
         OpDev &d = e->h_ops[nops];
         d.dad_slot = -1;
         d.child[0] = d.child[1] = b;
-        d.pad = 0;
+        d.prod0 = -1;
         d.len[0] = d.len[1] = len;
         d.mat_off = (long long)nops * e->op_stride;
-        d.pad2 = 0;
+        d.prod1 = -1;
         total++;
     }
     CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
@@ -715,9 +723,10 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
     return IQGPU_OK;
 }
 
-int iqgpu_set_schedule(iqgpu_engine *e, int32_t level_sync) {
-    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
-    e->level_sync = level_sync != 0;
+int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
+    if (!e || schedule < 0 || schedule > 2) { set_error("schedule must be 0, 1 or 2"); return IQGPU_ERR_ARG; }
+    e->level_sync = schedule == 1;
+    e->flow = schedule == 2;
     return IQGPU_OK;
 }
 

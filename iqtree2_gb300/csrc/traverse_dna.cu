@@ -8,8 +8,11 @@
 // stores its block in registers; the only barrier per op is the one that
 // publishes the op's TMA-staged P(t) matrices (double-buffered, so op k+1's
 // copy is in flight while op k computes). A level-synchronous form
-// (k_level_dna) runs each tree level as one launch.
+// (k_level_dna) runs each tree level as one launch, and a dataflow form
+// (k_flow_dna) runs the whole list as one persistent launch.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "mixed.cuh"
 
@@ -189,16 +192,15 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
     }
 }
 
-// Level-synchronous form: CTA (x, y) computes op op0 + y for patterns
-// 128 x .. 128 x + 127, one thread per pattern and all of its categories. All
-// (op, tile) pairs of a level are independent, so every child load of the
-// level can be in flight at once; the op's P(t) blocks (2 x ncat x 16 floats)
-// are read through the read-only cache (warp-uniform addresses).
-__global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0) {
+// One op k for the 128 patterns of tile `tile`, one thread per pattern and all
+// of its categories. Children and exponents are read at L2 (ld.global.cg):
+// under the dataflow schedule they were written by other CTAs of the same
+// launch. The op's P(t) blocks (2 x ncat x 16 floats) come through the
+// read-only cache (warp-uniform addresses).
+__device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile) {
     constexpr int n = 4, npad = 4;
     const int C = P.ncat, S = P.state_unknown;
-    const int k = op0 + blockIdx.y;
-    const long long p = (long long)blockIdx.x * kDnaTile + threadIdx.x;
+    const long long p = tile * kDnaTile + threadIdx.x;
     const long long ld = P.ldp;
     const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
     const long long PM = (long long)C * n * npad;
@@ -217,13 +219,14 @@ __global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const
     const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
     const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
     const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
-    const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+    const int e = (lint ? __ldcg(P.expo + (long long)lref * ld + p) : 0) +
+                  (rint ? __ldcg(P.expo + (long long)rref * ld + p) : 0);
     float4 lv[kDnaMaxCat], rv[kDnaMaxCat], out[kDnaMaxCat];
 #pragma unroll
     for (int c = 0; c < kDnaMaxCat; c++) {
         if (c < C) {
-            lv[c] = lint ? __ldcs(reinterpret_cast<const float4 *>(Lp + c * 32)) : ld4(tl + c * npad);
-            rv[c] = rint ? __ldcs(reinterpret_cast<const float4 *>(Rp + c * 32)) : ld4(tr + c * npad);
+            lv[c] = lint ? __ldcg(reinterpret_cast<const float4 *>(Lp + c * 32)) : ld4(tl + c * npad);
+            rv[c] = rint ? __ldcg(reinterpret_cast<const float4 *>(Rp + c * 32)) : ld4(tr + c * npad);
         }
     }
     float mx = 0.f;
@@ -270,6 +273,64 @@ __global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const
     P.expo[(long long)op.dad_slot * ld + p] = e - sh;
 }
 
+// Level-synchronous form: CTA (x, y) computes op op0 + y for tile x. All
+// (op, tile) pairs of a level are independent, so every child load of the
+// level can be in flight at once.
+__global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0) {
+    dna_op(P, op0 + blockIdx.y, blockIdx.x);
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Dataflow form: one persistent launch. CTAs take items i = k * ntiles + t
+// (op k of the level-ordered list, tile t) from an atomic ticket in increasing
+// order; before computing, an item waits until the items that produce its
+// children for the same tile carry this launch's epoch. Every producer has a
+// smaller index, so it was taken earlier by a CTA that is running, and the
+// waits end; they are bounded all the same (status word, then the CTA stops).
+__global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsigned *done, unsigned *ticket,
+                                                        const unsigned epoch, const int ntiles) {
+    __shared__ int s_item;
+    __shared__ int s_ok;
+    const long long total = (long long)P.nops * ntiles;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_item = (int)atomicAdd(ticket, 1u);
+            int ok = 1;
+            const long long i = s_item;
+            if (i < total) {
+                const int k = (int)(i / ntiles), t = (int)(i % ntiles);
+                const OpDev op = P.ops[k];
+                const int prod[2] = {op.prod0, (int)op.prod1};
+                for (int j = 0; j < 2 && ok; j++) {
+                    if (prod[j] < 0) continue;
+                    const unsigned *f = done + (long long)prod[j] * ntiles + t;
+                    unsigned polls = 0;
+                    while (ld_acquire(f) != epoch) {
+                        if (++polls >= kWaitPolls || *(volatile int *)P.status != 0) { ok = 0; break; }
+                    }
+                }
+                if (!ok) atomicExch(P.status, kStatusTimeout);
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        const long long i = s_item;
+        const int ok = s_ok;
+        __syncthreads();  // s_item / s_ok are rewritten by the next iteration
+        if (i >= total || !ok) return;
+        const int k = (int)(i / ntiles), t = (int)(i % ntiles);
+        dna_op(P, k, t);
+        __threadfence();  // this thread's outputs are visible device-wide before the flag
+        __syncthreads();
+        if (threadIdx.x == 0) atomicExch(done + i, epoch);
+    }
+}
+
 int launch_levels_dna(iqgpu_engine *e, const MixParams &P) {
     const int grid = (int)(e->Ppad / kDnaTile);
     for (int l = 0; l < e->nlevels; l++) {
@@ -280,6 +341,22 @@ int launch_levels_dna(iqgpu_engine *e, const MixParams &P) {
         if (err != cudaSuccess) return cuda_fail(err, "level_dna");
     }
     return IQGPU_OK;
+}
+
+int launch_flow_dna(iqgpu_engine *e, const MixParams &P) {
+    if (P.nops <= 0) return IQGPU_OK;
+    const int ntiles = (int)(e->Ppad / kDnaTile);
+    if (++e->flow_epoch == 0) e->flow_epoch = 1;  // 0 is the value of never-finished items
+    cudaError_t err = cudaMemsetAsync(e->d_flow_ticket, 0, 4, e->st);
+    if (err != cudaSuccess) return cuda_fail(err, "flow ticket reset");
+    int per_sm = 1, sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flow_dna, kDnaTile, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    const long long items = (long long)P.nops * ntiles;
+    const int grid = (int)std::min<long long>(items, (long long)per_sm * sms);
+    k_flow_dna<<<grid, kDnaTile, 0, e->st>>>(P, e->d_flow_done, e->d_flow_ticket, e->flow_epoch, ntiles);
+    return cuda_fail(cudaGetLastError(), "flow_dna");
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi) {

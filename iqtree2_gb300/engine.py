@@ -264,8 +264,9 @@ class Engine:
     def set_tile(self, patterns_per_cta):
         _check(lib().iqgpu_set_tile(self.h, int(patterns_per_cta)))
 
-    def set_schedule(self, level_sync):
-        _check(lib().iqgpu_set_schedule(self.h, int(bool(level_sync))))
+    def set_schedule(self, schedule):
+        """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel)."""
+        _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
 
     def set_stages(self, stages):
         """Ring depth of the tensor-core traversal (0 = default, 2, 3 or 4)."""
