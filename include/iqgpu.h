@@ -320,6 +320,26 @@ int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl);
 /* Pattern-node updates executed so far (throughput accounting). */
 int iqgpu_tree_num_updates(iqgpu_tree *t, int64_t *updates);
 
+/* ---- partitions: one graph launch over several engines ------------------- */
+/* Replaces the OpenMP loop of PhyloSuperTree::computeLikelihood
+ * (tree/phylosupertree.cpp:701-723) over per-partition PhyloTrees: a group of
+ * engines (one per partition, each with its own model, patterns, buffers and
+ * stream, all on one device) whose branch-lnL evaluations are captured into
+ * one CUDA graph (the partitions' kernels run concurrently on forked streams)
+ * and replayed with one launch. */
+typedef struct iqgpu_group iqgpu_group;
+int iqgpu_group_create(iqgpu_engine *const *engines, int32_t n, iqgpu_group **out);
+/* Per member: op list (ops[i], nops[i]) that makes partial a current, and the
+ * branch (a[i], b[i], len[i]) to evaluate. Stages the lists, captures and
+ * instantiates the graph. */
+int iqgpu_group_prepare(iqgpu_group *g, const iqgpu_op *const *ops, const int32_t *nops, const int32_t *a,
+                        const int32_t *b, const double *len);
+/* New branch lengths for the same traversals (same slots and children). */
+int iqgpu_group_set_lengths(iqgpu_group *g, const iqgpu_op *const *ops, const double *len);
+/* One replay: lnL of every member (per_part may be NULL) and their sum. */
+int iqgpu_group_lnl(iqgpu_group *g, double *per_part, double *total);
+int iqgpu_group_destroy(iqgpu_group *g);
+
 #ifdef __cplusplus
 }
 #endif

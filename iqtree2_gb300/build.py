@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libiqgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
-SOURCES = ["iqgpu.cu", "kernels_f64.cu", "kernels_mixed.cu", "traverse_mixed.cu", "noalloc.cu", "batch_nni.cu", "batch_rell.cu", "tree.cpp", "server.cpp", "simulate.cu", "traverse_dna.cu", "traverse_tc.cu"]
+SOURCES = ["iqgpu.cu", "kernels_f64.cu", "kernels_mixed.cu", "traverse_mixed.cu", "noalloc.cu", "batch_nni.cu", "batch_rell.cu", "tree.cpp", "server.cpp", "simulate.cu", "traverse_dna.cu", "traverse_tc.cu", "group.cu"]
 
 
 def nvcc():

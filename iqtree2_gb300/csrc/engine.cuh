@@ -111,9 +111,8 @@ struct iqgpu_engine {
     int nlevels;
     int *d_status;            // device status word (bounded waits that gave up)
     bool flow;                // dataflow schedule (4-state one-thread-per-pattern kernel)
-    unsigned *d_flow_done;    // [max_ops][Ppad/128] epoch at which each (op, tile) item finished
+    unsigned *d_flow_done;    // [max_ops][Ppad/128] nonzero once each (op, tile) item finished
     unsigned *d_flow_ticket;  // next item to hand out
-    unsigned flow_epoch;
     // tensor-core contraction (precision IQGPU_TF32X3, 16 <= n <= 64)
     bool tc;
     float *d_tcb;             // per op: [child 2][C][hi, lo][NP*KP] P(t) in core-matrix order
@@ -156,6 +155,11 @@ int tc_np(int npad);  // N of the MMA: npad padded to 32 or 64
 int tc_kp(int npad);  // K of the MMA: npad padded to the TF32 K step
 int tc_ksplit(const iqgpu_engine *e);  // K pieces per (category, side) stage
 int launch_tc_prep(iqgpu_engine *e, int nops);
+
+// op lists: host validation, level ordering and upload (stage_ops), and the
+// per-op precompute launches for an uploaded list (launch_op_info)
+int stage_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch, int32_t b, double len);
+int launch_op_info(iqgpu_engine *e, int nops, bool branch);
 
 // side buffers of the batched entry points, released with the engine
 void nni_release(iqgpu_engine *e);

@@ -412,7 +412,7 @@ static int check_ref(iqgpu_engine *e, int32_t r) {
 // branch evaluation appends one entry (index nops) whose child 0 is the far
 // end b of the branch with the branch length.
 static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch = false, int32_t b = 0,
-                      double len = 0.0) {
+                      double len = 0.0, bool stage_only = false) {
     if (nops < 0 || nops > e->cfg.max_ops || (nops > 0 && !ops)) {
         set_error("traversal length out of range");
         return IQGPU_ERR_ARG;
@@ -482,11 +482,28 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         total++;
     }
     CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
+    return stage_only ? IQGPU_OK : launch_op_info(e, nops, extra);
+}
+
+}  // extern "C"
+
+namespace iqg {
+// Per-op P(t) / echild and leaf tables for the uploaded list (+ the branch
+// block when `branch`), and the tensor-core B operands.
+int launch_op_info(iqgpu_engine *e, int nops, bool branch) {
+    const int total = nops + (branch ? 1 : 0);
     if (!is_mixed(&e->cfg)) return launch_partial_info_f64(e, total);
     int rc = launch_partial_info_mixed(e, total);
     if (rc == IQGPU_OK && e->tc) rc = launch_tc_prep(e, nops);
     return rc;
 }
+
+int stage_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch, int32_t b, double len) {
+    return upload_ops(e, ops, nops, branch, b, len, true);
+}
+}  // namespace iqg
+
+extern "C" {
 
 // Fold the last timed traversal into the running total.
 static int settle_timing(iqgpu_engine *e) {

@@ -288,8 +288,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 
 // Dataflow form: one persistent launch. CTAs take items i = k * ntiles + t
 // (op k of the level-ordered list, tile t) from an atomic ticket in increasing
-// order; before computing, an item waits until the items that produce its
-// children for the same tile carry this launch's epoch. Every producer has a
+// order; before computing, an item waits until the flags of the items that
+// produce its children for the same tile read `epoch` (flags are cleared
+// before every launch). Every producer has a
 // smaller index, so it was taken earlier by a CTA that is running, and the
 // waits end; they are bounded all the same (status word, then the CTA stops).
 __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsigned *done, unsigned *ticket,
@@ -331,31 +332,54 @@ __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsign
     }
 }
 
-int launch_levels_dna(iqgpu_engine *e, const MixParams &P) {
+int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
+
+// Level-synchronous schedule with a fused tail: levels whose (op, tile) pairs
+// fill the GPU (at least the resident CTAs of one wave) run one launch each;
+// the remaining narrow levels (a Yule tree ends in a chain of one-op levels)
+// and the branch epilogue run as one fused launch that walks them per tile.
+int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
     const int grid = (int)(e->Ppad / kDnaTile);
-    for (int l = 0; l < e->nlevels; l++) {
+    int per_sm = 1, sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level_dna, kDnaTile, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    const long long wave = (long long)per_sm * sms;
+    int l = 0;
+    for (; l < e->nlevels; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
+        if ((long long)nl * grid < wave) break;
         k_level_dna<<<dim3(grid, nl), kDnaTile, 0, e->st>>>(P, op0);
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "level_dna");
     }
-    return IQGPU_OK;
+    const int rest = l < e->nlevels ? e->level_off[l] : P.nops;
+    if (rest >= P.nops && epi == EPI_NONE) return IQGPU_OK;
+    // the tail ops [rest, nops) and the epilogue: shift the op list so the fused
+    // kernel sees them as ops 0.. (the branch matrices keep their block)
+    P.ops += rest;
+    P.opmats += (long long)rest * P.op_stride;
+    P.nops -= rest;
+    P.branch_op -= rest;
+    return launch_traverse_dna(e, P, epi);
 }
 
 int launch_flow_dna(iqgpu_engine *e, const MixParams &P) {
     if (P.nops <= 0) return IQGPU_OK;
     const int ntiles = (int)(e->Ppad / kDnaTile);
-    if (++e->flow_epoch == 0) e->flow_epoch = 1;  // 0 is the value of never-finished items
-    cudaError_t err = cudaMemsetAsync(e->d_flow_ticket, 0, 4, e->st);
-    if (err != cudaSuccess) return cuda_fail(err, "flow ticket reset");
+    // every launch starts from cleared flags and ticket (stream-ordered memsets,
+    // so the launch sequence can also be captured into a graph and replayed)
+    cudaError_t err = cudaMemsetAsync(e->d_flow_done, 0, (size_t)P.nops * ntiles * 4, e->st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(e->d_flow_ticket, 0, 4, e->st);
+    if (err != cudaSuccess) return cuda_fail(err, "flow flag reset");
     int per_sm = 1, sms = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flow_dna, kDnaTile, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
     const long long items = (long long)P.nops * ntiles;
     const int grid = (int)std::min<long long>(items, (long long)per_sm * sms);
-    k_flow_dna<<<grid, kDnaTile, 0, e->st>>>(P, e->d_flow_done, e->d_flow_ticket, e->flow_epoch, ntiles);
+    k_flow_dna<<<grid, kDnaTile, 0, e->st>>>(P, e->d_flow_done, e->d_flow_ticket, 1u, ntiles);
     return cuda_fail(cudaGetLastError(), "flow_dna");
 }
 

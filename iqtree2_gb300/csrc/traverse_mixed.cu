@@ -399,7 +399,7 @@ static int dispatch_mix(iqgpu_engine *e, MixParams P) {
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
-int launch_levels_dna(iqgpu_engine *e, const MixParams &P);
+int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi);
 int launch_flow_dna(iqgpu_engine *e, const MixParams &P);
 int launch_traverse_tc(iqgpu_engine *e, const MixParams &M);
 
@@ -429,7 +429,8 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     // per-category tile was chosen explicitly
     if (e->n == 4 && e->C <= 4 && e->tile == 1) {
         if (!e->level_sync && !e->flow) return launch_traverse_dna(e, P, epi);
-        int rc = e->flow ? launch_flow_dna(e, P) : launch_levels_dna(e, P);
+        if (e->level_sync) return launch_levels_dna(e, P, epi);
+        int rc = launch_flow_dna(e, P);
         if (rc || epi == EPI_NONE) return rc;
         P.nops = 0;  // the epilogue alone
         return launch_traverse_dna(e, P, epi);

@@ -95,6 +95,11 @@ def lib():
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
+        "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
+        "iqgpu_group_set_lengths": ([vp, ct.c_void_p, ct.c_void_p], ct.c_int),
+        "iqgpu_group_lnl": ([vp, ct.c_void_p, ct.c_void_p], ct.c_int),
+        "iqgpu_group_destroy": ([vp], ct.c_int),
         "iqgpu_set_kpieces": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
@@ -297,6 +302,55 @@ class Engine:
         out = np.zeros((plh.shape[0], self._nreps))
         _check(lib().iqgpu_rell(self.h, _dp(plh), plh.shape[0], _dp(out)))
         return out
+
+
+class Group:
+    """Partitions as one graph launch: engines (one per partition) evaluated together."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        arr = (ct.c_void_p * len(self.engines))(*[e.h.value for e in self.engines])
+        h = ct.c_void_p()
+        _check(lib().iqgpu_group_create(ct.cast(arr, ct.c_void_p), len(self.engines), ct.byref(h)))
+        self.h = h
+        self._keep = None
+
+    def _lists(self, ops_list):
+        arrs = [o if isinstance(o, np.ndarray) else Engine.ops_array(o) for o in ops_list]
+        ptrs = (ct.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        return arrs, ptrs
+
+    def prepare(self, ops_list, a, b, lengths):
+        arrs, ptrs = self._lists(ops_list)
+        self._keep = arrs
+        nops = np.array([len(x) for x in arrs], np.int32)
+        aa, bb = np.asarray(a, np.int32), np.asarray(b, np.int32)
+        ll = np.asarray(lengths, np.float64)
+        _check(lib().iqgpu_group_prepare(self.h, ct.cast(ptrs, ct.c_void_p), nops.ctypes.data, aa.ctypes.data,
+                                         bb.ctypes.data, ll.ctypes.data))
+
+    def set_lengths(self, ops_list, lengths):
+        arrs, ptrs = self._lists(ops_list)
+        self._keep = arrs
+        ll = np.asarray(lengths, np.float64)
+        _check(lib().iqgpu_group_set_lengths(self.h, ct.cast(ptrs, ct.c_void_p), ll.ctypes.data))
+
+    def lnl(self):
+        per = np.zeros(len(self.engines))
+        tot = ct.c_double()
+        _check(lib().iqgpu_group_lnl(self.h, per.ctypes.data, ct.byref(tot)))
+        return tot.value, per
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().iqgpu_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class GpuTree:

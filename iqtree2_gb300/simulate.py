@@ -144,6 +144,23 @@ def dna_gtr_dataset(ntaxa, nsites, seed, mean_bl=0.1, alpha=0.5):
     return Dataset(f"dna{ntaxa}x{nsites}", ntaxa, nsites, edges, lengths, model, pats, freq)
 
 
+def partitioned_dna_datasets(ntaxa, sizes, seed, mean_bl=0.1):
+    """Partitions on one shared tree (edge-linked, equal branch lengths), each
+    with its own GTR+G4 (exchangeabilities, frequencies, alpha) and site count:
+    the shape of a PhyloSuperTree with separate models per partition."""
+    rng = np.random.default_rng(seed)
+    edges, lengths = yule_tree(ntaxa, mean_bl, rng)
+    out = []
+    for k, nsites in enumerate(sizes):
+        exch = rng.uniform(0.5, 3.0, size=6)
+        pi = rng.dirichlet([5.0, 5.0, 5.0, 5.0])
+        model = models.gtr_model(exch, pi, float(rng.uniform(0.3, 1.5)))
+        aln = simulate_alignment(ntaxa, edges, lengths, model, int(nsites), rng)
+        pats, freq = compress_patterns(aln)
+        out.append(Dataset(f"part{k}_dna{ntaxa}x{nsites}", ntaxa, int(nsites), edges, lengths, model, pats, freq))
+    return out
+
+
 def protein_lg_dataset(ntaxa, nsites, seed, mean_bl=0.05, alpha=0.8):
     """LG+G4 simulated with LG frequencies; the model then uses the empirical
     frequencies of the sampled alignment (the reference's +F)."""

@@ -103,3 +103,45 @@ def test_rell_matches_numpy():
     want = plh @ w.astype(np.float64).T
     assert got.shape == (70, 200)
     assert np.max(np.abs(got - want) / np.abs(want)) < 1e-6
+
+
+@pytest.mark.parametrize("precision", [engine.F32, engine.F64])
+def test_partition_group_one_graph(oracle_mod, precision):
+    """12 uneven DNA partitions with separate GTR+G4 on one tree, evaluated by
+    one graph launch: each partition's lnL equals the same engine evaluated
+    alone (bit for bit: same kernels) and the oracle's (1e-6 relative mixed,
+    1e-10 FP64); new branch lengths through set_lengths as well."""
+    from iqtree2_gb300 import simulate
+    sizes = [2000, 3000, 5000, 800, 12000, 7000, 2500, 1500, 9000, 4000, 6000, 30000]
+    parts = simulate.partitioned_dna_datasets(24, sizes, 61)
+    ds0 = parts[0]
+    topo = Topology(ds0.edges, ds0.lengths, ds0.ntaxa)
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = topo.branch_ops(nb, leaf)
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    engs = []
+    for ds in parts:
+        e = engine.Engine(ds.nptn, 4, ds.model.ncat, ds.ntaxa, ds.model.state_unknown, topo.nslots,
+                          precision=precision, max_ops=topo.nslots)
+        e.set_model(ds.model)
+        e.set_patterns(ds.freq)
+        e.set_tip_states(ds.patterns)
+        engs.append(e)
+    alone = [e.compute_likelihood(ops, a, b, length) for e in engs]
+    grp = engine.Group(engs)
+    grp.prepare([ops] * len(engs), [a] * len(engs), [b] * len(engs), [length] * len(engs))
+    tot, per = grp.lnl()
+    tot2, per2 = grp.lnl()  # replay
+    assert list(per) == alone and list(per2) == alone
+    assert tot == pytest.approx(sum(alone), rel=1e-14)
+    tol = 1e-6 if precision == engine.F32 else 1e-10
+    for ds, v in zip(parts, per):
+        want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+        assert rel(v, want) < tol
+    # all branch lengths scaled by 1.3: same traversals, new lengths
+    ops2 = [(d, c0, c1, 1.3 * l0, 1.3 * l1) for (d, c0, c1, l0, l1) in ops]
+    grp.set_lengths([ops2] * len(engs), [1.3 * length] * len(engs))
+    _, per3 = grp.lnl()
+    for e, v in zip(engs, per3):
+        assert v == e.compute_likelihood(ops2, a, b, 1.3 * length)
+    grp.close()
