@@ -34,11 +34,14 @@ WORKLOADS = {
     # the headline: protein LG+G4, 100 taxa x 50,000 sites
     "protein": dict(workload="protein LG+G4 100 taxa x 50000 sites, full lnL (98 partial updates + root lnL)",
                     model="LG+G4", taxa=100, sites=50000, seed=2, mean_bl=0.05, alpha=0.8),
-    # the same model on 5,000 sites: the small case for ncu captures
-    "protein-small": dict(workload="protein LG+G4 100 taxa x 5000 sites, full lnL", model="LG+G4", taxa=100,
-                          sites=5000, seed=2, mean_bl=0.05, alpha=0.8),
+    # the same model on 10,000 sites (~1 GB of partials): the small case for ncu captures
+    "protein-small": dict(workload="protein LG+G4 100 taxa x 10000 sites, full lnL", model="LG+G4", taxa=100,
+                          sites=10000, seed=2, mean_bl=0.05, alpha=0.8),
     "dna": dict(workload="DNA GTR+G4 16 taxa x 1000 sites, full lnL", model="GTR+G4", taxa=16, sites=1000,
                 seed=1, mean_bl=0.1, alpha=0.5),
+    # 200 taxa on 30,000 sites (~1.1 GB of partials): the DNA case for ncu captures
+    "dna-mid": dict(workload="DNA GTR+G4 200 taxa x 30000 sites, full lnL", model="GTR+G4", taxa=200,
+                    sites=30000, seed=4, mean_bl=0.1, alpha=0.5),
     "dna-large": dict(workload="DNA GTR+G4 200 taxa x 100000 sites, full lnL", model="GTR+G4", taxa=200,
                       sites=100000, seed=4, mean_bl=0.1, alpha=0.5),
     "codon": dict(workload="codon GY94+G4 40 taxa x 10000 codons, full lnL", model="GY94+G4", taxa=40,
@@ -68,16 +71,6 @@ def topology_ops(ds):
     nb = topo.adj[leaf][0][0]
     ops = topo.branch_ops(nb, leaf)
     return topo, ops, topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
-
-
-def op_levels(ops):
-    """Tree levels of a post-order op list (every child produced in a lower level)."""
-    lev, top = {}, 0
-    for (dad, c0, c1, _, _) in ops:
-        l = 1 + max([lev.get(c, 0) for c in (c0, c1) if c >= 0] + [0])
-        lev[dad] = l
-        top = max(top, l)
-    return top
 
 
 def kernel_name(use_tc, n, tile, bf16=False):
@@ -259,11 +252,13 @@ def measure_path(eng, ops_arr, a, b, length, steps, warmup, stream, local, dist)
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    launches0 = eng.launches()
     ev0.record(stream)
     for _ in range(steps):
         lnl = eng.compute_likelihood(ops_arr, a, b, length)
     ev1.record(stream)
     torch.cuda.synchronize()
+    launches = eng.launches() - launches0
     clk = clocks.stop()
     elapsed_ms = ev0.elapsed_time(ev1)
     kern_ms, kern_n = eng.timing()
@@ -272,7 +267,8 @@ def measure_path(eng, ops_arr, a, b, length, steps, warmup, stream, local, dist)
         t = torch.tensor([elapsed_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
-    return dict(lnl=lnl, elapsed_ms=elapsed_ms, kern_avg_s=kern_ms / max(kern_n, 1) / 1e3, clocks=clk)
+    return dict(lnl=lnl, elapsed_ms=elapsed_ms, kern_avg_s=kern_ms / max(kern_n, 1) / 1e3, clocks=clk,
+                launches=launches)
 
 
 def make_engine(ds, topo, precision, local, stream):
@@ -309,10 +305,12 @@ def run_ours(args):
     peaks, peak_src = measured_peaks()
 
     # FP64 drop-in path, reported beside the headline
-    eng64 = make_engine(ds, topo, engine.F64, local, stream)
-    r64 = measure_path(eng64, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
-    eng64.close()
     b64, f64 = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=False)
+    r64 = None
+    if not args.headline_only:
+        eng64 = make_engine(ds, topo, engine.F64, local, stream)
+        r64 = measure_path(eng64, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
+        eng64.close()
 
     # headline: mixed-precision path (split-TF32 tensor cores for 16..64 states,
     # FP32 CUDA cores otherwise); schedule / pattern tile picked by the autotuner
@@ -320,7 +318,7 @@ def run_ours(args):
     use_tc = args.precision == "tf32x3" or (args.precision == "auto" and 16 <= m.nstates <= 64)
     prec = engine.TF32X3 if use_tc else engine.F32
     beside = None
-    if use_tc:  # the FP32 CUDA-core kernel, reported beside the tensor-core headline
+    if use_tc and not args.headline_only:  # the FP32 CUDA-core kernel, reported beside the tensor-core headline
         engc = make_engine(ds, topo, engine.F32, local, stream)
         ctile, ctile_ms = autotune.tune(engc, ops_arr, a, b, length)
         rc_ = measure_path(engc, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
@@ -328,15 +326,18 @@ def run_ours(args):
                       value=updates_per_step * max(3, args.steps // 4) / (rc_["elapsed_ms"] / 1e3))
         engc.close()
     eng = make_engine(ds, topo, prec, local, stream)
-    tile, tile_ms = autotune.tune(eng, ops_arr, a, b, length)
+    if args.config:  # fixed configuration (profiling runs): no tuning
+        fixed = next((c for c in autotune.candidates(eng) if autotune.label(c) == args.config), None)
+        if fixed is None:
+            raise SystemExit(f"--config {args.config}: not a candidate here "
+                             f"({', '.join(autotune.label(c) for c in autotune.candidates(eng))})")
+        autotune.apply(eng, fixed)
+        tile, tile_ms = args.config, {}
+    else:
+        tile, tile_ms = autotune.tune(eng, ops_arr, a, b, length)
     r = measure_path(eng, ops_arr, a, b, length, args.steps, args.warmup, stream, local, dist)
     value = updates_per_step * args.steps * world / (r["elapsed_ms"] / 1e3)
     bmx, fmx = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=True)
-    level_sched = "/level" in tile
-    nlev = op_levels(ops)
-    # launches per step: P(t) preparation, [B-operand prep], traversal (one per level
-    # on the level schedule), [separate branch epilogue]
-    launches = 1 + (nlev if level_sched else 1) + (2 if use_tc else (1 if level_sched else 0))
 
     # end to end through the C ABI from host buffers: inputs copied each step, lnL read back
     e2e_steps = max(2, min(args.steps, 10))
@@ -351,7 +352,7 @@ def run_ours(args):
     h2d = ds.patterns.nbytes + ds.freq.nbytes + sum(x.nbytes for x in (m.eval, m.evec, m.inv_evec, m.rates,
                                                                         m.props, m.tip_lh, m.pi)) + ops_arr.nbytes
     assert lnl_e2e == r["lnl"]
-    if use_tc:  # BF16 operands (one MMA pass), reported beside: speed and lnL error
+    if use_tc and not args.headline_only:  # BF16 operands (one MMA pass), reported beside: speed and lnL error
         engb = make_engine(ds, topo, engine.BF16, local, stream)
         btile, _ = autotune.tune(engb, ops_arr, a, b, length)
         rb = measure_path(engb, ops_arr, a, b, length, max(3, args.steps // 4), args.warmup, stream, local, dist)
@@ -359,7 +360,8 @@ def run_ours(args):
     if rank != 0:
         return
     achieved = bmx / r["kern_avg_s"] / 1e9
-    a64 = b64 / r64["kern_avg_s"] / 1e9
+    npad = (m.nstates + 3) // 4 * 4
+    slot_mb = (ds.nptn + 127) // 128 * 128 * m.ncat * npad * 4 / 1e6
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["elapsed_ms"] / args.steps, "higher_is_better": True,
@@ -369,35 +371,41 @@ def run_ours(args):
                        "FP32 standard-basis partials, per-pattern 2^k exponents, FP64 exp/log/sums",
                        nptn=ds.nptn, parallelism=f"replicas x{world}",
                        tile=tile, tile_ms={str(k): v for k, v in tile_ms.items()},
-                       l2="inputs larger than L2 (98 partials x 14 MB per step)"),
+                       l2=f"inputs larger than L2 ({len(ops)} partials x {slot_mb:.1f} MB written and read "
+                          f"per step, L2 129 MB)"),
         "full_lnl_evals_per_s": 1e3 * args.steps / r["elapsed_ms"],
-        "lnl": {"mixed": r["lnl"], "fp64": r64["lnl"], "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"])},
+        "lnl": {"mixed": r["lnl"], "fp64": r64["lnl"] if r64 else None,
+                "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"]) if r64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
                      "kernel": kernel_name(use_tc, m.nstates, tile), "algorithmic_bytes_per_launch": bmx,
                      "fp32_tflops": fmx / r["kern_avg_s"] / 1e12, "flops_per_launch": fmx,
                      "kernel_ms": r["kern_avg_s"] * 1e3},
-        "fp64_path": {"value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
-                      "ms_per_step": r64["elapsed_ms"] / max(3, args.steps // 4),
-                      "kernel": "k_traverse_f64<20,NORM,LNL>",
-                      "hbm_frac": a64 / peaks["hbm_gbs"],
-                      "fp64_tflops": f64 / r64["kern_avg_s"] / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
-                      "fp64_frac": f64 / r64["kern_avg_s"] / 1e12 / FP64_PEAK_TFLOPS_MEASURED},
+        "fp64_path": None if r64 is None else {
+            "value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
+            "ms_per_step": r64["elapsed_ms"] / max(3, args.steps // 4),
+            "kernel": f"k_traverse_f64<{m.nstates},NORM,LNL>",
+            "hbm_frac": b64 / r64["kern_avg_s"] / 1e9 / peaks["hbm_gbs"],
+            "fp64_tflops": f64 / r64["kern_avg_s"] / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
+            "fp64_frac": f64 / r64["kern_avg_s"] / 1e12 / FP64_PEAK_TFLOPS_MEASURED},
         "e2e": {"value": updates_per_step / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": 8 * 4},
         "clocks": r["clocks"],
-        "gpu_launches": launches * args.steps,
+        "gpu_launches": r["launches"],
     }
-    if use_tc:
+    if use_tc and not args.headline_only:
         line["bf16"] = dict(kernel_ms=rb["kern_avg_s"] * 1e3, tile=btile, kernel=kernel_name(True, m.nstates, btile, True),
                             value=updates_per_step * max(3, args.steps // 4) / (rb["elapsed_ms"] / 1e3),
                             lnl=rb["lnl"], rel_err_vs_fp64=abs(rb["lnl"] - r64["lnl"]) / abs(r64["lnl"]),
                             mma_tflops=tc_mma_flops(ops, m.nstates, m.ncat, ds.nptn, bf16=True) / rb["kern_avg_s"] / 1e12)
+        line["cuda_core_f32"] = beside
+    if use_tc:
         mma = tc_mma_flops(ops, m.nstates, m.ncat, ds.nptn)
         line["roofline"]["tensor"] = {"mma_flops_per_launch": mma, "mma_tflops": mma / r["kern_avg_s"] / 1e12,
-                                      "note": "executed split-TF32 MMA flops (3 passes, padded N/K)"}
-        line["cuda_core_f32"] = beside
-    line["speedup_vs_fp64_path"] = value / line["fp64_path"]["value"]
+                                      "note": "executed split-TF32 MMA flops (3 passes, padded N/K), upper "
+                                              "bound (tail ops may run on CUDA cores)"}
+    if r64:
+        line["speedup_vs_fp64_path"] = value / line["fp64_path"]["value"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(ds, ops, a, b, length)
     print(json.dumps(line))
@@ -464,6 +472,11 @@ def main():
     ap.add_argument("--max-active", type=int, default=16)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--no-fp64-serve", action="store_true")
+    ap.add_argument("--config", default=None,
+                    help="fixed traversal configuration instead of the autotuner, as the autotuner labels it "
+                         "(tile/schedule[/sD][/kP], e.g. 0/level/s2/k1)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the paths reported beside the headline (FP64, CUDA-core FP32, BF16)")
     ap.add_argument("--precision", default="auto", choices=["auto", "f32", "tf32x3"],
                     help="headline contraction: auto = split-TF32 tensor cores for 16..64 states")
     args = ap.parse_args()

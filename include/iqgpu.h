@@ -189,6 +189,8 @@ int iqgpu_set_stages(iqgpu_engine *e, int32_t stages);
  * split evenly. Chosen by the autotuner; results do not depend on it. */
 int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
+/* Kernel launches issued by this engine so far (all entry points). */
+int iqgpu_get_launches(iqgpu_engine *e, int64_t *launches);
 
 /* ---- batched evaluation ------------------------------------------------- */
 /* One NNI candidate around a central branch node1-node2 (getBestNNIForBran,

@@ -173,6 +173,7 @@ extern "C" int iqgpu_rell(iqgpu_engine *e, const double *pattern_lh, int32_t ntr
     }
     dim3 grid((b.nreps + kRR - 1) / kRR, (ntrees + kRT - 1) / kRT);
     k_rell<<<grid, 256, 0, e->st>>>(b.w, b.plh, b.nreps, ntrees, e->Ppad, (int)e->P, b.out);
+    e->launches++;
     CKR(cudaGetLastError());
     CKR(cudaMemcpyAsync(out, b.out, (size_t)ntrees * b.nreps * 8, cudaMemcpyDeviceToHost, e->st));
     CKR(cudaStreamSynchronize(e->st));

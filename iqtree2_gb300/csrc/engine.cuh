@@ -131,6 +131,7 @@ struct iqgpu_engine {
     bool timing, timing_pending;
     double timing_ms;
     long long timing_launches;
+    long long launches;       // kernel launches this engine has issued (throughput accounting)
 };
 
 namespace iqg {

@@ -765,6 +765,12 @@ int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces) {
     return IQGPU_OK;
 }
 
+int iqgpu_get_launches(iqgpu_engine *e, int64_t *launches) {
+    if (!e || !launches) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    *launches = e->launches;
+    return IQGPU_OK;
+}
+
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches) {
     if (!e || !total_ms || !launches) { set_error("null argument"); return IQGPU_ERR_ARG; }
     int rc = settle_timing(e);

@@ -493,6 +493,7 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops) {
     dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
     k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
                                                  e->d_tip, e->n, e->C, e->S);
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "partial_info_f64");
 }
 
@@ -507,6 +508,7 @@ static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
         if (err != cudaSuccess) return cuda_fail(err, "traverse_f64 smem attribute");
     }
     kern<<<e->nblk, kTPB, smem, e->st>>>(P);
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "traverse_f64");
 }
 
@@ -561,11 +563,13 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
 
 int launch_derv_f64(iqgpu_engine *e, double len) {
     k_derv_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "derv_f64");
 }
 
 int launch_from_buffer_f64(iqgpu_engine *e, double len) {
     k_from_buffer_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "from_buffer_f64");
 }
 

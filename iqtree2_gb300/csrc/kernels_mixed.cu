@@ -178,6 +178,7 @@ int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
     dim3 grid(nops_with_branch, 2, Z);
     k_partial_info_mixed<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv,
                                                    e->d_eval, e->d_rates, e->d_tip, e->n, e->npad, e->C, e->S);
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "partial_info_mixed");
 }
 
@@ -204,11 +205,13 @@ static MixBufParams mixbuf_params(iqgpu_engine *e, double len) {
 
 int launch_derv_mixed(iqgpu_engine *e, double len) {
     k_derv_mixed<<<e->nblk, kTPB, 0, e->st>>>(mixbuf_params(e, len));
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "derv_mixed");
 }
 
 int launch_from_buffer_mixed(iqgpu_engine *e, double len) {
     k_from_buffer_mixed<<<e->nblk, kTPB, 0, e->st>>>(mixbuf_params(e, len));
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "from_buffer_mixed");
 }
 

@@ -351,6 +351,7 @@ int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
         if (nl <= 0) continue;
         if ((long long)nl * grid < wave) break;
         k_level_dna<<<dim3(grid, nl), kDnaTile, 0, e->st>>>(P, op0);
+        e->launches++;
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "level_dna");
     }
@@ -380,11 +381,13 @@ int launch_flow_dna(iqgpu_engine *e, const MixParams &P) {
     const long long items = (long long)P.nops * ntiles;
     const int grid = (int)std::min<long long>(items, (long long)per_sm * sms);
     k_flow_dna<<<grid, kDnaTile, 0, e->st>>>(P, e->d_flow_done, e->d_flow_ticket, 1u, ntiles);
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "flow_dna");
 }
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi) {
     const int grid = (int)(e->Ppad / kDnaTile);
+    e->launches++;
     switch (epi) {
     case EPI_NONE: k_traverse_dna<EPI_NONE><<<grid, kDnaTile, 0, e->st>>>(P); break;
     case EPI_LNL: k_traverse_dna<EPI_LNL><<<grid, kDnaTile, 0, e->st>>>(P); break;

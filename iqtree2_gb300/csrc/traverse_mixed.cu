@@ -347,7 +347,6 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     const int TP = mix_tile(e);
     const int grid = (int)(e->Ppad / TP);
     const size_t pm_bytes = (size_t)2 * e->C * e->n * e->npad * 4;  // one op's two P(t) blocks
-    if (e->level_sync && EPI == EPI_NONE) return IQGPU_OK;  // ops ran level by level already
     const int nbuf = pm_bytes * 2 <= 96 * 1024 ? 2 : 1;
     const size_t smem = (P.nops > 0 ? nbuf : 1) * pm_bytes;
     auto kern = k_traverse_mixed<NQ, EPI>;
@@ -356,6 +355,7 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
         if (err != cudaSuccess) return cuda_fail(err, "traverse_mixed smem attribute");
     }
     kern<<<grid, TP * e->C, smem, e->st>>>(P, TP, nbuf);
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "traverse_mixed");
 }
 
@@ -373,6 +373,7 @@ static int launch_levels_t(iqgpu_engine *e, const MixParams &P) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
         kern<<<dim3(grid, nl), TP * e->C, smem, e->st>>>(P, TP, op0);
+        e->launches++;
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "level_mixed");
     }
@@ -401,12 +402,17 @@ static int dispatch_mix(iqgpu_engine *e, MixParams P) {
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
 int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi);
 int launch_flow_dna(iqgpu_engine *e, const MixParams &P);
-int launch_traverse_tc(iqgpu_engine *e, const MixParams &M);
+int launch_traverse_tc(iqgpu_engine *e, const MixParams &M, int *rest);
 
-// epilogue alone after the ops ran elsewhere (tensor cores)
+// ops [rest, nops) and the epilogue on the fused CUDA-core kernel, after ops
+// [0, rest) ran on the tensor cores: the op list is shifted so the kernel sees
+// them as ops 0.. (the branch matrices keep their block)
 template <int EPI>
-static int epilogue_only(iqgpu_engine *e, MixParams P) {
-    P.nops = 0;
+static int fused_rest(iqgpu_engine *e, MixParams P, int rest) {
+    P.ops += rest;
+    P.opmats += (long long)rest * P.op_stride;
+    P.nops -= rest;
+    P.branch_op -= rest;
     switch (e->npad) {
     case 4: return launch_mix_t<1, EPI>(e, P);
     case 20: return launch_mix_t<5, EPI>(e, P);
@@ -421,9 +427,14 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     P.len = len;
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
     if (e->tc) {
-        int rc = launch_traverse_tc(e, P);
-        if (rc || epi == EPI_NONE) return rc;
-        return epi == EPI_LNL ? epilogue_only<EPI_LNL>(e, P) : epilogue_only<EPI_THETA>(e, P);
+        int rest = nops;
+        int rc = launch_traverse_tc(e, P, &rest);
+        if (rc || (rest >= nops && epi == EPI_NONE)) return rc;
+        switch (epi) {
+        case EPI_NONE: return fused_rest<EPI_NONE>(e, P, rest);
+        case EPI_LNL: return fused_rest<EPI_LNL>(e, P, rest);
+        default: return fused_rest<EPI_THETA>(e, P, rest);
+        }
     }
     // 4-state models: one thread per pattern and all its categories, unless a
     // per-category tile was chosen explicitly

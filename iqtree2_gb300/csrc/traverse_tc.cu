@@ -475,11 +475,13 @@ int launch_tc_prep(iqgpu_engine *e, int nops) {
         k_tc_prep_b16<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32,
                                                                  reinterpret_cast<unsigned short *>(e->d_tcb),
                                                                  e->tcb_stride * 2, e->n, e->npad, e->C, NP, KS, KB, ks);
+        e->launches++;
         return cuda_fail(cudaGetLastError(), "tc_prep_b16");
     }
     const int NP = tc_np(e->npad), KP = tc_kp(e->npad);
     k_tc_prep_b<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32, e->d_tcb, e->tcb_stride,
                                                            e->n, e->npad, e->C, NP, KP, tc_ksplit(e));
+    e->launches++;
     return cuda_fail(cudaGetLastError(), "tc_prep_b");
 }
 
@@ -553,7 +555,7 @@ static size_t tc_smem_bytes(const TcParams &T, int nstage) {
 }
 
 template <int NP, int NSTAGE, bool BF>
-static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
+static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     int rc = tc_tensor_map(e);
     if (rc) return rc;
     const TcParams T = tc_params(e, M, NP, BF);
@@ -562,13 +564,8 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
-    if (!e->level_sync) {
-        kern<<<T.ntiles, kTcRows, smem, e->st>>>(tm, T, 0, 0, M.nops);
-        return cuda_fail(cudaGetLastError(), "traverse_tc");
-    }
-    // level schedule: a persistent grid of resident CTAs walks each level's (tile, op) pairs.
-    // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA reserve)
-    // and by tensor memory (512 columns, 4 * NP per CTA).
+    // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
+    // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
     int sms = 1, smem_sm = 0, reserve = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->dev);
@@ -579,12 +576,30 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
     const size_t per_cta = smem + stat + (size_t)reserve;
     int per_sm = (int)std::min<size_t>(512 / (4 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
     if (per_sm < 1) per_sm = 1;
-    for (int l = 0; l < e->nlevels; l++) {
+    const long long resident = (long long)per_sm * sms;
+    // Narrow tail: from the first level whose (tile, op) pairs no longer fill
+    // the resident CTAs, a tensor-core CTA would hold a single pair and expose
+    // its whole stage latency; for up to 32 padded states the fused CUDA-core
+    // kernel takes those ops instead (same split in both schedules).
+    int lt = e->nlevels;
+    if (NP == 32)
+        for (int l = 0; l < e->nlevels; l++)
+            if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < resident) { lt = l; break; }
+    *rest = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
+    if (*rest <= 0) return IQGPU_OK;
+    if (!e->level_sync) {
+        kern<<<T.ntiles, kTcRows, smem, e->st>>>(tm, T, 0, 0, *rest);
+        e->launches++;
+        return cuda_fail(cudaGetLastError(), "traverse_tc");
+    }
+    // level schedule: a persistent grid of resident CTAs walks each level's (tile, op) pairs
+    for (int l = 0; l < lt; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
         const long long items = (long long)T.ntiles * nl;
-        const int grid = (int)std::min<long long>(items, (long long)per_sm * std::max(sms, 1));
+        const int grid = (int)std::min<long long>(items, resident);
         kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
+        e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
     }
@@ -592,11 +607,11 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M) {
 }
 
 template <int NP, bool BF>
-static int launch_tc_depth(iqgpu_engine *e, const MixParams &M, int depth) {
+static int launch_tc_depth(iqgpu_engine *e, const MixParams &M, int depth, int *rest) {
     switch (depth) {
-    case 2: return launch_tc_t<NP, 2, BF>(e, M);
-    case 3: return launch_tc_t<NP, 3, BF>(e, M);
-    default: return launch_tc_t<NP, 4, BF>(e, M);
+    case 2: return launch_tc_t<NP, 2, BF>(e, M, rest);
+    case 3: return launch_tc_t<NP, 3, BF>(e, M, rest);
+    default: return launch_tc_t<NP, 4, BF>(e, M, rest);
     }
 }
 
@@ -612,16 +627,19 @@ int tc_depth(const iqgpu_engine *e) {
     return depth;
 }
 
-// The ops of a traversal on the tensor cores (the branch epilogue stays on
-// the CUDA-core kernel). Per CTA: a ring of `depth` shared-memory slots; the
+// The ops of a traversal on the tensor cores (the narrow tail of a <= 32-state
+// traversal and the branch epilogue run on the fused CUDA-core kernel). Per CTA: a ring of `depth` shared-memory slots; the
 // residency per SM follows from their size and from the 4 * NP tensor-memory
 // columns each CTA holds (depth 2: four CTAs per SM for 20 states, two for 61).
-int launch_traverse_tc(iqgpu_engine *e, const MixParams &M) {
+// Sets *rest to the first op left to the CUDA cores (M.nops when none).
+int launch_traverse_tc(iqgpu_engine *e, const MixParams &M, int *rest) {
+    *rest = M.nops;
     if (M.nops <= 0) return IQGPU_OK;
     const int depth = tc_depth(e);
     const bool BF = e->cfg.precision == IQGPU_BF16;
-    if (tc_np(e->npad) == 64) return BF ? launch_tc_depth<64, true>(e, M, depth) : launch_tc_depth<64, false>(e, M, depth);
-    return BF ? launch_tc_depth<32, true>(e, M, depth) : launch_tc_depth<32, false>(e, M, depth);
+    if (tc_np(e->npad) == 64)
+        return BF ? launch_tc_depth<64, true>(e, M, depth, rest) : launch_tc_depth<64, false>(e, M, depth, rest);
+    return BF ? launch_tc_depth<32, true>(e, M, depth, rest) : launch_tc_depth<32, false>(e, M, depth, rest);
 }
 
 }  // namespace iqg

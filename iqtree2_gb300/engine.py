@@ -101,6 +101,7 @@ def lib():
         "iqgpu_group_lnl": ([vp, ct.c_void_p, ct.c_void_p], ct.c_int),
         "iqgpu_group_destroy": ([vp], ct.c_int),
         "iqgpu_set_kpieces": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_get_launches": ([vp, ct.POINTER(ct.c_int64)], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
         "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
@@ -272,6 +273,12 @@ class Engine:
     def set_schedule(self, schedule):
         """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel)."""
         _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
+
+    def launches(self):
+        """Kernel launches this engine has issued so far."""
+        n = ct.c_int64()
+        _check(lib().iqgpu_get_launches(self.h, ct.byref(n)))
+        return n.value
 
     def set_stages(self, stages):
         """Ring depth of the tensor-core traversal (0 = default, 2, 3 or 4)."""
