@@ -144,14 +144,21 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling every 20 ms; returns once the first sample has arrived
+        (at most 5 s), so that samples cover the timed region that follows."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (FileNotFoundError, OSError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.005)
+        self.skip = len(self.lines)  # samples taken before the timed region
 
     def _read(self):
         for line in self.proc.stdout:
@@ -167,7 +174,8 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines[getattr(self, "skip", 0):] or self.lines[-1:]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -413,6 +421,141 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batched(args):
+    """Batched evaluation on DNA GTR+G4, 200 taxa x 100,000 sites: NNI candidates
+    (one graph-captured launch sequence for all candidates vs one candidate at a
+    time through the kernel-level calls), UFBoot RELL scores of 1,000 replicates
+    and 12 uneven partitions with separate GTR+G4 (one graph launch vs one
+    evaluation per partition). Synthetic data simulated under the model."""
+    import torch
+    from iqtree2_gb300 import autotune, engine
+    from iqtree2_gb300.topology import Topology
+    torch.cuda.set_device(0)
+    reps = max(args.steps, 3)
+    ds = simulate.dna_gtr_dataset(200, 100000, 4)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    m = ds.model
+    ncand = 64
+    cands = topo.nni_candidates(ncand)
+    ncand = len(cands)
+    nslots = topo.nslots + 2 * ncand
+    eng = engine.Engine(ds.nptn, 4, m.ncat, ds.ntaxa, m.state_unknown, nslots, precision=engine.F32,
+                        max_ops=max(nslots, 2 * ncand))
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    leaf, nb = 0, topo.adj[0][0][0]
+    bops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    autotune.tune(eng, bops, topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb))
+    eng.compute_partials(topo.all_partials_ops())
+    entries = topo.nni_batch_entries(cands, topo.nslots)
+
+    # NNI: all candidates in one batch (graph replay after the first call)
+    for _ in range(args.warmup):
+        lnl_b, bl_b = eng.nni_batch(entries)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        lnl_b, bl_b = eng.nni_batch(entries)
+    nni_batch_s = (time.perf_counter() - t0) / reps
+
+    # the same candidates one at a time: two partials, safeguarded Newton on the
+    # central branch (one derivative launch and read-back per step), final lnL
+    def one_by_one():
+        out = []
+        for (subs, scr, lens, central) in entries:
+            eng.compute_partials([(scr[0], subs[0], subs[1], lens[0], lens[1]),
+                                  (scr[1], subs[2], subs[3], lens[2], lens[3])])
+            x, first = central, True
+            for _ in range(10):
+                df, ddf = eng.likelihood_derv([], scr[0], scr[1], x, theta_computed=not first)
+                first = False
+                step = -df / ddf if ddf < 0 else (0.1 if df > 0 else -0.1) * x
+                nx = min(max(x + step, 1e-6), 10.0)
+                if abs(nx - x) < 1e-6:
+                    x = nx
+                    break
+                x = nx
+            out.append(eng.lnl_from_buffer(x))
+        return np.array(out)
+
+    lnl_seq = one_by_one()
+    t0 = time.perf_counter()
+    for _ in range(max(1, reps // 3)):
+        lnl_seq = one_by_one()
+    nni_seq_s = (time.perf_counter() - t0) / max(1, reps // 3)
+
+    # UFBoot RELL: 1,000 replicate weight vectors resident, scores for 64 trees
+    rng = np.random.default_rng(5)
+    weights = simulate.bootstrap_weights(ds.freq, 1000, rng)
+    eng.set_boot_weights(weights)
+    plh0 = eng.pattern_lh()
+    trees = plh0[None, :] + rng.normal(0.0, 1e-3, size=(64, ds.nptn))
+    for _ in range(args.warmup):
+        scores = eng.rell(trees)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        scores = eng.rell(trees)
+    rell_s = (time.perf_counter() - t0) / reps
+    want = trees @ weights.T.astype(np.float64)
+    rell_err = float(np.max(np.abs(scores - want) / np.abs(want)))
+    eng.close()
+
+    # 12 uneven partitions, separate GTR+G4, one tree
+    sizes = [2000, 4000, 6000, 8000, 10000, 12000, 14000, 16000, 20000, 24000, 28000, 30000]
+    parts = simulate.partitioned_dna_datasets(200, sizes, 7)
+    ptopo = Topology(parts[0].edges, parts[0].lengths, parts[0].ntaxa)
+    pnb = ptopo.adj[leaf][0][0]
+    pops = engine.Engine.ops_array(ptopo.branch_ops(pnb, leaf))
+    pa, pb, plen = ptopo.ref(leaf, pnb), ptopo.ref(pnb, leaf), ptopo.edge_len(leaf, pnb)
+    pengs = []
+    for d in parts:
+        e = engine.Engine(d.nptn, 4, d.model.ncat, d.ntaxa, d.model.state_unknown, ptopo.nslots,
+                          precision=engine.F32, max_ops=ptopo.nslots)
+        e.set_model(d.model)
+        e.set_patterns(d.freq)
+        e.set_tip_states(d.patterns)
+        autotune.tune(e, pops, pa, pb, plen)
+        pengs.append(e)
+    for _ in range(args.warmup):
+        seq = [e.compute_likelihood(pops, pa, pb, plen) for e in pengs]
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        seq = [e.compute_likelihood(pops, pa, pb, plen) for e in pengs]
+    part_seq_s = (time.perf_counter() - t0) / reps
+    grp = engine.Group(pengs)
+    grp.prepare([pops] * len(pengs), [pa] * len(pengs), [pb] * len(pengs), [plen] * len(pengs))
+    for _ in range(args.warmup):
+        tot, per = grp.lnl()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        tot, per = grp.lnl()
+    part_graph_s = (time.perf_counter() - t0) / reps
+    assert list(per) == seq
+    part_updates = len(pops) * sum(d.nptn for d in parts)
+    grp.close()
+    for e in pengs:
+        e.close()
+
+    line = {
+        "metric": "NNI candidate evaluations/s", "value": ncand / nni_batch_s,
+        "unit": "candidate evaluations/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup,
+        "higher_is_better": True, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "DNA GTR+G4 200 taxa x 100000 sites: 64 NNI candidates, 1000 UFBoot replicates, "
+                               "12 partitions of 2k-30k sites with separate GTR+G4", "nptn": ds.nptn},
+        "nni": {"candidates": ncand, "batch_ms": nni_batch_s * 1e3, "one_by_one_ms": nni_seq_s * 1e3,
+                "speedup": nni_seq_s / nni_batch_s,
+                "max_abs_dlnl_batch_vs_one_by_one": float(np.max(np.abs(lnl_b - lnl_seq))),
+                "note": "one evaluation = two partials + Newton-Raphson on the central branch + lnL"},
+        "rell": {"replicates": 1000, "trees": 64, "ms": rell_s * 1e3,
+                 "replicate_tree_scores_per_s": 64 * 1000 / rell_s, "max_rel_err_vs_fp64_numpy": rell_err},
+        "partitions": {"count": len(sizes), "sites": sizes, "graph_ms": part_graph_s * 1e3,
+                       "one_by_one_ms": part_seq_s * 1e3, "speedup": part_seq_s / part_graph_s,
+                       "graph_updates_per_s": part_updates / part_graph_s, "lnl": tot},
+    }
+    print(json.dumps(line))
+
+
 def run_serve(args):
     """Serving: seeded Poisson stream (mean --rate req/s) of lnL + one round of
     branch optimisation; 70% DNA GTR+G4 / 30% protein LG+G4, taxa log-U[8, max],
@@ -459,12 +602,12 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="protein", choices=sorted(WORKLOADS))
-    ap.add_argument("--mode", default="headline", choices=["headline", "serve"])
+    ap.add_argument("--mode", default="headline", choices=["headline", "serve", "batched"])
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--max-taxa", type=int, default=2000)
@@ -484,6 +627,8 @@ def main():
     WORKLOAD = WORKLOADS[args.workload]
     if args.mode == "serve":
         run_serve(args)
+    elif args.mode == "batched":
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

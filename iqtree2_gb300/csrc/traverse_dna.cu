@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
 // under the dataflow schedule they were written by other CTAs of the same
 // launch. The op's P(t) blocks (2 x ncat x 16 floats) come through the
 // read-only cache (warp-uniform addresses).
-__device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile) {
+__device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile, int dad_slot, int lref, int rref) {
     constexpr int n = 4, npad = 4;
     const int C = P.ncat, S = P.state_unknown;
     const long long p = tile * kDnaTile + threadIdx.x;
@@ -205,8 +205,6 @@ __device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile
     const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(S + 1) * C * npad;
-    const OpDev op = P.ops[k];
-    int lref = op.child[0], rref = op.child[1];
     const float *gbase = P.opmats + (long long)k * P.op_stride;
     const float *PL = gbase, *PR = gbase + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
     if (lref >= 0 && rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
@@ -261,7 +259,7 @@ __device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile
         sh = 1 - ex;
         mul = __int_as_float((127 + sh) << 23);
     }
-    float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+    float *dad = P.part + (long long)dad_slot * P.slot_floats + pbase;
 #pragma unroll
     for (int c = 0; c < kDnaMaxCat; c++) {
         if (c < C) {
@@ -270,14 +268,22 @@ __device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile
             *reinterpret_cast<float4 *>(dad + c * 32) = v;
         }
     }
-    P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+    P.expo[(long long)dad_slot * ld + p] = e - sh;
 }
 
 // Level-synchronous form: CTA (x, y) computes op op0 + y for tile x. All
 // (op, tile) pairs of a level are independent, so every child load of the
 // level can be in flight at once.
-__global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0) {
-    dna_op(P, op0 + blockIdx.y, blockIdx.x);
+// The level's op descriptors travel as a kernel parameter (constant bank), so a
+// CTA issues its child loads without first reading its op from global memory.
+constexpr int kLevelOps = 1024;
+struct LevelOps {
+    int3 op[kLevelOps];  // dad slot, child 0, child 1 of ops op0 .. op0 + count - 1
+};
+
+__global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0, const LevelOps L) {
+    const int3 o = L.op[blockIdx.y];
+    dna_op(P, op0 + blockIdx.y, blockIdx.x, o.x, o.y, o.z);
 }
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -325,7 +331,8 @@ __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsign
         __syncthreads();  // s_item / s_ok are rewritten by the next iteration
         if (i >= total || !ok) return;
         const int k = (int)(i / ntiles), t = (int)(i % ntiles);
-        dna_op(P, k, t);
+        const OpDev op = P.ops[k];
+        dna_op(P, k, t, op.dad_slot, op.child[0], op.child[1]);
         __threadfence();  // this thread's outputs are visible device-wide before the flag
         __syncthreads();
         if (threadIdx.x == 0) atomicExch(done + i, epoch);
@@ -350,10 +357,18 @@ int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
         if ((long long)nl * grid < wave) break;
-        k_level_dna<<<dim3(grid, nl), kDnaTile, 0, e->st>>>(P, op0);
-        e->launches++;
-        cudaError_t err = cudaGetLastError();
-        if (err != cudaSuccess) return cuda_fail(err, "level_dna");
+        for (int c0 = 0; c0 < nl; c0 += kLevelOps) {  // levels wider than one parameter block: several launches
+            const int cnt = std::min(kLevelOps, nl - c0);
+            LevelOps L;
+            for (int i = 0; i < cnt; i++) {
+                const OpDev &d = e->h_ops[op0 + c0 + i];
+                L.op[i] = make_int3(d.dad_slot, d.child[0], d.child[1]);
+            }
+            k_level_dna<<<dim3(grid, cnt), kDnaTile, 0, e->st>>>(P, op0 + c0, L);
+            e->launches++;
+            cudaError_t err = cudaGetLastError();
+            if (err != cudaSuccess) return cuda_fail(err, "level_dna");
+        }
     }
     const int rest = l < e->nlevels ? e->level_off[l] : P.nops;
     if (rest >= P.nops && epi == EPI_NONE) return IQGPU_OK;

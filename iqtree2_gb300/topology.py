@@ -53,3 +53,45 @@ class Topology:
             if w == v:
                 return self.lengths[k]
         raise KeyError
+
+    def all_partials_ops(self):
+        """Ops that make every directed partial of the tree current."""
+        done, ops = set(), []
+        for (u, v) in sorted(self.slot):
+            ops += self.ops_for(u, v, done)
+        return ops
+
+    def nni_candidates(self, nmax):
+        """Both NNI swaps of internal branches (reference: PhyloTree::getBestNNIForBran,
+        tree/phylotree.cpp:4069-4320), up to nmax, as dicts: branch (u, v); n1 = the two
+        subtrees at u after the swap, n2 = the two at v."""
+        out = []
+        for (u, v) in sorted(self.slot):
+            if u < self.ntaxa or v < self.ntaxa or u > v:
+                continue
+            a_, b_ = [w for (w, _) in self.adj[u] if w != v]
+            c_, d_ = [w for (w, _) in self.adj[v] if w != u]
+            for (x, y) in ((b_, c_), (b_, d_)):  # x leaves u for v, y leaves v for u
+                keep_u = a_ if x == b_ else b_
+                keep_v = d_ if y == c_ else c_
+                out.append(dict(u=u, v=v, n1=(keep_u, y), n2=(x, keep_v)))
+                if len(out) == nmax:
+                    return out
+        return out
+
+    def nni_batch_entries(self, cands, first_scratch):
+        """Engine.nni_batch entries for candidates: the four subtree partials with
+        their own branch lengths, two scratch slots per candidate starting at
+        first_scratch, and the current central length."""
+        arr = []
+        for k, c in enumerate(cands):
+            u, v = c["u"], c["v"]
+            old_of = {w: u for (w, _) in self.adj[u]}
+            old_of.update({w: v for (w, _) in self.adj[v]})
+            subs, lens = [], []
+            for s in (c["n1"][0], c["n1"][1], c["n2"][0], c["n2"][1]):
+                subs.append(self.ref(old_of[s], s))
+                lens.append(self.edge_len(old_of[s], s))
+            arr.append((tuple(subs), (first_scratch + 2 * k, first_scratch + 2 * k + 1), tuple(lens),
+                        self.edge_len(u, v)))
+        return arr

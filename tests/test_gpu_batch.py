@@ -16,20 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def nni_candidates(topo, nmax):
-    """Both swaps of every internal branch, as (u, v, subs, lens, swap tuple)."""
-    out = []
-    for (u, v) in sorted(topo.slot):
-        if u < topo.ntaxa or v < topo.ntaxa or u > v:
-            continue
-        a_, b_ = [w for (w, _) in topo.adj[u] if w != v]
-        c_, d_ = [w for (w, _) in topo.adj[v] if w != u]
-        for (x, y) in ((b_, c_), (b_, d_)):  # x leaves u for v, y leaves v for u
-            keep_u = a_ if x == b_ else b_
-            keep_v = d_ if y == c_ else c_
-            out.append(dict(u=u, v=v, n1=(keep_u, y), n2=(x, keep_v)))
-            if len(out) == nmax:
-                return out
-    return out
+    return topo.nni_candidates(nmax)
 
 
 def swapped_edges(ds, u, v, x, y):
@@ -53,28 +40,8 @@ def test_nni_batch_matches_oracle(oracle_mod):
     eng.set_model(ds.model)
     eng.set_patterns(ds.freq)
     eng.set_tip_states(ds.patterns)
-    done, ops = set(), []
-    for (u, w) in sorted(topo.slot):
-        ops += topo.ops_for(u, w, done)
-    eng.compute_partials(ops)
-    arr = []
-    for k, c in enumerate(cands):
-        u, v = c["u"], c["v"]
-        (s0, s1), (s2, s3) = c["n1"], c["n2"]
-        # subtrees hanging off u after the swap keep their own branch lengths
-        def side(sub, old):
-            return topo.ref(old, sub), topo.edge_len(old, sub)
-        old_of = {}
-        for w, _ in topo.adj[u]:
-            old_of[w] = u
-        for w, _ in topo.adj[v]:
-            old_of[w] = v
-        r0, l0 = side(s0, old_of[s0])
-        r1, l1 = side(s1, old_of[s1])
-        r2, l2 = side(s2, old_of[s2])
-        r3, l3 = side(s3, old_of[s3])
-        arr.append(((r0, r1, r2, r3), (topo.nslots + 2 * k, topo.nslots + 2 * k + 1), (l0, l1, l2, l3),
-                    topo.edge_len(u, v)))
+    eng.compute_partials(topo.all_partials_ops())
+    arr = topo.nni_batch_entries(cands, topo.nslots)
     lnl, blen = eng.nni_batch(arr, max_nr_step=10, min_bl=1e-6, max_bl=10.0)
     for k, c in enumerate(cands):
         u, v = c["u"], c["v"]
