@@ -167,8 +167,10 @@ int iqgpu_set_stream(iqgpu_engine *e, void *cuda_stream);
  * of timed launches since the last reset), reset. */
 int iqgpu_set_timing(iqgpu_engine *e, int32_t enable);
 /* Pattern tile (patterns per CTA, 32/64/128) of the mixed-precision traversal
- * kernel; 0 restores the default. Chosen by the autotuner in
- * iqtree2_gb300/autotune.py; results do not depend on it. */
+ * kernel; 0 restores the default. 4-state models also take 1 (one thread per
+ * pattern and all its categories) and 2 (as 1, two patterns per thread, level
+ * schedule). Chosen by the autotuner in iqtree2_gb300/autotune.py; results do
+ * not depend on it. */
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
 /* Schedule of the mixed-precision traversal: 0 = one fused launch walking the
  * whole op list per pattern tile; 1 = one launch per tree level, all of the

@@ -27,7 +27,8 @@ def candidates(eng):
         npad = (eng.nstates + 3) // 4 * 4
         pieces = (1, 2) if (npad > 32 and npad % 16 == 0) else (1,)
         return [(0, sched, st, kp) for sched in (0, 1) for st in (2, 3, 4) for kp in pieces]
-    out = [(1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0)] if eng.nstates == 4 and eng.ncat <= 4 else []
+    out = ([(1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (2, 1, 0, 0)]
+           if eng.nstates == 4 and eng.ncat <= 4 else [])
     for sched in (0, 1):
         for tile in TILES:
             if tile > 32 and tile * eng.ncat > 512:

@@ -732,8 +732,9 @@ int iqgpu_set_timing(iqgpu_engine *e, int32_t enable) {
 
 int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
     if (!e || !(patterns_per_cta == 0 || patterns_per_cta == 32 || patterns_per_cta == 64 ||
-                patterns_per_cta == 128 || (patterns_per_cta == 1 && e->n == 4))) {
-        set_error("tile must be 0, 32, 64 or 128 patterns (1 = one thread per pattern, 4-state models)");
+                patterns_per_cta == 128 || ((patterns_per_cta == 1 || patterns_per_cta == 2) && e->n == 4))) {
+        set_error("tile must be 0, 32, 64 or 128 patterns (4-state models: 1 = one thread per pattern, "
+                  "2 = two patterns per thread on the level schedule)");
         return IQGPU_ERR_ARG;
     }
     e->tile = patterns_per_cta;

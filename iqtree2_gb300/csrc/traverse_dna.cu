@@ -197,12 +197,11 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
 // under the dataflow schedule they were written by other CTAs of the same
 // launch. The op's P(t) blocks (2 x ncat x 16 floats) come through the
 // read-only cache (warp-uniform addresses).
+template <int PPT>
 __device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile, int dad_slot, int lref, int rref) {
     constexpr int n = 4, npad = 4;
     const int C = P.ncat, S = P.state_unknown;
-    const long long p = tile * kDnaTile + threadIdx.x;
     const long long ld = P.ldp;
-    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(S + 1) * C * npad;
     const float *gbase = P.opmats + (long long)k * P.op_stride;
@@ -213,62 +212,78 @@ __device__ __forceinline__ void dna_op(const MixParams &P, int k, long long tile
         q = TL; TL = TR; TR = q;
     }
     const bool lint = lref >= 0, rint = rref >= 0;
-    const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
-    const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
-    const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
-    const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
-    const int e = (lint ? __ldcg(P.expo + (long long)lref * ld + p) : 0) +
-                  (rint ? __ldcg(P.expo + (long long)rref * ld + p) : 0);
-    float4 lv[kDnaMaxCat], rv[kDnaMaxCat], out[kDnaMaxCat];
+    // PPT patterns per thread, 128 apart: every load of all of them is issued first
+    long long p[PPT], pbase[PPT];
+    bool live[PPT];
+    int e[PPT];
+    float4 lv[PPT][kDnaMaxCat], rv[PPT][kDnaMaxCat];
 #pragma unroll
-    for (int c = 0; c < kDnaMaxCat; c++) {
-        if (c < C) {
-            lv[c] = lint ? __ldcg(reinterpret_cast<const float4 *>(Lp + c * 32)) : ld4(tl + c * npad);
-            rv[c] = rint ? __ldcg(reinterpret_cast<const float4 *>(Rp + c * 32)) : ld4(tr + c * npad);
-        }
-    }
-    float mx = 0.f;
+    for (int j = 0; j < PPT; j++) {
+        p[j] = (tile * PPT + j) * kDnaTile + threadIdx.x;
+        live[j] = p[j] < ld;  // whole 128-pattern blocks: uniform per warp
+        pbase[j] = (p[j] >> 3) * (8LL * C * npad) + (p[j] & 7) * 4;
+        if (!live[j]) continue;
+        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase[j] : nullptr;
+        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase[j] : nullptr;
+        const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p[j]] * C * npad;
+        const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p[j]] * C * npad;
+        e[j] = (lint ? __ldcg(P.expo + (long long)lref * ld + p[j]) : 0) +
+               (rint ? __ldcg(P.expo + (long long)rref * ld + p[j]) : 0);
 #pragma unroll
-    for (int c = 0; c < kDnaMaxCat; c++) {
-        if (c < C) {
-            float yl[4], yr[4];
-#pragma unroll
-            for (int x = 0; x < 4; x++) {
-                if (lint) {
-                    const float4 m = ld4(PL + c * 16 + x * 4);
-                    yl[x] = fmaf(m.x, lv[c].x, fmaf(m.y, lv[c].y, fmaf(m.z, lv[c].z, m.w * lv[c].w)));
-                } else {
-                    yl[x] = x == 0 ? lv[c].x : x == 1 ? lv[c].y : x == 2 ? lv[c].z : lv[c].w;
-                }
-                if (rint) {
-                    const float4 m = ld4(PR + c * 16 + x * 4);
-                    yr[x] = fmaf(m.x, rv[c].x, fmaf(m.y, rv[c].y, fmaf(m.z, rv[c].z, m.w * rv[c].w)));
-                } else {
-                    yr[x] = x == 0 ? rv[c].x : x == 1 ? rv[c].y : x == 2 ? rv[c].z : rv[c].w;
-                }
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                lv[j][c] = lint ? __ldcg(reinterpret_cast<const float4 *>(Lp + c * 32)) : ld4(tl + c * npad);
+                rv[j][c] = rint ? __ldcg(reinterpret_cast<const float4 *>(Rp + c * 32)) : ld4(tr + c * npad);
             }
-            out[c] = make_float4(yl[0] * yr[0], yl[1] * yr[1], yl[2] * yr[2], yl[3] * yr[3]);
-            mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
         }
     }
-    int sh = 0;
-    float mul = 1.f;
-    if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
-        int ex;
-        frexpf(mx, &ex);
-        sh = 1 - ex;
-        mul = __int_as_float((127 + sh) << 23);
-    }
-    float *dad = P.part + (long long)dad_slot * P.slot_floats + pbase;
 #pragma unroll
-    for (int c = 0; c < kDnaMaxCat; c++) {
-        if (c < C) {
-            float4 v = out[c];
-            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-            *reinterpret_cast<float4 *>(dad + c * 32) = v;
+    for (int j = 0; j < PPT; j++) {
+        if (!live[j]) continue;
+        float4 out[kDnaMaxCat];
+        float mx = 0.f;
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                float yl[4], yr[4];
+#pragma unroll
+                for (int x = 0; x < 4; x++) {
+                    if (lint) {
+                        const float4 m = ld4(PL + c * 16 + x * 4);
+                        yl[x] = fmaf(m.x, lv[j][c].x, fmaf(m.y, lv[j][c].y, fmaf(m.z, lv[j][c].z, m.w * lv[j][c].w)));
+                    } else {
+                        yl[x] = x == 0 ? lv[j][c].x : x == 1 ? lv[j][c].y : x == 2 ? lv[j][c].z : lv[j][c].w;
+                    }
+                    if (rint) {
+                        const float4 m = ld4(PR + c * 16 + x * 4);
+                        yr[x] = fmaf(m.x, rv[j][c].x, fmaf(m.y, rv[j][c].y, fmaf(m.z, rv[j][c].z, m.w * rv[j][c].w)));
+                    } else {
+                        yr[x] = x == 0 ? rv[j][c].x : x == 1 ? rv[j][c].y : x == 2 ? rv[j][c].z : rv[j][c].w;
+                    }
+                }
+                out[c] = make_float4(yl[0] * yr[0], yl[1] * yr[1], yl[2] * yr[2], yl[3] * yr[3]);
+                mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
+            }
         }
+        int sh = 0;
+        float mul = 1.f;
+        if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
+            int ex;
+            frexpf(mx, &ex);
+            sh = 1 - ex;
+            mul = __int_as_float((127 + sh) << 23);
+        }
+        float *dad = P.part + (long long)dad_slot * P.slot_floats + pbase[j];
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++) {
+            if (c < C) {
+                float4 v = out[c];
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(dad + c * 32) = v;
+            }
+        }
+        P.expo[(long long)dad_slot * ld + p[j]] = e[j] - sh;
     }
-    P.expo[(long long)dad_slot * ld + p] = e - sh;
 }
 
 // Level-synchronous form: CTA (x, y) computes op op0 + y for tile x. All
@@ -281,9 +296,11 @@ struct LevelOps {
     int3 op[kLevelOps];  // dad slot, child 0, child 1 of ops op0 .. op0 + count - 1
 };
 
+// PPT patterns per thread: CTA (x, y) covers patterns 128 PPT x .. 128 PPT (x + 1) - 1.
+template <int PPT>
 __global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0, const LevelOps L) {
     const int3 o = L.op[blockIdx.y];
-    dna_op(P, op0 + blockIdx.y, blockIdx.x, o.x, o.y, o.z);
+    dna_op<PPT>(P, op0 + blockIdx.y, blockIdx.x, o.x, o.y, o.z);
 }
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -332,7 +349,7 @@ __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsign
         if (i >= total || !ok) return;
         const int k = (int)(i / ntiles), t = (int)(i % ntiles);
         const OpDev op = P.ops[k];
-        dna_op(P, k, t, op.dad_slot, op.child[0], op.child[1]);
+        dna_op<1>(P, k, t, op.dad_slot, op.child[0], op.child[1]);
         __threadfence();  // this thread's outputs are visible device-wide before the flag
         __syncthreads();
         if (threadIdx.x == 0) atomicExch(done + i, epoch);
@@ -341,14 +358,12 @@ __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsign
 
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi);
 
-// Level-synchronous schedule with a fused tail: levels whose (op, tile) pairs
-// fill the GPU (at least the resident CTAs of one wave) run one launch each;
-// the remaining narrow levels (a Yule tree ends in a chain of one-op levels)
-// and the branch epilogue run as one fused launch that walks them per tile.
-int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
-    const int grid = (int)(e->Ppad / kDnaTile);
+template <int PPT>
+static int launch_levels_dna_t(iqgpu_engine *e, MixParams P, int epi) {
+    const int grid = (int)((e->Ppad + kDnaTile * PPT - 1) / (kDnaTile * PPT));
     int per_sm = 1, sms = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level_dna, kDnaTile, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level_dna<PPT>, kDnaTile, 0) != cudaSuccess ||
+        per_sm < 1)
         per_sm = 1;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
     const long long wave = (long long)per_sm * sms;
@@ -364,7 +379,7 @@ int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
                 const OpDev &d = e->h_ops[op0 + c0 + i];
                 L.op[i] = make_int3(d.dad_slot, d.child[0], d.child[1]);
             }
-            k_level_dna<<<dim3(grid, cnt), kDnaTile, 0, e->st>>>(P, op0 + c0, L);
+            k_level_dna<PPT><<<dim3(grid, cnt), kDnaTile, 0, e->st>>>(P, op0 + c0, L);
             e->launches++;
             cudaError_t err = cudaGetLastError();
             if (err != cudaSuccess) return cuda_fail(err, "level_dna");
@@ -379,6 +394,15 @@ int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
     P.nops -= rest;
     P.branch_op -= rest;
     return launch_traverse_dna(e, P, epi);
+}
+
+// Level-synchronous schedule with a fused tail: levels whose (op, tile) pairs
+// fill the GPU (at least the resident CTAs of one wave) run one launch each;
+// the remaining narrow levels (a Yule tree ends in a chain of one-op levels)
+// and the branch epilogue run as one fused launch that walks them per tile.
+// Tile 2 selects two patterns per thread in the level launches.
+int launch_levels_dna(iqgpu_engine *e, MixParams P, int epi) {
+    return e->tile == 2 ? launch_levels_dna_t<2>(e, P, epi) : launch_levels_dna_t<1>(e, P, epi);
 }
 
 int launch_flow_dna(iqgpu_engine *e, const MixParams &P) {

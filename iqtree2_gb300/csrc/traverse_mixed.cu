@@ -438,7 +438,7 @@ int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t
     }
     // 4-state models: one thread per pattern and all its categories, unless a
     // per-category tile was chosen explicitly
-    if (e->n == 4 && e->C <= 4 && e->tile == 1) {
+    if (e->n == 4 && e->C <= 4 && (e->tile == 1 || (e->tile == 2 && e->level_sync))) {
         if (!e->level_sync && !e->flow) return launch_traverse_dna(e, P, epi);
         if (e->level_sync) return launch_levels_dna(e, P, epi);
         int rc = launch_flow_dna(e, P);

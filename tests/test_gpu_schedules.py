@@ -30,7 +30,7 @@ def test_all_schedules_agree(oracle_mod, name):
         autotune.apply(eng, cand)
         got[(tile, sched)] = eng.compute_likelihood(ops, a, b, length)
         assert rel(got[(tile, sched)], want) < 1e-6, (tile, sched)
-    for tile in (1,) + autotune.TILES:
+    for tile in (1, 2) + autotune.TILES:
         same_tile = [v for (t, _), v in got.items() if t == tile]
         assert len(set(same_tile)) <= 1, (tile, got)
 
@@ -52,8 +52,8 @@ def test_dna_dataflow_large(oracle_mod):
     a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
     want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
     got = []
-    for sched in (0, 1, 2, 2):
-        autotune.apply(eng, (1, sched, 0, 0))
+    for cand in ((1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (1, 2, 0, 0), (2, 1, 0, 0)):
+        autotune.apply(eng, cand)
         got.append(eng.compute_likelihood(ops, a, b, length))
     assert len(set(got)) == 1, got
     assert rel(got[0], want) < 1e-6
