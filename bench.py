@@ -499,6 +499,13 @@ def run_batched(args):
     rell_s = (time.perf_counter() - t0) / reps
     want = trees @ weights.T.astype(np.float64)
     rell_err = float(np.max(np.abs(scores - want) / np.abs(want)))
+    # the per-tree UFBoot step: scores of the tree just evaluated, inputs on the device
+    for _ in range(args.warmup):
+        cur = eng.rell_current()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cur = eng.rell_current()
+    rell_cur_s = (time.perf_counter() - t0) / reps
     eng.close()
 
     # 12 uneven partitions, separate GTR+G4, one tree
@@ -548,7 +555,9 @@ def run_batched(args):
                 "max_abs_dlnl_batch_vs_one_by_one": float(np.max(np.abs(lnl_b - lnl_seq))),
                 "note": "one evaluation = two partials + Newton-Raphson on the central branch + lnL"},
         "rell": {"replicates": 1000, "trees": 64, "ms": rell_s * 1e3,
-                 "replicate_tree_scores_per_s": 64 * 1000 / rell_s, "max_rel_err_vs_fp64_numpy": rell_err},
+                 "replicate_tree_scores_per_s": 64 * 1000 / rell_s, "max_rel_err_vs_fp64_numpy": rell_err,
+                 "current_tree_ms": rell_cur_s * 1e3,
+                 "note": "trees: host FP64 pattern lnL in; current tree: device-resident pattern lnL"},
         "partitions": {"count": len(sizes), "sites": sizes, "graph_ms": part_graph_s * 1e3,
                        "one_by_one_ms": part_seq_s * 1e3, "speedup": part_seq_s / part_graph_s,
                        "graph_updates_per_s": part_updates / part_graph_s, "lnl": tot},

@@ -224,6 +224,9 @@ int iqgpu_set_boot_weights(iqgpu_engine *e, const float *weights, int32_t nreps)
  * * weight[r][ptn] (saveCurrentTree, tree/iqtree.cpp:3551-3630); FP32 products
  * like the reference's float dot product, FP64 accumulation every 256 patterns. */
 int iqgpu_rell(iqgpu_engine *e, const double *pattern_lh, int32_t ntrees, double *out);
+/* RELL scores of the tree whose lnL was computed last, read from its pattern
+ * lnL on the device (no host copy): out[r] for every replicate r. */
+int iqgpu_rell_current(iqgpu_engine *e, double *out);
 
 /* ---- serving: continuous batching of jobs ------------------------------ */
 /* A job is one likelihood + branch-optimisation request on its own tree and

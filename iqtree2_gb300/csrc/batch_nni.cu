@@ -106,29 +106,26 @@ __device__ bool nni_reduce(double (&v)[kRedSlots], const NniDev &D, int k, doubl
 __global__ void __launch_bounds__(kTPB) k_nni_derv(const MixParams P, const NniDev D) {
     const int k = blockIdx.y;
     if (D.st[k].status != NR_RUNNING) return;  // uniform per CTA
-    __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
+    __shared__ float whi[3][kMaxCat * kMaxStates], wlo[3][kMaxCat * kMaxStates];
     const int n = P.n, C = P.ncat, B = n * C;
     const double len = D.st[k].rts;
     for (int t = threadIdx.x; t < B; t += blockDim.x) {
         const int c = t / n, i = t % n;
         const double cof = P.eval[i] * P.rates[c];
         const double val = exp(cof * len) * P.props[c];
-        v0[t] = val;
-        v1[t] = cof * val;
-        v2[t] = cof * cof * val;
+        const double v[3] = {val, cof * val, cof * cof * val};
+        for (int j = 0; j < 3; j++) {
+            whi[j][t] = (float)v[j];
+            wlo[j][t] = (float)(v[j] - (double)whi[j][t]);
+        }
     }
     __syncthreads();
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
     if (p < P.nptn) {
-        const float *th = D.theta + (long long)k * B * P.ldp + p;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-        for (int q = 0; q < B; q++) {
-            const double t0 = (double)th[(long long)q * P.ldp];
-            a0 = fma(v0[q], t0, a0);
-            a1 = fma(v1[q], t0, a1);
-            a2 = fma(v2[q], t0, a2);
-        }
+        double a[3];
+        theta_sums_df<3>(whi, wlo, D.theta + (long long)k * B * P.ldp + p, P.ldp, B, a);
+        const double a0 = a[0], a1 = a[1], a2 = a[2];
         const double bs = D.bscale[(long long)k * P.ldp + p];
         const double lh = fabs(a0) + P.invar[p] * exp(-bs);
         const double inv = 1.0 / lh;

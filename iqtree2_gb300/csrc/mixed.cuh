@@ -97,6 +97,40 @@ struct MixBufParams {
 
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
+// Per-pattern sums over the B = ncat * n eigen-space entries of theta (FP32 in
+// memory, row stride ld): s_j = sum_k w_j[k] theta[k] for NW weight rows held
+// as FP32 pairs (w = hi + lo, from the FP64 values). Double-float arithmetic:
+// each product's rounding error comes from an FMA and each addition's from
+// TwoSum (Knuth), so the sums carry about 44 bits; eigen-space terms cancel,
+// and plain FP32 sums lose too much for the derivatives. About 11 FP32
+// operations per term instead of one FP64 FMA, which GB300 runs ~60x slower.
+template <int NW>
+__device__ __forceinline__ void theta_sums_df(const float (*whi)[kMaxCat * kMaxStates],
+                                              const float (*wlo)[kMaxCat * kMaxStates], const float *th, long long ld,
+                                              int B, double (&s)[NW]) {
+    float sh[NW], sl[NW];
+#pragma unroll
+    for (int j = 0; j < NW; j++) sh[j] = sl[j] = 0.f;
+    for (int k = 0; k < B; k++) {
+        const float t = th[(long long)k * ld];
+#pragma unroll
+        for (int j = 0; j < NW; j++) {
+            // explicitly rounded operations: no contraction into FMAs may
+            // change the error terms
+            const float ph = __fmul_rn(whi[j][k], t);
+            float pl = fmaf(whi[j][k], t, -ph);  // exact error of the product
+            pl = fmaf(wlo[j][k], t, pl);
+            const float sum = __fadd_rn(sh[j], ph);  // TwoSum(sh, ph)
+            const float bp = __fsub_rn(sum, sh[j]);
+            const float err = __fadd_rn(__fsub_rn(sh[j], __fsub_rn(sum, bp)), __fsub_rn(ph, bp));
+            sh[j] = sum;
+            sl[j] = __fadd_rn(sl[j], __fadd_rn(err, pl));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NW; j++) s[j] = (double)sh[j] + (double)sl[j];
+}
+
 __device__ __forceinline__ void mix_warp_reduce(double (&v)[kRedSlots]) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)

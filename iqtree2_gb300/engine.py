@@ -102,6 +102,7 @@ def lib():
         "iqgpu_group_destroy": ([vp], ct.c_int),
         "iqgpu_set_kpieces": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_get_launches": ([vp, ct.POINTER(ct.c_int64)], ct.c_int),
+        "iqgpu_rell_current": ([vp, ct.c_void_p], ct.c_int),
         "iqgpu_derv_noalloc": ([vp, vp, vp, vp, ct.c_int32, ct.c_int64, ct.c_int32, ct.c_int32, _DP, _DP, _DP,
                                 ct.c_double, vp, vp], ct.c_int),
         "iqgpu_nni_batch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, _DP, _DP], ct.c_int),
@@ -303,6 +304,12 @@ class Engine:
         w = np.ascontiguousarray(weights, np.float32)
         _check(lib().iqgpu_set_boot_weights(self.h, w.ctypes.data_as(ct.POINTER(ct.c_float)), w.shape[0]))
         self._nreps = w.shape[0]
+
+    def rell_current(self):
+        """RELL scores of the last evaluated tree against every replicate (device-resident inputs)."""
+        out = np.zeros(self._nreps)
+        _check(lib().iqgpu_rell_current(self.h, _dp(out)))
+        return out
 
     def rell(self, pattern_lh):
         plh = np.ascontiguousarray(pattern_lh, np.float64)

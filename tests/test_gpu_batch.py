@@ -72,6 +72,28 @@ def test_rell_matches_numpy():
     assert np.max(np.abs(got - want) / np.abs(want)) < 1e-6
 
 
+def test_rell_current_tree_on_device(oracle_mod):
+    """RELL of the last evaluated tree from its device-resident pattern lnL
+    equals the host-input path on the same vector; 1,000 replicates."""
+    ds = simulate.dna_gtr_dataset(16, 20000, 44)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, 4, 4, ds.ntaxa, 18, topo.nslots, precision=engine.F32, max_ops=topo.nslots)
+    eng.set_model(ds.model)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    leaf, nb = 0, topo.adj[0][0][0]
+    eng.compute_likelihood(topo.branch_ops(nb, leaf), topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb))
+    w = simulate.bootstrap_weights(ds.freq, 1000, np.random.default_rng(8))
+    eng.set_boot_weights(w)
+    cur = eng.rell_current()
+    plh = eng.pattern_lh()
+    host = eng.rell(plh[None, :])[0]
+    want = w.astype(np.float64) @ plh
+    assert cur.shape == (1000,)
+    np.testing.assert_array_equal(cur, host)
+    assert np.max(np.abs(cur - want) / np.abs(want)) < 1e-6
+
+
 @pytest.mark.parametrize("precision", [engine.F32, engine.F64])
 def test_partition_group_one_graph(oracle_mod, precision):
     """12 uneven DNA partitions with separate GTR+G4 on one tree, evaluated by
