@@ -140,6 +140,53 @@ __device__ __forceinline__ unsigned bf16x2(float a, float b) {
     return v;
 }
 
+// ---- warp-specialised pipelines: non-blocking mbarrier test, plain arrive,
+// release/acquire counters in shared memory, a barrier over part of the CTA ----
+__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"((unsigned)__cvta_generic_to_shared(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((unsigned)__cvta_generic_to_shared(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void st_release_cta(unsigned *p, unsigned v) {
+    asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v)
+                 : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_cta(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];"
+                 : "=r"(v)
+                 : "r"((unsigned)__cvta_generic_to_shared(p))
+                 : "memory");
+    return v;
+}
+// named barrier 1 over the first `nthreads` threads (whole warps)
+__device__ __forceinline__ void bar_sync_part(unsigned nthreads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+// the same barrier, returning whether any participating thread passed true
+__device__ __forceinline__ bool bar_or_part(unsigned nthreads, bool flag) {
+    unsigned out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, 1, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(out)
+        : "r"((unsigned)flag), "r"(nthreads)
+        : "memory");
+    return out != 0;
+}
+
 // ---- TMA tiled load (tensor map), completion counted on an mbarrier ----
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
                                             unsigned long long *bar) {

@@ -133,6 +133,61 @@ __device__ __forceinline__ void tc_stage(const TcItem &it, int st, int ksplit, i
     kh = rem % ksplit;
 }
 
+// This thread's row of a landed stage: TF32 hi in place and lo beside it, or
+// the BF16 operand (zero beyond the category's states).
+template <bool BF>
+__device__ __forceinline__ void tc_convert_row(const TcParams &T, int r, float *ah, unsigned char *a2) {
+    const int kqs = T.kqs;
+    const int base = (r >> 3) * kqs * 32 + (r & 7) * 4;
+    if constexpr (BF) {
+        const int nch = T.kpb / 8;
+        uint4 *dst = reinterpret_cast<uint4 *>(a2 + (r >> 3) * nch * 128 + (r & 7) * 16);
+        for (int j = 0; j < nch; j++) {
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 v0 = 2 * j < kqs ? *reinterpret_cast<const float4 *>(ah + base + 2 * j * 32) : z;
+            const float4 v1 = 2 * j + 1 < kqs ? *reinterpret_cast<const float4 *>(ah + base + (2 * j + 1) * 32) : z;
+            dst[j * 8] = make_uint4(bf16x2(v0.x, v0.y), bf16x2(v0.z, v0.w), bf16x2(v1.x, v1.y), bf16x2(v1.z, v1.w));
+        }
+    } else {
+        float *al = reinterpret_cast<float *>(a2);
+        for (int q = 0; q < kqs; q++) {
+            const float4 v = *reinterpret_cast<const float4 *>(ah + base + q * 32);
+            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+            *reinterpret_cast<float4 *>(ah + base + q * 32) = h;
+            *reinterpret_cast<float4 *>(al + base + q * 32) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        }
+    }
+}
+
+// One stage's MMAs into accumulator d (one thread): three split-TF32 passes
+// per K step, or one BF16 pass; the first K step of the first piece starts the
+// accumulation.
+template <int NP, bool BF>
+__device__ __forceinline__ void tc_stage_mmas(const TcParams &T, unsigned d, unsigned char *slot, int kh) {
+    const unsigned ub = smem_u32(slot + T.b_off);
+    if constexpr (BF) {
+        const uint32_t idesc = idesc_bf16(kTcRows, NP);
+        const unsigned ua = smem_u32(slot + T.a2_off), sbo = (unsigned)(T.kpb / 8 * 128);
+        for (int ks = 0; ks < T.kpb / 16; ks++)
+            mma_bf16(d, smem_desc(ua + ks * 256, 128, sbo), smem_desc(ub + ks * 256, 128, sbo), idesc,
+                     ks > 0 || kh > 0);
+    } else {
+        const uint32_t idesc = idesc_tf32(kTcRows, NP);
+        const unsigned a_sbo = (unsigned)(T.kqs * 128), b_sbo = (unsigned)(T.kps / 4 * 128);
+        const unsigned uah = smem_u32(slot), ual = smem_u32(slot + T.a2_off);
+        const unsigned ubl = ub + (unsigned)T.b_bytes;
+        for (int ks = 0; ks < T.ksteps; ks++) {
+            const uint64_t dah = smem_desc(uah + ks * 256, 128, a_sbo);
+            const uint64_t dal = smem_desc(ual + ks * 256, 128, a_sbo);
+            const uint64_t dbh = smem_desc(ub + ks * 256, 128, b_sbo);
+            const uint64_t dbl = smem_desc(ubl + ks * 256, 128, b_sbo);
+            mma_tf32(d, dal, dbh, idesc, ks > 0 || kh > 0);
+            mma_tf32(d, dah, dbl, idesc, true);
+            mma_tf32(d, dah, dbh, idesc, true);
+        }
+    }
+}
+
 // BF: one BF16 pass (kind::f16, FP32 accumulate) instead of three TF32 passes.
 template <int NP, int NSTAGE, bool BF>
 __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constant__ CUtensorMap tmA, const TcParams T,
@@ -247,8 +302,6 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
         }
     };
 
-    const uint32_t idesc = BF ? idesc_bf16(kTcRows, NP) : idesc_tf32(kTcRows, NP);
-    const unsigned a_sbo = (unsigned)(kqs * 128), b_sbo = (unsigned)(T.kps / 4 * 128);
     int ecount0 = 0, ecount1 = 0;  // commits made to ebar[0], ebar[1]
     bool abort = false;
     try_issue(NSTAGE);
@@ -314,55 +367,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
                 const bool ok = mbar_wait(&full[s], (unsigned)((consumed / NSTAGE) & 1), kWaitPolls);
                 float *ah = reinterpret_cast<float *>(slot_at(s));
                 unsigned char *a2 = slot_at(s) + T.a2_off;
-                if (ok) {
-                    const int base = (r >> 3) * kqs * 32 + (r & 7) * 4;
-                    if constexpr (BF) {
-                        // this row's states, rounded to BF16, in [row group][8-state chunk][row][8] order
-                        const int nch = T.kpb / 8;
-                        uint4 *dst = reinterpret_cast<uint4 *>(a2 + (r >> 3) * nch * 128 + (r & 7) * 16);
-                        for (int j = 0; j < nch; j++) {
-                            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-                            const float4 v0 = 2 * j < kqs ? *reinterpret_cast<const float4 *>(ah + base + 2 * j * 32) : z;
-                            const float4 v1 =
-                                2 * j + 1 < kqs ? *reinterpret_cast<const float4 *>(ah + base + (2 * j + 1) * 32) : z;
-                            dst[j * 8] = make_uint4(bf16x2(v0.x, v0.y), bf16x2(v0.z, v0.w), bf16x2(v1.x, v1.y),
-                                                    bf16x2(v1.z, v1.w));
-                        }
-                    } else {
-                        float *al = reinterpret_cast<float *>(a2);
-                        for (int q = 0; q < kqs; q++) {
-                            const float4 v = *reinterpret_cast<const float4 *>(ah + base + q * 32);
-                            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-                            *reinterpret_cast<float4 *>(ah + base + q * 32) = h;
-                            *reinterpret_cast<float4 *>(al + base + q * 32) =
-                                make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-                        }
-                    }
-                }
+                if (ok) tc_convert_row<BF>(T, r, ah, a2);
                 fence_proxy_async_smem();
                 if (__syncthreads_or(!ok || (r == 0 && failed))) { abort = true; break; }
                 if (r == 0) {
                     tc_fence_after();
                     const unsigned d = tmem + (unsigned)((c & 1) * 2 * NP + side * NP);
-                    const unsigned ub = smem_u32(slot_at(s) + T.b_off);
-                    if constexpr (BF) {
-                        const unsigned ua = smem_u32(a2), sbo = (unsigned)(T.kpb / 8 * 128);
-                        for (int ks = 0; ks < T.kpb / 16; ks++)
-                            mma_bf16(d, smem_desc(ua + ks * 256, 128, sbo), smem_desc(ub + ks * 256, 128, sbo), idesc,
-                                     ks > 0 || kh > 0);
-                    } else {
-                        const unsigned uah = smem_u32(ah), ual = smem_u32(a2);
-                        const unsigned ubl = ub + (unsigned)T.b_bytes;
-                        for (int ks = 0; ks < T.ksteps; ks++) {
-                            const uint64_t dah = smem_desc(uah + ks * 256, 128, a_sbo);
-                            const uint64_t dal = smem_desc(ual + ks * 256, 128, a_sbo);
-                            const uint64_t dbh = smem_desc(ub + ks * 256, 128, b_sbo);
-                            const uint64_t dbl = smem_desc(ubl + ks * 256, 128, b_sbo);
-                            mma_tf32(d, dal, dbh, idesc, ks > 0 || kh > 0);
-                            mma_tf32(d, dah, dbl, idesc, true);
-                            mma_tf32(d, dah, dbh, idesc, true);
-                        }
-                    }
+                    tc_stage_mmas<NP, BF>(T, d, slot_at(s), kh);
                     mma_commit(&mmab[s]);
                     if (last) mma_commit(&ebar[c & 1]);
                 }
@@ -416,8 +427,262 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
     if (warp == 0) tmem_dealloc(tmem, 4 * NP);
 }
 
-// B operands: per op, child, category: hi and lo of P_c(t)[x][y] in
-// [x/8][y/4][x%8][y%4] order, zero outside x < n, y < n.
+// ---------------------------------------------------------------------------
+// Warp-specialised form of the level schedule. Warps 0-3 ("workers", one
+// pattern row per thread) convert landed stages and run the epilogues; warp 4
+// lane 0 ("issuer") keeps the copies and the MMAs going on its own:
+//  * it refills a ring slot the moment the slot's previous MMAs complete
+//    (mmab), instead of after the next stage's conversion;
+//  * it issues a stage's MMAs as soon as all 128 workers have converted it
+//    (conv mbarrier, 128 arrivals) and, for the first stage of a category,
+//    once the workers have read out the category that last used the same
+//    accumulator buffer (epi_done counter, release/acquire in shared memory).
+// Categories are numbered g = item * ncat + c over the CTA's items; buffer
+// g & 1 holds category g. Workers synchronise among themselves only with a
+// 128-thread named barrier per category epilogue. Every wait is bounded; a
+// wait that gives up raises the shared abort flag and the status word.
+template <int NP, int NSTAGE, bool BF>
+__global__ void __launch_bounds__(kTcRows + 32, 1)
+    k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl) {
+    const MixParams &P = T.M;
+    const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const bool worker = tid < kTcRows;
+    const long long ld = P.ldp;
+    const int total = T.ntiles * nl;
+    const int nitems =
+        (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(P.state_unknown + 1) * C * npad;
+    const int kqs = T.kqs, ksplit = T.ksplit;
+    const int a_raw = 16 * kqs * 128;
+    const unsigned stage_tx = (unsigned)(a_raw + T.b_total);
+
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    __shared__ unsigned long long full[NSTAGE], conv[NSTAGE], mmab[NSTAGE], ebar[2];
+    __shared__ unsigned tmem_base_s, epi_done, abort_flag;
+    __shared__ int4 opc[kTcOpCache];
+    unsigned char *const tc_smem = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+    auto slot_at = [&](int s) { return tc_smem + s * T.slot_bytes; };
+
+    if (!BF) {
+        for (int i = tid; i < NSTAGE * 2 * 32; i += blockDim.x) {
+            float *pad = (float *)(slot_at(i / 64) + ((i / 32) & 1) * T.a2_off + a_raw);
+            pad[i & 31] = 0.f;
+        }
+    }
+    for (int i = tid; i < nl && i < kTcOpCache; i += blockDim.x) {
+        const OpDev op = P.ops[op0 + i];
+        opc[i] = make_int4(op.dad_slot, op.child[0], op.child[1], 0);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&conv[s], kTcRows);
+            mbar_init(&mmab[s], 1);
+        }
+        mbar_init(&ebar[0], 1);
+        mbar_init(&ebar[1], 1);
+        epi_done = 0;
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&tmem_base_s), 4 * NP);
+        tmem_relinquish();
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = tmem_base_s;
+
+    if (!worker) {
+        // ---------------- issuer ----------------
+        if ((tid & 31) == 0 && nitems > 0) {
+            int ti = 0, ts = 0, issued = 0;  // copy cursor: item, stage within item, stages issued
+            int mi = 0, ms = 0, mdone = 0;   // MMA cursor
+            TcItem tit = tc_item(T, 0, false, op0, opc), mit = tit;
+            auto skip = [&](int &item, int &st, TcItem &it) {
+                while (item < nitems && st >= tc_nstages(it, C, ksplit)) {
+                    item++;
+                    st = 0;
+                    if (item < nitems) it = tc_item(T, item, false, op0, opc);
+                }
+            };
+            skip(ti, ts, tit);
+            skip(mi, ms, mit);
+            unsigned idle = 0;
+            while (mi < nitems) {
+                bool progress = false;
+                // copies: as far ahead as the ring allows
+                while (ti < nitems && issued < mdone + NSTAGE) {
+                    const int s = issued % NSTAGE;
+                    if (issued >= NSTAGE && !mbar_test(&mmab[s], (unsigned)((issued / NSTAGE - 1) & 1))) break;
+                    int c, side, kh;
+                    tc_stage(tit, ts, ksplit, c, side, kh);
+                    const int child = side == 0 ? tit.lref : tit.rref;
+                    unsigned char *slot = slot_at(s);
+                    mbar_expect_tx(&full[s], stage_tx);
+                    tma_load_3d(slot, &tmA, 0, c * kq + kh * kqs, child * T.groups_per_slot + tit.tile * 16,
+                                &full[s]);
+                    const int ch = side == 0 ? tit.lch : 1 - tit.lch;
+                    const float *bsrc = T.tcb + (long long)tit.k * T.tcb_stride +
+                                        (long long)((ch * C + c) * ksplit + kh) * T.b_stage;
+                    tma_load_1d(slot + T.b_off, bsrc, (unsigned)T.b_total, &full[s]);
+                    issued++;
+                    ts++;
+                    skip(ti, ts, tit);
+                    progress = true;
+                }
+                // the next stage's MMAs, once converted and its accumulator is free
+                {
+                    const int s = mdone % NSTAGE;
+                    int c, side, kh;
+                    tc_stage(mit, ms, ksplit, c, side, kh);
+                    const int per = (int)mit.lint + (int)mit.rint;
+                    const int sk = ms % (per * ksplit);
+                    const int g = mi * C + c;
+                    const bool first = sk == 0, last = sk == per * ksplit - 1;
+                    if (mdone < issued && mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
+                        (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
+                        tc_fence_after();
+                        const unsigned d = tmem + (unsigned)((g & 1) * 2 * NP + side * NP);
+                        tc_stage_mmas<NP, BF>(T, d, slot_at(s), kh);
+                        mma_commit(&mmab[s]);
+                        if (last) mma_commit(&ebar[g & 1]);
+                        mdone++;
+                        ms++;
+                        skip(mi, ms, mit);
+                        progress = true;
+                    }
+                }
+                if (progress) {
+                    idle = 0;
+                } else if (__nanosleep(64), ++idle >= kWaitPolls / 16 || *(volatile unsigned *)&abort_flag) {
+                    if (idle >= kWaitPolls / 16) {
+                        atomicExch(&abort_flag, 1u);
+                        atomicExch(P.status, kStatusTimeout);
+                    }
+                    break;
+                }
+            }
+            // bounded waits for copies and MMAs still in flight before the memory is released
+            for (int i = mdone; i < issued; i++) mbar_wait(&full[i % NSTAGE], (unsigned)((i / NSTAGE) & 1), kWaitPolls);
+            if (mdone > 0)
+                mbar_wait(&mmab[(mdone - 1) % NSTAGE], (unsigned)(((mdone - 1) / NSTAGE) & 1), kWaitPolls);
+        }
+        __syncwarp();  // the issuer warp reconverges before the final barrier
+    } else {
+        // ---------------- workers ----------------
+        const int r = tid;
+        const unsigned lane_off = (unsigned)(warp * 32) << 16;
+        int consumed = 0, ecount0 = 0, ecount1 = 0;
+        bool abort = false;
+        auto epilogue = [&](const TcItem &it, int c, int g, float *dad, long long p, const float *TL, int sl, int sr,
+                            float &cmax) -> bool {
+            const int per = (int)it.lint + (int)it.rint;
+            const float *tl = it.lint ? nullptr : TL + (long long)sl * C * npad + c * npad;
+            const float *tr = it.rint ? nullptr : TL + (it.lch ? -TB : TB) + (long long)sr * C * npad + c * npad;
+            bool ok = !*(volatile unsigned *)&abort_flag;
+            if (per > 0 && ok) {
+                const int ec = (g & 1) ? ecount1 : ecount0;
+                ok = mbar_wait(&ebar[g & 1], (unsigned)((ec - 1) & 1), kWaitPolls);
+            }
+            if (bar_or_part(kTcRows, !ok)) return false;  // uniform stop for every worker
+            if (per > 0) tc_fence_after();
+            const unsigned dL = tmem + lane_off + (unsigned)((g & 1) * 2 * NP), dR = dL + NP;
+            float *out = dad + (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * kq * 32;
+            for (int q = 0; q < kq; q++) {
+                float lv[4], rv[4];
+                if (it.lint && it.rint) {
+                    tmem_ld4x2(dL + 4 * q, dR + 4 * q, lv, rv);
+                } else if (it.rint) {
+                    tmem_ld4(dR + 4 * q, rv);
+                    const float4 t4 = ld4(tl + 4 * q);
+                    lv[0] = t4.x; lv[1] = t4.y; lv[2] = t4.z; lv[3] = t4.w;
+                } else {
+                    const float4 a4 = ld4(tl + 4 * q), b4 = ld4(tr + 4 * q);
+                    lv[0] = a4.x; lv[1] = a4.y; lv[2] = a4.z; lv[3] = a4.w;
+                    rv[0] = b4.x; rv[1] = b4.y; rv[2] = b4.z; rv[3] = b4.w;
+                }
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    o[i] = (4 * q + i < n) ? lv[i] * rv[i] : 0.f;
+                    cmax = fmaxf(cmax, o[i]);
+                }
+                *reinterpret_cast<float4 *>(out + q * 32) = make_float4(o[0], o[1], o[2], o[3]);
+            }
+            // every worker has read its row of buffer g & 1: the issuer may reuse it
+            tc_fence_before();
+            bar_sync_part(kTcRows);
+            if (r == 0) st_release_cta(&epi_done, (unsigned)(g + 1));
+            return true;
+        };
+        for (int j = 0; j < nitems && !abort; j++) {
+            const TcItem it = tc_item(T, j, false, op0, opc);
+            const long long p = (long long)it.tile * kTcRows + r;
+            const int sl = it.lint ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
+            const int sr = it.rint ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
+            const int e_in = (it.lint ? P.expo[(long long)it.lref * ld + p] : 0) +
+                             (it.rint ? P.expo[(long long)it.rref * ld + p] : 0);
+            const int per = (int)it.lint + (int)it.rint;
+            const float *TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
+            float *dad = P.part + (long long)it.dad * P.slot_floats;
+            float cmax = 0.f;
+            for (int c = 0; c < C && !abort; c++) {
+                const int g = j * C + c;
+                for (int sk = 0; sk < per * ksplit; sk++) {
+                    // no barrier per stage: a wait that gives up raises the abort flag, the
+                    // stage is skipped, and the next epilogue's vote stops every worker
+                    const int s = consumed % NSTAGE;
+                    const bool ok = !*(volatile unsigned *)&abort_flag &&
+                                    mbar_wait(&full[s], (unsigned)((consumed / NSTAGE) & 1), kWaitPolls);
+                    if (ok) {
+                        tc_convert_row<BF>(T, r, reinterpret_cast<float *>(slot_at(s)), slot_at(s) + T.a2_off);
+                        fence_proxy_async_smem();
+                    } else {
+                        atomicExch(&abort_flag, 1u);
+                    }
+                    mbar_arrive(&conv[s]);
+                    consumed++;
+                }
+                if (abort) break;
+                if (per > 0) {  // category g's last stage commits ebar[g & 1]
+                    if (g & 1) ecount1++;
+                    else ecount0++;
+                }
+                if (c > 0 && !epilogue(it, c - 1, g - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+            }
+            if (abort) break;
+            if (!epilogue(it, C - 1, j * C + C - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+            int sh = 0;
+            if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale
+                int ex;
+                frexpf(cmax, &ex);
+                sh = 1 - ex;
+                const float mul = __int_as_float((127 + sh) << 23);
+                float *row = dad + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+                for (int q = 0; q < C * kq; q++) {
+                    float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+                    v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                    *reinterpret_cast<float4 *>(row + q * 32) = v;
+                }
+            }
+            P.expo[(long long)it.dad * ld + p] = e_in - sh;
+        }
+        if (abort && r == 0) {
+            atomicExch(&abort_flag, 1u);
+            atomicExch(P.status, kStatusTimeout);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 4 * NP);
+}
+
 // B operands: per op, child, category and K piece kh: hi and lo of
 // P_c(t)[x][y] for y in piece kh, in [x/8][y'/4][x%8][y'%4] order (y' = y - kh
 // KS), zero outside x < n, y < n.
@@ -562,7 +827,11 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
     const size_t smem = tc_smem_bytes(T, NSTAGE);
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
-    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF>;
+    const bool ws = e->level_sync && e->tc_ws;  // warp-specialised level kernel
+    const int nthr = ws ? kTcRows + 32 : kTcRows;
+    cudaError_t err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                         : cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
     // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
@@ -572,9 +841,14 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, e->dev);
     cudaFuncAttributes fa;
     size_t stat = 0;
-    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess) stat = fa.sharedSizeBytes;
+    int regs = 0;
+    if ((ws ? cudaFuncGetAttributes(&fa, kern_ws) : cudaFuncGetAttributes(&fa, kern)) == cudaSuccess) {
+        stat = fa.sharedSizeBytes;
+        regs = fa.numRegs;
+    }
     const size_t per_cta = smem + stat + (size_t)reserve;
     int per_sm = (int)std::min<size_t>(512 / (4 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
+    if (regs > 0) per_sm = std::min(per_sm, 65536 / (regs * nthr));  // and by the register file
     if (per_sm < 1) per_sm = 1;
     const long long resident = (long long)per_sm * sms;
     // Narrow tail: from the first level whose (tile, op) pairs no longer fill
@@ -598,7 +872,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
         if (nl <= 0) continue;
         const long long items = (long long)T.ntiles * nl;
         const int grid = (int)std::min<long long>(items, resident);
-        kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
+        if (ws)
+            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl);
+        else
+            kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
         e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");

@@ -272,7 +272,8 @@ class Engine:
         _check(lib().iqgpu_set_tile(self.h, int(patterns_per_cta)))
 
     def set_schedule(self, schedule):
-        """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel)."""
+        """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel),
+        3 = level-synchronous on the warp-specialised tensor-core kernel."""
         _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
 
     def launches(self):
