@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 // 128-thread named barrier per category epilogue. Every wait is bounded; a
 // wait that gives up raises the shared abort flag and the status word.
 template <int NP, int NSTAGE, bool BF>
-__global__ void __launch_bounds__(kTcRows + 32, 1)
+__global__ void __launch_bounds__(kTcRows + 32, 4)
     k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl) {
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
@@ -832,6 +832,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     const int nthr = ws ? kTcRows + 32 : kTcRows;
     cudaError_t err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                          : cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the whole unified L1/shared array as shared memory: residency is set by shared memory
+    if (err == cudaSuccess)
+        err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributePreferredSharedMemoryCarveout, 100)
+                 : cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
     // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
@@ -848,7 +852,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     }
     const size_t per_cta = smem + stat + (size_t)reserve;
     int per_sm = (int)std::min<size_t>(512 / (4 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
-    if (regs > 0) per_sm = std::min(per_sm, 65536 / (regs * nthr));  // and by the register file
+    if (regs > 0) {  // and by the register file (allocated per warp in units of 256)
+        const int per_warp = ((regs * 32 + 255) / 256) * 256;
+        per_sm = std::min(per_sm, 65536 / (per_warp * (nthr / 32)));
+    }
     if (per_sm < 1) per_sm = 1;
     const long long resident = (long long)per_sm * sms;
     // Narrow tail: from the first level whose (tile, op) pairs no longer fill
