@@ -77,7 +77,10 @@ def kernel_name(use_tc, n, tile, bf16=False):
     """Dominant kernel of a path, from the autotuned label (tile/schedule[/sD][/kP])."""
     if use_tc:
         depth = next((int(t[1:]) for t in tile.split("/") if t.startswith("s")), 2)
-        return f"k_traverse_tc<{64 if n > 32 else 32},{depth},{'true' if bf16 else 'false'}>"
+        if "/level-tm" in tile and not bf16:
+            return "k_traverse_tc_tm"
+        name = "k_traverse_tc_ws" if "/level-ws" in tile else "k_traverse_tc"
+        return f"{name}<{64 if n > 32 else 32},{depth},{'true' if bf16 else 'false'}>"
     if tile.startswith("1/"):
         return "k_level_dna" if "/level" in tile else "k_traverse_dna<LNL>"
     nq = {4: 1, 20: 5}.get((n + 3) // 4 * 4, 0)

@@ -65,6 +65,87 @@ __global__ void k_partial_info_mixed(const OpDev *__restrict__ ops, float *__res
     }
 }
 
+// Double-float product a * b accumulated into (sh, sl): the product's rounding
+// error from FMAs, the addition's from TwoSum (Knuth), explicitly rounded
+// operations so no contraction changes the error terms. About 44 bits.
+__device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, float &sh, float &sl) {
+    const float p = __fmul_rn(ah, bh);
+    float pe = fmaf(ah, bh, -p);
+    pe = fmaf(ah, bl, pe);
+    pe = fmaf(al, bh, pe);
+    const float sum = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(sum, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(sum, bp)), __fsub_rn(p, bp));
+    sh = sum;
+    sl = __fadd_rn(sl, __fadd_rn(err, pe));
+}
+
+__device__ __forceinline__ void df_split(double v, float &h, float &l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+// Same outputs as k_partial_info_mixed for 16..64 states, one CTA per (op,
+// child, category): U diag(exp(lambda r_c t)) and U^-1 (and the tip vectors
+// when the child is a tip) staged in shared memory as FP32 pairs; each output
+// is a double-float dot product of length n, rounded once to FP32 at the end.
+// GB300 runs FP64 FMAs ~60x slower than FP32; the result is stored in FP32, so
+// the 44-bit double-float sums lose nothing that is kept.
+__global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict__ ops, float *__restrict__ opmats,
+                                                         long long op_stride, const double *__restrict__ evec,
+                                                         const double *__restrict__ inv,
+                                                         const double *__restrict__ eval,
+                                                         const double *__restrict__ rates,
+                                                         const double *__restrict__ tip_lh, int n, int npad, int C,
+                                                         int S) {
+    extern __shared__ float pi_smem[];
+    const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z;
+    const int child = ch ? ops[k].child[1] : ops[k].child[0];
+    const double len = ch ? ops[k].len[1] : ops[k].len[0];
+    const bool tip = child < 0;
+    const int nn = n * n;
+    float *ue_h = pi_smem, *ue_l = ue_h + nn, *iv_h = ue_l + nn, *iv_l = iv_h + nn;
+    float *tp_h = iv_l + nn, *tp_l = tp_h + S * n;  // tip vectors of the S observed states (tips only)
+    const double rl = rates[c] * len;
+    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+        const int i = t % n;
+        df_split(evec[t] * exp(eval[i] * rl), ue_h[t], ue_l[t]);
+        df_split(inv[t], iv_h[t], iv_l[t]);
+    }
+    if (tip)
+        for (int t = threadIdx.x; t < S * n; t += blockDim.x) df_split(tip_lh[t], tp_h[t], tp_l[t]);
+    __syncthreads();
+    float *base = opmats + (long long)k * op_stride;
+    const long long PM = (long long)C * n * npad;
+    float *Pm = base + ch * PM + (long long)c * n * npad;
+    for (int e = threadIdx.x; e < n * npad; e += blockDim.x) {
+        const int x = e / npad, y = e % npad;
+        float sh = 0.f, sl = 0.f;
+        if (y < n)
+            for (int i = 0; i < n; i++) df_mac(ue_h[x * n + i], ue_l[x * n + i], iv_h[i * n + y], iv_l[i * n + y], sh, sl);
+        Pm[e] = __fadd_rn(sh, sl);
+    }
+    if (!tip) return;
+    // leaf table[s][c][x] = sum_i (U e)[x][i] tip_lh[s][i]; the unknown state gives 1
+    const long long TB = (long long)(S + 1) * C * npad;
+    float *tab = base + 2 * PM + ch * TB;
+    for (int u = threadIdx.x; u < (S + 1) * npad; u += blockDim.x) {
+        const int st = u / npad, x = u % npad;
+        float v = 0.f;
+        if (x < n) {
+            if (st == S) {
+                v = 1.f;
+            } else {
+                float sh = 0.f, sl = 0.f;
+                for (int i = 0; i < n; i++)
+                    df_mac(ue_h[x * n + i], ue_l[x * n + i], tp_h[st * n + i], tp_l[st * n + i], sh, sl);
+                v = __fadd_rn(sh, sl);
+            }
+        }
+        tab[(long long)st * C * npad + (long long)c * npad + x] = v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // derivatives and lnL from the FP32 theta buffer, FP64 sums
 // (tree/phylokernelnew.h:2233-2633 and :3232-3428)
@@ -174,6 +255,16 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
 
 int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
     if (nops_with_branch <= 0) return IQGPU_OK;
+    if (e->n >= 16) {  // double-float products, one CTA per (op, child, category)
+        const size_t smem = (size_t)(4 * e->n * e->n + 2 * e->S * e->n) * 4;
+        cudaError_t err = cudaFuncSetAttribute(k_partial_info_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "partial_info_df smem attribute");
+        k_partial_info_df<<<dim3(nops_with_branch, 2, e->C), 256, smem, e->st>>>(
+            e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv, e->d_eval, e->d_rates, e->d_tip, e->n,
+            e->npad, e->C, e->S);
+        e->launches++;
+        return cuda_fail(cudaGetLastError(), "partial_info_df");
+    }
     const int Z = e->n > 20 ? 32 : 4;
     dim3 grid(nops_with_branch, 2, Z);
     k_partial_info_mixed<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv,

@@ -179,5 +179,10 @@ __device__ __forceinline__ void mix_grid_reduce(double (&v)[kRedSlots], const Re
 }
 
 MixParams mix_params(iqgpu_engine *e, int nops);
+// Ops [op0, op0 + nl) of the uploaded list whose children are both tips: true
+// when every one is, so the level can run on k_tiptip_level.
+bool level_all_tiptip(const iqgpu_engine *e, int op0, int nl);
+// One launch for such a level (traverse_mixed.cu).
+int launch_tiptip_level(iqgpu_engine *e, const MixParams &P, int op0, int nl);
 
 }  // namespace iqg

@@ -71,6 +71,17 @@ __device__ __forceinline__ void mma_bf16(unsigned d_taddr, uint64_t adesc, uint6
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)accumulate)
         : "memory");
 }
+// A from tensor memory (lanes = rows of A, one TF32 element per 32-bit column,
+// K step = 8 columns from a_taddr), B from shared memory.
+__device__ __forceinline__ void mma_tf32_ts(unsigned d_taddr, unsigned a_taddr, uint64_t bdesc, uint32_t idesc,
+                                            bool accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "r"(a_taddr), "l"(bdesc), "r"(idesc), "r"((unsigned)accumulate)
+        : "memory");
+}
 // Arrive once on the mbarrier when every tcgen05 operation this thread has
 // issued so far is complete.
 __device__ __forceinline__ void mma_commit(unsigned long long *bar) {
@@ -122,6 +133,35 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
 #pragma unroll
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
+
+// 20 consecutive columns of this thread's lane (x16 + x4), waited in the same block.
+__device__ __forceinline__ void tmem_ld20(unsigned taddr, float (&v)[20]) {
+    unsigned r[20];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%20];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16, %17, %18, %19}, [%21];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19])
+        : "r"(taddr), "r"(taddr + 16u)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 20; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- registers -> TMEM (32x32b: this thread's lane, 8 consecutive columns) ----
+__device__ __forceinline__ void tmem_st8(unsigned taddr, const float *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
+}
+// every tcgen05.st this thread issued has completed
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // TF32 split: hi = x rounded to the nearest TF32 value (10 explicit mantissa
 // bits; ties away from zero), formed on the bit pattern so that hi is exactly

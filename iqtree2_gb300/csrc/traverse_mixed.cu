@@ -20,6 +20,8 @@
 // The autotuner picks the schedule and the tile per workload.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mixed.cuh"
 
 namespace iqg {
@@ -334,6 +336,73 @@ __global__ void __launch_bounds__(512) k_level_mixed(const MixParams P, const in
     mixed_op<NQ>(P, k, smem, s_max, c, pl, p, pbase, TP);
 }
 
+// Tip-tip ops of one level (both children tips: the first level of every
+// traversal). Each output entry is the product of two leaf-table entries
+// (P_c(t) times the tip vector, computed per op by the precompute), so the op
+// is a pure store stream: one thread per pattern with all its categories,
+// grid (128-pattern blocks, ops of the level), full occupancy. The products,
+// the zero padding, the running maximum and the power-of-two rescale are
+// those of the tip-tip case of every other mixed kernel, so the partials are
+// bit-identical (tree/phylokernelnew.h:1632-1747 computes this case from the
+// same lookup tables).
+__global__ void __launch_bounds__(128) k_tiptip_level(const MixParams P, const int op0) {
+    const int C = P.ncat, n = P.n, npad = P.npad, kq = npad >> 2;
+    const long long ld = P.ldp;
+    const long long p = (long long)blockIdx.x * 128 + threadIdx.x;
+    const int k = op0 + blockIdx.y;
+    const OpDev op = P.ops[k];
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(P.state_unknown + 1) * C * npad;
+    const float *T0 = P.opmats + (long long)k * P.op_stride + 2 * PM;
+    const float *tl = T0 + (long long)P.states[(long long)(-1 - op.child[0]) * ld + p] * C * npad;
+    const float *tr = T0 + TB + (long long)P.states[(long long)(-1 - op.child[1]) * ld + p] * C * npad;
+    float *row = P.part + (long long)op.dad_slot * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+    float cmax = 0.f;
+    for (int c = 0; c < C; c++) {
+        for (int q = 0; q < kq; q++) {
+            const float4 a = ld4(tl + c * npad + 4 * q), b = ld4(tr + c * npad + 4 * q);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+            float o[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                o[i] = (4 * q + i < n) ? av[i] * bv[i] : 0.f;
+                cmax = fmaxf(cmax, o[i]);
+            }
+            *reinterpret_cast<float4 *>(row + (c * kq + q) * 32) = make_float4(o[0], o[1], o[2], o[3]);
+        }
+    }
+    int sh = 0;
+    if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale (rare: re-reads its own stores)
+        int ex;
+        frexpf(cmax, &ex);
+        sh = 1 - ex;
+        const float mul = __int_as_float((127 + sh) << 23);
+        for (int q = 0; q < C * kq; q++) {
+            float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+            *reinterpret_cast<float4 *>(row + q * 32) = v;
+        }
+    }
+    P.expo[(long long)op.dad_slot * ld + p] = -sh;
+}
+
+bool level_all_tiptip(const iqgpu_engine *e, int op0, int nl) {
+    for (int i = op0; i < op0 + nl; i++)
+        if (e->h_ops[i].child[0] >= 0 || e->h_ops[i].child[1] >= 0) return false;
+    return nl > 0;
+}
+
+int launch_tiptip_level(iqgpu_engine *e, const MixParams &P, int op0, int nl) {
+    for (int c0 = 0; c0 < nl; c0 += 65535) {
+        const int cnt = std::min(65535, nl - c0);
+        k_tiptip_level<<<dim3((unsigned)(e->Ppad / 128), cnt), 128, 0, e->st>>>(P, op0 + c0);
+        e->launches++;
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "tiptip_level");
+    }
+    return IQGPU_OK;
+}
+
 // Patterns per CTA: the autotuned value when set (iqgpu_set_tile), else 32.
 // TP * ncat <= 512.
 static int mix_tile(const iqgpu_engine *e) {
@@ -372,6 +441,11 @@ static int launch_levels_t(iqgpu_engine *e, const MixParams &P) {
     for (int l = 0; l < e->nlevels; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
+        if (level_all_tiptip(e, op0, nl)) {
+            int rc = launch_tiptip_level(e, P, op0, nl);
+            if (rc) return rc;
+            continue;
+        }
         kern<<<dim3(grid, nl), TP * e->C, smem, e->st>>>(P, TP, op0);
         e->launches++;
         cudaError_t err = cudaGetLastError();

@@ -683,6 +683,342 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     if (warp == 0) tmem_dealloc(tmem, 4 * NP);
 }
 
+// ---------------------------------------------------------------------------
+// A in tensor memory (20 states, split TF32, level schedule 4)
+// ---------------------------------------------------------------------------
+// The shared-memory-operand kernels above move every A byte through shared
+// memory about seven times per stage (copy in, conversion read, hi and lo
+// writes, and three MMA passes that re-read A for an N of only 32), so shared
+// memory, not HBM, bounds them. Here A never touches shared memory: each
+// worker thread loads its own pattern row of a category straight from HBM (a
+// warp's 32 rows of one 4-state chunk are four whole 128-byte lines), splits
+// it into TF32 hi/lo in registers and writes both into tensor memory with
+// tcgen05.st (row r = lane r). The issuer runs the MMAs with A read from
+// tensor memory and only B = P_c(t) (hi, lo) from shared memory, staged by
+// bulk copies up to kTmNB stages ahead.
+//
+// Stage m = (item, category) of an item with at least one internal child.
+// TMEM (256 columns per CTA, two CTAs per SM): accumulators D[m & 1][side] at
+// column (m & 1) * 64 + side * 32; A hi of side s at 128 + s * 2 KP, A lo KP
+// further. A is single-buffered: workers write stage m's A once the MMAs of
+// stage m-1 have completed (mdone), then arrive on conv; the issuer waits for
+// conv and the stage's B, issues the MMAs and commits them to mdone and to the
+// B slot's empty barrier. Workers read stage m-1's accumulators (epilogue)
+// while stage m's MMAs run, and the loads of the next stage's rows are in
+// flight meanwhile (two register buffers, used alternately). An item whose
+// children are both tips has no stage: its categories come from the leaf
+// tables alone.
+constexpr int kTmNB = 4;      // B slots
+constexpr int kTmKQ = 5;      // 4-state chunks per category (npad = 20)
+constexpr int kTmKP = 24;     // K padded to the TF32 K step
+constexpr int kTmCols = 256;  // TMEM columns per CTA
+
+__global__ void __launch_bounds__(kTcRows + 32, 2) k_traverse_tc_tm(const TcParams T, const int op0, const int nl) {
+    constexpr int KQ = kTmKQ, KP = kTmKP, NP = 32, KSTEPS = KP / 8;
+    const MixParams &P = T.M;
+    const int C = P.ncat, n = P.n, npad = P.npad;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const long long ld = P.ldp;
+    const int total = T.ntiles * nl;
+    const int nitems =
+        (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(P.state_unknown + 1) * C * npad;
+    const unsigned bside = (unsigned)T.b_total;  // B hi + lo of one side
+
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    __shared__ unsigned long long bfull[kTmNB], bempty[kTmNB], conv, mdone;
+    __shared__ unsigned tmem_base_s, abort_flag;
+    __shared__ int4 opc[kTcOpCache];
+    unsigned char *const bring = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+
+    for (int i = tid; i < nl && i < kTcOpCache; i += blockDim.x) {
+        const OpDev op = P.ops[op0 + i];
+        opc[i] = make_int4(op.dad_slot, op.child[0], op.child[1], 0);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTmNB; s++) {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], 1);
+        }
+        mbar_init(&conv, kTcRows);
+        mbar_init(&mdone, 1);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&tmem_base_s), kTmCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = tmem_base_s;
+
+    // (item, category) cursors over the stages: skip items without an internal child
+    auto skip_tips = [&](int &j, int &c, TcItem &it) {
+        while (j < nitems && !(it.lint || it.rint)) {
+            j++;
+            c = 0;
+            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+        }
+    };
+    auto advance = [&](int &j, int &c, TcItem &it) {
+        if (++c == C) {
+            c = 0;
+            j++;
+            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+        }
+        skip_tips(j, c, it);
+    };
+
+    if (warp == kTcRows / 32) {
+        // ---------------- issuer ----------------
+        if ((tid & 31) == 0 && nitems > 0) {
+            const uint32_t idesc = idesc_tf32(kTcRows, NP);
+            const unsigned b_sbo = (unsigned)(KP / 4 * 128);
+            int bj = 0, bc = 0, mj = 0, mc = 0, bissued = 0, mdone_n = 0;
+            TcItem bit = tc_item(T, 0, false, op0, opc), mit = bit;
+            skip_tips(bj, bc, bit);
+            skip_tips(mj, mc, mit);
+            unsigned idle = 0;
+            while (mj < nitems) {
+                bool progress = false;
+                // B of the coming stages, as far ahead as the slots allow
+                while (bj < nitems && bissued < mdone_n + kTmNB) {
+                    const int s = bissued % kTmNB;
+                    if (bissued >= kTmNB && !mbar_test(&bempty[s], (unsigned)((bissued / kTmNB - 1) & 1))) break;
+                    unsigned char *slot = bring + s * 2 * bside;
+                    mbar_expect_tx(&bfull[s], bside * ((unsigned)bit.lint + (unsigned)bit.rint));
+                    for (int side = 0; side < 2; side++) {
+                        if (!(side == 0 ? bit.lint : bit.rint)) continue;
+                        const int ch = side == 0 ? bit.lch : 1 - bit.lch;
+                        const float *src =
+                            T.tcb + (long long)bit.k * T.tcb_stride + (long long)(ch * C + bc) * T.b_stage;
+                        tma_load_1d(slot + side * bside, src, bside, &bfull[s]);
+                    }
+                    bissued++;
+                    advance(bj, bc, bit);
+                    progress = true;
+                }
+                // the next stage's MMAs, once its A is in tensor memory and its B has landed
+                if (mdone_n < bissued && mbar_test(&conv, (unsigned)(mdone_n & 1)) &&
+                    mbar_test(&bfull[mdone_n % kTmNB], (unsigned)((mdone_n / kTmNB) & 1))) {
+                    tc_fence_after();
+                    const int s = mdone_n % kTmNB;
+                    const unsigned ub = smem_u32(bring + s * 2 * bside);
+                    for (int side = 0; side < 2; side++) {
+                        if (!(side == 0 ? mit.lint : mit.rint)) continue;
+                        const unsigned d = tmem + (unsigned)((mdone_n & 1) * 2 * NP + side * NP);
+                        const unsigned ah = tmem + 128u + (unsigned)(side * 2 * KP), al = ah + (unsigned)KP;
+                        const unsigned bh = ub + (unsigned)side * bside, bl = bh + bside / 2;
+#pragma unroll
+                        for (int ks = 0; ks < KSTEPS; ks++) {
+                            const uint64_t dbh = smem_desc(bh + ks * 256, 128, b_sbo);
+                            const uint64_t dbl = smem_desc(bl + ks * 256, 128, b_sbo);
+                            mma_tf32_ts(d, al + 8 * ks, dbh, idesc, ks > 0);
+                            mma_tf32_ts(d, ah + 8 * ks, dbl, idesc, true);
+                            mma_tf32_ts(d, ah + 8 * ks, dbh, idesc, true);
+                        }
+                    }
+                    mma_commit(&bempty[s]);
+                    mma_commit(&mdone);
+                    mdone_n++;
+                    advance(mj, mc, mit);
+                    progress = true;
+                }
+                if (progress) {
+                    idle = 0;
+                } else if (__nanosleep(64), ++idle >= kWaitPolls / 16 || *(volatile unsigned *)&abort_flag) {
+                    if (idle >= kWaitPolls / 16) {
+                        atomicExch(&abort_flag, 1u);
+                        atomicExch(P.status, kStatusTimeout);
+                    }
+                    break;
+                }
+            }
+            // bounded waits for the copies and MMAs still in flight before the memory is released
+            for (int i = mdone_n; i < bissued; i++)
+                mbar_wait(&bfull[i % kTmNB], (unsigned)((i / kTmNB) & 1), kWaitPolls);
+            if (mdone_n > 0)
+                mbar_wait(&bempty[(mdone_n - 1) % kTmNB], (unsigned)(((mdone_n - 1) / kTmNB) & 1), kWaitPolls);
+        }
+        __syncwarp();
+    } else {
+        // ---------------- workers: one pattern row each ----------------
+        const int r = tid;
+        const unsigned lane_off = (unsigned)(warp * 32) << 16;
+        float4 bufA[2][KQ], bufB[2][KQ];
+        int m = 0;  // stages whose A this thread has written
+        bool abort = false;
+
+        // load cursor: the next stage whose rows are not requested yet
+        int lj = 0, lc = 0;
+        TcItem lit = tc_item(T, 0, false, op0, opc);
+        if (nitems > 0) skip_tips(lj, lc, lit);
+        auto load = [&](float4 (&b)[2][KQ]) {
+            if (lj >= nitems) return;
+            const long long p = (long long)lit.tile * kTcRows + r;
+            const long long off = (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)lc * KQ * 32;
+            if (lit.lint) {
+                const float *s = P.part + (long long)lit.lref * P.slot_floats + off;
+#pragma unroll
+                for (int q = 0; q < KQ; q++) b[0][q] = __ldcg(reinterpret_cast<const float4 *>(s + q * 32));
+            }
+            if (lit.rint) {
+                const float *s = P.part + (long long)lit.rref * P.slot_floats + off;
+#pragma unroll
+                for (int q = 0; q < KQ; q++) b[1][q] = __ldcg(reinterpret_cast<const float4 *>(s + q * 32));
+            }
+            advance(lj, lc, lit);
+        };
+
+        // the item being computed
+        int j = 0, c = 0, sl = 0, sr = 0, e_in = 0;
+        long long p = 0;
+        TcItem it{};
+        const float *TL = nullptr;
+        float *row = nullptr;  // this pattern's output block in the dad slot
+        float cmax = 0.f;
+        auto begin_item = [&]() {
+            it = tc_item(T, j, false, op0, opc);
+            p = (long long)it.tile * kTcRows + r;
+            sl = it.lint ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
+            sr = it.rint ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
+            e_in = (it.lint ? P.expo[(long long)it.lref * ld + p] : 0) +
+                   (it.rint ? P.expo[(long long)it.rref * ld + p] : 0);
+            TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
+            row = P.part + (long long)it.dad * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+            cmax = 0.f;
+        };
+        // category cc of the current item: internal sides from accumulator buffer pb
+        auto epilogue = [&](int cc, int pb) {
+            float lv[4 * KQ], rv[4 * KQ];
+            if (it.lint) {
+                tmem_ld20(tmem + lane_off + (unsigned)(pb * 2 * NP), lv);
+            } else {
+                const float *tl = TL + (long long)sl * C * npad + cc * npad;
+#pragma unroll
+                for (int q = 0; q < KQ; q++) {
+                    const float4 t4 = ld4(tl + 4 * q);
+                    lv[4 * q] = t4.x; lv[4 * q + 1] = t4.y; lv[4 * q + 2] = t4.z; lv[4 * q + 3] = t4.w;
+                }
+            }
+            if (it.rint) {
+                tmem_ld20(tmem + lane_off + (unsigned)(pb * 2 * NP + NP), rv);
+            } else {
+                const float *tr = TL + (it.lch ? -TB : TB) + (long long)sr * C * npad + cc * npad;
+#pragma unroll
+                for (int q = 0; q < KQ; q++) {
+                    const float4 t4 = ld4(tr + 4 * q);
+                    rv[4 * q] = t4.x; rv[4 * q + 1] = t4.y; rv[4 * q + 2] = t4.z; rv[4 * q + 3] = t4.w;
+                }
+            }
+            float *out = row + (long long)cc * KQ * 32;
+#pragma unroll
+            for (int q = 0; q < KQ; q++) {
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    o[i] = (4 * q + i < n) ? lv[4 * q + i] * rv[4 * q + i] : 0.f;
+                    cmax = fmaxf(cmax, o[i]);
+                }
+                *reinterpret_cast<float4 *>(out + q * 32) = make_float4(o[0], o[1], o[2], o[3]);
+            }
+        };
+        auto finish_item = [&]() {
+            int sh = 0;
+            if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale
+                int ex;
+                frexpf(cmax, &ex);
+                sh = 1 - ex;
+                const float mul = __int_as_float((127 + sh) << 23);
+                for (int q = 0; q < C * KQ; q++) {
+                    float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+                    v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                    *reinterpret_cast<float4 *>(row + q * 32) = v;
+                }
+            }
+            P.expo[(long long)it.dad * ld + p] = e_in - sh;
+        };
+        // next item with an internal child; items of two tips are completed on the way
+        auto begin_next = [&]() -> bool {
+            while (j < nitems) {
+                begin_item();
+                if (it.lint || it.rint) return true;
+                for (int cc = 0; cc < C; cc++) epilogue(cc, 0);
+                finish_item();
+                j++;
+            }
+            return false;
+        };
+        // this thread's row of one side into A hi / lo (zero in the K padding)
+        auto put_a = [&](const float4 (&v)[KQ], unsigned col) {
+            float h[KP], l[KP];
+#pragma unroll
+            for (int q = 0; q < KQ; q++) {
+                const float x[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    h[4 * q + i] = tf32_hi(x[i]);
+                    l[4 * q + i] = x[i] - h[4 * q + i];
+                }
+            }
+#pragma unroll
+            for (int k = 4 * KQ; k < KP; k++) h[k] = l[k] = 0.f;
+            const unsigned a = tmem + lane_off + col;
+#pragma unroll
+            for (int t = 0; t < KSTEPS; t++) {
+                tmem_st8(a + 8 * t, &h[8 * t]);
+                tmem_st8(a + KP + 8 * t, &l[8 * t]);
+            }
+        };
+        // one stage: `use` holds its rows; the next stage's rows go to `nxt`
+        auto stage = [&](float4 (&use)[2][KQ], float4 (&nxt)[2][KQ]) -> bool {
+            load(nxt);
+            bool ok = m == 0 || (!*(volatile unsigned *)&abort_flag &&
+                                 mbar_wait(&mdone, (unsigned)((m - 1) & 1), kWaitPolls));
+            if (bar_or_part(kTcRows, !ok)) { abort = true; return false; }
+            tc_fence_after();
+            if (it.lint) put_a(use[0], 128u);
+            if (it.rint) put_a(use[1], 128u + 2 * KP);
+            tmem_st_wait();
+            tc_fence_before();
+            mbar_arrive(&conv);
+            if (c > 0) epilogue(c - 1, (m - 1) & 1);
+            m++;
+            if (c < C - 1) {
+                c++;
+                return true;
+            }
+            ok = !*(volatile unsigned *)&abort_flag && mbar_wait(&mdone, (unsigned)((m - 1) & 1), kWaitPolls);
+            if (bar_or_part(kTcRows, !ok)) { abort = true; return false; }
+            tc_fence_after();
+            epilogue(C - 1, (m - 1) & 1);
+            finish_item();
+            j++;
+            c = 0;
+            return begin_next();
+        };
+
+        load(bufA);
+        if (begin_next()) {
+            for (;;) {
+                if (!stage(bufA, bufB)) break;
+                if (!stage(bufB, bufA)) break;
+            }
+        }
+        if (abort && r == 0) {
+            atomicExch(&abort_flag, 1u);
+            atomicExch(P.status, kStatusTimeout);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kTmCols);
+}
+
 // B operands: per op, child, category and K piece kh: hi and lo of
 // P_c(t)[x][y] for y in piece kh, in [x/8][y'/4][x%8][y'%4] order (y' = y - kh
 // KS), zero outside x < n, y < n.
@@ -828,7 +1164,7 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     const size_t smem = tc_smem_bytes(T, NSTAGE);
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF>;
-    const bool ws = e->level_sync && e->tc_ws;  // warp-specialised level kernel
+    const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
     cudaError_t err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                          : cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -873,10 +1209,16 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
         e->launches++;
         return cuda_fail(cudaGetLastError(), "traverse_tc");
     }
-    // level schedule: a persistent grid of resident CTAs walks each level's (tile, op) pairs
+    // level schedule: a persistent grid of resident CTAs walks each level's (tile, op) pairs;
+    // a level of tip-tip ops only (no contraction) is a store stream on the CUDA cores
     for (int l = 0; l < lt; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
+        if (level_all_tiptip(e, op0, nl)) {
+            rc = launch_tiptip_level(e, M, op0, nl);
+            if (rc) return rc;
+            continue;
+        }
         const long long items = (long long)T.ntiles * nl;
         const int grid = (int)std::min<long long>(items, resident);
         if (ws)
@@ -886,6 +1228,59 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
         e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
+    }
+    return IQGPU_OK;
+}
+
+// Level schedule on k_traverse_tc_tm (20 states, split TF32). Residency: two
+// CTAs per SM by tensor memory (256 columns each), lowered if shared memory or
+// registers allow fewer; the narrow tail goes to the CUDA cores as above.
+static int launch_tc_tm(iqgpu_engine *e, const MixParams &M, int *rest) {
+    const TcParams T = tc_params(e, M, 32, false);
+    const size_t smem = (size_t)kTmNB * 2 * T.b_total + 128;
+    cudaError_t err = cudaFuncSetAttribute(k_traverse_tc_tm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess) err = cudaFuncSetAttribute(k_traverse_tc_tm, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_tm smem attribute");
+    int sms = 1, smem_sm = 0, reserve = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->dev);
+    cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, e->dev);
+    cudaFuncAttributes fa;
+    size_t stat = 0;
+    int regs = 0;
+    if (cudaFuncGetAttributes(&fa, k_traverse_tc_tm) == cudaSuccess) {
+        stat = fa.sharedSizeBytes;
+        regs = fa.numRegs;
+    }
+    const int nthr = kTcRows + 32;
+    const size_t per_cta = smem + stat + (size_t)reserve;
+    int per_sm = (int)std::min<size_t>(512 / kTmCols, per_cta ? (size_t)smem_sm / per_cta : 1);
+    if (regs > 0) {
+        const int per_warp = ((regs * 32 + 255) / 256) * 256;
+        per_sm = std::min(per_sm, 65536 / (per_warp * (nthr / 32)));
+    }
+    if (per_sm < 1) per_sm = 1;
+    const long long resident = (long long)per_sm * sms;
+    // narrow tail: levels with fewer than two items per resident CTA (an item
+    // is a serial chain of ncat stages, so one item per CTA exposes all of it)
+    int lt = e->nlevels;
+    for (int l = 0; l < e->nlevels; l++)
+        if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < 2 * resident) { lt = l; break; }
+    *rest = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
+    for (int l = 0; l < lt; l++) {
+        const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+        if (nl <= 0) continue;
+        if (level_all_tiptip(e, op0, nl)) {
+            const int rc = launch_tiptip_level(e, M, op0, nl);
+            if (rc) return rc;
+            continue;
+        }
+        const long long items = (long long)T.ntiles * nl;
+        const int grid = (int)std::min<long long>(items, resident);
+        k_traverse_tc_tm<<<grid, nthr, smem, e->st>>>(T, op0, nl);
+        e->launches++;
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_tm level");
     }
     return IQGPU_OK;
 }
@@ -921,6 +1316,8 @@ int launch_traverse_tc(iqgpu_engine *e, const MixParams &M, int *rest) {
     if (M.nops <= 0) return IQGPU_OK;
     const int depth = tc_depth(e);
     const bool BF = e->cfg.precision == IQGPU_BF16;
+    if (e->level_sync && e->tc_tm && !BF && e->npad == 4 * kTmKQ && tc_ksplit(e) == 1)
+        return launch_tc_tm(e, M, rest);
     if (tc_np(e->npad) == 64)
         return BF ? launch_tc_depth<64, true>(e, M, depth, rest) : launch_tc_depth<64, false>(e, M, depth, rest);
     return BF ? launch_tc_depth<32, true>(e, M, depth, rest) : launch_tc_depth<32, false>(e, M, depth, rest);

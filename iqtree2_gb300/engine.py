@@ -273,7 +273,8 @@ class Engine:
 
     def set_schedule(self, schedule):
         """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel),
-        3 = level-synchronous on the warp-specialised tensor-core kernel."""
+        3 = level-synchronous on the warp-specialised tensor-core kernel,
+        4 = level-synchronous with operand A in tensor memory (20 states)."""
         _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
 
     def launches(self):

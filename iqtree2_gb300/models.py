@@ -97,6 +97,44 @@ def gamma_rates_mean(alpha, ncat):
     return rates, props
 
 
+def gamma_invar_rates(alpha, p_invar, ncat):
+    """+I+G: rates and proportions of the variable-site categories.
+
+    Restates ``RateGammaInvar`` (model/rategammainvar.cpp:25-42 sets every
+    rate to 1/(1-p_inv) before ``RateGamma::computeRates``, which rescales the
+    discrete-gamma rates to that sum, model/rategamma.cpp:98-141) and its
+    ``getProp`` = (1-p_inv)/ncat (model/rategammainvar.h:69).
+    """
+    rates, _ = gamma_rates_mean(alpha, ncat)
+    return rates / (1.0 - p_invar), np.full(ncat, (1.0 - p_invar) / ncat)
+
+
+def free_rates(rates, props):
+    """+R (FreeRate) categories from given weights and rates: weights
+    normalised to sum 1, rates divided by sum(prop * rate) so the mean rate is
+    1 (the ``RateFree`` constructor, model/ratefree.cpp:38-75)."""
+    r = np.asarray(rates, np.float64)
+    p = np.asarray(props, np.float64)
+    p = p / p.sum()
+    return r / float(p @ r), p
+
+
+def invariant_site_lh(patterns, pi, p_invar, nstates):
+    """Per-pattern +I term (``ptn_invar``): p_inv times the summed frequency of
+    the states every taxon of the pattern allows.
+
+    Restates ``Alignment::computeConst`` (alignment/alignment.cpp:925-1012:
+    the intersection of the taxa's state sets, ``getAppearance``
+    :4769-4800) and ``PhyloTree::computePtnInvar``
+    (tree/phylotreesse.cpp:549-610): a pattern of one state s gives
+    p_inv * pi[s], an all-unknown pattern p_inv, an ambiguous intersection
+    (DNA masks, protein B/Z/J) the sum over its states, an empty one 0.
+    """
+    app = tip_vectors(nstates)[np.asarray(patterns)]  # (taxa, patterns, states): which states each code allows
+    common = np.prod(app, axis=0)
+    return p_invar * (common @ np.asarray(pi, np.float64))
+
+
 def tip_vectors(nstates):
     """Standard-basis tip likelihood per alignment state, rows 0..STATE_UNKNOWN.
 

@@ -9,7 +9,7 @@ import numpy as np
 from scipy.linalg import expm
 
 
-def tree_lnl(model, patterns, freq, edges, lengths, ntaxa, root=None):
+def tree_lnl(model, patterns, freq, edges, lengths, ntaxa, root=None, invar=None):
     nnode = 2 * ntaxa - 2
     adj = [[] for _ in range(nnode)]
     for k, (u, v) in enumerate(edges):
@@ -49,5 +49,7 @@ def tree_lnl(model, patterns, freq, edges, lengths, ntaxa, root=None):
             out[c] *= cp[c] @ P.T
         logs += cl
     lh = np.einsum("cpx,x,c->p", out, model.pi, model.props)
+    if invar is not None:  # +I: the invariant-site term, in the same scaled units
+        lh = lh + np.asarray(invar) * np.exp(-logs)
     plh = np.log(lh) + logs
     return float(plh @ freq), plh

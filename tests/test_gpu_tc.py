@@ -116,6 +116,40 @@ def test_tc_schedules_agree_and_match_cuda_cores(oracle_mod, kind):
     assert rel(cc.compute_likelihood(ops, a, b, length), vals.pop()) < LNL_RTOL
 
 
+def test_tc_level_kernels_protein(oracle_mod):
+    """Protein 100 taxa x 20,000 sites: wide enough that the level schedules
+    launch the tensor-core level kernels (single-issuer, warp-specialised and
+    A-in-tensor-memory) on the wide levels, with tip-tip, tip-internal and
+    internal-internal items mixed in one launch and a ragged last tile. Every
+    candidate within 1e-6 of the FP64 oracle; the shared-memory-operand
+    kernels bit-identical to each other; the A-in-tensor-memory kernel (the
+    MMA reads A through another datapath, which may order the K sum
+    differently) deterministic and within 1e-7 of them."""
+    ds = simulate.protein_lg_dataset(100, 20000, 35)
+    topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    eng = _engine(ds, topo)
+    got, launches = {}, {}
+    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0)]:
+        autotune.apply(eng, cand)
+        l0 = eng.launches()
+        got[cand] = eng.compute_likelihood(ops, a, b, length)
+        launches[cand] = eng.launches() - l0
+        assert rel(got[cand], want) < LNL_RTOL, (cand, got[cand], want)
+    print("lnL", got, "rel err", {k: rel(v, want) for k, v in got.items()}, "launches per evaluation", launches)
+    # the level schedules launch one kernel per wide level on top of the tail
+    assert launches[(0, 4, 0, 0)] > launches[(0, 0, 2, 1)]
+    tm = got.pop((0, 4, 0, 0))
+    assert len(set(got.values())) == 1, got
+    assert rel(tm, got[(0, 0, 2, 1)]) < 1e-7
+    autotune.apply(eng, (0, 4, 0, 0))
+    again = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
+    assert again == [tm] * 3
+
+
 def test_tc_deep_tree_exponents(oracle_mod):
     """200-taxon protein tree with long branches: the per-pattern exponents are
     exercised on the tensor-core path."""

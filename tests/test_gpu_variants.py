@@ -1,0 +1,118 @@
+"""Rate-heterogeneity variants on every path against the FP64 oracle.
+
++I+G4: a per-pattern invariant-site term (``ptn_invar``, built as the
+reference's computePtnInvar does) added to each pattern's likelihood, and in
+the FP64 path no 2^-256 rescaling of a pattern that carries one. +R4
+(FreeRate): unequal category weights and rates.
+
+Tolerances, as for each path: FP64 lnL <= 1e-10 relative and scale counts
+identical; FP32 mixed and split-TF32 lnL <= 1e-6 relative; first and second
+derivatives relative 1e-9 (FP64) or 1e-4 / 1e-3 (mixed) with, on the mixed
+paths, an absolute floor of 1e-5 per site: each pattern's FP32 ratio carries
+~1e-6 of its own size, and those errors add over patterns even where the sum
+itself cancels (near the optimum the derivative is a few units over
+thousands of sites).
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from helpers import rel
+from iqtree2_gb300 import engine, models, simulate
+from iqtree2_gb300.topology import Topology
+
+pytestmark = pytest.mark.gpu
+
+P_INVAR = 0.3
+
+
+def _variant(ds, kind):
+    m = ds.model
+    if kind == "+I+G4":
+        r, p = models.gamma_invar_rates(0.5, P_INVAR, 4)
+        inv = models.invariant_site_lh(ds.patterns, m.pi, P_INVAR, m.nstates)
+    else:  # +R4
+        r, p = models.free_rates([0.05, 0.4, 1.2, 3.5], [0.2, 0.3, 0.35, 0.15])
+        inv = None
+    return dataclasses.replace(m, rates=r, props=p), inv
+
+
+def _dataset(data):
+    return (simulate.dna_gtr_dataset(24, 2000, 61) if data == "dna"
+            else simulate.protein_lg_dataset(16, 800, 62))
+
+
+@pytest.mark.parametrize("kind", ["+I+G4", "+R4"])
+@pytest.mark.parametrize("data,precision", [("dna", engine.F64), ("dna", engine.F32), ("protein", engine.F64),
+                                            ("protein", engine.F32), ("protein", engine.TF32X3)])
+def test_variant_lnl_and_derivatives(oracle_mod, kind, data, precision):
+    ds = _dataset(data)
+    m, inv = _variant(ds, kind)
+    if inv is not None:
+        assert (inv > 0).sum() > 0  # constant patterns carry the +I term
+    tol = 1e-10 if precision == engine.F64 else 1e-6
+    t = engine.GpuTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=precision, invar=inv)
+    o = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)
+    lg, plh = t.compute_likelihood(want_pattern_lh=True)
+    lo, plo = o.compute_likelihood(want_pattern_lh=True)
+    assert rel(lg, lo) < tol, (lg, lo)
+    np.testing.assert_allclose(plh, plo, atol=1e-8 if precision == engine.F64 else 1e-4)
+
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots, precision=precision,
+                        max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq, inv)
+    eng.set_tip_states(ds.patterns)
+    internal = [tuple(map(int, e)) for e in ds.edges if min(e) >= ds.ntaxa]
+    done = set()
+    for (n1, n2) in [tuple(map(int, ds.edges[0]))] + internal[:2]:
+        node, dad = (n2, n1) if n2 >= ds.ntaxa else (n1, n2)
+        ops = topo.ops_for(dad, node, done) + topo.ops_for(node, dad, done)
+        a, b = topo.ref(dad, node), topo.ref(node, dad)
+        o = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)  # derv moves the branch
+        for i, length in enumerate((0.03, 0.4)):
+            df, ddf = eng.likelihood_derv(ops if i == 0 else [], a, b, length, theta_computed=i > 0)
+            odf, oddf = o.derv(n1, n2, length)
+            if precision == engine.F64:
+                assert abs(df - odf) <= 1e-9 * abs(odf) + 1e-9
+                assert abs(ddf - oddf) <= 1e-9 * abs(oddf) + 1e-9
+            else:
+                floor = 1e-5 * float(ds.freq.sum())
+                assert abs(df - odf) <= 1e-4 * abs(odf) + floor, (df, odf)
+                assert abs(ddf - oddf) <= 1e-3 * abs(oddf) + floor, (ddf, oddf)
+
+
+@pytest.mark.parametrize("safe", [False, True])
+def test_invar_scaling_counts_identical(oracle_mod, safe):
+    """300-taxon long-branch DNA under +I+G4: patterns underflow 2^-256, and a
+    pattern with an invariant-site term is never rescaled (the reference's
+    condition lh_max < 2^-256 && ptn_invar == 0)."""
+    ds = simulate.dna_gtr_dataset(300, 300, 5, mean_bl=0.5)
+    m, inv = _variant(ds, "+I+G4")
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots, safe=safe,
+                        max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq, inv)
+    eng.set_tip_states(ds.patterns)
+    nb = topo.adj[0][0][0]
+    ops = topo.branch_ops(nb, 0)
+    lg = eng.compute_likelihood(ops, topo.ref(0, nb), topo.ref(nb, 0), topo.edge_len(0, nb))
+    orc = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe, invar=inv)
+    _, s_or = orc.partial(0, nb)
+    assert s_or.max() >= 1
+    _, s_gpu = eng.partial(topo.ref(0, nb))
+    np.testing.assert_array_equal(s_gpu, s_or)
+    assert rel(lg, orc.lnl_branch(nb, 0)) < 1e-10
+
+
+def test_invar_optimize_all_branches(oracle_mod):
+    ds = _dataset("dna")
+    m, inv = _variant(ds, "+I+G4")
+    t = engine.GpuTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)
+    o = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)
+    lg, lo = t.optimize_all_branches(), o.optimize_all_branches()
+    assert rel(lg, lo) < 1e-10
+    np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-5)

@@ -107,3 +107,41 @@ def test_exact_derivative_matches_finite_difference_and_reference_quirk(oracle_m
     b = oracle_mod.OracleTree(d.model, d.patterns, d.freq, d.edges, d.lengths,
                               ref_triple_tail=True).derv(*map(int, d.edges[0]), 0.05)
     assert a == b
+
+
+def test_invariant_site_terms():
+    """+I term per pattern (computePtnInvar): constant state s -> p*pi[s];
+    all unknown -> p; a DNA ambiguity shared by every taxon -> p * sum of its
+    states; a variable pattern -> 0."""
+    from iqtree2_gb300 import models
+    pi = np.array([0.1, 0.2, 0.3, 0.4])
+    su = models.STATE_UNKNOWN[4]
+    R = 5 + 3  # DNA code of the mask A|G (bits 0 and 2): state = mask + 3
+    pats = np.array([[2, su, 0, 2, R],
+                     [2, su, 1, su, 0],
+                     [2, su, 0, 2, 2]], dtype=np.uint8)
+    got = models.invariant_site_lh(pats, pi, 0.25, 4)
+    np.testing.assert_allclose(got, [0.25 * 0.3, 0.25, 0.0, 0.25 * 0.3, 0.0])
+    pats2 = np.array([[R], [R], [su]], dtype=np.uint8)
+    np.testing.assert_allclose(models.invariant_site_lh(pats2, pi, 0.25, 4), [0.25 * (0.1 + 0.3)])
+
+
+@pytest.mark.parametrize("kind", ["+I+G4", "+R4"])
+def test_rate_variants_match_standard_basis(oracle_mod, kind):
+    """Oracle under +I+G4 and +R4 against the independent numpy pruning."""
+    import dataclasses
+    from iqtree2_gb300 import models, simulate
+    ds = simulate.dna_gtr_dataset(10, 300, 71)
+    if kind == "+I+G4":
+        r, p = models.gamma_invar_rates(0.7, 0.2, 4)
+        inv = models.invariant_site_lh(ds.patterns, ds.model.pi, 0.2, 4)
+        np.testing.assert_allclose(p.sum(), 0.8)
+        np.testing.assert_allclose(p @ r, 1.0)  # variable sites carry the whole mean rate
+    else:
+        r, p = models.free_rates([0.1, 0.5, 1.5, 4.0], [1, 2, 2, 1])
+        inv = None
+        np.testing.assert_allclose(p @ r, 1.0)
+    m = dataclasses.replace(ds.model, rates=r, props=p)
+    o = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)
+    want, _ = stdbasis.tree_lnl(m, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa, invar=inv)
+    assert rel(o.compute_likelihood(), want) < 1e-12
