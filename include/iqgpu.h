@@ -149,8 +149,22 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
                           double len, int32_t theta_computed, double *df, double *ddf);
 /* computeLikelihoodFromBufferPointer (tree/phylokernelnew.h:3232-3428). */
 int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl);
-/* Per-pattern lnL of the last branch/from-buffer evaluation (_pattern_lh). */
+/* Per-pattern lnL of the last branch/from-buffer evaluation (_pattern_lh);
+ * with +ASC the observed patterns carry the correction term. */
 int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
+/* +ASC (Lewis ascertainment bias correction, ASC_VARIANT): the last `nconst`
+ * patterns of the engine are the unobserved constant patterns IQ-TREE appends
+ * with weight 0 (one per state whose taxa all show it and that the alignment
+ * lacks: Alignment::getUnobservedConstPatterns, alignment/alignment.cpp:
+ * 4140-4156). With P_const the sum of their likelihoods, every lnL entry point
+ * returns lnL - nsite * log(1 - P_const) and the observed patterns' lnL drop
+ * by log(1 - P_const) (tree/phylokernelnew.h:3198-3222, 3405-3420); the
+ * derivative adds nsite * (d1/(1-P)) and nsite * (d2/(1-P) + (d1/(1-P))^2)
+ * with d1, d2 the constant patterns' summed derivatives (:2620-2628).
+ * nconst = 0 switches it off. The batched NNI, group and on-device RELL entry
+ * points refuse +ASC engines (IQGPU_ERR_ARG); iqgpu_rell takes the corrected
+ * pattern lnL from iqgpu_get_pattern_lh. */
+int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
 /* Copy a slot back in the reference layout: partial[ptn*B + c*n + x] in eigen
  * space (F64) or standard basis (mixed), and scale counts (NORM: nptn bytes,
  * SAFE: nptn*ncat bytes, pattern-major). Either output may be NULL. */

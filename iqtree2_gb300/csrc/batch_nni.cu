@@ -343,6 +343,10 @@ extern "C" int iqgpu_nni_batch(iqgpu_engine *e, const iqgpu_nni_candidate *cand,
         set_error("bad argument");
         return IQGPU_ERR_ARG;
     }
+    if (e->asc_n > 0) {
+        set_error("+ASC engines: evaluate NNI candidates with the per-branch entry points");
+        return IQGPU_ERR_ARG;
+    }
     iqgpu_config cfg;
     iqgpu_get_config(e, &cfg);
     if (cfg.precision == IQGPU_F64) {

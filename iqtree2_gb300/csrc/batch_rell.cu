@@ -210,6 +210,10 @@ extern "C" int iqgpu_rell_current(iqgpu_engine *e, double *out) {
         set_error("bad argument");
         return IQGPU_ERR_ARG;
     }
+    if (e->asc_n > 0) {
+        set_error("+ASC engines: pass iqgpu_get_pattern_lh's corrected values to iqgpu_rell");
+        return IQGPU_ERR_ARG;
+    }
     std::lock_guard<std::mutex> lock(g_rell_mu);
     auto it = g_rell.find(e);
     if (it == g_rell.end() || !it->second.w) {

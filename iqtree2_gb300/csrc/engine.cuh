@@ -92,6 +92,12 @@ struct iqgpu_engine {
     double *d_red_partials;
     unsigned *d_ticket;
     double *d_red_out, *h_red_out;
+    // +ASC (Lewis): the last asc_n patterns are the unobserved constant
+    // patterns; d_asc/h_asc hold their (lh, df, ddf) from the derivative
+    // kernels, asc_lc the log(1 - P_const) of the latest lnL
+    int asc_n;
+    double asc_nsite, asc_lc;
+    double *d_asc, *h_asc;
     bool theta_valid;
     int32_t theta_a, theta_b;
     // mixed-precision (FP32 standard-basis) state

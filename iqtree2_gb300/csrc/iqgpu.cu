@@ -85,6 +85,7 @@ static Sizes sizes(const iqgpu_config *c) {
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
     s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + 2 * s.Ppad * 8 +
+              3 * kMaxStates * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
     return s;
 }
@@ -288,8 +289,10 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
     e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
     CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
+    CKE(dalloc(e, &e->d_asc, 3 * kMaxStates * 8));
     CKE(halloc(e, &e->h_ops, s.ops));
     CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
+    CKE(halloc(e, &e->h_asc, 3 * kMaxStates * 8));
     CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
     CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
     CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
@@ -562,6 +565,25 @@ int iqgpu_compute_partials(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
     return traverse(e, nops, EPI_NONE, 0, 0, 0.0);
 }
 
+// +ASC (Lewis) on a tree lnL whose per-pattern lnL is in d_plh: P_const =
+// sum of the unobserved constant patterns' likelihoods (exp of their pattern
+// lnL, which carries their scaling), lnL -= nsite * log(1 - P_const)
+// (tree/phylokernelnew.h:3198-3222 and 3405-3420).
+static int asc_lnl(iqgpu_engine *e, double *lnl) {
+    if (e->asc_n <= 0) return IQGPU_OK;
+    CK(cudaMemcpyAsync(e->h_asc, e->d_plh + (e->P - e->asc_n), (size_t)e->asc_n * 8, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    double pc = 0.0;
+    for (int i = 0; i < e->asc_n; i++) pc += std::exp(e->h_asc[i]);
+    if (!(pc < 1.0 && pc >= 0.0)) {
+        set_error("+ASC: the unobserved constant patterns' probability is outside [0, 1)");
+        return IQGPU_ERR_NONFINITE;
+    }
+    e->asc_lc = std::log(1.0 - pc);
+    *lnl -= e->asc_nsite * e->asc_lc;
+    return IQGPU_OK;
+}
+
 static int lnl_common(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b, double len,
                       double *lnl) {
     int rc = ready(e);
@@ -578,7 +600,7 @@ static int lnl_common(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_
     if ((rc = fetch_result(e))) return rc;
     const double *r = e->h_red_out;
     *lnl = std::isfinite(r[0]) ? r[0] : r[1];
-    return IQGPU_OK;
+    return asc_lnl(e, lnl);
 }
 
 int iqgpu_branch_lnl(iqgpu_engine *e, int32_t a, int32_t b, double len, double *lnl) {
@@ -617,13 +639,24 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
     if ((rc = fetch_result(e))) return rc;
     *df = e->h_red_out[0];
     *ddf = e->h_red_out[1];
-    if (!std::isfinite(*df)) {
-        if (!e->cfg.safe && !is_mixed(&e->cfg)) {
-            set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this");
-            return IQGPU_ERR_NONFINITE;
-        }
-        *df = *ddf = 0.0;
+    if (!std::isfinite(*df) && !e->cfg.safe && !is_mixed(&e->cfg)) {
+        set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this");
+        return IQGPU_ERR_NONFINITE;
     }
+    if (e->asc_n > 0) {  // Lewis +ASC (tree/phylokernelnew.h:2620-2628)
+        CK(cudaMemcpyAsync(e->h_asc, e->d_asc, (size_t)e->asc_n * 24, cudaMemcpyDeviceToHost, e->st));
+        CK(cudaStreamSynchronize(e->st));
+        double lh = 0.0, d1 = 0.0, d2 = 0.0;
+        for (int i = 0; i < e->asc_n; i++) {
+            lh += e->h_asc[3 * i];
+            d1 += e->h_asc[3 * i + 1];
+            d2 += e->h_asc[3 * i + 2];
+        }
+        const double pv = 1.0 - lh, df_frac = d1 / pv, ddf_frac = d2 / pv;
+        *df += e->asc_nsite * df_frac;
+        *ddf += e->asc_nsite * (ddf_frac + df_frac * df_frac);
+    }
+    if (!std::isfinite(*df)) *df = *ddf = 0.0;
     return IQGPU_OK;
 }
 
@@ -642,7 +675,7 @@ int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
         return IQGPU_ERR_NONFINITE;
     }
     *lnl = std::isfinite(r[0]) ? r[0] : r[1];
-    return IQGPU_OK;
+    return asc_lnl(e, lnl);
 }
 
 int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out) {
@@ -650,6 +683,19 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out) {
     CK(cudaSetDevice(e->dev));
     CK(cudaMemcpyAsync(out, e->d_plh, (size_t)e->P * 8, cudaMemcpyDeviceToHost, e->st));
     CK(cudaStreamSynchronize(e->st));
+    if (e->asc_n > 0)  // the observed patterns' lnL carry the +ASC term of the latest lnL
+        for (long long p = 0; p < e->P - e->asc_n; p++) out[p] -= e->asc_lc;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite) {
+    if (!e || nconst < 0 || nconst > e->n || nconst >= e->P || !(nsite >= 0.0)) {
+        set_error("+ASC: need 0 <= nconst <= nstates, nconst < patterns and nsite >= 0");
+        return IQGPU_ERR_ARG;
+    }
+    e->asc_n = nconst;
+    e->asc_nsite = nsite;
+    e->asc_lc = 0.0;
     return IQGPU_OK;
 }
 

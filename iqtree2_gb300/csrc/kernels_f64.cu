@@ -372,6 +372,8 @@ struct BufParams {
     double len;
     double *pattern_lh;
     Reduce red;
+    int asc_first;    // +ASC: patterns from here on are the unobserved constant ones (nptn: none)
+    double *asc_out;  // their (lh, df, ddf), unscaled once as the reference does
 };
 
 // (tree/phylokernelnew.h:2233-2633): df = sum freq*d1/lh, ddf = sum freq*(d2/lh - (d1/lh)^2)
@@ -409,6 +411,13 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
         }
         double lh = a0 + b0, d1 = a1 + b1, d2 = a2 + b2;
         lh = fabs(lh) + P.invar[p];
+        if (p >= P.asc_first) {  // +ASC constant pattern (tree/phylokernelnew.h:2506-2546); weight 0 below
+            const double u = P.buffer_scale[p] != 0.0 ? kScaleThreshold : 1.0;
+            double *o = P.asc_out + 3 * (p - P.asc_first);
+            o[0] = lh * u;
+            o[1] = d1 * u;
+            o[2] = d2 * u;
+        }
         const double inv = 1.0 / lh;
         const double df_frac = d1 * inv, ddf_frac = d2 * inv;
         const double f = P.freq[p];
@@ -558,6 +567,8 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
     P.red.partials = e->d_red_partials;
     P.red.ticket = e->d_ticket;
     P.red.out = e->d_red_out;
+    P.asc_first = (int)(e->P - e->asc_n);
+    P.asc_out = e->d_asc;
     return P;
 }
 

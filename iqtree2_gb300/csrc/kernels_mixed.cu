@@ -176,6 +176,13 @@ __global__ void __launch_bounds__(kTPB) k_derv_mixed(const MixBufParams P) {
         }
         // the +I term is in true scale: bring it to the stored scale
         const double lh = fabs(a0) + P.invar[p] * exp(-P.buffer_scale[p]);
+        if (p >= P.asc_first) {  // +ASC constant pattern, in true scale (weight 0 below)
+            const double u = exp(P.buffer_scale[p]);
+            double *o = P.asc_out + 3 * (p - P.asc_first);
+            o[0] = lh * u;
+            o[1] = a1 * u;
+            o[2] = a2 * u;
+        }
         const double inv = 1.0 / lh;
         const double df_frac = a1 * inv, ddf_frac = a2 * inv;
         const double f = P.freq[p];
@@ -291,6 +298,8 @@ static MixBufParams mixbuf_params(iqgpu_engine *e, double len) {
     P.red.partials = e->d_red_partials;
     P.red.ticket = e->d_ticket;
     P.red.out = e->d_red_out;
+    P.asc_first = (int)(e->P - e->asc_n);
+    P.asc_out = e->d_asc;
     return P;
 }
 

@@ -93,6 +93,8 @@ struct MixBufParams {
     double len;
     double *pattern_lh;
     Reduce red;
+    int asc_first;    // +ASC: patterns from here on are the unobserved constant ones (nptn: none)
+    double *asc_out;  // their (lh, df, ddf) in true scale
 };
 
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }

@@ -22,7 +22,7 @@ constexpr int kDnaTile = 128;  // patterns (= threads) per CTA
 constexpr int kDnaMaxCat = 4;  // register-resident categories (ncat <= 4 uses this kernel)
 
 template <int EPI>
-__global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
+__global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P) {
     constexpr int n = 4, npad = 4;
     const int C = P.ncat, S = P.state_unknown;
     const long long p = (long long)blockIdx.x * kDnaTile + threadIdx.x;
@@ -45,6 +45,26 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
     }
     __syncthreads();
 
+    // The previous op's output for this pattern stays in registers (as
+    // stored), and one internal child of the next op that it does not produce
+    // is requested one op ahead: along a chain of ops (each taking the
+    // previous op's output as one child, as the one-op levels near the root
+    // do) every child is then in flight or in registers when its op starts.
+    int prev_dad = -1, prev_e = 0, nx_ref = -1, nx_e = 0;
+    float4 prev[kDnaMaxCat], nx[kDnaMaxCat];
+    auto request = [&](int k, int skip) {
+        const OpDev o = P.ops[k];
+        const int r0 = o.child[0], r1 = o.child[1];
+        nx_ref = (r0 >= 0 && r0 != skip) ? r0 : ((r1 >= 0 && r1 != skip) ? r1 : -1);
+        if (nx_ref < 0) return;
+        const float *src = P.part + (long long)nx_ref * P.slot_floats + pbase;
+#pragma unroll
+        for (int c = 0; c < kDnaMaxCat; c++)
+            if (c < C) nx[c] = *reinterpret_cast<const float4 *>(src + c * 32);
+        nx_e = P.expo[(long long)nx_ref * ld + p];
+    };
+    if (P.nops > 0) request(0, -1);
+
     for (int k = 0; k < P.nops; ++k) {
         const int buf = k & 1;
         const bool lost = !mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
@@ -64,26 +84,50 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
         int lref = op.child[0], rref = op.child[1];
         const float *gbase = P.opmats + (long long)k * P.op_stride;
         const float *PL = sP[buf], *PR = sP[buf] + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
-        if (lref >= 0 && rref < 0) {
+        const bool sw = lref >= 0 && rref < 0;  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+        if (sw) {
             int t = lref; lref = rref; rref = t;
             const float *q = PL; PL = PR; PR = q;
             q = TL; TL = TR; TR = q;
         }
         const bool lint = lref >= 0, rint = rref >= 0;
-        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
-        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
         const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
         const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
         float4 out[kDnaMaxCat];
         float mx = 0.f;
-        // issue every load of the op first: ncat float4 per child
+        // an internal side comes from registers (previous output or the
+        // requested child) or, when the op's children are both internal and
+        // neither chains, is loaded here
         float4 lv[kDnaMaxCat], rv[kDnaMaxCat];
+        int e = 0;
+        auto side = [&](int ref, float4 (&v)[kDnaMaxCat]) {
+            if (ref == prev_dad) {
 #pragma unroll
-        for (int c = 0; c < kDnaMaxCat; c++) {
-            if (c < C) {
-                lv[c] = lint ? *reinterpret_cast<const float4 *>(Lp + c * 32) : ld4(tl + c * npad);
-                rv[c] = rint ? *reinterpret_cast<const float4 *>(Rp + c * 32) : ld4(tr + c * npad);
+                for (int c = 0; c < kDnaMaxCat; c++) v[c] = prev[c];
+                e += prev_e;
+            } else if (ref == nx_ref) {
+#pragma unroll
+                for (int c = 0; c < kDnaMaxCat; c++) v[c] = nx[c];
+                e += nx_e;
+            } else {
+                const float *src = P.part + (long long)ref * P.slot_floats + pbase;
+#pragma unroll
+                for (int c = 0; c < kDnaMaxCat; c++)
+                    if (c < C) v[c] = *reinterpret_cast<const float4 *>(src + c * 32);
+                e += P.expo[(long long)ref * ld + p];
             }
+        };
+        if (lint) {
+            side(lref, lv);
+        } else {
+#pragma unroll
+            for (int c = 0; c < kDnaMaxCat; c++) if (c < C) lv[c] = ld4(tl + c * npad);
+        }
+        if (rint) {
+            side(rref, rv);
+        } else {
+#pragma unroll
+            for (int c = 0; c < kDnaMaxCat; c++) if (c < C) rv[c] = ld4(tr + c * npad);
         }
 #pragma unroll
         for (int c = 0; c < kDnaMaxCat; c++) {
@@ -109,6 +153,7 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
                 mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
             }
         }
+        if (k + 1 < P.nops) request(k + 1, op.dad_slot);  // in flight across the stores and the next barrier
         int sh = 0;
         float mul = 1.f;
         if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
@@ -124,10 +169,12 @@ __global__ void __launch_bounds__(kDnaTile) k_traverse_dna(const MixParams P) {
                 float4 v = out[c];
                 v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
                 *reinterpret_cast<float4 *>(dad + c * 32) = v;
+                prev[c] = v;
             }
         }
-        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
         P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+        prev_dad = op.dad_slot;
+        prev_e = e - sh;
     }
 
     if constexpr (EPI == EPI_NONE) return;
@@ -372,6 +419,11 @@ static int launch_levels_dna_t(iqgpu_engine *e, MixParams P, int epi) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
         if ((long long)nl * grid < wave) break;
+        if (level_all_tiptip(e, op0, nl)) {  // a store stream: several patterns per thread
+            const int rc = launch_tiptip_level(e, P, op0, nl);
+            if (rc) return rc;
+            continue;
+        }
         for (int c0 = 0; c0 < nl; c0 += kLevelOps) {  // levels wider than one parameter block: several launches
             const int cnt = std::min(kLevelOps, nl - c0);
             LevelOps L;

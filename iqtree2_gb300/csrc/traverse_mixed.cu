@@ -185,16 +185,35 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
     const bool btip = P.b < 0;
     const float *pb = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pbase;
     const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+    // this thread's chunks of a and b, read once (NQ > 0: registers)
+    constexpr int RQ = NQ ? NQ : 1;
+    float4 a4[RQ], b4[RQ];
+    if constexpr (NQ > 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            a4[q] = *reinterpret_cast<const float4 *>(pa + q * 32);
+            b4[q] = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + q * 32);
+        }
+    }
+    auto achunk = [&](int q) -> float4 {
+        if constexpr (NQ > 0) return a4[q];
+        else return *reinterpret_cast<const float4 *>(pa + q * 32);
+    };
+    auto bchunk = [&](int q) -> float4 {
+        if constexpr (NQ > 0) return b4[q];
+        else return *reinterpret_cast<const float4 *>(pb + q * 32);
+    };
     if constexpr (EPI == EPI_THETA) {
         // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i in eigen space (tree/phylokernelnew.h:2048-2231)
         float *th = P.theta + p;
         for (int i = 0; i < n; i++) {
             const float *urow = P.inv32 + (long long)i * npad;
             float ua = 0.f, ub = 0.f;
+#pragma unroll
             for (int q = 0; q < nq; q++) {
                 const float4 u = ld4(urow + 4 * q);
-                ua = dot4(u, *reinterpret_cast<const float4 *>(pa + q * 32), ua);
-                if (!btip) ub = dot4(u, *reinterpret_cast<const float4 *>(pb + q * 32), ub);
+                ua = dot4(u, achunk(q), ua);
+                if (!btip) ub = dot4(u, bchunk(q), ub);
             }
             if (btip) ub = (float)__ldg(P.tip_lh + (long long)sb * n + i);
             th[(long long)(c * n + i) * ld] = ua * ub;
@@ -208,18 +227,29 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
         // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
         const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
         float lc = 0.f;
-        for (int x = 0; x < n; x++) {
+        auto term = [&](int x, float av) {
             float w;
             if (btip) {
                 w = __ldg(base + 2 * PM + (long long)sb * C * npad + c * npad + x);
             } else {
                 const float *prow = base + (long long)(c * n + x) * npad;
                 float s0 = 0.f;
-                for (int q = 0; q < nq; q++) s0 = dot4(ld4(prow + 4 * q), *reinterpret_cast<const float4 *>(pb + q * 32), s0);
+#pragma unroll
+                for (int q = 0; q < nq; q++) s0 = dot4(ld4(prow + 4 * q), bchunk(q), s0);
                 w = s0;
             }
-            const float av = pa[(x >> 2) * 32 + (x & 3)];
             lc = fmaf((float)__ldg(P.pi + x) * av, w, lc);
+        };
+        if constexpr (NQ > 0) {  // x in order, a from the register chunks
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const float av[4] = {a4[q].x, a4[q].y, a4[q].z, a4[q].w};
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (4 * q + j < n) term(4 * q + j, av[j]);
+            }
+        } else {
+            for (int x = 0; x < n; x++) term(x, pa[(x >> 2) * 32 + (x & 3)]);
         }
         s_lc[threadIdx.x] = lc;
         __syncthreads();
@@ -339,51 +369,57 @@ __global__ void __launch_bounds__(512) k_level_mixed(const MixParams P, const in
 // Tip-tip ops of one level (both children tips: the first level of every
 // traversal). Each output entry is the product of two leaf-table entries
 // (P_c(t) times the tip vector, computed per op by the precompute), so the op
-// is a pure store stream: one thread per pattern with all its categories,
-// grid (128-pattern blocks, ops of the level), full occupancy. The products,
-// the zero padding, the running maximum and the power-of-two rescale are
-// those of the tip-tip case of every other mixed kernel, so the partials are
-// bit-identical (tree/phylokernelnew.h:1632-1747 computes this case from the
-// same lookup tables).
+// is a pure store stream: a thread takes PPT patterns 128 apart (one for 16+
+// states; four for 4-state models, which write only 16 floats per pattern)
+// with all their categories, grid (128 PPT-pattern blocks, ops of the level),
+// full occupancy. The products, the zero padding, the running maximum and the
+// power-of-two rescale are those of the tip-tip case of every other mixed
+// kernel, so the partials are bit-identical (tree/phylokernelnew.h:1632-1747
+// computes this case from the same lookup tables).
+template <int PPT>
 __global__ void __launch_bounds__(128) k_tiptip_level(const MixParams P, const int op0) {
     const int C = P.ncat, n = P.n, npad = P.npad, kq = npad >> 2;
     const long long ld = P.ldp;
-    const long long p = (long long)blockIdx.x * 128 + threadIdx.x;
     const int k = op0 + blockIdx.y;
     const OpDev op = P.ops[k];
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(P.state_unknown + 1) * C * npad;
     const float *T0 = P.opmats + (long long)k * P.op_stride + 2 * PM;
-    const float *tl = T0 + (long long)P.states[(long long)(-1 - op.child[0]) * ld + p] * C * npad;
-    const float *tr = T0 + TB + (long long)P.states[(long long)(-1 - op.child[1]) * ld + p] * C * npad;
-    float *row = P.part + (long long)op.dad_slot * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
-    float cmax = 0.f;
-    for (int c = 0; c < C; c++) {
-        for (int q = 0; q < kq; q++) {
-            const float4 a = ld4(tl + c * npad + 4 * q), b = ld4(tr + c * npad + 4 * q);
-            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-            float o[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                o[i] = (4 * q + i < n) ? av[i] * bv[i] : 0.f;
-                cmax = fmaxf(cmax, o[i]);
+    for (int j = 0; j < PPT; j++) {
+        const long long p = ((long long)blockIdx.x * PPT + j) * 128 + threadIdx.x;
+        if (p >= ld) break;  // whole 128-pattern blocks: uniform per warp
+        const float *tl = T0 + (long long)P.states[(long long)(-1 - op.child[0]) * ld + p] * C * npad;
+        const float *tr = T0 + TB + (long long)P.states[(long long)(-1 - op.child[1]) * ld + p] * C * npad;
+        float *row = P.part + (long long)op.dad_slot * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+        float cmax = 0.f;
+        for (int c = 0; c < C; c++) {
+            for (int q = 0; q < kq; q++) {
+                const float4 a = ld4(tl + c * npad + 4 * q), b = ld4(tr + c * npad + 4 * q);
+                const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    o[i] = (4 * q + i < n) ? av[i] * bv[i] : 0.f;
+                    cmax = fmaxf(cmax, o[i]);
+                }
+                *reinterpret_cast<float4 *>(row + (c * kq + q) * 32) = make_float4(o[0], o[1], o[2], o[3]);
             }
-            *reinterpret_cast<float4 *>(row + (c * kq + q) * 32) = make_float4(o[0], o[1], o[2], o[3]);
         }
-    }
-    int sh = 0;
-    if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale (rare: re-reads its own stores)
-        int ex;
-        frexpf(cmax, &ex);
-        sh = 1 - ex;
-        const float mul = __int_as_float((127 + sh) << 23);
-        for (int q = 0; q < C * kq; q++) {
-            float4 v = *reinterpret_cast<float4 *>(row + q * 32);
-            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-            *reinterpret_cast<float4 *>(row + q * 32) = v;
+        int sh = 0;
+        if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale (rare: re-reads its own stores)
+            int ex;
+            frexpf(cmax, &ex);
+            sh = 1 - ex;
+            const float mul = __int_as_float((127 + sh) << 23);
+            for (int q = 0; q < C * kq; q++) {
+                float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(row + q * 32) = v;
+            }
         }
+        P.expo[(long long)op.dad_slot * ld + p] = -sh;
     }
-    P.expo[(long long)op.dad_slot * ld + p] = -sh;
 }
 
 bool level_all_tiptip(const iqgpu_engine *e, int op0, int nl) {
@@ -395,7 +431,10 @@ bool level_all_tiptip(const iqgpu_engine *e, int op0, int nl) {
 int launch_tiptip_level(iqgpu_engine *e, const MixParams &P, int op0, int nl) {
     for (int c0 = 0; c0 < nl; c0 += 65535) {
         const int cnt = std::min(65535, nl - c0);
-        k_tiptip_level<<<dim3((unsigned)(e->Ppad / 128), cnt), 128, 0, e->st>>>(P, op0 + c0);
+        if (e->npad == 4)
+            k_tiptip_level<4><<<dim3((unsigned)((e->Ppad + 511) / 512), cnt), 128, 0, e->st>>>(P, op0 + c0);
+        else
+            k_tiptip_level<1><<<dim3((unsigned)(e->Ppad / 128), cnt), 128, 0, e->st>>>(P, op0 + c0);
         e->launches++;
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "tiptip_level");
@@ -428,8 +467,9 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     return cuda_fail(cudaGetLastError(), "traverse_mixed");
 }
 
+// Levels l0 .. of the uploaded list, one launch each.
 template <int NQ>
-static int launch_levels_t(iqgpu_engine *e, const MixParams &P) {
+static int launch_levels_t(iqgpu_engine *e, const MixParams &P, int l0 = 0) {
     const int TP = mix_tile(e);
     const int grid = (int)(e->Ppad / TP);
     const size_t smem = (size_t)2 * e->C * e->n * e->npad * 4;
@@ -438,7 +478,7 @@ static int launch_levels_t(iqgpu_engine *e, const MixParams &P) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "level_mixed smem attribute");
     }
-    for (int l = 0; l < e->nlevels; l++) {
+    for (int l = l0; l < e->nlevels; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
         if (level_all_tiptip(e, op0, nl)) {

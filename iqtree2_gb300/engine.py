@@ -94,6 +94,7 @@ def lib():
         "iqgpu_get_timing": ([vp, _DP, ct.POINTER(ct.c_int64)], ct.c_int),
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_set_asc": ([vp, ct.c_int32, ct.c_double], ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
         "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
@@ -198,6 +199,12 @@ class Engine:
         f = np.ascontiguousarray(freq, np.float64)
         iv = None if invar is None else _dp(np.ascontiguousarray(invar, np.float64))
         _check(lib().iqgpu_set_patterns(self.h, _dp(f), iv))
+
+    def set_asc(self, nconst, nsite):
+        """+ASC (Lewis): the last ``nconst`` patterns are the unobserved constant
+        patterns (``models.asc_lewis_patterns``); lnL and derivatives are
+        corrected with ``nsite`` sites. 0 switches it off."""
+        _check(lib().iqgpu_set_asc(self.h, int(nconst), float(nsite)))
 
     def set_tip_states(self, patterns):
         s = np.ascontiguousarray(patterns, np.uint8)
@@ -373,7 +380,9 @@ class GpuTree:
     """PhyloTree drivers on the GPU engine (one engine per tree)."""
 
     def __init__(self, model, patterns, freq, edges, lengths, safe=False, precision=F64, device=0, invar=None,
-                 flags=0):
+                 flags=0, asc=None):
+        """asc=(nconst, nsite): +ASC (Lewis) with the last nconst patterns as
+        the unobserved constant patterns (``models.asc_lewis_patterns``)."""
         ntaxa = patterns.shape[0]
         self.ntaxa = ntaxa
         self.nedge = 2 * ntaxa - 3
@@ -383,6 +392,8 @@ class GpuTree:
         self.engine.set_model(model)
         self.engine.set_patterns(freq, invar)
         self.engine.set_tip_states(patterns)
+        if asc:
+            self.engine.set_asc(*asc)
         self.edges = np.ascontiguousarray(edges, np.int32)
         h = ct.c_void_p()
         _check(lib().iqgpu_tree_create(self.engine.h, self.edges.ctypes.data_as(_I32P),

@@ -135,6 +135,33 @@ def invariant_site_lh(patterns, pi, p_invar, nstates):
     return p_invar * (common @ np.asarray(pi, np.float64))
 
 
+def variable_patterns(patterns, freq, nstates):
+    """The patterns +ASC accepts: drops every pattern whose taxa share an
+    allowed state (``is_invariant`` of alignment/alignment.cpp:1017-1019; the
+    reference refuses +ASC on an alignment that has any,
+    model/modelfactory.cpp:686-704)."""
+    app = tip_vectors(nstates)[np.asarray(patterns)]
+    keep = np.prod(app, axis=0).sum(axis=1) == 0
+    return np.ascontiguousarray(np.asarray(patterns)[:, keep]), np.ascontiguousarray(np.asarray(freq)[keep])
+
+
+def asc_lewis_patterns(patterns, freq, nstates, pi=None):
+    """Appends +ASC's unobserved constant patterns: for every state s (with
+    frequency >= 1e-8), the pattern of all taxa in s unless it is observed
+    (``Alignment::getUnobservedConstPatterns`` ASC_VARIANT,
+    alignment/alignment.cpp:4143-4156; rare states dropped as in
+    model/modelfactory.cpp:679-682), with weight 0. Returns (patterns, freq,
+    nconst, nsite) for ``Engine.set_asc`` and the oracle."""
+    pats = np.asarray(patterns)
+    seen = {tuple(col) for col in pats.T}
+    extra = [s for s in range(nstates)
+             if (pi is None or pi[s] >= 1e-8) and tuple([s] * pats.shape[0]) not in seen]
+    cols = np.array([[s] * pats.shape[0] for s in extra], dtype=pats.dtype).T.reshape(pats.shape[0], len(extra))
+    out = np.ascontiguousarray(np.concatenate([pats, cols], axis=1))
+    f = np.concatenate([np.asarray(freq, np.float64), np.zeros(len(extra))])
+    return out, f, len(extra), float(np.asarray(freq).sum())
+
+
 def tip_vectors(nstates):
     """Standard-basis tip likelihood per alignment state, rows 0..STATE_UNKNOWN.
 

@@ -31,7 +31,7 @@ def lib():
         L.orc_branch_lnl.argtypes = [ct.c_void_p, dp, u8p, ct.c_int, ct.c_int, ct.c_double, dp, ct.c_int]
         L.orc_branch_lnl.restype = ct.c_double
         L.orc_compute_theta.argtypes = [ct.c_void_p, dp, u8p, ct.c_int, ct.c_int, dp, dp, ct.c_int]
-        L.orc_derv.argtypes = [ct.c_void_p, dp, ct.c_double, dp, dp, ct.c_int]
+        L.orc_derv.argtypes = [ct.c_void_p, dp, dp, ct.c_double, dp, dp, ct.c_int]
         L.orc_lnl_from_buffer.argtypes = [ct.c_void_p, dp, dp, ct.c_double, dp, ct.c_int]
         L.orc_lnl_from_buffer.restype = ct.c_double
         L.orc_tree_new.argtypes = [ct.c_void_p, ip, dp, ct.c_int]
@@ -61,7 +61,7 @@ class _Model(ct.Structure):
                 ("eval", ct.c_void_p), ("evec", ct.c_void_p), ("inv_evec", ct.c_void_p),
                 ("rates", ct.c_void_p), ("props", ct.c_void_p), ("tip_lh", ct.c_void_p),
                 ("ptn_freq", ct.c_void_p), ("ptn_invar", ct.c_void_p), ("tip_states", ct.c_void_p),
-                ("ref_triple_tail", ct.c_int)]
+                ("ref_triple_tail", ct.c_int), ("asc_n", ct.c_int), ("asc_nsite", ct.c_double)]
 
 
 def _dp(a):
@@ -71,7 +71,9 @@ def _dp(a):
 class OracleModel:
     """Owns the arrays an ``orc_model`` points at."""
 
-    def __init__(self, model, patterns, freq, safe=False, invar=None, ref_triple_tail=False):
+    def __init__(self, model, patterns, freq, safe=False, invar=None, ref_triple_tail=False, asc=None):
+        """asc=(nconst, nsite): the last nconst patterns are +ASC's unobserved
+        constant patterns (weight 0), corrected for with nsite sites."""
         self.arrays = dict(
             eval=np.ascontiguousarray(model.eval, np.float64),
             evec=np.ascontiguousarray(model.evec, np.float64),
@@ -90,7 +92,7 @@ class OracleModel:
         self.s = _Model(self.nptn, model.nstates, model.ncat, self.ntaxa, model.state_unknown, int(safe),
                         *[a[k].ctypes.data for k in ("eval", "evec", "inv_evec", "rates", "props",
                                                      "tip_lh", "ptn_freq", "ptn_invar", "tip_states")],
-                        int(ref_triple_tail))
+                        int(ref_triple_tail), int(asc[0]) if asc else 0, float(asc[1]) if asc else 0.0)
 
     @property
     def ptr(self):
@@ -105,10 +107,11 @@ class OracleTree:
     """PhyloTree restatement: computeLikelihood / optimizeOneBranch / optimizeAllBranches."""
 
     def __init__(self, model, patterns, freq, edges, lengths, safe=False, nthreads=0, invar=None,
-                 ref_triple_tail=False):
+                 ref_triple_tail=False, asc=None):
         """ref_triple_tail=True reproduces the reference's derivative sum exactly,
         including its double-counted last entry for odd nstates (codon +G4)."""
-        self.m = OracleModel(model, patterns, freq, safe=safe, invar=invar, ref_triple_tail=ref_triple_tail)
+        self.m = OracleModel(model, patterns, freq, safe=safe, invar=invar, ref_triple_tail=ref_triple_tail,
+                             asc=asc)
         self.edges = np.ascontiguousarray(edges, np.int32)
         self.nedge = len(self.edges)
         L = lib()

@@ -325,6 +325,17 @@ static void make_val(const orc_model *m, double len, double *val) {
     }
 }
 
+/* Lewis correction of a tree lnL (tree/phylokernelnew.h:3198-3222): the
+ * observed patterns' lnL drop by log(1 - P_const), the total by nsite times
+ * that. Returns NAN when P_const is outside [0, 1) (the reference asserts). */
+double orc_asc_lewis_lnl(const orc_model *m, double tree_lh, double prob_const, double *plh) {
+    if (!(prob_const < 1.0 && prob_const >= 0.0)) return NAN;
+    const double lc = log(1.0 - prob_const);
+    if (plh)
+        for (int ptn = 0; ptn < m->nptn - m->asc_n; ptn++) plh[ptn] -= lc;
+    return tree_lh - m->asc_nsite * lc;
+}
+
 double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t *scale,
                       int a, int b, double len, double *pattern_lh, int nthreads) {
     const int n = m->nstates, C = m->ncat, B = n * C, S = m->state_unknown, safe = m->safe;
@@ -347,8 +358,8 @@ double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t 
     const double *pb = b >= 0 ? partials + (size_t)b * pstride : NULL;
     const uint8_t *sb = b >= 0 ? scale + (size_t)b * sstride : NULL;
     double *plh = pattern_lh ? pattern_lh : malloc(sizeof(double) * m->nptn);
-    const int nptn = m->nptn;
-    double *thread_sum = calloc(nth, sizeof(double));
+    const int nptn = m->nptn, orig = m->nptn - m->asc_n;
+    double *thread_sum = calloc(nth, sizeof(double)), *thread_const = calloc(nth, sizeof(double));
 
 #pragma omp parallel num_threads(nth)
     {
@@ -356,7 +367,7 @@ double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t 
 #ifdef _OPENMP
         tid = omp_get_thread_num();
 #endif
-        double acc = 0.0;
+        double acc = 0.0, pconst = 0.0;
 #pragma omp for schedule(static)
         for (int ptn = 0; ptn < nptn; ptn++) {
             double lh_cat[16], lh = 0.0, min_scale = 0.0;
@@ -405,23 +416,35 @@ double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t 
             }
             double sc = min_scale * ORC_LOG_SCALING_THRESHOLD;
             lh = fabs(lh) + m->ptn_invar[ptn];
+            if (ptn >= orig) {  /* unobserved constant pattern: its likelihood, once unscaled */
+                if (min_scale != 0.0) lh *= ORC_SCALING_THRESHOLD;
+                pconst += lh;
+                plh[ptn] = 0.0;
+                continue;
+            }
             lh = log(lh) + sc;
             plh[ptn] = lh;
             acc = fma(lh, m->ptn_freq[ptn], acc);
         }
         thread_sum[tid] = acc;
+        thread_const[tid] = pconst;
     }
-    double tree_lh = 0.0;
-    for (int t = 0; t < nth; t++) tree_lh += thread_sum[t];
+    double tree_lh = 0.0, prob_const = 0.0;
+    for (int t = 0; t < nth; t++) {
+        tree_lh += thread_sum[t];
+        prob_const += thread_const[t];
+    }
     if (!isfinite(tree_lh)) {
         /* arbitrarily fix underflown sites (tree/phylokernelnew.h:3119-3132) */
         tree_lh = 0.0;
-        for (int ptn = 0; ptn < nptn; ptn++) {
+        for (int ptn = 0; ptn < orig; ptn++) {
             if (!isfinite(plh[ptn])) plh[ptn] = ORC_LOG_SCALING_THRESHOLD * 4;
             tree_lh += plh[ptn] * m->ptn_freq[ptn];
         }
     }
+    if (m->asc_n > 0) tree_lh = orc_asc_lewis_lnl(m, tree_lh, prob_const, plh);
     free(thread_sum);
+    free(thread_const);
     free(val);
     free(lh_node_tab);
     if (!pattern_lh) free(plh);
@@ -491,7 +514,8 @@ void orc_compute_theta(const orc_model *m, const double *partials, const uint8_t
     }
 }
 
-void orc_derv(const orc_model *m, const double *theta, double len, double *df, double *ddf, int nthreads) {
+void orc_derv(const orc_model *m, const double *theta, const double *buffer_scale, double len, double *df,
+              double *ddf, int nthreads) {
     const int n = m->nstates, C = m->ncat, B = n * C;
     int nth = num_threads(nthreads);
     double *val0 = malloc(sizeof(double) * B), *val1 = malloc(sizeof(double) * B), *val2 = malloc(sizeof(double) * B);
@@ -506,15 +530,16 @@ void orc_derv(const orc_model *m, const double *theta, double len, double *df, d
             val2[c * n + i] = cof * v1;
         }
     }
-    const int nptn = m->nptn;
+    const int nptn = m->nptn, orig = m->nptn - m->asc_n;
     double *tdf = calloc(nth, sizeof(double)), *tddf = calloc(nth, sizeof(double));
+    double *tc = calloc(3 * (size_t)nth, sizeof(double));
 #pragma omp parallel num_threads(nth)
     {
         int tid = 0;
 #ifdef _OPENMP
         tid = omp_get_thread_num();
 #endif
-        double my_df = 0.0, my_ddf = 0.0;
+        double my_df = 0.0, my_ddf = 0.0, c_lh = 0.0, c_df = 0.0, c_ddf = 0.0;
 #pragma omp for schedule(static)
         for (int ptn = 0; ptn < nptn; ptn++) {
             double lh, d1, d2;
@@ -522,6 +547,17 @@ void orc_derv(const orc_model *m, const double *theta, double len, double *df, d
              * parity of B itself gives the exact sum */
             dot_triple(val0, val1, val2, theta + (size_t)ptn * B, B, m->ref_triple_tail ? n : B, &lh, &d1, &d2);
             lh = fabs(lh) + m->ptn_invar[ptn];
+            if (ptn >= orig) {  /* unobserved constant pattern (tree/phylokernelnew.h:2506-2546) */
+                if (buffer_scale[ptn] != 0.0) {
+                    lh *= ORC_SCALING_THRESHOLD;
+                    d1 *= ORC_SCALING_THRESHOLD;
+                    d2 *= ORC_SCALING_THRESHOLD;
+                }
+                c_lh += lh;
+                c_df += d1;
+                c_ddf += d2;
+                continue;
+            }
             lh = 1.0 / lh;
             double df_frac = d1 * lh, ddf_frac = d2 * lh;
             double freq = m->ptn_freq[ptn];
@@ -531,13 +567,27 @@ void orc_derv(const orc_model *m, const double *theta, double len, double *df, d
         }
         tdf[tid] = my_df;
         tddf[tid] = my_ddf;
+        tc[3 * tid] = c_lh;
+        tc[3 * tid + 1] = c_df;
+        tc[3 * tid + 2] = c_ddf;
     }
-    double sdf = 0.0, sddf = 0.0;
-    for (int t = 0; t < nth; t++) { sdf += tdf[t]; sddf += tddf[t]; }
+    double sdf = 0.0, sddf = 0.0, clh = 0.0, cdf = 0.0, cddf = 0.0;
+    for (int t = 0; t < nth; t++) {
+        sdf += tdf[t];
+        sddf += tddf[t];
+        clh += tc[3 * t];
+        cdf += tc[3 * t + 1];
+        cddf += tc[3 * t + 2];
+    }
+    if (m->asc_n > 0) {  /* Lewis correction (tree/phylokernelnew.h:2620-2628) */
+        const double pv = 1.0 - clh, df_frac = cdf / pv, ddf_frac = cddf / pv;
+        sdf += m->asc_nsite * df_frac;
+        sddf += m->asc_nsite * (ddf_frac + df_frac * df_frac);
+    }
     if (!isfinite(sdf)) sdf = sddf = 0.0; /* tree/phylokernelnew.h:2629-2632 */
     *df = sdf;
     *ddf = sddf;
-    free(tdf); free(tddf); free(val0); free(val1); free(val2);
+    free(tdf); free(tddf); free(tc); free(val0); free(val1); free(val2);
 }
 
 double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double *buffer_scale,
@@ -546,36 +596,48 @@ double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double
     int nth = num_threads(nthreads);
     double *val0 = malloc(sizeof(double) * B);
     make_val(m, len, val0);
-    const int nptn = m->nptn;
+    const int nptn = m->nptn, orig = m->nptn - m->asc_n;
     double *plh = pattern_lh ? pattern_lh : malloc(sizeof(double) * nptn);
-    double *tsum = calloc(nth, sizeof(double));
+    double *tsum = calloc(nth, sizeof(double)), *tconst = calloc(nth, sizeof(double));
 #pragma omp parallel num_threads(nth)
     {
         int tid = 0;
 #ifdef _OPENMP
         tid = omp_get_thread_num();
 #endif
-        double acc = 0.0;
+        double acc = 0.0, pconst = 0.0;
 #pragma omp for schedule(static)
         for (int ptn = 0; ptn < nptn; ptn++) {
             double lh = dot_vec(val0, theta + (size_t)ptn * B, B);
             lh = fabs(lh) + m->ptn_invar[ptn];
+            if (ptn >= orig) {  /* unobserved constant pattern (tree/phylokernelnew.h:3341-3365) */
+                if (buffer_scale[ptn] != 0.0) lh *= ORC_SCALING_THRESHOLD;
+                pconst += lh;
+                plh[ptn] = 0.0;
+                continue;
+            }
             lh = log(fabs(lh)) + buffer_scale[ptn];
             plh[ptn] = lh;
             acc = fma(lh, m->ptn_freq[ptn], acc);
         }
         tsum[tid] = acc;
+        tconst[tid] = pconst;
     }
-    double tree_lh = 0.0;
-    for (int t = 0; t < nth; t++) tree_lh += tsum[t];
+    double tree_lh = 0.0, prob_const = 0.0;
+    for (int t = 0; t < nth; t++) {
+        tree_lh += tsum[t];
+        prob_const += tconst[t];
+    }
     if (!isfinite(tree_lh)) {
         tree_lh = 0.0;
-        for (int ptn = 0; ptn < nptn; ptn++) {
+        for (int ptn = 0; ptn < orig; ptn++) {
             if (!isfinite(plh[ptn])) plh[ptn] = ORC_LOG_SCALING_THRESHOLD * 4;
             tree_lh += plh[ptn] * m->ptn_freq[ptn];
         }
     }
+    if (m->asc_n > 0) tree_lh = orc_asc_lewis_lnl(m, tree_lh, prob_const, plh);
     free(tsum);
+    free(tconst);
     free(val0);
     if (!pattern_lh) free(plh);
     return tree_lh;
@@ -763,7 +825,7 @@ static void func_derv(orc_tree *t, double value, double *f, double *df) {
         t->theta_computed = 1;
     }
     double d1, d2;
-    orc_derv(&t->m, t->theta, value, &d1, &d2, t->nth);
+    orc_derv(&t->m, t->theta, t->buffer_scale, value, &d1, &d2, t->nth);
     *f = -d1;
     *df = -d2;
 }

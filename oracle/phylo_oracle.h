@@ -48,6 +48,14 @@ typedef struct {
      * second time when nstates is odd and nstates*ncat even
      * (tree/phylokernelnew.h:699-718); 0: the exact derivative sum. */
     int ref_triple_tail;
+    /* +ASC (Lewis): the last asc_n patterns are the unobserved constant
+     * patterns appended with weight 0 (alignment/alignment.cpp:4140-4156);
+     * lnL, pattern lnL and derivatives are corrected for them with asc_nsite
+     * sites (tree/phylokernelnew.h:2506-2546 and 2620-2628 derivatives,
+     * 2936-2966 and 3198-3222 branch lnL, 3341-3365 and 3405-3420 lnL from
+     * the buffer). 0 = off. */
+    int asc_n;
+    double asc_nsite;
 } orc_model;
 
 /* A reference to a directed partial: >= 0 is a slot, < 0 is tip taxon (-1-ref). */
@@ -73,8 +81,10 @@ void orc_compute_theta(const orc_model *m, const double *partials, const uint8_t
 
 /* First and second derivative sums of lnL w.r.t. the branch length
  * (computeLikelihoodDervGenericSIMD). */
-void orc_derv(const orc_model *m, const double *theta, double len,
+void orc_derv(const orc_model *m, const double *theta, const double *buffer_scale, double len,
               double *df, double *ddf, int nthreads);
+/* Lewis +ASC correction of a tree lnL and of the observed patterns' lnL. */
+double orc_asc_lewis_lnl(const orc_model *m, double tree_lh, double prob_const, double *plh);
 
 /* lnL from the theta buffer (computeLikelihoodFromBufferGenericSIMD). */
 double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double *buffer_scale,

@@ -116,3 +116,74 @@ def test_invar_optimize_all_branches(oracle_mod):
     lg, lo = t.optimize_all_branches(), o.optimize_all_branches()
     assert rel(lg, lo) < 1e-10
     np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-5)
+
+
+@pytest.mark.parametrize("data,precision", [("dna", engine.F64), ("dna", engine.F32), ("protein", engine.F64),
+                                            ("protein", engine.TF32X3)])
+def test_asc_lewis(oracle_mod, data, precision):
+    """+ASC (Lewis) on variable-site data: the unobserved constant patterns
+    appended with weight 0; lnL, the observed patterns' lnL, derivatives
+    (FP64 1e-9, mixed with the floor above) and optimised branch lengths
+    against the oracle's restatement."""
+    ds = _dataset(data)
+    n = ds.model.nstates
+    vp, vf = models.variable_patterns(ds.patterns, ds.freq, n)
+    pats, freq, nconst, nsite = models.asc_lewis_patterns(vp, vf, n, ds.model.pi)
+    assert nconst > 0
+    m = ds.model
+    tol = 1e-10 if precision == engine.F64 else 1e-6
+    t = engine.GpuTree(m, pats, freq, ds.edges, ds.lengths, precision=precision, asc=(nconst, nsite))
+    o = oracle_mod.OracleTree(m, pats, freq, ds.edges, ds.lengths, asc=(nconst, nsite))
+    lg, plh = t.compute_likelihood(want_pattern_lh=True)
+    lo, plo = o.compute_likelihood(want_pattern_lh=True)
+    plain = oracle_mod.OracleTree(m, pats, freq, ds.edges, ds.lengths).compute_likelihood()
+    assert abs(lo - plain) > 1.0  # the correction is not negligible here
+    assert rel(lg, lo) < tol, (lg, lo)
+    nobs = pats.shape[1] - nconst
+    np.testing.assert_allclose(plh[:nobs], plo[:nobs], atol=1e-8 if precision == engine.F64 else 1e-4)
+
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(pats.shape[1], n, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots, precision=precision,
+                        max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(freq)
+    eng.set_tip_states(pats)
+    eng.set_asc(nconst, nsite)
+    internal = [tuple(map(int, e)) for e in ds.edges if min(e) >= ds.ntaxa]
+    done = set()
+    for (n1, n2) in internal[:2]:
+        ops = topo.ops_for(n1, n2, done) + topo.ops_for(n2, n1, done)
+        a, b = topo.ref(n1, n2), topo.ref(n2, n1)
+        oo = oracle_mod.OracleTree(m, pats, freq, ds.edges, ds.lengths, asc=(nconst, nsite))
+        for i, length in enumerate((0.03, 0.4)):
+            df, ddf = eng.likelihood_derv(ops if i == 0 else [], a, b, length, theta_computed=i > 0)
+            odf, oddf = oo.derv(n1, n2, length)
+            if precision == engine.F64:
+                assert abs(df - odf) <= 1e-9 * abs(odf) + 1e-9, (df, odf)
+                assert abs(ddf - oddf) <= 1e-9 * abs(oddf) + 1e-9, (ddf, oddf)
+            else:
+                floor = 1e-5 * float(freq.sum())
+                assert abs(df - odf) <= 1e-4 * abs(odf) + floor, (df, odf)
+                assert abs(ddf - oddf) <= 1e-3 * abs(oddf) + floor, (ddf, oddf)
+            assert rel(eng.lnl_from_buffer(length), oo.lnl_branch(n2, n1)) < tol
+    if precision == engine.F64 and data == "dna":
+        lg2, lo2 = t.optimize_all_branches(), o.optimize_all_branches()
+        assert rel(lg2, lo2) < 1e-10
+        np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-5)
+
+
+def test_asc_refused_by_batched_paths():
+    ds = _dataset("dna")
+    vp, vf = models.variable_patterns(ds.patterns, ds.freq, 4)
+    pats, freq, nconst, nsite = models.asc_lewis_patterns(vp, vf, 4, ds.model.pi)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(pats.shape[1], 4, ds.model.ncat, ds.ntaxa, ds.model.state_unknown, topo.nslots,
+                        precision=engine.F32, max_ops=topo.nslots)
+    eng.set_model(ds.model)
+    eng.set_patterns(freq)
+    eng.set_tip_states(pats)
+    eng.set_asc(nconst, nsite)
+    with pytest.raises(engine.EngineError):
+        engine.Group([eng])
+    with pytest.raises(engine.EngineError):
+        eng.set_asc(99, nsite)  # more constant patterns than states

@@ -145,3 +145,36 @@ def test_rate_variants_match_standard_basis(oracle_mod, kind):
     o = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths, invar=inv)
     want, _ = stdbasis.tree_lnl(m, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa, invar=inv)
     assert rel(o.compute_likelihood(), want) < 1e-12
+
+
+def test_asc_lewis_matches_standard_basis_and_finite_differences(oracle_mod):
+    """+ASC (Lewis) in the oracle: the corrected lnL equals the independent
+    numpy pruning's sum over observed patterns minus nsite*log(1 - sum of the
+    constant patterns' likelihoods); the corrected derivative matches central
+    finite differences of the corrected lnL."""
+    from iqtree2_gb300 import models, simulate
+    ds = simulate.dna_gtr_dataset(8, 400, 81)
+    vp, vf = models.variable_patterns(ds.patterns, ds.freq, 4)
+    pats, freq, nconst, nsite = models.asc_lewis_patterns(vp, vf, 4, ds.model.pi)
+    assert nconst == 4 and nsite == vf.sum()
+    o = oracle_mod.OracleTree(ds.model, pats, freq, ds.edges, ds.lengths, asc=(nconst, nsite))
+    got, plh = o.compute_likelihood(want_pattern_lh=True)
+    _, p_std = stdbasis.tree_lnl(ds.model, pats, freq, ds.edges, ds.lengths, ds.ntaxa)
+    nobs = pats.shape[1] - nconst
+    pc = np.exp(p_std[nobs:]).sum()
+    want = float(p_std[:nobs] @ freq[:nobs]) - nsite * np.log(1.0 - pc)
+    assert rel(got, want) < 1e-12
+    np.testing.assert_allclose(plh[:nobs], p_std[:nobs] - np.log(1.0 - pc), rtol=1e-12, atol=1e-12)
+    # derivative of the corrected lnL along one internal branch
+    k = next(i for i, e in enumerate(ds.edges) if min(e) >= ds.ntaxa)
+    n1, n2 = map(int, ds.edges[k])
+    t0 = float(ds.lengths[k])
+    df, ddf = oracle_mod.OracleTree(ds.model, pats, freq, ds.edges, ds.lengths, asc=(nconst, nsite)).derv(n1, n2, t0)
+
+    def lnl(t):
+        lens = ds.lengths.copy()
+        lens[k] = t
+        return oracle_mod.OracleTree(ds.model, pats, freq, ds.edges, lens, asc=(nconst, nsite)).compute_likelihood()
+    h = 1e-5
+    assert abs(df - (lnl(t0 + h) - lnl(t0 - h)) / (2 * h)) < 1e-5 * max(1.0, abs(df))
+    assert abs(ddf - (lnl(t0 + h) - 2 * lnl(t0) + lnl(t0 - h)) / h ** 2) < 1e-3 * max(1.0, abs(ddf))
