@@ -130,6 +130,8 @@ struct iqgpu_engine {
     int tc_kpieces;           // K pieces per stage (0/1 = whole K, 2 = halves)
     bool tc_ws;               // level schedule on the warp-specialised tensor-core kernel
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
+    float *d_cmax;            // category-split levels: per (op, category, pattern) maxima
+    size_t cmax_bytes;
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;

@@ -27,7 +27,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 static long long round_up(long long v, long long g) { return (v + g - 1) / g * g; }
 
 struct Sizes {
-    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, flow, total, op_stride;
+    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, flow, cmax, total, op_stride;
 };
 
 static int check_config(const iqgpu_config *c) {
@@ -81,10 +81,14 @@ static Sizes sizes(const iqgpu_config *c) {
         s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
     }
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
+    // category-split tensor-core levels hold fewer than 4 pairs per resident CTA
+    // (<= 4 per SM): nl * Ppad < 16 * SMs * 128 patterns, SMs <= 160
+    s.cmax = uses_tc(c) ? 16LL * 160 * 128 * C * 4 : 0;
     s.flow = is_mixed(c) ? (long long)(c->max_ops + 1) * (s.Ppad / 128) * 4 : 0;
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
-    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + 2 * s.Ppad * 8 +
+    s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + s.cmax +
+              2 * s.Ppad * 8 +
               3 * kMaxStates * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
     return s;
@@ -144,15 +148,17 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
-                        e->d_flow_done};
+                        e->d_flow_done, e->d_asc, e->d_cmax};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
         if (e->h_ops) cudaFreeHost(e->h_ops);
         if (e->h_red_out) cudaFreeHost(e->h_red_out);
+        if (e->h_asc) cudaFreeHost(e->h_asc);
     } else {
         std::free(e->h_ops);
         std::free(e->h_red_out);
+        std::free(e->h_asc);
     }
     std::free(e->level_off);
     if (e->ev_t0) cudaEventDestroy(e->ev_t0);
@@ -274,6 +280,8 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
             e->tc = true;
             e->tcb_stride = tcb_stride(cfg);
             CKE(dalloc(e, &e->d_tcb, s.tcb));
+            CKE(dalloc(e, &e->d_cmax, s.cmax));
+            e->cmax_bytes = (size_t)s.cmax;
         }
     } else {
         CKE(dalloc(e, &e->d_part, s.part));

@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
                                                          const double *__restrict__ tip_lh, int n, int npad, int C,
                                                          int S) {
     extern __shared__ float pi_smem[];
+    __shared__ double s_exp[kMaxStates];
     const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z;
     const int child = ch ? ops[k].child[1] : ops[k].child[0];
     const double len = ch ? ops[k].len[1] : ops[k].len[0];
@@ -107,9 +108,11 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
     float *ue_h = pi_smem, *ue_l = ue_h + nn, *iv_h = ue_l + nn, *iv_l = iv_h + nn;
     float *tp_h = iv_l + nn, *tp_l = tp_h + S * n;  // tip vectors of the S observed states (tips only)
     const double rl = rates[c] * len;
+    // n FP64 exponentials per CTA (GB300's FP64 rate is ~1/60 of FP32), then the entries
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_exp[i] = exp(eval[i] * rl);
+    __syncthreads();
     for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-        const int i = t % n;
-        df_split(evec[t] * exp(eval[i] * rl), ue_h[t], ue_l[t]);
+        df_split(evec[t] * s_exp[t % n], ue_h[t], ue_l[t]);
         df_split(inv[t], iv_h[t], iv_l[t]);
     }
     if (tip)

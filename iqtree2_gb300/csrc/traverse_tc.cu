@@ -79,6 +79,7 @@ struct TcParams {
 
 struct TcItem {
     int k, tile, dad, lref, rref, lch;  // lch: original child index of the left side (after the tip-left swap)
+    int cat;                            // the item's one rate category (category-split items), else -1
     bool lint, rint;
 };
 
@@ -87,14 +88,22 @@ constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged i
 // Item j of this CTA. Fused: every op of the (level-ordered) list for pattern
 // tile blockIdx.x. Level: (tile, op) pairs of one level, strided over the
 // grid, tiles of the same op adjacent (their B operands share L2 lines).
-__device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc) {
+// Category-split (csplit): (tile, op, category) triples, the categories of a
+// pair on adjacent CTAs; the per-pattern rescale then waits for k_tc_fixup.
+__device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc,
+                                          bool csplit = false) {
     const MixParams &P = T.M;
     TcItem it;
+    it.cat = -1;
     if (fused) {
         it.k = j;
         it.tile = blockIdx.x;
     } else {
-        const int i = blockIdx.x + j * gridDim.x;
+        int i = blockIdx.x + j * gridDim.x;
+        if (csplit) {
+            it.cat = i % P.ncat;
+            i /= P.ncat;
+        }
         it.tile = i % T.ntiles;
         it.k = op0 + i / T.ntiles;
     }
@@ -123,11 +132,11 @@ __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, 
 // stages of an item: for each category, the internal sides in order L, R,
 // each in ksplit pieces of K
 __device__ __forceinline__ int tc_nstages(const TcItem &it, int C, int ksplit) {
-    return C * ((int)it.lint + (int)it.rint) * ksplit;
+    return (it.cat >= 0 ? 1 : C) * ((int)it.lint + (int)it.rint) * ksplit;
 }
 __device__ __forceinline__ void tc_stage(const TcItem &it, int st, int ksplit, int &c, int &side, int &kh) {
     const int per = (int)it.lint + (int)it.rint;
-    c = st / (per * ksplit);
+    c = it.cat >= 0 ? it.cat : st / (per * ksplit);
     const int rem = st % (per * ksplit);
     side = per == 2 ? rem / ksplit : (it.lint ? 0 : 1);
     kh = rem % ksplit;
@@ -437,19 +446,27 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 //    (conv mbarrier, 128 arrivals) and, for the first stage of a category,
 //    once the workers have read out the category that last used the same
 //    accumulator buffer (epi_done counter, release/acquire in shared memory).
-// Categories are numbered g = item * ncat + c over the CTA's items; buffer
-// g & 1 holds category g. Workers synchronise among themselves only with a
-// 128-thread named barrier per category epilogue. Every wait is bounded; a
-// wait that gives up raises the shared abort flag and the status word.
-template <int NP, int NSTAGE, bool BF>
+// Categories are numbered g = item * CI + c over the CTA's items (CI = ncat
+// categories per item, or 1 for category-split items); buffer g & 1 holds
+// category g. Workers synchronise among themselves only with a 128-thread
+// named barrier per category epilogue. Every wait is bounded; a wait that
+// gives up raises the shared abort flag and the status word.
+// csplit: items are (tile, op, category) triples (narrow levels: ncat times
+// the parallelism); an item stores its category's products unscaled and the
+// category's per-pattern maximum in cmax[(op - op0) * ncat + c][pattern], and
+// k_tc_fixup applies the rescale and writes the exponents afterwards.
+template <int NP, int NSTAGE, bool BF, bool CSPLIT>
 __global__ void __launch_bounds__(kTcRows + 32, 4)
-    k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl) {
+    k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl,
+                     float *__restrict__ cmax_out) {
+    constexpr bool csplit = CSPLIT;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
+    const int CI = csplit ? 1 : C;
     const int tid = threadIdx.x, warp = tid >> 5;
     const bool worker = tid < kTcRows;
     const long long ld = P.ldp;
-    const int total = T.ntiles * nl;
+    const int total = T.ntiles * nl * (csplit ? C : 1);
     const int nitems =
         (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
     const long long PM = (long long)C * n * npad;
@@ -502,12 +519,12 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
         if ((tid & 31) == 0 && nitems > 0) {
             int ti = 0, ts = 0, issued = 0;  // copy cursor: item, stage within item, stages issued
             int mi = 0, ms = 0, mdone = 0;   // MMA cursor
-            TcItem tit = tc_item(T, 0, false, op0, opc), mit = tit;
+            TcItem tit = tc_item(T, 0, false, op0, opc, csplit), mit = tit;
             auto skip = [&](int &item, int &st, TcItem &it) {
                 while (item < nitems && st >= tc_nstages(it, C, ksplit)) {
                     item++;
                     st = 0;
-                    if (item < nitems) it = tc_item(T, item, false, op0, opc);
+                    if (item < nitems) it = tc_item(T, item, false, op0, opc, csplit);
                 }
             };
             skip(ti, ts, tit);
@@ -542,7 +559,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     tc_stage(mit, ms, ksplit, c, side, kh);
                     const int per = (int)mit.lint + (int)mit.rint;
                     const int sk = ms % (per * ksplit);
-                    const int g = mi * C + c;
+                    const int g = mi * CI + (csplit ? 0 : c);
                     const bool first = sk == 0, last = sk == per * ksplit - 1;
                     if (mdone < issued && mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
                         (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
@@ -621,7 +638,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
             return true;
         };
         for (int j = 0; j < nitems && !abort; j++) {
-            const TcItem it = tc_item(T, j, false, op0, opc);
+            const TcItem it = tc_item(T, j, false, op0, opc, csplit);
             const long long p = (long long)it.tile * kTcRows + r;
             const int sl = it.lint ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
             const int sr = it.rint ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
@@ -631,8 +648,9 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
             const float *TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
             float *dad = P.part + (long long)it.dad * P.slot_floats;
             float cmax = 0.f;
-            for (int c = 0; c < C && !abort; c++) {
-                const int g = j * C + c;
+            for (int cc = 0; cc < CI && !abort; cc++) {
+                const int c = csplit ? it.cat : cc;
+                const int g = j * CI + cc;
                 for (int sk = 0; sk < per * ksplit; sk++) {
                     // no barrier per stage: a wait that gives up raises the abort flag, the
                     // stage is skipped, and the next epilogue's vote stops every worker
@@ -653,10 +671,17 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     if (g & 1) ecount1++;
                     else ecount0++;
                 }
-                if (c > 0 && !epilogue(it, c - 1, g - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+                if (cc > 0 && !epilogue(it, c - 1, g - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
             }
             if (abort) break;
-            if (!epilogue(it, C - 1, j * C + C - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
+            if (!epilogue(it, csplit ? it.cat : C - 1, j * CI + CI - 1, dad, p, TL, sl, sr, cmax)) {
+                abort = true;
+                break;
+            }
+            if (csplit) {  // the rescale and the exponent wait for all categories (k_tc_fixup)
+                cmax_out[((long long)(it.k - op0) * C + it.cat) * ld + p] = cmax;
+                continue;
+            }
             int sh = 0;
             if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale
                 int ex;
@@ -681,6 +706,46 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, 4 * NP);
+}
+
+// Per-pattern rescale and exponent of a level that ran as category-split
+// items: the maximum over the categories' maxima (exact, so the same value the
+// whole-pattern items find), the same exact power-of-two rescale (rare: it
+// re-reads the row) and exponent = children's exponents - shift.
+// 61-state partials fall below the threshold every few levels, so the rescale
+// is common there: the warp rescales its patterns' rows together (lane q takes
+// chunks q, q + 32, ...), one pattern after another.
+__global__ void __launch_bounds__(128) k_tc_fixup(const MixParams P, const int op0, const float *__restrict__ cmax) {
+    const int C = P.ncat, npad = P.npad, kq = npad >> 2;
+    const long long ld = P.ldp;
+    const long long p = (long long)blockIdx.x * 128 + threadIdx.x;
+    const int kr = blockIdx.y, lane = threadIdx.x & 31;
+    const OpDev op = P.ops[op0 + kr];
+    float mx = 0.f;
+    for (int c = 0; c < C; c++) mx = fmaxf(mx, cmax[((long long)kr * C + c) * ld + p]);
+    const int e_in = (op.child[0] >= 0 ? P.expo[(long long)op.child[0] * ld + p] : 0) +
+                     (op.child[1] >= 0 ? P.expo[(long long)op.child[1] * ld + p] : 0);
+    int sh = 0;
+    if (mx < kMixThreshold && mx > 0.f) {
+        int ex;
+        frexpf(mx, &ex);
+        sh = 1 - ex;
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, sh != 0);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int shs = __shfl_sync(0xffffffffu, sh, src);
+        const long long ps = p - lane + src;
+        const float mul = __int_as_float((127 + shs) << 23);
+        float *row = P.part + (long long)op.dad_slot * P.slot_floats + (ps >> 3) * (8LL * C * npad) + (ps & 7) * 4;
+        for (int q = lane; q < C * kq; q += 32) {
+            float4 v = *reinterpret_cast<float4 *>(row + q * 32);
+            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+            *reinterpret_cast<float4 *>(row + q * 32) = v;
+        }
+    }
+    P.expo[(long long)op.dad_slot * ld + p] = e_in - sh;
 }
 
 // ---------------------------------------------------------------------------
@@ -1163,15 +1228,20 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
     const size_t smem = tc_smem_bytes(T, NSTAGE);
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
-    auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF>;
+    auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF, false>;
+    auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, NP == 64>;
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
     cudaError_t err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                          : cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess && ws && NP == 64)
+        err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // the whole unified L1/shared array as shared memory: residency is set by shared memory
     if (err == cudaSuccess)
         err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributePreferredSharedMemoryCarveout, 100)
                  : cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err == cudaSuccess && ws && NP == 64)
+        err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
     // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
@@ -1198,10 +1268,19 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     // the resident CTAs, a tensor-core CTA would hold a single pair and expose
     // its whole stage latency; for up to 32 padded states the fused CUDA-core
     // kernel takes those ops instead (same split in both schedules).
+    // Category-split items (warp-specialised kernel): levels with fewer than
+    // four (tile, op) pairs per resident CTA run as (tile, op, category)
+    // triples, each pair's chain of stages cut into ncat independent ones
+    // (61 states only: a 20-state item is 8 short stages and the narrow levels
+    // run faster on the CUDA-core tail than split plus the fix-up launch)
+    const bool can_split = ws && NP == 64 && e->d_cmax != nullptr;
     int lt = e->nlevels;
     if (NP == 32)
         for (int l = 0; l < e->nlevels; l++)
-            if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < resident) { lt = l; break; }
+            if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles * (can_split ? e->C : 1) < resident) {
+                lt = l;
+                break;
+            }
     *rest = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
     if (*rest <= 0) return IQGPU_OK;
     if (!e->level_sync) {
@@ -1220,14 +1299,24 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
             continue;
         }
         const long long items = (long long)T.ntiles * nl;
-        const int grid = (int)std::min<long long>(items, resident);
-        if (ws)
-            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl);
+        const bool cs = can_split && items < 4 * resident &&
+                        (size_t)nl * e->C * (size_t)e->Ppad * sizeof(float) <= e->cmax_bytes;
+        const int grid = (int)std::min<long long>(items * (cs ? e->C : 1), resident);
+        if (ws && cs)
+            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax);
+        else if (ws)
+            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax);
         else
             kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
         e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
+        if (cs) {
+            k_tc_fixup<<<dim3((unsigned)(e->Ppad / kTcRows), nl), kTcRows, 0, e->st>>>(M, op0, e->d_cmax);
+            e->launches++;
+            err = cudaGetLastError();
+            if (err != cudaSuccess) return cuda_fail(err, "tc_fixup");
+        }
     }
     return IQGPU_OK;
 }
