@@ -110,6 +110,12 @@ struct iqgpu_engine {
     float *d_opmats32;
     long long op_stride32;    // floats per op
     double h_evec[iqg::kMaxStates * iqg::kMaxStates];
+    // host copies of U^-1 and of the eigen-space tip vectors: unit_tips is set
+    // when every unambiguous state's tip vector is exactly column s of U^-1,
+    // so its leaf-table row equals column s of P(t)
+    double h_inv[iqg::kMaxStates * iqg::kMaxStates];
+    double h_tipv[iqg::kMaxStates * iqg::kMaxStates];  // rows of the n unambiguous states
+    bool unit_tips;
     bool have_pi, tipstd_ready;
     int tile;                 // patterns per CTA of the mixed traversal (0 = default)
     bool level_sync;          // mixed traversal schedule: one launch per tree level
@@ -130,6 +136,7 @@ struct iqgpu_engine {
     int tc_kpieces;           // K pieces per stage (0/1 = whole K, 2 = halves)
     bool tc_ws;               // level schedule on the warp-specialised tensor-core kernel
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
+    float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs
     float *d_cmax;            // category-split levels: per (op, category, pattern) maxima
     size_t cmax_bytes;
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it

@@ -72,7 +72,8 @@ static Sizes sizes(const iqgpu_config *c) {
         s.scale = 0;
         s.op_stride = round_up(2 * C * n * npad + 2 * (S + 1) * C * npad, 4);
         s.opmats = ((long long)(c->max_ops + 1) * s.op_stride + n * npad) * 4;
-        s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double);
+        s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double) +
+                  (n >= 16 ? (2 * n * n + 2 * (S + 1) * n) * 4 : 0);  // + the hi/lo split of U^-1 and tips
     } else {
         s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
         s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
@@ -148,7 +149,7 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
-                        e->d_flow_done, e->d_asc, e->d_cmax};
+                        e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -270,6 +271,10 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
         CKE(dalloc(e, &e->d_opmats32, s.opmats));
         CKE(dalloc(e, &e->d_theta32, B * e->Ppad * 4));
         CKE(dalloc(e, &e->d_pi, n * 8));
+        if (n >= 16) {
+            CKE(dalloc(e, &e->d_ivhl, 2 * n * n * 4));
+            CKE(dalloc(e, &e->d_tiphl, 2 * (S + 1) * n * 4));
+        }
         // padding states of every slot stay zero: finite inputs for the float4 matvecs
         CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
         CKE(cudaMemsetAsync(e->d_exp, 0, (long long)cfg->nslots * e->Ppad * 4, e->st));
@@ -327,6 +332,24 @@ int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out) {
     return IQGPU_OK;
 }
 
+// FP64 values as FP32 pairs hi = fl(v), lo = fl(v - hi) ([hi x count][lo x count]),
+// the split the double-float precompute multiplies with
+static cudaError_t upload_hilo(float *dst, const double *v, size_t count) {
+    std::vector<float> hl(2 * count);
+    for (size_t i = 0; i < count; i++) {
+        hl[i] = (float)v[i];
+        hl[count + i] = (float)(v[i] - (double)hl[i]);
+    }
+    return cudaMemcpy(dst, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice);
+}
+
+static void check_unit_tips(iqgpu_engine *e) {
+    e->unit_tips = e->have_model && e->have_tips;
+    for (int s = 0; s < e->n && e->unit_tips; s++)
+        for (int i = 0; i < e->n; i++)
+            if (e->h_tipv[s * e->n + i] != e->h_inv[i * e->n + s]) { e->unit_tips = false; break; }
+}
+
 int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
                     const double *rates, const double *props) {
     if (!e || !eval || !evec || !inv_evec || !rates || !props) { set_error("null argument"); return IQGPU_ERR_ARG; }
@@ -342,6 +365,7 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
     std::memcpy(e->h_evec, evec, n * n * 8);
+    std::memcpy(e->h_inv, inv_evec, n * n * 8);
     if (is_mixed(&e->cfg)) {
         // FP32 copy of U^-1, rows padded to npad, after the op matrix blocks
         std::vector<float> inv32((size_t)n * e->npad, 0.f);
@@ -349,9 +373,11 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
             for (size_t j = 0; j < n; j++) inv32[i * e->npad + j] = (float)inv_evec[i * n + j];
         float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
         CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
+        if (e->d_ivhl) CK(upload_hilo(e->d_ivhl, inv_evec, n * n));
     }
     e->have_model = true;
     e->theta_valid = false;
+    check_unit_tips(e);
     return IQGPU_OK;
 }
 
@@ -370,7 +396,10 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
     CK(cudaMemcpy(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice));
+    if (e->d_tiphl) CK(upload_hilo(e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n));
+    std::memcpy(e->h_tipv, tip_lh, (size_t)e->n * e->n * 8);
     e->have_tips = true;
+    check_unit_tips(e);
     return IQGPU_OK;
 }
 

@@ -85,63 +85,74 @@ __device__ __forceinline__ void df_split(double v, float &h, float &l) {
     l = (float)(v - (double)h);
 }
 
-// Same outputs as k_partial_info_mixed for 16..64 states, one CTA per (op,
-// child, category): U diag(exp(lambda r_c t)) and U^-1 (and the tip vectors
-// when the child is a tip) staged in shared memory as FP32 pairs; each output
-// is a double-float dot product of length n, rounded once to FP32 at the end.
-// GB300 runs FP64 FMAs ~60x slower than FP32; the result is stored in FP32, so
-// the 44-bit double-float sums lose nothing that is kept.
+// Same outputs as k_partial_info_mixed for 16..64 states. One CTA per (op,
+// child, category, block of 16 rows): U diag(exp(lambda r_c t)) for its rows
+// is split into FP32 pairs in shared memory; U^-1 and the eigen-space tip
+// vectors were split once per model (d_ivhl, d_tiphl) and are read through
+// L1. Each output is a double-float dot product of length n, rounded once to
+// FP32 at the end. GB300 runs FP64 FMAs ~60x slower than FP32; the result is
+// stored in FP32, so the 44-bit double-float sums lose nothing that is kept.
+constexpr int kPiRows = 16;
 __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict__ ops, float *__restrict__ opmats,
                                                          long long op_stride, const double *__restrict__ evec,
-                                                         const double *__restrict__ inv,
                                                          const double *__restrict__ eval,
                                                          const double *__restrict__ rates,
-                                                         const double *__restrict__ tip_lh, int n, int npad, int C,
-                                                         int S) {
-    extern __shared__ float pi_smem[];
+                                                         const float *__restrict__ ivhl,
+                                                         const float *__restrict__ tiphl, int n, int npad, int C,
+                                                         int S, int unit_tips) {
+    __shared__ float ue_h[kPiRows * kMaxStates], ue_l[kPiRows * kMaxStates];
+    __shared__ float s_p[kPiRows * kMaxStates];  // this block's rows of P(t), for unit tip vectors
     __shared__ double s_exp[kMaxStates];
-    const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z;
+    const int rb = (npad + kPiRows - 1) / kPiRows;
+    const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z / rb, x0 = (blockIdx.z % rb) * kPiRows;
     const int child = ch ? ops[k].child[1] : ops[k].child[0];
     const double len = ch ? ops[k].len[1] : ops[k].len[0];
     const bool tip = child < 0;
     const int nn = n * n;
-    float *ue_h = pi_smem, *ue_l = ue_h + nn, *iv_h = ue_l + nn, *iv_l = iv_h + nn;
-    float *tp_h = iv_l + nn, *tp_l = tp_h + S * n;  // tip vectors of the S observed states (tips only)
     const double rl = rates[c] * len;
-    // n FP64 exponentials per CTA (GB300's FP64 rate is ~1/60 of FP32), then the entries
+    // n FP64 exponentials per CTA, then this block's rows of U diag(exp)
     for (int i = threadIdx.x; i < n; i += blockDim.x) s_exp[i] = exp(eval[i] * rl);
     __syncthreads();
-    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-        df_split(evec[t] * s_exp[t % n], ue_h[t], ue_l[t]);
-        df_split(inv[t], iv_h[t], iv_l[t]);
+    for (int t = threadIdx.x; t < kPiRows * n; t += blockDim.x) {
+        const int xr = t / n, i = t % n, x = x0 + xr;
+        if (x < n) df_split(evec[x * n + i] * s_exp[i], ue_h[xr * n + i], ue_l[xr * n + i]);
     }
-    if (tip)
-        for (int t = threadIdx.x; t < S * n; t += blockDim.x) df_split(tip_lh[t], tp_h[t], tp_l[t]);
     __syncthreads();
     float *base = opmats + (long long)k * op_stride;
     const long long PM = (long long)C * n * npad;
     float *Pm = base + ch * PM + (long long)c * n * npad;
-    for (int e = threadIdx.x; e < n * npad; e += blockDim.x) {
-        const int x = e / npad, y = e % npad;
+    for (int e = threadIdx.x; e < kPiRows * npad; e += blockDim.x) {
+        const int xr = e / npad, y = e % npad, x = x0 + xr;
+        if (x >= n) continue;
         float sh = 0.f, sl = 0.f;
         if (y < n)
-            for (int i = 0; i < n; i++) df_mac(ue_h[x * n + i], ue_l[x * n + i], iv_h[i * n + y], iv_l[i * n + y], sh, sl);
-        Pm[e] = __fadd_rn(sh, sl);
+            for (int i = 0; i < n; i++)
+                df_mac(ue_h[xr * n + i], ue_l[xr * n + i], __ldg(ivhl + i * n + y), __ldg(ivhl + nn + i * n + y), sh,
+                       sl);
+        const float pv = __fadd_rn(sh, sl);
+        Pm[x * npad + y] = pv;
+        s_p[xr * npad + y] = pv;
     }
     if (!tip) return;
+    __syncthreads();  // s_p complete
     // leaf table[s][c][x] = sum_i (U e)[x][i] tip_lh[s][i]; the unknown state gives 1
     const long long TB = (long long)(S + 1) * C * npad;
+    const int ts = (S + 1) * n;  // floats of one half of tiphl
     float *tab = base + 2 * PM + ch * TB;
-    for (int u = threadIdx.x; u < (S + 1) * npad; u += blockDim.x) {
-        const int st = u / npad, x = u % npad;
+    for (int u = threadIdx.x; u < (S + 1) * kPiRows; u += blockDim.x) {
+        const int st = u / kPiRows, xr = u % kPiRows, x = x0 + xr;
+        if (x >= npad) continue;
         float v = 0.f;
         if (x < n) {
             if (st == S) {
                 v = 1.f;
+            } else if (unit_tips && st < n) {  // tip vector = column st of U^-1: the same sums as P[x][st]
+                v = s_p[xr * npad + st];
             } else {
                 float sh = 0.f, sl = 0.f;
                 for (int i = 0; i < n; i++)
-                    df_mac(ue_h[x * n + i], ue_l[x * n + i], tp_h[st * n + i], tp_l[st * n + i], sh, sl);
+                    df_mac(ue_h[xr * n + i], ue_l[xr * n + i], __ldg(tiphl + st * n + i),
+                           __ldg(tiphl + ts + st * n + i), sh, sl);
                 v = __fadd_rn(sh, sl);
             }
         }
@@ -265,13 +276,11 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
 
 int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
     if (nops_with_branch <= 0) return IQGPU_OK;
-    if (e->n >= 16) {  // double-float products, one CTA per (op, child, category)
-        const size_t smem = (size_t)(4 * e->n * e->n + 2 * e->S * e->n) * 4;
-        cudaError_t err = cudaFuncSetAttribute(k_partial_info_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (err != cudaSuccess) return cuda_fail(err, "partial_info_df smem attribute");
-        k_partial_info_df<<<dim3(nops_with_branch, 2, e->C), 256, smem, e->st>>>(
-            e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv, e->d_eval, e->d_rates, e->d_tip, e->n,
-            e->npad, e->C, e->S);
+    if (e->n >= 16 && e->d_ivhl) {  // double-float products, one CTA per (op, child, category, 16 rows)
+        const int rb = (e->npad + kPiRows - 1) / kPiRows;
+        k_partial_info_df<<<dim3(nops_with_branch, 2, e->C * rb), 256, 0, e->st>>>(
+            e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_eval, e->d_rates, e->d_ivhl, e->d_tiphl, e->n,
+            e->npad, e->C, e->S, e->unit_tips ? 1 : 0);
         e->launches++;
         return cuda_fail(cudaGetLastError(), "partial_info_df");
     }

@@ -274,6 +274,206 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
     }
 }
 
+// Chain form of the fused schedule for up to kChainCat categories: one thread
+// per pattern with all of its categories (the fused kernel above uses one per
+// (pattern, category)), so that a traversal tail of one-op levels, whose ops
+// depend on each other one after the other, runs with every pattern of the
+// alignment resident at once instead of in several waves that repeat the
+// whole chain. The next category's children are requested while the current
+// one is computed; the outputs are stored as computed and, in the uncommon
+// case that the pattern needs the rescale, re-read and scaled (the register
+// file holds one wave of patterns only without a copy of all outputs). Same
+// arithmetic as mixed_op / mixed_epilogue
+// (row_dot_s, products, maximum, power-of-two rescale; the lnL terms in the
+// same order), so the results are bit-identical to k_traverse_mixed.
+constexpr int kChainCat = 4;
+template <int NQ, int EPI>
+__global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
+    const int C = P.ncat, n = P.n, npad = P.npad, S = P.state_unknown;
+    const long long ld = P.ldp;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;  // + (c * NQ + q) * 32
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(S + 1) * C * npad;
+    const unsigned pbytes = (unsigned)(2 * PM * 4);
+    extern __shared__ __align__(128) float chain_smem[];  // [2][2 * PM] P(t) double buffer
+    __shared__ unsigned long long bars[2];
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        if (P.nops > 0) {
+            mbar_expect_tx(&bars[0], pbytes);
+            tma_load_1d(chain_smem, P.opmats, pbytes, &bars[0]);
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < P.nops; ++k) {
+        const int buf = k & 1;
+        const bool lost = !mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
+        if (__syncthreads_or(lost)) {
+            if (threadIdx.x == 0) {
+                atomicExch(P.status, kStatusTimeout);
+                mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
+            }
+            return;
+        }
+        if (threadIdx.x == 0 && k + 1 < P.nops) {
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[buf ^ 1], pbytes);
+            tma_load_1d(chain_smem + (buf ^ 1) * 2 * PM, P.opmats + (long long)(k + 1) * P.op_stride, pbytes,
+                        &bars[buf ^ 1]);
+        }
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const float *gbase = P.opmats + (long long)k * P.op_stride;
+        const float *PL = chain_smem + buf * 2 * PM, *PR = PL + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
+        if (lref >= 0 && rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+            int t = lref; lref = rref; rref = t;
+            const float *q = PL; PL = PR; PR = q;
+            q = TL; TL = TR; TR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
+        const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
+        const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
+        const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
+        float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
+        float4 lv[NQ], rv[NQ], nl[NQ], nr[NQ];
+        auto fetch = [&](int c, float4 (&a)[NQ], float4 (&b)[NQ]) {
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                if (lint) a[q] = *reinterpret_cast<const float4 *>(Lp + (c * NQ + q) * 32);
+                if (rint) b[q] = *reinterpret_cast<const float4 *>(Rp + (c * NQ + q) * 32);
+            }
+        };
+        fetch(0, lv, rv);
+        float cmax = 0.f;
+#pragma unroll
+        for (int c = 0; c < kChainCat; c++) {
+            if (c < C) {
+                if (c + 1 < C) fetch(c + 1, nl, nr);
+                const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
+#pragma unroll
+                for (int q = 0; q < NQ; q++) {
+                    float o[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int x = 4 * q + j;
+                        float v = 0.f;
+                        if (x < n) {
+                            const float yl = lint ? row_dot_s<NQ>(PLc + x * npad, lv) : __ldg(tl + c * npad + x);
+                            const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : __ldg(tr + c * npad + x);
+                            v = yl * yr;
+                        }
+                        o[j] = v;
+                        cmax = fmaxf(cmax, v);
+                    }
+                    *reinterpret_cast<float4 *>(dad + (c * NQ + q) * 32) = make_float4(o[0], o[1], o[2], o[3]);
+                }
+#pragma unroll
+                for (int q = 0; q < NQ; q++) {
+                    lv[q] = nl[q];
+                    rv[q] = nr[q];
+                }
+            }
+        }
+        int sh = 0;
+        if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale of this thread's own stores
+            int ex;
+            frexpf(cmax, &ex);
+            sh = 1 - ex;
+            const float mul = __int_as_float((127 + sh) << 23);
+            for (int q = 0; q < C * NQ; q++) {
+                float4 v = *reinterpret_cast<float4 *>(dad + q * 32);
+                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                *reinterpret_cast<float4 *>(dad + q * 32) = v;
+            }
+        }
+        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+        P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+    }
+    if constexpr (EPI == EPI_NONE) return;
+
+    const float *pa = P.part + (long long)P.a * P.slot_floats + pbase;
+    const bool btip = P.b < 0;
+    const float *pb = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pbase;
+    const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+    const int ea = P.expo[(long long)P.a * ld + p];
+    const int eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
+    if constexpr (EPI == EPI_THETA) {
+        // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i (tree/phylokernelnew.h:2048-2231)
+        float *th = P.theta + p;
+        for (int c = 0; c < C; c++) {
+            float4 a4[NQ], b4[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                a4[q] = *reinterpret_cast<const float4 *>(pa + (c * NQ + q) * 32);
+                b4[q] = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + (c * NQ + q) * 32);
+            }
+            for (int i = 0; i < n; i++) {
+                const float *urow = P.inv32 + (long long)i * npad;
+                float ua = 0.f, ub = 0.f;
+#pragma unroll
+                for (int q = 0; q < NQ; q++) {
+                    const float4 u = ld4(urow + 4 * q);
+                    ua = dot4(u, a4[q], ua);
+                    if (!btip) ub = dot4(u, b4[q], ub);
+                }
+                if (btip) ub = (float)__ldg(P.tip_lh + (long long)sb * n + i);
+                th[(long long)(c * n + i) * ld] = ua * ub;
+            }
+        }
+        P.buffer_scale[p] = (double)(ea + eb) * kLn2;
+    } else {
+        // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
+        const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
+        double lh = 0.0;
+        for (int c = 0; c < C; c++) {
+            float4 a4[NQ], b4[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                a4[q] = *reinterpret_cast<const float4 *>(pa + (c * NQ + q) * 32);
+                b4[q] = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + (c * NQ + q) * 32);
+            }
+            float lc = 0.f;
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const float av[4] = {a4[q].x, a4[q].y, a4[q].z, a4[q].w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int x = 4 * q + j;
+                    if (x < n) {
+                        float w;
+                        if (btip) {
+                            w = __ldg(base + 2 * PM + (long long)sb * C * npad + c * npad + x);
+                        } else {
+                            const float *prow = base + (long long)(c * n + x) * npad;
+                            float s0 = 0.f;
+#pragma unroll
+                            for (int qq = 0; qq < NQ; qq++) s0 = dot4(ld4(prow + 4 * qq), b4[qq], s0);
+                            w = s0;
+                        }
+                        lc = fmaf((float)__ldg(P.pi + x) * av[j], w, lc);
+                    }
+                }
+            }
+            lh = fma((double)lc, P.props[c], lh);
+        }
+        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));
+        const double plh = log(lh) + (double)(ea + eb) * kLn2;
+        P.pattern_lh[p] = plh;
+        if (p < P.nptn) {
+            const double f = P.freq[p];
+            v[0] = plh * f;
+            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+            v[2] = isfinite(plh) ? 0.0 : 1.0;
+        }
+        mix_grid_reduce(v, P.red);
+    }
+}
+
 // fused schedule: NQ = npad/4 float4 chunks per category held in registers
 // (1 DNA, 5 protein); NQ = 0 is the chunked path for larger n (codon)
 template <int NQ, int EPI>
@@ -468,6 +668,28 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
 }
 
 // Levels l0 .. of the uploaded list, one launch each.
+// The chain kernel: 128 patterns per CTA, or 64 when that is what it takes for
+// every pattern tile to be resident in one wave.
+template <int NQ, int EPI>
+static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
+    const size_t smem = (size_t)2 * 2 * e->C * e->n * e->npad * 4;  // double-buffered P(t) of one op
+    auto kern = k_chain_mixed<NQ, EPI>;
+    cudaError_t err = cudaSuccess;
+    if (smem > 48 * 1024) err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return cuda_fail(err, "chain_mixed smem attribute");
+    int sms = 1, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    int tb = 128;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem) == cudaSuccess &&
+        e->Ppad / 128 > (long long)per_sm * sms &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 64, smem) == cudaSuccess &&
+        e->Ppad / 64 <= (long long)per_sm * sms)
+        tb = 64;
+    kern<<<(unsigned)(e->Ppad / tb), tb, smem, e->st>>>(P);
+    e->launches++;
+    return cuda_fail(cudaGetLastError(), "chain_mixed");
+}
+
 template <int NQ>
 static int launch_levels_t(iqgpu_engine *e, const MixParams &P, int l0 = 0) {
     const int TP = mix_tile(e);
@@ -529,7 +751,7 @@ static int fused_rest(iqgpu_engine *e, MixParams P, int rest) {
     P.branch_op -= rest;
     switch (e->npad) {
     case 4: return launch_mix_t<1, EPI>(e, P);
-    case 20: return launch_mix_t<5, EPI>(e, P);
+    case 20: return e->C <= kChainCat ? launch_chain_t<5, EPI>(e, P) : launch_mix_t<5, EPI>(e, P);
     default: return launch_mix_t<0, EPI>(e, P);
     }
 }

@@ -1232,8 +1232,9 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, NP == 64>;
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
-    cudaError_t err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                         : cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess && ws)
+        err = cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err == cudaSuccess && ws && NP == 64)
         err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // the whole unified L1/shared array as shared memory: residency is set by shared memory
