@@ -243,6 +243,7 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
     P.ncat = e->C;
     P.state_unknown = e->S;
     P.nops = nops;
+    P.op_base = 0;
     P.nptn = (int)e->P;
     P.ldp = e->Ppad;
     P.slot_floats = e->Ppad * e->bp;

@@ -26,6 +26,7 @@ struct MixParams {
     long long slot_floats;  // Ppad * C * npad
     long long op_stride;    // floats per op
     const OpDev *ops;
+    int op_base;            // index of ops[0] in the uploaded list (the producer indices' origin)
     const float *opmats;    // per op: P child0 [C][n][npad], P child1, table child0 [S+1][C][npad], table child1
     const float *inv32;     // [n][npad] FP32 copy of U^-1
     const double *pi;       // [n]

@@ -21,6 +21,22 @@ namespace iqg {
 constexpr int kDnaTile = 128;  // patterns (= threads) per CTA
 constexpr int kDnaMaxCat = 4;  // register-resident categories (ncat <= 4 uses this kernel)
 
+// cp.async (LDGSTS): 16-byte and 4-byte global -> shared copies that complete
+// per thread, grouped and waited for in order (no registers held meanwhile)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+constexpr int kDnaAhead = 4;  // ops whose other child is in flight ahead of the one computed
+
 template <int EPI>
 __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P) {
     constexpr int n = 4, npad = 4;
@@ -46,24 +62,43 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
     __syncthreads();
 
     // The previous op's output for this pattern stays in registers (as
-    // stored), and one internal child of the next op that it does not produce
-    // is requested one op ahead: along a chain of ops (each taking the
-    // previous op's output as one child, as the one-op levels near the root
-    // do) every child is then in flight or in registers when its op starts.
-    int prev_dad = -1, prev_e = 0, nx_ref = -1, nx_e = 0;
-    float4 prev[kDnaMaxCat], nx[kDnaMaxCat];
-    auto request = [&](int k, int skip) {
-        const OpDev o = P.ops[k];
-        const int r0 = o.child[0], r1 = o.child[1];
-        nx_ref = (r0 >= 0 && r0 != skip) ? r0 : ((r1 >= 0 && r1 != skip) ? r1 : -1);
-        if (nx_ref < 0) return;
-        const float *src = P.part + (long long)nx_ref * P.slot_floats + pbase;
+    // stored), and the other internal child of each of the next kDnaAhead ops
+    // is copied ahead into this thread's slots of a shared-memory ring with
+    // cp.async: along a chain of ops (each taking the previous op's output as
+    // one child, as the one-op levels near the root do) the children of the
+    // coming ops are in flight while the current one computes. The request
+    // for op j is issued after op j - kDnaAhead has stored its outputs, and
+    // names (pick) a child produced before that op, so its values are in
+    // memory a whole op before the copy starts; every thread derives the same
+    // choice from the op list.
+    __shared__ __align__(16) float4 pf[kDnaAhead][kDnaMaxCat][kDnaTile];
+    __shared__ int pfe[kDnaAhead][kDnaTile];
+    int prev_dad = -1, prev_e = 0;
+    float4 prev[kDnaMaxCat];
+    auto pick = [&](int j) -> int {
+        const OpDev o = P.ops[j];
+        const int skip = j > 0 ? P.ops[j - 1].dad_slot : -1;
 #pragma unroll
-        for (int c = 0; c < kDnaMaxCat; c++)
-            if (c < C) nx[c] = *reinterpret_cast<const float4 *>(src + c * 32);
-        nx_e = P.expo[(long long)nx_ref * ld + p];
+        for (int ch = 0; ch < 2; ch++) {
+            const int r = o.child[ch];
+            const long long prod = ch ? o.prod1 : (long long)o.prod0;
+            if (r >= 0 && r != skip && (prod < 0 || prod - P.op_base < (long long)j - kDnaAhead)) return r;
+        }
+        return -1;
     };
-    if (P.nops > 0) request(0, -1);
+    auto request = [&](int j) {  // one commit group per op, empty when nothing is requested
+        const int ref = j < P.nops ? pick(j) : -1;
+        if (ref >= 0) {
+            const int d = j % kDnaAhead;
+            const float *src = P.part + (long long)ref * P.slot_floats + pbase;
+#pragma unroll
+            for (int c = 0; c < kDnaMaxCat; c++)
+                if (c < C) cp_async16(&pf[d][c][threadIdx.x], src + c * 32);
+            cp_async4(&pfe[d][threadIdx.x], P.expo + (long long)ref * ld + p);
+        }
+        cp_async_commit();
+    };
+    for (int j = 0; j < kDnaAhead; j++) request(j);
 
     for (int k = 0; k < P.nops; ++k) {
         const int buf = k & 1;
@@ -73,6 +108,7 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
                 atomicExch(P.status, kStatusTimeout);
                 mbar_wait(&bars[buf], (k >> 1) & 1, kWaitPolls);
             }
+            cp_async_wait<0>();  // no copy into this CTA's shared memory outlives it
             return;
         }
         if (threadIdx.x == 0 && k + 1 < P.nops) {
@@ -95,9 +131,10 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
         const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
         float4 out[kDnaMaxCat];
         float mx = 0.f;
-        // an internal side comes from registers (previous output or the
-        // requested child) or, when the op's children are both internal and
-        // neither chains, is loaded here
+        // an internal side comes from registers (previous output), from the
+        // ring (the child requested for this op), or is loaded here
+        cp_async_wait<kDnaAhead - 1>();  // this thread's copies for ops <= k have landed
+        const int got = pick(k), d = k % kDnaAhead;
         float4 lv[kDnaMaxCat], rv[kDnaMaxCat];
         int e = 0;
         auto side = [&](int ref, float4 (&v)[kDnaMaxCat]) {
@@ -105,10 +142,10 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
 #pragma unroll
                 for (int c = 0; c < kDnaMaxCat; c++) v[c] = prev[c];
                 e += prev_e;
-            } else if (ref == nx_ref) {
+            } else if (ref == got) {
 #pragma unroll
-                for (int c = 0; c < kDnaMaxCat; c++) v[c] = nx[c];
-                e += nx_e;
+                for (int c = 0; c < kDnaMaxCat; c++) v[c] = pf[d][c][threadIdx.x];
+                e += pfe[d][threadIdx.x];
             } else {
                 const float *src = P.part + (long long)ref * P.slot_floats + pbase;
 #pragma unroll
@@ -153,7 +190,6 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
                 mx = fmaxf(mx, fmaxf(fmaxf(out[c].x, out[c].y), fmaxf(out[c].z, out[c].w)));
             }
         }
-        if (k + 1 < P.nops) request(k + 1, op.dad_slot);  // in flight across the stores and the next barrier
         int sh = 0;
         float mul = 1.f;
         if (mx < kMixThreshold && mx > 0.f) {  // exact power-of-two rescale
@@ -175,6 +211,8 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
         P.expo[(long long)op.dad_slot * ld + p] = e - sh;
         prev_dad = op.dad_slot;
         prev_e = e - sh;
+        // after this op's stores; slot d is free again (its values are in lv / rv)
+        request(k + kDnaAhead);
     }
 
     if constexpr (EPI == EPI_NONE) return;
@@ -442,6 +480,7 @@ static int launch_levels_dna_t(iqgpu_engine *e, MixParams P, int epi) {
     // the tail ops [rest, nops) and the epilogue: shift the op list so the fused
     // kernel sees them as ops 0.. (the branch matrices keep their block)
     P.ops += rest;
+    P.op_base += rest;
     P.opmats += (long long)rest * P.op_stride;
     P.nops -= rest;
     P.branch_op -= rest;

@@ -746,6 +746,7 @@ int launch_traverse_tc(iqgpu_engine *e, const MixParams &M, int *rest);
 template <int EPI>
 static int fused_rest(iqgpu_engine *e, MixParams P, int rest) {
     P.ops += rest;
+    P.op_base += rest;
     P.opmats += (long long)rest * P.op_stride;
     P.nops -= rest;
     P.branch_op -= rest;
