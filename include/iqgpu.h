@@ -165,6 +165,19 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
  * points refuse +ASC engines (IQGPU_ERR_ARG); iqgpu_rell takes the corrected
  * pattern lnL from iqgpu_get_pattern_lh. */
 int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
+/* Mixture model (ModelMixture: profile mixtures such as C10-C60, LG4X, ...)
+ * on the mixed-precision path: nmix classes, each with its own eigen system
+ * and state frequencies; the ncat categories (a multiple of nmix) are class
+ * blocks of ncat/nmix rate categories, category c belonging to class
+ * c / (ncat/nmix) (tree/phylokernelnew.h:908-918; with fused mix-rate,
+ * ncat = nmix and category c is class c). Arrays by class: eval [nmix][n],
+ * evec and inv_evec [nmix][n][n], state_freq [nmix][n]; tip_lh
+ * [STATE_UNKNOWN+1][nmix][n] (the reference's tip_partial_lh layout); rates
+ * and props per category (props = rate proportion x class weight,
+ * :2327). iqgpu_set_model goes back to one class. FP64 engines and the
+ * batched NNI entry point refuse mixtures (IQGPU_ERR_ARG). */
+int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const double *evec, const double *inv_evec,
+                      const double *rates, const double *props, const double *tip_lh, const double *state_freq);
 /* Copy a slot back in the reference layout: partial[ptn*B + c*n + x] in eigen
  * space (F64) or standard basis (mixed), and scale counts (NORM: nptn bytes,
  * SAFE: nptn*ncat bytes, pattern-major). Either output may be NULL. */

@@ -71,9 +71,10 @@ static Sizes sizes(const iqgpu_config *c) {
         s.part = (long long)c->nslots * s.Ppad * (C * npad * 4 + 4);
         s.scale = 0;
         s.op_stride = round_up(2 * C * n * npad + 2 * (S + 1) * C * npad, 4);
-        s.opmats = ((long long)(c->max_ops + 1) * s.op_stride + n * npad) * 4;
+        s.opmats = ((long long)(c->max_ops + 1) * s.op_stride + C * n * npad) * 4;  // + U^-1 of each class
         s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double) +
-                  (n >= 16 ? (2 * n * n + 2 * (S + 1) * n) * 4 : 0);  // + the hi/lo split of U^-1 and tips
+                  (n >= 16 ? C * (2 * n * n + 2 * (S + 1) * n) * 4 : 0) +  // + the hi/lo split of U^-1 and tips
+                  (C - 1) * (n + 2 * n * n + (S + 2) * n) * 8;              // + the other classes' model arrays
     } else {
         s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
         s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
@@ -252,12 +253,16 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     CKE(cudaEventCreate(&e->ev_t0));
     CKE(cudaEventCreate(&e->ev_t1));
     const long long n = e->n, C = e->C, B = e->B, S = e->S;
-    CKE(dalloc(e, &e->d_eval, n * 8));
-    CKE(dalloc(e, &e->d_evec, n * n * 8));
-    CKE(dalloc(e, &e->d_inv, n * n * 8));
+    // model arrays per mixture class: up to ncat classes on the mixed path (one otherwise)
+    const long long K = is_mixed(cfg) ? C : 1;
+    e->nmix = 1;
+    e->cpc = (int)C;
+    CKE(dalloc(e, &e->d_eval, K * n * 8));
+    CKE(dalloc(e, &e->d_evec, K * n * n * 8));
+    CKE(dalloc(e, &e->d_inv, K * n * n * 8));
     CKE(dalloc(e, &e->d_rates, C * 8));
     CKE(dalloc(e, &e->d_props, C * 8));
-    CKE(dalloc(e, &e->d_tip, (S + 1) * n * 8));
+    CKE(dalloc(e, &e->d_tip, (S + 1) * K * n * 8));
     CKE(dalloc(e, &e->d_freq, e->Ppad * 8));
     CKE(dalloc(e, &e->d_invar, e->Ppad * 8));
     CKE(dalloc(e, &e->d_states, s.states));
@@ -270,10 +275,10 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
         CKE(dalloc(e, &e->d_exp, (long long)cfg->nslots * e->Ppad * 4));
         CKE(dalloc(e, &e->d_opmats32, s.opmats));
         CKE(dalloc(e, &e->d_theta32, B * e->Ppad * 4));
-        CKE(dalloc(e, &e->d_pi, n * 8));
+        CKE(dalloc(e, &e->d_pi, K * n * 8));
         if (n >= 16) {
-            CKE(dalloc(e, &e->d_ivhl, 2 * n * n * 4));
-            CKE(dalloc(e, &e->d_tiphl, 2 * (S + 1) * n * 4));
+            CKE(dalloc(e, &e->d_ivhl, 2 * K * n * n * 4));
+            CKE(dalloc(e, &e->d_tiphl, 2 * (S + 1) * K * n * 4));
         }
         // padding states of every slot stay zero: finite inputs for the float4 matvecs
         CKE(cudaMemsetAsync(e->d_part32, 0, (long long)cfg->nslots * e->Ppad * e->bp * 4, e->st));
@@ -377,7 +382,62 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     }
     e->have_model = true;
     e->theta_valid = false;
+    if (e->nmix != 1) {  // back to one class: the class-indexed tip vectors must be set again
+        e->nmix = 1;
+        e->cpc = e->C;
+        e->have_tips = false;
+    }
     check_unit_tips(e);
+    return IQGPU_OK;
+}
+
+int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const double *evec, const double *inv_evec,
+                      const double *rates, const double *props, const double *tip_lh, const double *state_freq) {
+    if (!e || !eval || !evec || !inv_evec || !rates || !props || !tip_lh || !state_freq) {
+        set_error("null argument");
+        return IQGPU_ERR_ARG;
+    }
+    if (!is_mixed(&e->cfg)) {
+        set_error("mixture models run on the mixed-precision path (IQGPU_F32, IQGPU_TF32X3, IQGPU_BF16)");
+        return IQGPU_ERR_ARG;
+    }
+    if (nmix < 1 || nmix > e->C || e->C % nmix != 0) {
+        set_error("mixture: need 1 <= nmix <= ncat with ncat a multiple of nmix");
+        return IQGPU_ERR_ARG;
+    }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    const size_t n = e->n, C = e->C, K = (size_t)nmix, S1 = (size_t)e->S + 1;
+    CK(cudaMemcpy(e->d_eval, eval, K * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_evec, evec, K * n * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_inv, inv_evec, K * n * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_tip, tip_lh, S1 * K * n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_pi, state_freq, K * n * 8, cudaMemcpyHostToDevice));
+    std::vector<float> inv32(K * n * e->npad, 0.f);
+    for (size_t m = 0; m < K; m++)
+        for (size_t i = 0; i < n; i++)
+            for (size_t j = 0; j < n; j++) inv32[(m * n + i) * e->npad + j] = (float)inv_evec[(m * n + i) * n + j];
+    float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
+    CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
+    if (e->d_ivhl) {
+        for (size_t m = 0; m < K; m++) CK(upload_hilo(e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n));
+        CK(upload_hilo(e->d_tiphl, tip_lh, S1 * K * n));
+    }
+    // leaf-table shortcut: every class's unambiguous tip vectors are columns of its U^-1
+    bool unit = true;
+    for (size_t m = 0; m < K && unit; m++)
+        for (size_t st = 0; st < n && unit; st++)
+            for (size_t i = 0; i < n; i++)
+                if (tip_lh[(st * K + m) * n + i] != inv_evec[(m * n + i) * n + st]) { unit = false; break; }
+    std::memcpy(e->h_rates, rates, C * 8);
+    std::memcpy(e->h_props, props, C * 8);
+    e->nmix = nmix;
+    e->cpc = (int)(C / K);
+    e->unit_tips = unit;
+    e->have_model = e->have_tips = e->have_pi = true;
+    e->theta_valid = false;
     return IQGPU_OK;
 }
 

@@ -21,14 +21,16 @@ namespace iqg {
 __global__ void k_partial_info_mixed(const OpDev *__restrict__ ops, float *__restrict__ opmats, long long op_stride,
                                      const double *__restrict__ evec, const double *__restrict__ inv,
                                      const double *__restrict__ eval, const double *__restrict__ rates,
-                                     const double *__restrict__ tip_lh, int n, int npad, int C, int S) {
+                                     const double *__restrict__ tip_lh, int n, int npad, int C, int S, int nmix,
+                                     int cpc) {
     const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
     const OpDev op = ops[k];
     const double len = op.len[ch];
+    const long long nn = (long long)n * n;
     __shared__ double sexp[kMaxCat * kMaxStates];
     for (int t = threadIdx.x; t < C * n; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        sexp[t] = exp(eval[i] * (rates[c] * len));
+        sexp[t] = exp(eval[(c / cpc) * n + i] * (rates[c] * len));
     }
     __syncthreads();
     float *base = opmats + (long long)k * op_stride;
@@ -43,21 +45,23 @@ __global__ void k_partial_info_mixed(const OpDev *__restrict__ ops, float *__res
             // P_c[x][y] = sum_i U[x][i] exp(lambda_i r_c t) U^-1[i][y]
             const int c = (int)(t / ((long long)n * npad)), r = (int)(t % ((long long)n * npad));
             const int x = r / npad, y = r % npad;
+            const double *U = evec + (c / cpc) * nn, *Ui = inv + (c / cpc) * nn;
             double acc = 0.0;
             if (y < n)
-                for (int i = 0; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], inv[i * n + y], acc);
+                for (int i = 0; i < n; i++) acc = fma(U[x * n + i] * sexp[c * n + i], Ui[i * n + y], acc);
             Pm[t] = (float)acc;
         } else {
             // leaf table[s][c][x] = (P_c . tipvec_s)[x] = sum_i U[x][i] exp(.) tip_lh[s][i]
             const long long u = t - nP;
             const int s = (int)(u / ((long long)C * npad)), r = (int)(u % ((long long)C * npad));
-            const int c = r / npad, x = r % npad;
+            const int c = r / npad, x = r % npad, m = c / cpc;
+            const double *U = evec + m * nn, *tv = tip_lh + ((long long)s * nmix + m) * n;
             double acc = 0.0;
             if (x < n) {
                 if (s == S) {
                     acc = 1.0;  // unknown state: P . 1 = 1
                 } else {
-                    for (int i = 0; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], tip_lh[s * n + i], acc);
+                    for (int i = 0; i < n; i++) acc = fma(U[x * n + i] * sexp[c * n + i], tv[i], acc);
                 }
             }
             tab[u] = (float)acc;
@@ -99,7 +103,7 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
                                                          const double *__restrict__ rates,
                                                          const float *__restrict__ ivhl,
                                                          const float *__restrict__ tiphl, int n, int npad, int C,
-                                                         int S, int unit_tips) {
+                                                         int S, int unit_tips, int nmix, int cpc) {
     __shared__ float ue_h[kPiRows * kMaxStates], ue_l[kPiRows * kMaxStates];
     __shared__ float s_p[kPiRows * kMaxStates];  // this block's rows of P(t), for unit tip vectors
     __shared__ double s_exp[kMaxStates];
@@ -108,14 +112,15 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
     const int child = ch ? ops[k].child[1] : ops[k].child[0];
     const double len = ch ? ops[k].len[1] : ops[k].len[0];
     const bool tip = child < 0;
-    const int nn = n * n;
+    const int nn = n * n, m = c / cpc;  // mixture class of category c
     const double rl = rates[c] * len;
+    ivhl += (long long)m * 2 * nn;  // this class's U^-1 split: [hi nn][lo nn]
     // n FP64 exponentials per CTA, then this block's rows of U diag(exp)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s_exp[i] = exp(eval[i] * rl);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_exp[i] = exp(eval[m * n + i] * rl);
     __syncthreads();
     for (int t = threadIdx.x; t < kPiRows * n; t += blockDim.x) {
         const int xr = t / n, i = t % n, x = x0 + xr;
-        if (x < n) df_split(evec[x * n + i] * s_exp[i], ue_h[xr * n + i], ue_l[xr * n + i]);
+        if (x < n) df_split(evec[(long long)m * nn + x * n + i] * s_exp[i], ue_h[xr * n + i], ue_l[xr * n + i]);
     }
     __syncthreads();
     float *base = opmats + (long long)k * op_stride;
@@ -137,7 +142,7 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
     __syncthreads();  // s_p complete
     // leaf table[s][c][x] = sum_i (U e)[x][i] tip_lh[s][i]; the unknown state gives 1
     const long long TB = (long long)(S + 1) * C * npad;
-    const int ts = (S + 1) * n;  // floats of one half of tiphl
+    const int ts = (S + 1) * nmix * n;  // floats of one half of tiphl ([state][class][i])
     float *tab = base + 2 * PM + ch * TB;
     for (int u = threadIdx.x; u < (S + 1) * kPiRows; u += blockDim.x) {
         const int st = u / kPiRows, xr = u % kPiRows, x = x0 + xr;
@@ -150,9 +155,10 @@ __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict
                 v = s_p[xr * npad + st];
             } else {
                 float sh = 0.f, sl = 0.f;
+                const int tb = (st * nmix + m) * n;
                 for (int i = 0; i < n; i++)
-                    df_mac(ue_h[xr * n + i], ue_l[xr * n + i], __ldg(tiphl + st * n + i),
-                           __ldg(tiphl + ts + st * n + i), sh, sl);
+                    df_mac(ue_h[xr * n + i], ue_l[xr * n + i], __ldg(tiphl + tb + i), __ldg(tiphl + ts + tb + i), sh,
+                           sl);
                 v = __fadd_rn(sh, sl);
             }
         }
@@ -169,7 +175,7 @@ __global__ void __launch_bounds__(kTPB) k_derv_mixed(const MixBufParams P) {
     const int n = P.n, C = P.ncat, B = n * C;
     for (int t = threadIdx.x; t < B; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        const double cof = P.eval[i] * P.rates[c];
+        const double cof = P.eval[(c / P.cpc) * n + i] * P.rates[c];
         const double val = exp(cof * P.len) * P.props[c];
         const double val1 = cof * val;
         v0[t] = val;
@@ -213,7 +219,7 @@ __global__ void __launch_bounds__(kTPB) k_from_buffer_mixed(const MixBufParams P
     const int n = P.n, C = P.ncat, B = n * C;
     for (int t = threadIdx.x; t < B; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        v0[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+        v0[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
     }
     __syncthreads();
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -254,6 +260,8 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
     P.inv32 = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
     P.pi = e->d_pi;
     P.tip_lh = e->d_tip;
+    P.nmix = e->nmix;
+    P.cpc = e->cpc;
     P.freq = e->d_freq;
     P.invar = e->d_invar;
     P.eval = e->d_eval;
@@ -281,14 +289,15 @@ int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
         const int rb = (e->npad + kPiRows - 1) / kPiRows;
         k_partial_info_df<<<dim3(nops_with_branch, 2, e->C * rb), 256, 0, e->st>>>(
             e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_eval, e->d_rates, e->d_ivhl, e->d_tiphl, e->n,
-            e->npad, e->C, e->S, e->unit_tips ? 1 : 0);
+            e->npad, e->C, e->S, e->unit_tips ? 1 : 0, e->nmix, e->cpc);
         e->launches++;
         return cuda_fail(cudaGetLastError(), "partial_info_df");
     }
     const int Z = e->n > 20 ? 32 : 4;
     dim3 grid(nops_with_branch, 2, Z);
     k_partial_info_mixed<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats32, e->op_stride32, e->d_evec, e->d_inv,
-                                                   e->d_eval, e->d_rates, e->d_tip, e->n, e->npad, e->C, e->S);
+                                                   e->d_eval, e->d_rates, e->d_tip, e->n, e->npad, e->C, e->S,
+                                                   e->nmix, e->cpc);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "partial_info_mixed");
 }
@@ -297,6 +306,7 @@ static MixBufParams mixbuf_params(iqgpu_engine *e, double len) {
     MixBufParams P;
     P.n = e->n;
     P.ncat = e->C;
+    P.cpc = e->cpc;
     P.nptn = (int)e->P;
     P.ldp = e->Ppad;
     P.theta = e->d_theta32;

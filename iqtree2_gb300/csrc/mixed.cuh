@@ -29,8 +29,9 @@ struct MixParams {
     int op_base;            // index of ops[0] in the uploaded list (the producer indices' origin)
     const float *opmats;    // per op: P child0 [C][n][npad], P child1, table child0 [S+1][C][npad], table child1
     const float *inv32;     // [n][npad] FP32 copy of U^-1
-    const double *pi;       // [n]
-    const double *tip_lh;   // eigen-space tip vectors (S+1)*n
+    const double *pi;       // [nmix][n]
+    const double *tip_lh;   // eigen-space tip vectors [S+1][nmix][n]
+    int nmix, cpc;          // mixture classes; category c uses class c / cpc (eval, U, U^-1, pi, tips)
     const double *freq, *invar;
     const double *eval, *rates, *props;
     const uint8_t *states;
@@ -88,6 +89,7 @@ constexpr int kStatusTimeout = 1;
 
 struct MixBufParams {
     int n, ncat, nptn;
+    int cpc;          // categories per mixture class (eval of category c: eval + (c / cpc) * n)
     long long ldp;
     const float *theta;
     const double *buffer_scale, *freq, *invar, *eval, *rates, *props;

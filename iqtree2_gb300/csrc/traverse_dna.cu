@@ -229,11 +229,12 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
         for (int c = 0; c < C; c++) {
             const float4 av = *reinterpret_cast<const float4 *>(pa + c * 32);
             const float4 bv = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + c * 32);
+            const int m = c / P.cpc;  // mixture class of this category
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const float4 u = ld4(P.inv32 + i * npad);
+                const float4 u = ld4(P.inv32 + (m * n + i) * npad);
                 const float ua = fmaf(u.x, av.x, fmaf(u.y, av.y, fmaf(u.z, av.z, u.w * av.w)));
-                const float ub = btip ? (float)__ldg(P.tip_lh + (long long)sb * n + i)
+                const float ub = btip ? (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i)
                                       : fmaf(u.x, bv.x, fmaf(u.y, bv.y, fmaf(u.z, bv.z, u.w * bv.w)));
                 th[(long long)(c * n + i) * ld] = ua * ub;
             }
@@ -257,10 +258,11 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
                     w[x] = fmaf(m.x, bv.x, fmaf(m.y, bv.y, fmaf(m.z, bv.z, m.w * bv.w)));
                 }
             }
-            float lc = (float)__ldg(P.pi) * av.x * w[0];
-            lc = fmaf((float)__ldg(P.pi + 1) * av.y, w[1], lc);
-            lc = fmaf((float)__ldg(P.pi + 2) * av.z, w[2], lc);
-            lc = fmaf((float)__ldg(P.pi + 3) * av.w, w[3], lc);
+            const double *pic = P.pi + (c / P.cpc) * n;  // root frequencies of this category's class
+            float lc = (float)__ldg(pic) * av.x * w[0];
+            lc = fmaf((float)__ldg(pic + 1) * av.y, w[1], lc);
+            lc = fmaf((float)__ldg(pic + 2) * av.z, w[2], lc);
+            lc = fmaf((float)__ldg(pic + 3) * av.w, w[3], lc);
             lh = fma((double)lc, P.props[c], lh);
         }
         lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));

@@ -206,8 +206,9 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
     if constexpr (EPI == EPI_THETA) {
         // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i in eigen space (tree/phylokernelnew.h:2048-2231)
         float *th = P.theta + p;
+        const int m = c / P.cpc;  // mixture class of this category
         for (int i = 0; i < n; i++) {
-            const float *urow = P.inv32 + (long long)i * npad;
+            const float *urow = P.inv32 + ((long long)m * n + i) * npad;
             float ua = 0.f, ub = 0.f;
 #pragma unroll
             for (int q = 0; q < nq; q++) {
@@ -215,7 +216,7 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
                 ua = dot4(u, achunk(q), ua);
                 if (!btip) ub = dot4(u, bchunk(q), ub);
             }
-            if (btip) ub = (float)__ldg(P.tip_lh + (long long)sb * n + i);
+            if (btip) ub = (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i);
             th[(long long)(c * n + i) * ld] = ua * ub;
         }
         if (c == 0) {
@@ -227,6 +228,7 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
         // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
         const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
         float lc = 0.f;
+        const double *pic = P.pi + (long long)(c / P.cpc) * n;  // root frequencies of this category's class
         auto term = [&](int x, float av) {
             float w;
             if (btip) {
@@ -238,7 +240,7 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
                 for (int q = 0; q < nq; q++) s0 = dot4(ld4(prow + 4 * q), bchunk(q), s0);
                 w = s0;
             }
-            lc = fmaf((float)__ldg(P.pi + x) * av, w, lc);
+            lc = fmaf((float)__ldg(pic + x) * av, w, lc);
         };
         if constexpr (NQ > 0) {  // x in order, a from the register chunks
 #pragma unroll
@@ -411,8 +413,9 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                 a4[q] = *reinterpret_cast<const float4 *>(pa + (c * NQ + q) * 32);
                 b4[q] = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(pb + (c * NQ + q) * 32);
             }
+            const int m = c / P.cpc;  // mixture class of this category
             for (int i = 0; i < n; i++) {
-                const float *urow = P.inv32 + (long long)i * npad;
+                const float *urow = P.inv32 + ((long long)m * n + i) * npad;
                 float ua = 0.f, ub = 0.f;
 #pragma unroll
                 for (int q = 0; q < NQ; q++) {
@@ -420,7 +423,7 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                     ua = dot4(u, a4[q], ua);
                     if (!btip) ub = dot4(u, b4[q], ub);
                 }
-                if (btip) ub = (float)__ldg(P.tip_lh + (long long)sb * n + i);
+                if (btip) ub = (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i);
                 th[(long long)(c * n + i) * ld] = ua * ub;
             }
         }
@@ -454,7 +457,7 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                             for (int qq = 0; qq < NQ; qq++) s0 = dot4(ld4(prow + 4 * qq), b4[qq], s0);
                             w = s0;
                         }
-                        lc = fmaf((float)__ldg(P.pi + x) * av[j], w, lc);
+                        lc = fmaf((float)__ldg(P.pi + (long long)(c / P.cpc) * n + x) * av[j], w, lc);
                     }
                 }
             }

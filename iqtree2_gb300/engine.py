@@ -95,6 +95,7 @@ def lib():
         "iqgpu_set_tile": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_asc": ([vp, ct.c_int32, ct.c_double], ct.c_int),
+        "iqgpu_set_mixture": ([vp, ct.c_int32] + [ct.c_void_p] * 7, ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
         "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
@@ -189,11 +190,20 @@ class Engine:
         return self.nstates * self.ncat
 
     def set_model(self, model):
+        if getattr(model, "nmix", 1) > 1:
+            return self.set_mixture(model)
         a = [np.ascontiguousarray(x, np.float64) for x in (model.eval, model.evec, model.inv_evec,
                                                             model.rates, model.props)]
         _check(lib().iqgpu_set_model(self.h, *[_dp(x) for x in a]))
         _check(lib().iqgpu_set_state_freq(self.h, _dp(np.ascontiguousarray(model.pi, np.float64))))
         _check(lib().iqgpu_set_tip_partials(self.h, _dp(np.ascontiguousarray(model.tip_lh, np.float64))))
+
+    def set_mixture(self, mix):
+        """A ``models.MixtureModel``: per-class eigen systems, profiles and tip
+        vectors, per-category rates and proportions (mixed-precision engines)."""
+        arrs = [np.ascontiguousarray(x, np.float64) for x in (mix.eval, mix.evec, mix.inv_evec, mix.rates,
+                                                               mix.props, mix.tip_lh, mix.pi)]
+        _check(lib().iqgpu_set_mixture(self.h, int(mix.nmix), *[_dp(x) for x in arrs]))
 
     def set_patterns(self, freq, invar=None):
         f = np.ascontiguousarray(freq, np.float64)

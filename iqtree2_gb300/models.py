@@ -302,3 +302,77 @@ def gy94_model(kappa, omega, pi, alpha, ncat=4):
     rates, props = gamma_rates_mean(alpha, ncat)
     pi = np.asarray(pi, dtype=np.float64)
     return SubstModel("GY94+G%d" % ncat, 61, normalize_rate_matrix(R, pi), pi, rates, props)
+
+
+@dataclass
+class MixtureModel:
+    """A mixture of reversible classes with +G rate categories, in the
+    engine's input form (``Engine.set_mixture``): category c = m * ncat_rate
+    + k is rate category k of class m (tree/phylokernelnew.h:908-918), its
+    proportion the class weight times the rate proportion
+    (tree/phylokernelnew.h:2327)."""
+
+    name: str
+    nstates: int
+    classes: list
+    weights: np.ndarray
+    rate_rates: np.ndarray
+    rate_props: np.ndarray
+
+    @property
+    def nmix(self):
+        return len(self.classes)
+
+    @property
+    def ncat(self):
+        return self.nmix * len(self.rate_rates)
+
+    @property
+    def state_unknown(self):
+        return STATE_UNKNOWN.get(self.nstates, self.nstates)
+
+    @property
+    def cat_class(self):
+        return np.repeat(np.arange(self.nmix), len(self.rate_rates))
+
+    @property
+    def rates(self):
+        return np.tile(self.rate_rates, self.nmix)
+
+    @property
+    def props(self):
+        return np.repeat(self.weights, len(self.rate_rates)) * np.tile(self.rate_props, self.nmix)
+
+    @property
+    def eval(self):
+        return np.stack([c.eval for c in self.classes])
+
+    @property
+    def evec(self):
+        return np.stack([c.evec for c in self.classes])
+
+    @property
+    def inv_evec(self):
+        return np.stack([c.inv_evec for c in self.classes])
+
+    @property
+    def pi(self):
+        return np.stack([c.pi for c in self.classes])
+
+    @property
+    def tip_lh(self):
+        """[STATE_UNKNOWN+1][nmix][n]: class m's eigen-space tip vectors U_m^-1 tipvec."""
+        return np.ascontiguousarray(np.stack([c.tip_lh for c in self.classes], axis=1))
+
+
+def profile_mixture(exch, pis, weights, alpha, ncat_rate=4):
+    """Profile mixture (the C10-C60 kind, ModelMixture): shared
+    exchangeabilities, one state-frequency profile per class, class weights
+    summing to 1, +G on top. Each class's Q is normalised to one substitution
+    per unit time under its own profile."""
+    n = len(pis[0])
+    classes = [SubstModel("class%d" % m, n, normalize_rate_matrix(exch, p), np.asarray(p, np.float64),
+                          np.ones(1), np.ones(1)) for m, p in enumerate(pis)]
+    rr, rp = gamma_rates_mean(alpha, ncat_rate)
+    w = np.asarray(weights, np.float64)
+    return MixtureModel("MIX%d+G%d" % (len(pis), ncat_rate), n, classes, w / w.sum(), rr, rp)

@@ -53,3 +53,49 @@ def tree_lnl(model, patterns, freq, edges, lengths, ntaxa, root=None, invar=None
         lh = lh + np.asarray(invar) * np.exp(-logs)
     plh = np.log(lh) + logs
     return float(plh @ freq), plh
+
+
+def tree_lnl_mixture(mix, patterns, freq, edges, lengths, ntaxa, root=None):
+    """Mixture-model pruning in the standard basis: category c uses the Q and
+    the root frequencies of its class; lh = sum_c p_c sum_x pi_m(c)[x] L_c[x]."""
+    nnode = 2 * ntaxa - 2
+    adj = [[] for _ in range(nnode)]
+    for k, (u, v) in enumerate(edges):
+        adj[u].append((v, k))
+        adj[v].append((u, k))
+    tips = np.asarray(__import__("iqtree2_gb300.models", fromlist=["x"]).tip_vectors(mix.nstates))
+    nptn = patterns.shape[1]
+    C, cls, rates = mix.ncat, mix.cat_class, mix.rates
+    Qs = [c.Q for c in mix.classes]
+
+    def partial(node, dad):
+        if node < ntaxa:
+            v = tips[patterns[node]]
+            return np.broadcast_to(v, (C, nptn, mix.nstates)).copy(), np.zeros(nptn)
+        out = np.ones((C, nptn, mix.nstates))
+        logs = np.zeros(nptn)
+        for (ch, k) in adj[node]:
+            if ch == dad:
+                continue
+            cp, cl = partial(ch, node)
+            for c in range(C):
+                P = expm(Qs[cls[c]] * rates[c] * lengths[k])
+                out[c] *= cp[c] @ P.T
+            logs += cl
+        mx = out.max(axis=(0, 2))
+        mx = np.where(mx > 0, mx, 1.0)
+        out /= mx[None, :, None]
+        return out, logs + np.log(mx)
+
+    r = ntaxa if root is None else root
+    out = np.ones((C, nptn, mix.nstates))
+    logs = np.zeros(nptn)
+    for (ch, k) in adj[r]:
+        cp, cl = partial(ch, r)
+        for c in range(C):
+            P = expm(Qs[cls[c]] * rates[c] * lengths[k])
+            out[c] *= cp[c] @ P.T
+        logs += cl
+    lh = np.einsum("cpx,cx,c->p", out, mix.pi[cls], mix.props)
+    plh = np.log(lh) + logs
+    return float(plh @ freq), plh

@@ -187,3 +187,71 @@ def test_asc_refused_by_batched_paths():
         engine.Group([eng])
     with pytest.raises(engine.EngineError):
         eng.set_asc(99, nsite)  # more constant patterns than states
+
+
+def _mixture(data, nclass, ncat_rate, seed):
+    rng = np.random.default_rng(seed)
+    if data == "dna":
+        ds = simulate.dna_gtr_dataset(20, 1500, 63)
+        R = rng.uniform(0.5, 3.0, size=(4, 4))
+        R = (R + R.T) / 2
+        n = 4
+    else:
+        ds = simulate.protein_lg_dataset(16, 800, 64)
+        R, _ = models.lg_exchangeabilities()
+        n = 20
+    pis = [rng.dirichlet(np.full(n, 3.0)) for _ in range(nclass)]
+    w = rng.uniform(0.5, 1.5, size=nclass)
+    return ds, models.profile_mixture(R, pis, w, 0.6, ncat_rate)
+
+
+@pytest.mark.parametrize("data,precision,nclass,ncat_rate", [("dna", engine.F32, 2, 2), ("dna", engine.F32, 3, 2),
+                                                             ("protein", engine.F32, 3, 2),
+                                                             ("protein", engine.TF32X3, 3, 2),
+                                                             ("protein", engine.TF32X3, 4, 1)])
+def test_mixture_lnl_and_derivatives(data, precision, nclass, ncat_rate):
+    """Profile mixtures on the mixed path (4-state kernel for 2 x 2
+    categories, the generic CUDA-core and tensor-core kernels otherwise, one
+    fused mix-rate case): lnL and pattern lnL against the independent numpy
+    mixture pruning (1e-6 relative), the derivatives against its central
+    differences, the lnL from the theta buffer against it."""
+    import stdbasis
+    ds, mix = _mixture(data, nclass, ncat_rate, 70 + nclass)
+    want, pwant = stdbasis.tree_lnl_mixture(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
+    t = engine.GpuTree(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=precision)
+    lg, plh = t.compute_likelihood(want_pattern_lh=True)
+    assert rel(lg, want) < 1e-6, (lg, want)
+    np.testing.assert_allclose(plh, pwant, atol=1e-4)
+
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, mix.nstates, mix.ncat, ds.ntaxa, mix.state_unknown, topo.nslots, precision=precision,
+                        max_ops=topo.nslots)
+    eng.set_model(mix)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    k = next(i for i, e in enumerate(ds.edges) if min(e) >= ds.ntaxa)
+    n1, n2 = map(int, ds.edges[k])
+    ops = topo.ops_for(n1, n2, set()) + topo.ops_for(n2, n1, set())
+    a, b = topo.ref(n1, n2), topo.ref(n2, n1)
+
+    def lnl_at(x):
+        lens = ds.lengths.copy()
+        lens[k] = x
+        return stdbasis.tree_lnl_mixture(mix, ds.patterns, ds.freq, ds.edges, lens, ds.ntaxa)[0]
+    h = 1e-5
+    for i, x in enumerate((0.05, 0.3)):
+        df, ddf = eng.likelihood_derv(ops if i == 0 else [], a, b, x, theta_computed=i > 0)
+        l0, lp, lm = lnl_at(x), lnl_at(x + h), lnl_at(x - h)
+        fd1, fd2 = (lp - lm) / (2 * h), (lp - 2 * l0 + lm) / h ** 2
+        floor = 1e-5 * float(ds.freq.sum())
+        assert abs(df - fd1) <= 1e-4 * abs(fd1) + floor, (df, fd1)
+        assert abs(ddf - fd2) <= 1e-2 * abs(fd2) + floor, (ddf, fd2)
+        assert rel(eng.lnl_from_buffer(x), l0) < 1e-6
+
+
+def test_mixture_refused_in_fp64():
+    ds, mix = _mixture("dna", 2, 2, 5)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, 4, mix.ncat, ds.ntaxa, mix.state_unknown, topo.nslots, max_ops=topo.nslots)
+    with pytest.raises(engine.EngineError):
+        eng.set_model(mix)

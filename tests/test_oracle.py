@@ -178,3 +178,22 @@ def test_asc_lewis_matches_standard_basis_and_finite_differences(oracle_mod):
     h = 1e-5
     assert abs(df - (lnl(t0 + h) - lnl(t0 - h)) / (2 * h)) < 1e-5 * max(1.0, abs(df))
     assert abs(ddf - (lnl(t0 + h) - 2 * lnl(t0) + lnl(t0 - h)) / h ** 2) < 1e-3 * max(1.0, abs(ddf))
+
+
+def test_mixture_reference_one_class_and_root_invariance():
+    """The numpy mixture pruning the mixture GPU tests compare with: one class
+    equals the plain-model pruning; the lnL does not depend on the root."""
+    from iqtree2_gb300 import models, simulate
+    ds = simulate.dna_gtr_dataset(9, 300, 77)
+    m = ds.model
+    R = np.ones((4, 4))
+    one = models.profile_mixture(R, [m.pi], [1.0], 0.8, 4)
+    plain = models.SubstModel("x", 4, one.classes[0].Q, m.pi, one.rates, one.props)
+    a, _ = stdbasis.tree_lnl_mixture(one, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
+    b, _ = stdbasis.tree_lnl(plain, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
+    assert rel(a, b) < 1e-12
+    rng = np.random.default_rng(3)
+    mix = models.profile_mixture(R, [rng.dirichlet(np.ones(4) * 2) for _ in range(3)], [0.2, 0.5, 0.3], 0.5, 2)
+    l1, _ = stdbasis.tree_lnl_mixture(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
+    l2, _ = stdbasis.tree_lnl_mixture(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa, root=ds.ntaxa + 3)
+    assert rel(l1, l2) < 1e-10
