@@ -207,17 +207,45 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
         // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i in eigen space (tree/phylokernelnew.h:2048-2231)
         float *th = P.theta + p;
         const int m = c / P.cpc;  // mixture class of this category
-        for (int i = 0; i < n; i++) {
-            const float *urow = P.inv32 + ((long long)m * n + i) * npad;
-            float ua = 0.f, ub = 0.f;
+        if constexpr (NQ > 0) {
+            for (int i = 0; i < n; i++) {
+                const float *urow = P.inv32 + ((long long)m * n + i) * npad;
+                float ua = 0.f, ub = 0.f;
 #pragma unroll
-            for (int q = 0; q < nq; q++) {
-                const float4 u = ld4(urow + 4 * q);
-                ua = dot4(u, achunk(q), ua);
-                if (!btip) ub = dot4(u, bchunk(q), ub);
+                for (int q = 0; q < nq; q++) {
+                    const float4 u = ld4(urow + 4 * q);
+                    ua = dot4(u, achunk(q), ua);
+                    if (!btip) ub = dot4(u, bchunk(q), ub);
+                }
+                if (btip) ub = (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i);
+                th[(long long)(c * n + i) * ld] = ua * ub;
             }
-            if (btip) ub = (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i);
-            th[(long long)(c * n + i) * ld] = ua * ub;
+        } else {  // 16 rows at a time: each chunk of a and b read once per block (same order per row)
+            for (int i0 = 0; i0 < n; i0 += 16) {
+                float ua[16], ub[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) ua[j] = ub[j] = 0.f;
+                for (int q = 0; q < nq; q++) {
+                    const float4 a4 = achunk(q);
+                    const float4 b4 = btip ? make_float4(0.f, 0.f, 0.f, 0.f) : bchunk(q);
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        if (i0 + j < n) {
+                            const float4 u = ld4(P.inv32 + ((long long)m * n + i0 + j) * npad + 4 * q);
+                            ua[j] = dot4(u, a4, ua[j]);
+                            if (!btip) ub[j] = dot4(u, b4, ub[j]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int i = i0 + j;
+                    if (i < n) {
+                        const float vb = btip ? (float)__ldg(P.tip_lh + ((long long)sb * P.nmix + m) * n + i) : ub[j];
+                        th[(long long)(c * n + i) * ld] = ua[j] * vb;
+                    }
+                }
+            }
         }
         if (c == 0) {
             const int ea = P.expo[(long long)P.a * ld + p];
@@ -250,8 +278,30 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
                 for (int j = 0; j < 4; j++)
                     if (4 * q + j < n) term(4 * q + j, av[j]);
             }
-        } else {
-            for (int x = 0; x < n; x++) term(x, pa[(x >> 2) * 32 + (x & 3)]);
+        } else {  // 16 states at a time: each chunk of b read once per block of x (same order per x)
+            for (int x0 = 0; x0 < n; x0 += 16) {
+                float w16[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) w16[j] = 0.f;
+                if (btip) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (x0 + j < n) w16[j] = __ldg(base + 2 * PM + (long long)sb * C * npad + c * npad + x0 + j);
+                } else {
+                    for (int q = 0; q < nq; q++) {
+                        const float4 b4 = *reinterpret_cast<const float4 *>(pb + q * 32);
+#pragma unroll
+                        for (int j = 0; j < 16; j++)
+                            if (x0 + j < n)
+                                w16[j] = dot4(ld4(base + (long long)(c * n + x0 + j) * npad + 4 * q), b4, w16[j]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int x = x0 + j;
+                    if (x < n) lc = fmaf((float)__ldg(pic + x) * pa[(x >> 2) * 32 + (x & 3)], w16[j], lc);
+                }
+            }
         }
         s_lc[threadIdx.x] = lc;
         __syncthreads();
@@ -659,7 +709,8 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     const int grid = (int)(e->Ppad / TP);
     const size_t pm_bytes = (size_t)2 * e->C * e->n * e->npad * 4;  // one op's two P(t) blocks
     const int nbuf = pm_bytes * 2 <= 96 * 1024 ? 2 : 1;
-    const size_t smem = (P.nops > 0 ? nbuf : 1) * pm_bytes;
+    // an epilogue-only launch stages no P(t): no dynamic shared memory, full occupancy
+    const size_t smem = P.nops > 0 ? nbuf * pm_bytes : 0;
     auto kern = k_traverse_mixed<NQ, EPI>;
     if (smem > 48 * 1024) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -675,7 +726,7 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
 // every pattern tile to be resident in one wave.
 template <int NQ, int EPI>
 static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
-    const size_t smem = (size_t)2 * 2 * e->C * e->n * e->npad * 4;  // double-buffered P(t) of one op
+    const size_t smem = P.nops > 0 ? (size_t)2 * 2 * e->C * e->n * e->npad * 4 : 0;  // double-buffered P(t) of one op
     auto kern = k_chain_mixed<NQ, EPI>;
     cudaError_t err = cudaSuccess;
     if (smem > 48 * 1024) err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
