@@ -18,6 +18,7 @@ constexpr double kTwoPow256 = 1.157920892373161954235709850086879078532699846656
 
 constexpr int kTPB = 128;        // threads (= patterns) per CTA in the pattern-tile kernels
 constexpr int kMaxStates = 64;
+constexpr int kPairCounters = 8192;  // (op, tile) pairs of one category-split tensor-core level
 constexpr int kMaxCat = 16;
 
 // Device copy of one traversal entry plus the offset of its per-op matrices.
@@ -140,6 +141,7 @@ struct iqgpu_engine {
     int nmix, cpc;            // mixture classes; categories per class (category c belongs to class c / cpc)
     float *d_cmax;            // category-split levels: per (op, category, pattern) maxima
     size_t cmax_bytes;
+    unsigned *d_pair_cnt;     // category-split levels: arrivals per (op, tile) pair, re-armed to 0
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;

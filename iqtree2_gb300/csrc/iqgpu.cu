@@ -85,7 +85,7 @@ static Sizes sizes(const iqgpu_config *c) {
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
     // category-split tensor-core levels hold fewer than 4 pairs per resident CTA
     // (<= 4 per SM): nl * Ppad < 16 * SMs * 128 patterns, SMs <= 160
-    s.cmax = uses_tc(c) ? 16LL * 160 * 128 * C * 4 : 0;
+    s.cmax = uses_tc(c) ? 16LL * 160 * 128 * C * 4 + kPairCounters * 4 : 0;
     s.flow = is_mixed(c) ? (long long)(c->max_ops + 1) * (s.Ppad / 128) * 4 : 0;
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
@@ -150,7 +150,7 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
-                        e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl};
+                        e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl, e->d_pair_cnt};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -292,6 +292,8 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
             CKE(dalloc(e, &e->d_tcb, s.tcb));
             CKE(dalloc(e, &e->d_cmax, s.cmax));
             e->cmax_bytes = (size_t)s.cmax;
+            CKE(dalloc(e, &e->d_pair_cnt, kPairCounters * 4));
+            CKE(cudaMemsetAsync(e->d_pair_cnt, 0, kPairCounters * 4, e->st));
         }
     } else {
         CKE(dalloc(e, &e->d_part, s.part));
@@ -640,6 +642,7 @@ static int check_status(iqgpu_engine *e) {
     CK(cudaStreamSynchronize(e->st));
     if (*h_status != 0) {
         CK(cudaMemsetAsync(e->d_status, 0, 4, e->st));
+        if (e->d_pair_cnt) CK(cudaMemsetAsync(e->d_pair_cnt, 0, kPairCounters * 4, e->st));  // partial arrivals
         set_error("a device-side wait gave up (TMA copy not completed); results of that launch are invalid");
         return IQGPU_ERR_TIMEOUT;
     }

@@ -89,7 +89,7 @@ constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged i
 // tile blockIdx.x. Level: (tile, op) pairs of one level, strided over the
 // grid, tiles of the same op adjacent (their B operands share L2 lines).
 // Category-split (csplit): (tile, op, category) triples, the categories of a
-// pair on adjacent CTAs; the per-pattern rescale then waits for k_tc_fixup.
+// pair on adjacent CTAs; the last of them to finish applies the rescale.
 __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc,
                                           bool csplit = false) {
     const MixParams &P = T.M;
@@ -453,12 +453,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 // gives up raises the shared abort flag and the status word.
 // csplit: items are (tile, op, category) triples (narrow levels: ncat times
 // the parallelism); an item stores its category's products unscaled and the
-// category's per-pattern maximum in cmax[(op - op0) * ncat + c][pattern], and
-// k_tc_fixup applies the rescale and writes the exponents afterwards.
+// category's per-pattern maximum in cmax[(op - op0) * ncat + c][pattern]; the
+// item that completes a (tile, op) pair applies the rescale and writes the
+// exponents.
 template <int NP, int NSTAGE, bool BF, bool CSPLIT>
 __global__ void __launch_bounds__(kTcRows + 32, 4)
     k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl,
-                     float *__restrict__ cmax_out) {
+                     float *__restrict__ cmax_out, unsigned *__restrict__ pair_cnt) {
     constexpr bool csplit = CSPLIT;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
@@ -478,6 +479,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     extern __shared__ __align__(128) unsigned char tc_smem_raw[];
     __shared__ unsigned long long full[NSTAGE], conv[NSTAGE], mmab[NSTAGE], ebar[2];
     __shared__ unsigned tmem_base_s, epi_done, abort_flag;
+    __shared__ bool s_last;
     __shared__ int4 opc[kTcOpCache];
     unsigned char *const tc_smem = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
     auto slot_at = [&](int s) { return tc_smem + s * T.slot_bytes; };
@@ -678,8 +680,46 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                 abort = true;
                 break;
             }
-            if (csplit) {  // the rescale and the exponent wait for all categories (k_tc_fixup)
+            if constexpr (CSPLIT) {
+                // The rescale and the exponent need every category's maximum: the
+                // item that completes its (tile, op) pair applies them (last-arriver
+                // pattern: fences and one counter per pair, no waiting).
+                const long long pair = (long long)(it.k - op0) * T.ntiles + it.tile;
                 cmax_out[((long long)(it.k - op0) * C + it.cat) * ld + p] = cmax;
+                __threadfence();  // this thread's products and maximum are visible device-wide
+                bar_sync_part(kTcRows);
+                if (r == 0) s_last = atomicAdd(pair_cnt + pair, 1u) == (unsigned)(C - 1);
+                bar_sync_part(kTcRows);
+                if (s_last) {
+                    __threadfence();
+                    float mx = 0.f;
+                    for (int cc = 0; cc < C; cc++)
+                        mx = fmaxf(mx, __ldcg(cmax_out + ((long long)(it.k - op0) * C + cc) * ld + p));
+                    int sh = 0;
+                    if (mx < kMixThreshold && mx > 0.f) {
+                        int ex;
+                        frexpf(mx, &ex);
+                        sh = 1 - ex;
+                    }
+                    // rows that need the rescale, one warp-wide pass per row (lane q: chunks q, q + 32, ...)
+                    const int lane = r & 31;
+                    unsigned todo = __ballot_sync(0xffffffffu, sh != 0);
+                    while (todo) {
+                        const int src = __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        const int shs = __shfl_sync(0xffffffffu, sh, src);
+                        const long long ps = p - lane + src;
+                        const float mul = __int_as_float((127 + shs) << 23);
+                        float *row = dad + (ps >> 3) * (8LL * C * npad) + (ps & 7) * 4;
+                        for (int q = lane; q < C * kq; q += 32) {
+                            float4 v = __ldcg(reinterpret_cast<const float4 *>(row + q * 32));
+                            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                            *reinterpret_cast<float4 *>(row + q * 32) = v;
+                        }
+                    }
+                    P.expo[(long long)it.dad * ld + p] = e_in - sh;
+                    if (r == 0) pair_cnt[pair] = 0u;  // re-armed for the next level and evaluation
+                }
                 continue;
             }
             int sh = 0;
@@ -706,46 +746,6 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, 4 * NP);
-}
-
-// Per-pattern rescale and exponent of a level that ran as category-split
-// items: the maximum over the categories' maxima (exact, so the same value the
-// whole-pattern items find), the same exact power-of-two rescale (rare: it
-// re-reads the row) and exponent = children's exponents - shift.
-// 61-state partials fall below the threshold every few levels, so the rescale
-// is common there: the warp rescales its patterns' rows together (lane q takes
-// chunks q, q + 32, ...), one pattern after another.
-__global__ void __launch_bounds__(128) k_tc_fixup(const MixParams P, const int op0, const float *__restrict__ cmax) {
-    const int C = P.ncat, npad = P.npad, kq = npad >> 2;
-    const long long ld = P.ldp;
-    const long long p = (long long)blockIdx.x * 128 + threadIdx.x;
-    const int kr = blockIdx.y, lane = threadIdx.x & 31;
-    const OpDev op = P.ops[op0 + kr];
-    float mx = 0.f;
-    for (int c = 0; c < C; c++) mx = fmaxf(mx, cmax[((long long)kr * C + c) * ld + p]);
-    const int e_in = (op.child[0] >= 0 ? P.expo[(long long)op.child[0] * ld + p] : 0) +
-                     (op.child[1] >= 0 ? P.expo[(long long)op.child[1] * ld + p] : 0);
-    int sh = 0;
-    if (mx < kMixThreshold && mx > 0.f) {
-        int ex;
-        frexpf(mx, &ex);
-        sh = 1 - ex;
-    }
-    unsigned todo = __ballot_sync(0xffffffffu, sh != 0);
-    while (todo) {
-        const int src = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int shs = __shfl_sync(0xffffffffu, sh, src);
-        const long long ps = p - lane + src;
-        const float mul = __int_as_float((127 + shs) << 23);
-        float *row = P.part + (long long)op.dad_slot * P.slot_floats + (ps >> 3) * (8LL * C * npad) + (ps & 7) * 4;
-        for (int q = lane; q < C * kq; q += 32) {
-            float4 v = *reinterpret_cast<float4 *>(row + q * 32);
-            v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-            *reinterpret_cast<float4 *>(row + q * 32) = v;
-        }
-    }
-    P.expo[(long long)op.dad_slot * ld + p] = e_in - sh;
 }
 
 // ---------------------------------------------------------------------------
@@ -1300,24 +1300,18 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
             continue;
         }
         const long long items = (long long)T.ntiles * nl;
-        const bool cs = can_split && items < 4 * resident &&
+        const bool cs = can_split && items < 4 * resident && items <= kPairCounters &&
                         (size_t)nl * e->C * (size_t)e->Ppad * sizeof(float) <= e->cmax_bytes;
         const int grid = (int)std::min<long long>(items * (cs ? e->C : 1), resident);
         if (ws && cs)
-            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax);
+            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt);
         else if (ws)
-            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax);
+            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt);
         else
             kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
         e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
-        if (cs) {
-            k_tc_fixup<<<dim3((unsigned)(e->Ppad / kTcRows), nl), kTcRows, 0, e->st>>>(M, op0, e->d_cmax);
-            e->launches++;
-            err = cudaGetLastError();
-            if (err != cudaSuccess) return cuda_fail(err, "tc_fixup");
-        }
     }
     return IQGPU_OK;
 }
