@@ -51,6 +51,15 @@ WORKLOAD = WORKLOADS["protein"]
 METRIC = "pattern-node updates/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_PEAK_TFLOPS_MEASURED = 1.20  # FMA-chain probe on this machine's GB300 (all SMs)
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum, one pass, caches
+# kept warm between launches) of the traversal kernels of one full evaluation at
+# the workload's own size, from the captures summarised in profiles/ (the bench
+# does not run ncu itself); None where no capture was made.
+TRAFFIC_BYTES = {
+    "protein": (2579.8e6, "profiles/k_traverse_tc_ws_protein100x50k.md"),
+    "dna-large": (2219.6e6, "profiles/k_level_dna_dna200x100k.md"),
+    "codon": (418.7e6, "profiles/k_traverse_tc_ws_codon40x10k.md"),
+}
 
 
 def dataset():
@@ -388,7 +397,9 @@ def run_ours(args):
         "lnl": {"mixed": r["lnl"], "fp64": r64["lnl"] if r64 else None,
                 "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"]) if r64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
+                     "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": TRAFFIC_BYTES.get(args.workload, (None, None))[0],
+                     "traffic_source": TRAFFIC_BYTES.get(args.workload, (None, None))[1], "peak_source": peak_src,
                      "kernel": kernel_name(use_tc, m.nstates, tile), "algorithmic_bytes_per_launch": bmx,
                      "fp32_tflops": fmx / r["kern_avg_s"] / 1e12, "flops_per_launch": fmx,
                      "kernel_ms": r["kern_avg_s"] * 1e3},
