@@ -26,16 +26,28 @@
 
 namespace iqg {
 
+// (a0, a1) = (x0 * y0 + a0, x1 * y1 + a1) in one packed FP32 instruction
+// (fma.rn.f32x2, sm_100 and later): two IEEE round-to-nearest FMAs, the same
+// results as two fmaf calls at half the issue slots.
+__device__ __forceinline__ void fma2(float &a0, float &a1, float x0, float x1, float y0, float y1) {
+    unsigned long long x, y, a;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(x0), "f"(x1));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(y0), "f"(y1));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(a) : "l"(x), "l"(y));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a0), "=f"(a1) : "l"(a));
+}
+
+// Row of P(t) (shared memory) times the child's states: even and odd states
+// accumulate separately and are added at the end.
 template <int NQ>
 __device__ __forceinline__ float row_dot_s(const float *prow, const float4 (&v)[NQ]) {
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
         const float4 m = *reinterpret_cast<const float4 *>(prow + 4 * q);
-        a0 = fmaf(m.x, v[q].x, a0);
-        a1 = fmaf(m.y, v[q].y, a1);
-        a0 = fmaf(m.z, v[q].z, a0);
-        a1 = fmaf(m.w, v[q].w, a1);
+        fma2(a0, a1, m.x, m.y, v[q].x, v[q].y);
+        fma2(a0, a1, m.z, m.w, v[q].z, v[q].w);
     }
     return a0 + a1;
 }
