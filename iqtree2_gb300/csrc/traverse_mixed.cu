@@ -338,24 +338,28 @@ __device__ __forceinline__ void mixed_epilogue(const MixParams &P, int c, int pl
     }
 }
 
-// Chain form of the fused schedule for up to kChainCat categories: one thread
-// per pattern with all of its categories (the fused kernel above uses one per
-// (pattern, category)), so that a traversal tail of one-op levels, whose ops
-// depend on each other one after the other, runs with every pattern of the
-// alignment resident at once instead of in several waves that repeat the
-// whole chain. The next category's children are requested while the current
-// one is computed; the outputs are stored as computed and, in the uncommon
-// case that the pattern needs the rescale, re-read and scaled (the register
-// file holds one wave of patterns only without a copy of all outputs). Same
-// arithmetic as mixed_op / mixed_epilogue
-// (row_dot_s, products, maximum, power-of-two rescale; the lnL terms in the
-// same order), so the results are bit-identical to k_traverse_mixed.
+// Chain form of the fused schedule for up to kChainCat categories: two lanes
+// per pattern, lane h of the pair (half-warps h = 0, 1 over the same 16
+// patterns) taking categories h and h + 2. A traversal tail of one-op levels,
+// whose ops depend on each other one after the other, then runs with every
+// pattern of the alignment resident at once instead of in several waves that
+// repeat the whole chain, on twice the warps of one thread per pattern. The
+// two half-warps read P(t) rows of adjacent categories, 400 floats apart for
+// 20 states (opposite bank halves), so the row reads stay one wavefront. Each
+// category's children are loaded when it starts (96 registers, no spills:
+// the other warps cover the latency); the outputs are stored as
+// computed and, in the uncommon case that the pattern needs the rescale,
+// re-read and scaled. Same arithmetic as mixed_op / mixed_epilogue
+// (row_dot_s, products, maximum, power-of-two rescale; the lnL terms summed
+// over the categories in the same order), so the results are bit-identical
+// to k_traverse_mixed.
 constexpr int kChainCat = 4;
 template <int NQ, int EPI>
-__global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
+__global__ void __launch_bounds__(128, 5) k_chain_mixed(const MixParams P) {
     const int C = P.ncat, n = P.n, npad = P.npad, S = P.state_unknown;
     const long long ld = P.ldp;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = (threadIdx.x >> 4) & 1;  // category parity of this lane
+    const long long p = (long long)blockIdx.x * (blockDim.x >> 1) + (threadIdx.x >> 5) * 16 + (threadIdx.x & 15);
     const long long pbase = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;  // + (c * NQ + q) * 32
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(S + 1) * C * npad;
@@ -403,20 +407,17 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
         const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad;
         const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad;
         float *dad = P.part + (long long)op.dad_slot * P.slot_floats + pbase;
-        float4 lv[NQ], rv[NQ], nl[NQ], nr[NQ];
-        auto fetch = [&](int c, float4 (&a)[NQ], float4 (&b)[NQ]) {
-#pragma unroll
-            for (int q = 0; q < NQ; q++) {
-                if (lint) a[q] = *reinterpret_cast<const float4 *>(Lp + (c * NQ + q) * 32);
-                if (rint) b[q] = *reinterpret_cast<const float4 *>(Rp + (c * NQ + q) * 32);
-            }
-        };
-        fetch(0, lv, rv);
         float cmax = 0.f;
 #pragma unroll
-        for (int c = 0; c < kChainCat; c++) {
+        for (int i = 0; i < kChainCat / 2; i++) {
+            const int c = h + 2 * i;
             if (c < C) {
-                if (c + 1 < C) fetch(c + 1, nl, nr);
+                float4 lv[NQ], rv[NQ];
+#pragma unroll
+                for (int q = 0; q < NQ; q++) {
+                    if (lint) lv[q] = *reinterpret_cast<const float4 *>(Lp + (c * NQ + q) * 32);
+                    if (rint) rv[q] = *reinterpret_cast<const float4 *>(Rp + (c * NQ + q) * 32);
+                }
                 const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
 #pragma unroll
                 for (int q = 0; q < NQ; q++) {
@@ -435,27 +436,26 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                     }
                     *reinterpret_cast<float4 *>(dad + (c * NQ + q) * 32) = make_float4(o[0], o[1], o[2], o[3]);
                 }
-#pragma unroll
-                for (int q = 0; q < NQ; q++) {
-                    lv[q] = nl[q];
-                    rv[q] = nr[q];
-                }
             }
         }
+        cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, 16));  // the pair's maximum over all categories
         int sh = 0;
-        if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale of this thread's own stores
+        if (cmax < kMixThreshold && cmax > 0.f) {  // exact power-of-two rescale of this lane's own stores
             int ex;
             frexpf(cmax, &ex);
             sh = 1 - ex;
             const float mul = __int_as_float((127 + sh) << 23);
-            for (int q = 0; q < C * NQ; q++) {
-                float4 v = *reinterpret_cast<float4 *>(dad + q * 32);
-                v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-                *reinterpret_cast<float4 *>(dad + q * 32) = v;
-            }
+            for (int c = h; c < C; c += 2)
+                for (int q = 0; q < NQ; q++) {
+                    float4 v = *reinterpret_cast<float4 *>(dad + (c * NQ + q) * 32);
+                    v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                    *reinterpret_cast<float4 *>(dad + (c * NQ + q) * 32) = v;
+                }
         }
-        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
-        P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+        if (h == 0) {
+            const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+            P.expo[(long long)op.dad_slot * ld + p] = e - sh;
+        }
     }
     if constexpr (EPI == EPI_NONE) return;
 
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
     if constexpr (EPI == EPI_THETA) {
         // theta[c][i] = (U^-1 a_c)_i (U^-1 b_c)_i (tree/phylokernelnew.h:2048-2231)
         float *th = P.theta + p;
-        for (int c = 0; c < C; c++) {
+        for (int c = h; c < C; c += 2) {
             float4 a4[NQ], b4[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
@@ -489,12 +489,15 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                 th[(long long)(c * n + i) * ld] = ua * ub;
             }
         }
-        P.buffer_scale[p] = (double)(ea + eb) * kLn2;
+        if (h == 0) P.buffer_scale[p] = (double)(ea + eb) * kLn2;
     } else {
         // branch lnL: lh = sum_c p_c sum_x pi_x a[c][x] (P_c b)[x] (tree/phylokernelnew.h:2641-3223)
         const float *base = P.opmats + (long long)P.branch_op * P.op_stride;  // branch matrices, child 0 = b
-        double lh = 0.0;
-        for (int c = 0; c < C; c++) {
+        float lcv[kChainCat / 2] = {0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < kChainCat / 2; i++) {
+            const int c = h + 2 * i;
+            if (c >= C) continue;
             float4 a4[NQ], b4[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
@@ -523,17 +526,24 @@ __global__ void __launch_bounds__(128, 3) k_chain_mixed(const MixParams P) {
                     }
                 }
             }
-            lh = fma((double)lc, P.props[c], lh);
+            lcv[i] = lc;
         }
+        // lane 0 of the pair sums the categories in order 0, 1, 2, 3
+        const float o0 = __shfl_xor_sync(0xffffffffu, lcv[0], 16), o1 = __shfl_xor_sync(0xffffffffu, lcv[1], 16);
         double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
-        lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));
-        const double plh = log(lh) + (double)(ea + eb) * kLn2;
-        P.pattern_lh[p] = plh;
-        if (p < P.nptn) {
-            const double f = P.freq[p];
-            v[0] = plh * f;
-            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
-            v[2] = isfinite(plh) ? 0.0 : 1.0;
+        if (h == 0) {
+            const float lc_all[kChainCat] = {lcv[0], o0, lcv[1], o1};
+            double lh = 0.0;
+            for (int c = 0; c < C; c++) lh = fma((double)lc_all[c], P.props[c], lh);
+            lh = fabs(lh) + ldexp(P.invar[p], -(ea + eb));
+            const double plh = log(lh) + (double)(ea + eb) * kLn2;
+            P.pattern_lh[p] = plh;
+            if (p < P.nptn) {
+                const double f = P.freq[p];
+                v[0] = plh * f;
+                v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+                v[2] = isfinite(plh) ? 0.0 : 1.0;
+            }
         }
         mix_grid_reduce(v, P.red);
     }
@@ -733,9 +743,9 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     return cuda_fail(cudaGetLastError(), "traverse_mixed");
 }
 
-// Levels l0 .. of the uploaded list, one launch each.
-// The chain kernel: 128 patterns per CTA, or 64 when that is what it takes for
-// every pattern tile to be resident in one wave.
+// The chain kernel: two lanes per pattern, 64 patterns per 128-thread CTA, or
+// 32 per 64-thread CTA when that is what it takes for every pattern tile to be
+// resident in one wave.
 template <int NQ, int EPI>
 static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
     const size_t smem = P.nops > 0 ? (size_t)2 * 2 * e->C * e->n * e->npad * 4 : 0;  // double-buffered P(t) of one op
@@ -747,15 +757,16 @@ static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
     int tb = 128;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem) == cudaSuccess &&
-        e->Ppad / 128 > (long long)per_sm * sms &&
+        e->Ppad / 64 > (long long)per_sm * sms &&
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 64, smem) == cudaSuccess &&
-        e->Ppad / 64 <= (long long)per_sm * sms)
+        e->Ppad / 32 <= (long long)per_sm * sms)
         tb = 64;
-    kern<<<(unsigned)(e->Ppad / tb), tb, smem, e->st>>>(P);
+    kern<<<(unsigned)(e->Ppad / (tb / 2)), tb, smem, e->st>>>(P);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "chain_mixed");
 }
 
+// Levels l0 .. of the uploaded list, one launch each.
 template <int NQ>
 static int launch_levels_t(iqgpu_engine *e, const MixParams &P, int l0 = 0) {
     const int TP = mix_tile(e);
