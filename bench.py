@@ -359,14 +359,17 @@ def run_ours(args):
     value = updates_per_step * args.steps * world / (r["elapsed_ms"] / 1e3)
     bmx, fmx = algorithmic_cost(ops, ds.ntaxa, m.nstates, m.ncat, ds.nptn, mixed=True)
 
-    # end to end through the C ABI from host buffers: inputs copied each step, lnL read back
+    # end to end through the C ABI from pinned host buffers: inputs copied each
+    # step, lnL read back
     e2e_steps = max(2, min(args.steps, 10))
+    pinned = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (ds.patterns, ds.freq)]
+    h_patterns, h_freq = (t.numpy() for t in pinned)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         eng.set_model(m)
-        eng.set_patterns(ds.freq)
-        eng.set_tip_states(ds.patterns)
+        eng.set_patterns(h_freq)
+        eng.set_tip_states(h_patterns)
         lnl_e2e = eng.compute_likelihood(ops_arr, a, b, length)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     h2d = ds.patterns.nbytes + ds.freq.nbytes + sum(x.nbytes for x in (m.eval, m.evec, m.inv_evec, m.rates,

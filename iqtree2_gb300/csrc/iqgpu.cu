@@ -305,7 +305,7 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     CKE(dalloc(e, &e->d_bscale, e->Ppad * 8));
     CKE(dalloc(e, &e->d_plh, e->Ppad * 8));
     CKE(dalloc(e, &e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
-    CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at byte 32, flow ticket at 48
+    CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at 32, flow ticket at 48, state check at 56
     e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
     e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
     CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
@@ -476,17 +476,47 @@ int iqgpu_set_patterns(iqgpu_engine *e, const double *ptn_freq, const double *pt
     return IQGPU_OK;
 }
 
+// Sets *bad when any byte of the uploaded tip-state rows is above S (the
+// padding columns hold S): 16 bytes per thread, grid-stride.
+__global__ void k_check_states(const uint4 *__restrict__ st, long long n16, unsigned S, int *bad) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (long long)gridDim.x * blockDim.x) {
+        const uint4 v = st[i];
+        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+        unsigned over = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) over |= ((w[j] >> (8 * b)) & 0xffu) > S;
+        if (over) {
+            atomicOr(bad, 1);
+            return;
+        }
+    }
+}
+
 int iqgpu_set_tip_states(iqgpu_engine *e, const uint8_t *states) {
     if (!e || !states) { set_error("null argument"); return IQGPU_ERR_ARG; }
-    for (long long i = 0; i < (long long)e->cfg.ntaxa * e->P; i++)
-        if (states[i] > e->S) {
-            set_error("tip state above STATE_UNKNOWN");
-            return IQGPU_ERR_ARG;
-        }
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
+    e->have_states = false;
     CK(cudaMemcpy2D(e->d_states, (size_t)e->Ppad, states, (size_t)e->P, (size_t)e->P, (size_t)e->cfg.ntaxa,
                     cudaMemcpyHostToDevice));
+    // the range check runs on the uploaded copy (a byte loop over the host
+    // array would cost more than the whole likelihood evaluation)
+    int *bad = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 56);
+    CK(cudaMemsetAsync(bad, 0, 4, e->st));
+    const long long n16 = (long long)e->cfg.ntaxa * e->Ppad / 16;
+    k_check_states<<<(unsigned)std::min<long long>((n16 + 255) / 256, 4 * 152), 256, 0, e->st>>>(
+        reinterpret_cast<const uint4 *>(e->d_states), n16, (unsigned)e->S, bad);
+    e->launches++;
+    CK(cudaGetLastError());
+    int h_bad = 0;
+    CK(cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    if (h_bad) {
+        set_error("tip state above STATE_UNKNOWN");
+        return IQGPU_ERR_ARG;
+    }
     e->have_states = true;
     return IQGPU_OK;
 }

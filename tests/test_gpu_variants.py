@@ -255,3 +255,21 @@ def test_mixture_refused_in_fp64():
     eng = engine.Engine(ds.nptn, 4, mix.ncat, ds.ntaxa, mix.state_unknown, topo.nslots, max_ops=topo.nslots)
     with pytest.raises(engine.EngineError):
         eng.set_model(mix)
+
+
+@pytest.mark.parametrize("precision", [engine.F64, engine.TF32X3])
+def test_tip_states_out_of_range_rejected(precision):
+    """A tip state above STATE_UNKNOWN is an argument error (the range check
+    runs on the uploaded copy); the engine then refuses to compute until valid
+    states are set, and valid states give the same lnL as before."""
+    ds = simulate.protein_lg_dataset(12, 600, 63)
+    t = engine.GpuTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=precision)
+    l0 = t.compute_likelihood()
+    bad = ds.patterns.copy()
+    bad[5, bad.shape[1] - 1] = ds.model.state_unknown + 1
+    with pytest.raises(engine.EngineError, match="STATE_UNKNOWN"):
+        t.engine.set_tip_states(bad)
+    with pytest.raises(engine.EngineError):
+        t.compute_likelihood()
+    t.engine.set_tip_states(ds.patterns)
+    assert rel(t.compute_likelihood(), l0) < 1e-12
