@@ -84,13 +84,23 @@ typedef struct {
 #define IQGPU_FLAG_REF_TRIPLE_TAIL 1
 
 /* One TraversalInfo entry (tree/phylotree.h:320-333): compute the partial of
- * dad_slot from two children with their branch lengths. */
+ * dad_slot from two children with their branch lengths. flags is 0 for
+ * reversible models; with a non-reversible model (iqgpu_set_model_nonrev) it
+ * carries, per child, the reference's edge direction and root leaf
+ * (tree/phylokernelnew.h:932-963): TRANSPOSE uses P(t)^T for a child reached
+ * against the edge direction (child->direction == TOWARD_ROOT), ROOTLEAF makes
+ * a tip child the root leaf, whose leaf-table rows are P(t) times the root
+ * frequencies whatever its states (isRootLeaf). */
 typedef struct {
     int32_t dad_slot;
     int32_t child[2];
-    int32_t reserved;
+    int32_t flags;
     double len[2];
 } iqgpu_op;
+#define IQGPU_OP_TRANSPOSE0 1
+#define IQGPU_OP_TRANSPOSE1 2
+#define IQGPU_OP_ROOTLEAF0 4
+#define IQGPU_OP_ROOTLEAF1 8
 
 typedef struct iqgpu_engine iqgpu_engine;
 typedef struct iqgpu_tree iqgpu_tree;
@@ -178,6 +188,25 @@ int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
  * batched NNI entry point refuse mixtures (IQGPU_ERR_ARG). */
 int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const double *evec, const double *inv_evec,
                       const double *rates, const double *props, const double *tip_lh, const double *state_freq);
+/* Non-reversible model (ModelMarkov with is_reversible false: UNREST, NONREV,
+ * Lie-Markov; model/modelmarkov.cpp:463-505, 732-756) on the mixed-precision
+ * path. The partials stay in the standard basis (the reference's nonrev
+ * kernels, tree/phylokernelnonrev.h); P(r_c t) = Re(V diag(exp(lambda r_c t))
+ * V^-1) from the complex eigen system of the normalised rate matrix, each
+ * array given as real and imaginary parts: ceval [n], cevec and cinv_evec
+ * [n][n] row-major. tip_vec [STATE_UNKNOWN+1][n] are the standard-basis tip
+ * vectors (the unknown state's row all ones), root_freq [n] the root-leaf
+ * vector. The branch lnL and derivatives weigh the dad side by the state
+ * frequencies of iqgpu_set_state_freq: the stationary frequencies for an
+ * unrooted tree (tree/phylokernelnonrev.h:1117-1130), all ones for a rooted
+ * tree whose root leaf carries root_freq. Derivatives use r_c lambda and
+ * (r_c lambda)^2 on the same eigen system (Q P and Q^2 P,
+ * tree/phylokernelnonrev.h:628-660). FP64 engines, mixtures, +ASC and the
+ * batched NNI / group entry points refuse non-reversible models. */
+int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double *ceval_im, const double *cevec_re,
+                           const double *cevec_im, const double *cinv_re, const double *cinv_im,
+                           const double *rates, const double *props, const double *tip_vec,
+                           const double *root_freq);
 /* Copy a slot back in the reference layout: partial[ptn*B + c*n + x] in eigen
  * space (F64) or standard basis (mixed), and scale counts (NORM: nptn bytes,
  * SAFE: nptn*ncat bytes, pattern-major). Either output may be NULL. */

@@ -343,8 +343,8 @@ extern "C" int iqgpu_nni_batch(iqgpu_engine *e, const iqgpu_nni_candidate *cand,
         set_error("bad argument");
         return IQGPU_ERR_ARG;
     }
-    if (e->asc_n > 0 || e->nmix > 1) {
-        set_error("+ASC and mixture engines: evaluate NNI candidates with the per-branch entry points");
+    if (e->asc_n > 0 || e->nmix > 1 || e->nonrev) {
+        set_error("+ASC, mixture and non-reversible engines: evaluate NNI candidates with the per-branch entry points");
         return IQGPU_ERR_ARG;
     }
     iqgpu_config cfg;

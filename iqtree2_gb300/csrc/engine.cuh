@@ -28,7 +28,8 @@ struct OpDev {
     int32_t prod0;      // mixed engines: index (in the uploaded list) of the op writing child 0, or -1
     double len[2];
     long long mat_off;  // doubles into Engine::d_opmats
-    long long prod1;    // as prod0, for child 1
+    int32_t prod1;      // as prod0, for child 1
+    int32_t flags;      // IQGPU_OP_* (non-reversible models): transpose / root leaf per child
 };
 
 // Deterministic grid reduction: each CTA writes its partial sums, the last
@@ -117,6 +118,13 @@ struct iqgpu_engine {
     double h_inv[iqg::kMaxStates * iqg::kMaxStates];
     double h_tipv[iqg::kMaxStates * iqg::kMaxStates];  // rows of the n unambiguous states
     bool unit_tips;
+    // non-reversible model (mixed engines): complex eigen system of Q, root
+    // frequencies and standard-basis tip vectors in d_nr ([ceval re, im][cevec
+    // re, im][cinv re, im][root freq][tip vectors (S+1) x n]); d_nrmats holds
+    // prop * P, P', P'' of the evaluated branch ([3][C][n][npad] FP32)
+    bool nonrev;
+    double *d_nr;
+    float *d_nrmats;
     bool have_pi, tipstd_ready;
     int tile;                 // patterns per CTA of the mixed traversal (0 = default)
     bool level_sync;          // mixed traversal schedule: one launch per tree level
@@ -170,6 +178,9 @@ int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch);
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_mixed(iqgpu_engine *e, double len);
 int launch_from_buffer_mixed(iqgpu_engine *e, double len);
+// non-reversible models: branch lnL (derv false) or lnL and derivatives
+// (derv true) from the partials of the branch ends theta_a / theta_b
+int launch_branch_nonrev(iqgpu_engine *e, double len, bool derv);
 
 // tensor-core pattern-node update (traverse_tc.cu)
 int tc_np(int npad);  // N of the MMA: npad padded to 32 or 64

@@ -111,7 +111,10 @@ int iqgpu_group_create(iqgpu_engine *const *engines, int32_t n, iqgpu_group **ou
     for (int i = 0; i < n; i++) {
         if (!engines[i]) { set_error("null engine in group"); return IQGPU_ERR_ARG; }
         if (engines[i]->dev != engines[0]->dev) { set_error("group engines must share a device"); return IQGPU_ERR_ARG; }
-        if (engines[i]->asc_n > 0) { set_error("+ASC engines cannot join a group"); return IQGPU_ERR_ARG; }
+        if (engines[i]->asc_n > 0 || engines[i]->nonrev) {
+            set_error("+ASC and non-reversible engines cannot join a group");
+            return IQGPU_ERR_ARG;
+        }
         for (int j = 0; j < i; j++)
             if (engines[j] == engines[i]) { set_error("an engine appears twice in the group"); return IQGPU_ERR_ARG; }
     }

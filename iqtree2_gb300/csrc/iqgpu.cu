@@ -74,7 +74,8 @@ static Sizes sizes(const iqgpu_config *c) {
         s.opmats = ((long long)(c->max_ops + 1) * s.op_stride + C * n * npad) * 4;  // + U^-1 of each class
         s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double) +
                   (n >= 16 ? C * (2 * n * n + 2 * (S + 1) * n) * 4 : 0) +  // + the hi/lo split of U^-1 and tips
-                  (C - 1) * (n + 2 * n * n + (S + 2) * n) * 8;              // + the other classes' model arrays
+                  (C - 1) * (n + 2 * n * n + (S + 2) * n) * 8 +             // + the other classes' model arrays
+                  (3 * n + 4 * n * n + (S + 1) * n) * 8 + 3 * C * n * npad * 4;  // + non-reversible model data
     } else {
         s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
         s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
@@ -150,7 +151,8 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_invar, e->d_states, e->d_part, e->d_scale, e->d_ops, e->d_opmats,
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
-                        e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl, e->d_pair_cnt};
+                        e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl, e->d_pair_cnt,
+                        e->d_nr, e->d_nrmats};
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -310,6 +312,10 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
     CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
     CKE(dalloc(e, &e->d_asc, 3 * kMaxStates * 8));
+    if (is_mixed(cfg)) {
+        CKE(dalloc(e, &e->d_nr, (3 * e->n + 4LL * e->n * e->n + (long long)(S + 1) * e->n) * 8));
+        CKE(dalloc(e, &e->d_nrmats, 3LL * e->C * e->n * e->npad * 4));
+    }
     CKE(halloc(e, &e->h_ops, s.ops));
     CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
     CKE(halloc(e, &e->h_asc, 3 * kMaxStates * 8));
@@ -384,6 +390,10 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     }
     e->have_model = true;
     e->theta_valid = false;
+    if (e->nonrev) {  // back to a reversible model: its tip vectors must be set again
+        e->nonrev = false;
+        e->have_tips = false;
+    }
     if (e->nmix != 1) {  // back to one class: the class-indexed tip vectors must be set again
         e->nmix = 1;
         e->cpc = e->C;
@@ -437,8 +447,51 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
     std::memcpy(e->h_props, props, C * 8);
     e->nmix = nmix;
     e->cpc = (int)(C / K);
+    e->nonrev = false;
     e->unit_tips = unit;
     e->have_model = e->have_tips = e->have_pi = true;
+    e->theta_valid = false;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double *ceval_im, const double *cevec_re,
+                           const double *cevec_im, const double *cinv_re, const double *cinv_im,
+                           const double *rates, const double *props, const double *tip_vec,
+                           const double *root_freq) {
+    if (!e || !ceval_re || !ceval_im || !cevec_re || !cevec_im || !cinv_re || !cinv_im || !rates || !props ||
+        !tip_vec || !root_freq) {
+        set_error("null argument");
+        return IQGPU_ERR_ARG;
+    }
+    if (!is_mixed(&e->cfg)) {
+        set_error("non-reversible models run on the mixed-precision path (IQGPU_F32, IQGPU_TF32X3, IQGPU_BF16)");
+        return IQGPU_ERR_ARG;
+    }
+    if (e->asc_n > 0) { set_error("+ASC is not available with non-reversible models"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    const size_t n = e->n, nn = n * n, C = e->C, S1 = (size_t)e->S + 1;
+    // [ceval re, im][cevec re, im][cinv re, im][root freq][tip vectors]
+    std::vector<double> nr(3 * n + 4 * nn + S1 * n);
+    double *q = nr.data();
+    std::memcpy(q, ceval_re, n * 8); q += n;
+    std::memcpy(q, ceval_im, n * 8); q += n;
+    std::memcpy(q, cevec_re, nn * 8); q += nn;
+    std::memcpy(q, cevec_im, nn * 8); q += nn;
+    std::memcpy(q, cinv_re, nn * 8); q += nn;
+    std::memcpy(q, cinv_im, nn * 8); q += nn;
+    std::memcpy(q, root_freq, n * 8); q += n;
+    std::memcpy(q, tip_vec, S1 * n * 8);
+    CK(cudaMemcpy(e->d_nr, nr.data(), nr.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
+    std::memcpy(e->h_rates, rates, C * 8);
+    std::memcpy(e->h_props, props, C * 8);
+    e->nonrev = true;
+    e->nmix = 1;
+    e->cpc = (int)C;
+    e->unit_tips = false;
+    e->have_model = e->have_tips = true;
     e->theta_valid = false;
     return IQGPU_OK;
 }
@@ -455,6 +508,10 @@ int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq) {
 
 int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
     if (!e || !tip_lh) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    if (e->nonrev) {
+        set_error("a non-reversible model takes its tip vectors with iqgpu_set_model_nonrev");
+        return IQGPU_ERR_STATE;
+    }
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
     CK(cudaMemcpy(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice));
@@ -560,6 +617,13 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
             set_error("bad traversal entry " + std::to_string(k));
             return IQGPU_ERR_ARG;
         }
+        if (o.flags & ~(IQGPU_OP_TRANSPOSE0 | IQGPU_OP_TRANSPOSE1 | IQGPU_OP_ROOTLEAF0 | IQGPU_OP_ROOTLEAF1) ||
+            (o.flags && !e->nonrev) || ((o.flags & IQGPU_OP_ROOTLEAF0) && o.child[0] >= 0) ||
+            ((o.flags & IQGPU_OP_ROOTLEAF1) && o.child[1] >= 0)) {
+            set_error("bad flags in traversal entry " + std::to_string(k) +
+                      " (non-reversible models only; root-leaf flags on tip children only)");
+            return IQGPU_ERR_ARG;
+        }
     }
     // Mixed engines take the ops in tree-level order (a valid post-order: every
     // child is produced in a lower level), so that a level-synchronous launch
@@ -600,6 +664,7 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         d.len[1] = o.len[1];
         d.mat_off = (long long)i * e->op_stride;
         d.prod1 = (!writer.empty() && o.child[1] >= 0) ? writer[o.child[1]] : -1;
+        d.flags = o.flags;
         if (!writer.empty()) writer[o.dad_slot] = i;
     }
     int total = nops;
@@ -611,6 +676,7 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         d.len[0] = d.len[1] = len;
         d.mat_off = (long long)nops * e->op_stride;
         d.prod1 = -1;
+        d.flags = 0;
         total++;
     }
     CK(cudaMemcpyAsync(e->d_ops, e->h_ops, sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
@@ -759,12 +825,14 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
             return IQGPU_ERR_STATE;
         }
         if ((rc = upload_ops(e, ops, nops))) return rc;
-        if ((rc = traverse(e, nops, EPI_THETA, a, b, len))) return rc;
+        // non-reversible: no eigen-space theta; the derivative kernel reads the two ends
+        if ((rc = traverse(e, nops, e->nonrev ? EPI_NONE : EPI_THETA, a, b, len))) return rc;
         e->theta_valid = true;
         e->theta_a = a;
         e->theta_b = b;
     }
-    rc = is_mixed(&e->cfg) ? launch_derv_mixed(e, len) : launch_derv_f64(e, len);
+    rc = e->nonrev ? launch_branch_nonrev(e, len, true)
+                   : is_mixed(&e->cfg) ? launch_derv_mixed(e, len) : launch_derv_f64(e, len);
     if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;
     *df = e->h_red_out[0];
@@ -796,7 +864,8 @@ int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
     if (!lnl) { set_error("null output"); return IQGPU_ERR_ARG; }
     if (!e->theta_valid) { set_error("no theta buffer: call iqgpu_likelihood_derv first"); return IQGPU_ERR_STATE; }
     CK(cudaSetDevice(e->dev));
-    rc = is_mixed(&e->cfg) ? launch_from_buffer_mixed(e, len) : launch_from_buffer_f64(e, len);
+    rc = e->nonrev ? launch_branch_nonrev(e, len, false)
+                   : is_mixed(&e->cfg) ? launch_from_buffer_mixed(e, len) : launch_from_buffer_f64(e, len);
     if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;
     const double *r = e->h_red_out;
@@ -819,6 +888,10 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out) {
 }
 
 int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite) {
+    if (e && e->nonrev && nconst > 0) {
+        set_error("+ASC is not available with non-reversible models");
+        return IQGPU_ERR_ARG;
+    }
     if (!e || nconst < 0 || nconst > e->n || nconst >= e->P || !(nsite >= 0.0)) {
         set_error("+ASC: need 0 <= nconst <= nstates, nconst < patterns and nsite >= 0");
         return IQGPU_ERR_ARG;

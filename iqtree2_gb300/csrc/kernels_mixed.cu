@@ -240,6 +240,178 @@ __global__ void __launch_bounds__(kTPB) k_from_buffer_mixed(const MixBufParams P
 }
 
 // ---------------------------------------------------------------------------
+// non-reversible models (tree/phylokernelnonrev.h; P(t) from the complex eigen
+// system as ModelMarkov::computeTransMatrixNonrev, model/modelmarkov.cpp:480-490)
+// ---------------------------------------------------------------------------
+struct NonrevModel {
+    const double *er, *ei, *vr, *vi, *wr, *wi, *root, *tipv;  // ceval, cevec, cinv_evec (re, im), root freq, tip vectors
+};
+__host__ __device__ inline NonrevModel nonrev_model(const double *nr, int n, int S) {
+    const long long nn = (long long)n * n;
+    NonrevModel m;
+    m.er = nr;
+    m.ei = nr + n;
+    m.vr = nr + 2 * n;
+    m.vi = m.vr + nn;
+    m.wr = m.vi + nn;
+    m.wi = m.wr + nn;
+    m.root = m.wi + nn;
+    m.tipv = m.root + n;
+    (void)S;
+    return m;
+}
+
+// out[x][y] = Re(sum_i V[x][i] (lambda_i r)^k exp(lambda_i r t) V^-1[i][y]) for
+// x, y < n, FP64, into shared memory (n*n doubles); e holds 2n doubles of scratch.
+__device__ void nonrev_matrix(const NonrevModel &m, int n, double r, double t, int k, double *e, double *out) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double a = m.er[i] * r, b = m.ei[i] * r;  // lambda_i r
+        const double g = exp(a * t);
+        double re = g * cos(b * t), im = g * sin(b * t);
+        for (int j = 0; j < k; j++) {  // times (lambda_i r)^k
+            const double nr = re * a - im * b, ni = re * b + im * a;
+            re = nr;
+            im = ni;
+        }
+        e[i] = re;
+        e[n + i] = im;
+    }
+    __syncthreads();
+    for (int t2 = threadIdx.x; t2 < n * n; t2 += blockDim.x) {
+        const int x = t2 / n, y = t2 % n;
+        double acc = 0.0;
+        for (int i = 0; i < n; i++) {
+            // (V[x][i] * E_i) * W[i][y], real part
+            const double pr = m.vr[x * n + i] * e[i] - m.vi[x * n + i] * e[n + i];
+            const double pi = m.vr[x * n + i] * e[n + i] + m.vi[x * n + i] * e[i];
+            acc = fma(pr, m.wr[i * n + y], acc);
+            acc = fma(-pi, m.wi[i * n + y], acc);
+        }
+        out[t2] = acc;
+    }
+    __syncthreads();
+}
+
+// Per-op P(t) blocks and leaf tables for a non-reversible model, in the layout
+// of k_partial_info_mixed: one CTA per (op, child, category). A child reached
+// against the edge direction takes P^T; the root leaf's rows are P . root
+// frequencies for every state (tree/phylokernelnew.h:932-963).
+__global__ void __launch_bounds__(256) k_partial_info_nonrev(const OpDev *__restrict__ ops, float *__restrict__ opmats,
+                                                             long long op_stride, const double *__restrict__ nr,
+                                                             const double *__restrict__ rates, int n, int npad, int C,
+                                                             int S) {
+    extern __shared__ double nv_smem[];  // [n*n] P, [2n] exp scratch
+    const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z;
+    const OpDev op = ops[k];
+    const NonrevModel m = nonrev_model(nr, n, S);
+    double *Pd = nv_smem, *ex = nv_smem + n * n;
+    nonrev_matrix(m, n, rates[c], op.len[ch], 0, ex, Pd);
+    const bool tr = (op.flags >> ch) & 1, root = (op.flags >> (2 + ch)) & 1;
+    float *base = opmats + (long long)k * op_stride;
+    const long long PM = (long long)C * n * npad, TB = (long long)(S + 1) * C * npad;
+    float *Pm = base + ch * PM + (long long)c * n * npad;
+    for (int t = threadIdx.x; t < n * npad; t += blockDim.x) {
+        const int x = t / npad, y = t % npad;
+        Pm[t] = y < n ? (float)(tr ? Pd[y * n + x] : Pd[x * n + y]) : 0.f;
+    }
+    if (op.child[ch] >= 0) return;
+    float *tab = base + 2 * PM + ch * TB;
+    for (int t = threadIdx.x; t < (S + 1) * npad; t += blockDim.x) {
+        const int st = t / npad, x = t % npad;
+        double acc = 0.0;
+        if (x < n) {
+            const double *v = root ? m.root : m.tipv + (long long)st * n;
+            for (int y = 0; y < n; y++) acc = fma(tr ? Pd[y * n + x] : Pd[x * n + y], v[y], acc);
+        }
+        tab[(long long)st * C * npad + (long long)c * npad + x] = (float)acc;
+    }
+}
+
+// prop_c * (r_c lambda)^k-weighted P(r_c t) for k = 0, 1, 2 (P, dP/dt, d2P/dt2):
+// one CTA per (category, k), FP32 [3][C][n][npad]
+__global__ void __launch_bounds__(256) k_nonrev_branch_mats(float *__restrict__ out, const double *__restrict__ nr,
+                                                            const double *__restrict__ rates,
+                                                            const double *__restrict__ props, double len, int n,
+                                                            int npad, int C, int S) {
+    extern __shared__ double nv_smem[];
+    const int c = blockIdx.x, k = blockIdx.y;
+    double *Pd = nv_smem, *ex = nv_smem + n * n;
+    nonrev_matrix(nonrev_model(nr, n, S), n, rates[c], len, k, ex, Pd);
+    float *o = out + ((long long)k * C + c) * n * npad;
+    for (int t = threadIdx.x; t < n * npad; t += blockDim.x) {
+        const int x = t / npad, y = t % npad;
+        o[t] = y < n ? (float)(props[c] * Pd[x * n + y]) : 0.f;
+    }
+}
+
+// Branch lnL (and, with DERV, the Newton-Raphson sums) of a non-reversible
+// model straight from the two ends' partials: per pattern and category
+// lh_k = sum_x pi_x a[x] (M_k b)[x], M_k the branch matrices above
+// (tree/phylokernelnonrev.h:586-1056, 1062-1528); a is the dad side. FP32
+// products per category, FP64 sums over categories and patterns; the same
+// reductions as k_derv_mixed / k_from_buffer_mixed.
+template <bool DERV>
+__global__ void __launch_bounds__(kTPB) k_branch_nonrev(const MixParams P, const float *__restrict__ mats,
+                                                        const double *__restrict__ tipv) {
+    const int n = P.n, npad = P.npad, C = P.ncat;
+    const long long ld = P.ldp;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double r[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const long long pb = (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+        const float *pa = P.part + (long long)P.a * P.slot_floats + pb;
+        const bool btip = P.b < 0;
+        const float *pbp = btip ? nullptr : P.part + (long long)P.b * P.slot_floats + pb;
+        const int sb = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+        const int ea = P.expo[(long long)P.a * ld + p], eb = btip ? 0 : P.expo[(long long)P.b * ld + p];
+        double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+        for (int c = 0; c < C; c++) {
+            float bv[kMaxStates];
+            for (int y = 0; y < n; y++)
+                bv[y] = btip ? (float)tipv[(long long)sb * n + y] : pbp[(c * npad + (y & ~3)) * 8 + (y & 3)];
+            float l0 = 0.f, l1 = 0.f, l2 = 0.f;
+            for (int x = 0; x < n; x++) {
+                const float *m0 = mats + ((long long)c * n + x) * npad;
+                float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+                for (int y = 0; y < n; y++) {
+                    w0 = fmaf(__ldg(m0 + y), bv[y], w0);
+                    if (DERV) {
+                        w1 = fmaf(__ldg(m0 + (long long)C * n * npad + y), bv[y], w1);
+                        w2 = fmaf(__ldg(m0 + 2LL * C * n * npad + y), bv[y], w2);
+                    }
+                }
+                const float av = (float)__ldg(P.pi + x) * pa[(c * npad + (x & ~3)) * 8 + (x & 3)];
+                l0 = fmaf(av, w0, l0);
+                if (DERV) {
+                    l1 = fmaf(av, w1, l1);
+                    l2 = fmaf(av, w2, l2);
+                }
+            }
+            h0 += l0;
+            h1 += l1;
+            h2 += l2;
+        }
+        // the +I term is in true scale: bring it to the stored scale 2^-(ea+eb)
+        const double lh = fabs(h0) + ldexp(P.invar[p], -(ea + eb));
+        const double plh = log(lh) + (double)(ea + eb) * kLn2;
+        const double f = P.freq[p];
+        if (DERV) {
+            const double df_frac = h1 / lh, ddf_frac = h2 / lh;
+            const double tmp1 = df_frac * f, tmp2 = ddf_frac * f;
+            r[0] = tmp1;
+            r[1] = fma(-tmp1, df_frac, tmp2);
+            r[2] = plh * f;
+        } else {
+            P.pattern_lh[p] = plh;
+            r[0] = plh * f;
+            r[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+            r[2] = isfinite(plh) ? 0.0 : 1.0;
+        }
+    }
+    mix_grid_reduce(r, P.red);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 MixParams mix_params(iqgpu_engine *e, int nops) {
@@ -285,6 +457,13 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
 
 int launch_partial_info_mixed(iqgpu_engine *e, int nops_with_branch) {
     if (nops_with_branch <= 0) return IQGPU_OK;
+    if (e->nonrev) {
+        const size_t smem = ((size_t)e->n * e->n + 2 * e->n) * 8;
+        k_partial_info_nonrev<<<dim3(nops_with_branch, 2, e->C), 256, smem, e->st>>>(
+            e->d_ops, e->d_opmats32, e->op_stride32, e->d_nr, e->d_rates, e->n, e->npad, e->C, e->S);
+        e->launches++;
+        return cuda_fail(cudaGetLastError(), "partial_info_nonrev");
+    }
     if (e->n >= 16 && e->d_ivhl) {  // double-float products, one CTA per (op, child, category, 16 rows)
         const int rb = (e->npad + kPiRows - 1) / kPiRows;
         k_partial_info_df<<<dim3(nops_with_branch, 2, e->C * rb), 256, 0, e->st>>>(
@@ -330,6 +509,25 @@ int launch_derv_mixed(iqgpu_engine *e, double len) {
     k_derv_mixed<<<e->nblk, kTPB, 0, e->st>>>(mixbuf_params(e, len));
     e->launches++;
     return cuda_fail(cudaGetLastError(), "derv_mixed");
+}
+
+int launch_branch_nonrev(iqgpu_engine *e, double len, bool derv) {
+    const size_t smem = ((size_t)e->n * e->n + 2 * e->n) * 8;
+    k_nonrev_branch_mats<<<dim3(e->C, derv ? 3 : 1), 256, smem, e->st>>>(e->d_nrmats, e->d_nr, e->d_rates, e->d_props,
+                                                                        len, e->n, e->npad, e->C, e->S);
+    e->launches++;
+    int rc = cuda_fail(cudaGetLastError(), "nonrev_branch_mats");
+    if (rc) return rc;
+    MixParams P = mix_params(e, 0);
+    P.a = e->theta_a;
+    P.b = e->theta_b;
+    const NonrevModel m = nonrev_model(e->d_nr, e->n, e->S);
+    if (derv)
+        k_branch_nonrev<true><<<e->nblk, kTPB, 0, e->st>>>(P, e->d_nrmats, m.tipv);
+    else
+        k_branch_nonrev<false><<<e->nblk, kTPB, 0, e->st>>>(P, e->d_nrmats, m.tipv);
+    e->launches++;
+    return cuda_fail(cudaGetLastError(), "branch_nonrev");
 }
 
 int launch_from_buffer_mixed(iqgpu_engine *e, double len) {

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P)
 #pragma unroll
         for (int ch = 0; ch < 2; ch++) {
             const int r = o.child[ch];
-            const long long prod = ch ? o.prod1 : (long long)o.prod0;
+            const long long prod = ch ? (long long)o.prod1 : (long long)o.prod0;
             if (r >= 0 && r != skip && (prod < 0 || prod - P.op_base < (long long)j - kDnaAhead)) return r;
         }
         return -1;

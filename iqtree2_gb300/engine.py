@@ -38,11 +38,14 @@ FLAG_REF_TRIPLE_TAIL = 1
 
 
 class Op(ct.Structure):
-    _fields_ = [("dad_slot", ct.c_int32), ("child", ct.c_int32 * 2), ("reserved", ct.c_int32),
+    _fields_ = [("dad_slot", ct.c_int32), ("child", ct.c_int32 * 2), ("flags", ct.c_int32),
                 ("len", ct.c_double * 2)]
 
 
-OP_DTYPE = np.dtype([("dad_slot", np.int32), ("child", np.int32, (2,)), ("reserved", np.int32),
+# iqgpu_op flags (non-reversible models): transpose P for a child reached
+# against the edge direction; a tip child that is the root leaf
+OP_TRANSPOSE0, OP_TRANSPOSE1, OP_ROOTLEAF0, OP_ROOTLEAF1 = 1, 2, 4, 8
+OP_DTYPE = np.dtype([("dad_slot", np.int32), ("child", np.int32, (2,)), ("flags", np.int32),
                      ("len", np.float64, (2,))])
 assert OP_DTYPE.itemsize == ct.sizeof(Op) == 32
 NNI_DTYPE = np.dtype([("sub", np.int32, (4,)), ("scratch", np.int32, (2,)), ("len", np.float64, (4,)),
@@ -96,6 +99,7 @@ def lib():
         "iqgpu_set_schedule": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_asc": ([vp, ct.c_int32, ct.c_double], ct.c_int),
         "iqgpu_set_mixture": ([vp, ct.c_int32] + [ct.c_void_p] * 7, ct.c_int),
+        "iqgpu_set_model_nonrev": ([vp] + [ct.c_void_p] * 10, ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
         "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
@@ -192,6 +196,8 @@ class Engine:
     def set_model(self, model):
         if getattr(model, "nmix", 1) > 1:
             return self.set_mixture(model)
+        if hasattr(model, "ceval"):
+            return self.set_model_nonrev(model)
         a = [np.ascontiguousarray(x, np.float64) for x in (model.eval, model.evec, model.inv_evec,
                                                             model.rates, model.props)]
         _check(lib().iqgpu_set_model(self.h, *[_dp(x) for x in a]))
@@ -204,6 +210,18 @@ class Engine:
         arrs = [np.ascontiguousarray(x, np.float64) for x in (mix.eval, mix.evec, mix.inv_evec, mix.rates,
                                                                mix.props, mix.tip_lh, mix.pi)]
         _check(lib().iqgpu_set_mixture(self.h, int(mix.nmix), *[_dp(x) for x in arrs]))
+
+    def set_model_nonrev(self, model, rooted=False):
+        """A ``models.NonrevModel``. Unrooted (default): the evaluated branch
+        is weighted by the stationary frequencies. Rooted: branches carry no
+        frequencies; the root leaf (op flag ``ROOTLEAF``) carries them."""
+        c = lambda x: np.ascontiguousarray(x, np.float64)
+        arrs = [c(model.ceval.real), c(model.ceval.imag), c(model.cevec.real), c(model.cevec.imag),
+                c(model.cinv_evec.real), c(model.cinv_evec.imag), c(model.rates), c(model.props),
+                c(model.tip_vec), c(model.pi)]
+        _check(lib().iqgpu_set_model_nonrev(self.h, *[_dp(x) for x in arrs]))
+        w = np.ones(model.nstates) if rooted else model.pi
+        _check(lib().iqgpu_set_state_freq(self.h, _dp(c(w))))
 
     def set_patterns(self, freq, invar=None):
         f = np.ascontiguousarray(freq, np.float64)
@@ -222,9 +240,12 @@ class Engine:
 
     @staticmethod
     def ops_array(ops):
+        """(dad, child0, child1, len0, len1[, flags]) tuples; flags are the
+        OP_* bits of non-reversible models."""
         arr = np.zeros(len(ops), OP_DTYPE)
-        for k, (dad, c0, c1, l0, l1) in enumerate(ops):
-            arr[k] = (dad, (c0, c1), 0, (l0, l1))
+        for k, op in enumerate(ops):
+            dad, c0, c1, l0, l1 = op[:5]
+            arr[k] = (dad, (c0, c1), op[5] if len(op) > 5 else 0, (l0, l1))
         return arr
 
     def compute_partials(self, ops):

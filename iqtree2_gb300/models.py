@@ -376,3 +376,67 @@ def profile_mixture(exch, pis, weights, alpha, ncat_rate=4):
     rr, rp = gamma_rates_mean(alpha, ncat_rate)
     w = np.asarray(weights, np.float64)
     return MixtureModel("MIX%d+G%d" % (len(pis), ncat_rate), n, classes, w / w.sum(), rr, rp)
+
+
+def stationary_frequencies(Q):
+    """pi with pi Q = 0 and sum(pi) = 1 (the left null vector of Q)."""
+    n = Q.shape[0]
+    A = np.vstack([Q.T, np.ones(n)])
+    rhs = np.zeros(n + 1)
+    rhs[-1] = 1.0
+    return np.linalg.lstsq(A, rhs, rcond=None)[0]
+
+
+@dataclass
+class NonrevModel:
+    """A non-reversible model plus +G categories, in the engine's input form.
+
+    Q is a general rate matrix (rows sum to zero), scaled so that one unit of
+    branch length is one expected substitution at stationarity, sum_i pi_i
+    (-q_ii) = 1 (the normalisation of ModelMarkov for non-reversible models);
+    pi is its stationary distribution. P(t) = Re(V diag(exp(lambda t)) V^-1)
+    from the complex eigen system (ModelMarkov::computeTransMatrixNonrev,
+    model/modelmarkov.cpp:480-490). Tip vectors stay in the standard basis.
+    """
+
+    name: str
+    nstates: int
+    Q: np.ndarray
+    rates: np.ndarray
+    props: np.ndarray
+    pi: np.ndarray = field(init=False)
+    ceval: np.ndarray = field(init=False)
+    cevec: np.ndarray = field(init=False)
+    cinv_evec: np.ndarray = field(init=False)
+    tip_vec: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        self.pi = stationary_frequencies(self.Q)
+        self.Q = self.Q / float(-(self.pi * np.diag(self.Q)).sum())
+        self.ceval, self.cevec = np.linalg.eig(self.Q)
+        self.cinv_evec = np.linalg.inv(self.cevec)
+        self.tip_vec = np.ascontiguousarray(tip_vectors(self.nstates))
+
+    @property
+    def ncat(self):
+        return len(self.rates)
+
+    @property
+    def state_unknown(self):
+        return STATE_UNKNOWN.get(self.nstates, self.nstates)
+
+    def trans_matrix(self, t):
+        """P(t) from the complex eigen system (real part)."""
+        return ((self.cevec * np.exp(self.ceval * t)[None, :]) @ self.cinv_evec).real
+
+
+def unrest_model(nstates, seed, alpha, ncat=4, spread=(0.2, 3.0)):
+    """A random general (UNREST-style) rate matrix: every off-diagonal rate
+    drawn independently from U(spread), so q_ij != q_ji and the stationary
+    distribution is not uniform. Seeded."""
+    rng = np.random.default_rng(seed)
+    Q = rng.uniform(spread[0], spread[1], (nstates, nstates))
+    np.fill_diagonal(Q, 0.0)
+    np.fill_diagonal(Q, -Q.sum(axis=1))
+    rates, props = gamma_rates_mean(alpha, ncat)
+    return NonrevModel("UNREST+G%d" % ncat, nstates, Q, rates, props)

@@ -99,3 +99,59 @@ def tree_lnl_mixture(mix, patterns, freq, edges, lengths, ntaxa, root=None):
     lh = np.einsum("cpx,cx,c->p", out, mix.pi[cls], mix.props)
     plh = np.log(lh) + logs
     return float(plh @ freq), plh
+
+
+def branch_lnl_nonrev(model, patterns, freq, edges, lengths, ntaxa, dad, node, weights=None, blen=None,
+                      derivatives=False):
+    """lnL of a non-reversible model evaluated on branch (dad, node): per
+    pattern sum_c p_c sum_x w_x A_c[x] (P_c(t) B_c)[x], A the conditional
+    likelihood of dad's side (edges directed away from dad), B node's side,
+    P_c(t) = expm(Q r_c t) straight from the rate matrix (no eigen system).
+    w defaults to the stationary frequencies (the unrooted convention);
+    ``blen`` overrides the branch's length. With ``derivatives`` also the
+    Newton-Raphson sums df = sum f lh'/lh and ddf = sum f (lh''/lh -
+    (lh'/lh)^2), dP/dt = r Q P and d2P/dt2 = (r Q)^2 P."""
+    from iqtree2_gb300 import models
+    w = model.pi if weights is None else np.asarray(weights, np.float64)
+    T = models.tip_vectors(model.nstates)
+    adj = [[] for _ in range(2 * ntaxa - 2)]
+    for k, (u, v) in enumerate(edges):
+        adj[int(u)].append((int(v), k))
+        adj[int(v)].append((int(u), k))
+    lengths = np.asarray(lengths, np.float64).copy()
+    Ps = {}
+
+    def P(c, t):
+        key = (c, t)
+        if key not in Ps:
+            Ps[key] = expm(model.Q * (model.rates[c] * t))
+        return Ps[key]
+
+    def cond(n, d):  # [C, nptn, n] conditional likelihood of n's subtree seen from d
+        if n < ntaxa:
+            v = T[patterns[n]]
+            return np.broadcast_to(v, (model.ncat,) + v.shape).copy()
+        out = None
+        for (c, k) in adj[n]:
+            if c == d:
+                continue
+            L = cond(c, n)
+            m = np.stack([L[ci] @ P(ci, lengths[k]).T for ci in range(model.ncat)])
+            out = m if out is None else out * m
+        return out
+
+    k_b = next(k for (c, k) in adj[dad] if c == node)
+    t = lengths[k_b] if blen is None else blen
+    A, B = cond(dad, node), cond(node, dad)
+    lh, d1, d2 = (np.zeros(patterns.shape[1]) for _ in range(3))
+    for ci in range(model.ncat):
+        Pt = P(ci, t)
+        rQ = model.Q * model.rates[ci]
+        Aw = A[ci] * w[None, :]
+        lh += model.props[ci] * (Aw * (B[ci] @ Pt.T)).sum(axis=1)
+        d1 += model.props[ci] * (Aw * (B[ci] @ (rQ @ Pt).T)).sum(axis=1)
+        d2 += model.props[ci] * (Aw * (B[ci] @ (rQ @ rQ @ Pt).T)).sum(axis=1)
+    lnl = float((np.log(lh) * freq).sum())
+    if not derivatives:
+        return lnl
+    return lnl, float((freq * d1 / lh).sum()), float((freq * (d2 / lh - (d1 / lh) ** 2)).sum())
