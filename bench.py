@@ -56,7 +56,7 @@ FP64_PEAK_TFLOPS_MEASURED = 1.20  # FMA-chain probe on this machine's GB300 (all SM
 # the workload's own size, from the captures summarised in profiles/ (the bench
 # does not run ncu itself); None where no capture was made.
 TRAFFIC_BYTES = {
-    "protein": (2579.8e6, "profiles/k_traverse_tc_ws_protein100x50k.md"),
+    "protein": (2583.1e6, "profiles/k_traverse_tc_ws_protein100x50k.md"),
     "dna-large": (2219.6e6, "profiles/k_level_dna_dna200x100k.md"),
     "codon": (418.7e6, "profiles/k_traverse_tc_ws_codon40x10k.md"),
 }
