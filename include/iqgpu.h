@@ -176,7 +176,7 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
  * pattern lnL from iqgpu_get_pattern_lh. */
 int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
 /* Mixture model (ModelMixture: profile mixtures such as C10-C60, LG4X, ...)
- * on the mixed-precision path: nmix classes, each with its own eigen system
+ * on every path: nmix classes, each with its own eigen system
  * and state frequencies; the ncat categories (a multiple of nmix) are class
  * blocks of ncat/nmix rate categories, category c belonging to class
  * c / (ncat/nmix) (tree/phylokernelnew.h:908-918; with fused mix-rate,
@@ -184,8 +184,9 @@ int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
  * evec and inv_evec [nmix][n][n], state_freq [nmix][n]; tip_lh
  * [STATE_UNKNOWN+1][nmix][n] (the reference's tip_partial_lh layout); rates
  * and props per category (props = rate proportion x class weight,
- * :2327). iqgpu_set_model goes back to one class. FP64 engines and the
- * batched NNI entry point refuse mixtures (IQGPU_ERR_ARG). */
+ * :2327). iqgpu_set_model goes back to one class. On FP64 engines each
+ * category's partial lives in its class's eigen basis, as in the reference's
+ * kernels. The batched NNI entry point refuses mixtures (IQGPU_ERR_ARG). */
 int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const double *evec, const double *inv_evec,
                       const double *rates, const double *props, const double *tip_lh, const double *state_freq);
 /* Non-reversible model (ModelMarkov with is_reversible false: UNREST, NONREV,

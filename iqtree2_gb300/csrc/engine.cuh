@@ -51,7 +51,8 @@ struct TravParams {
     const double *opmats;
     const double *inv_evec;    // n*n
     const double *eval, *rates, *props;
-    const double *tip_lh;      // (S+1)*n
+    const double *tip_lh;      // (S+1)*nmix*n
+    int nmix, cpc;             // mixture classes; category c belongs to class c / cpc
     const double *freq, *invar;
     const uint8_t *states;     // ntaxa*ldp
     double *partials;

@@ -81,7 +81,8 @@ static Sizes sizes(const iqgpu_config *c) {
         s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
         s.op_stride = round_up(2 * C * n * n + 2 * (S + 1) * B, 4);
         s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
-        s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double);
+        s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double) +
+                  (C - 1) * (n + 2 * n * n + (S + 1) * n) * 8;  // + the other mixture classes' model arrays
     }
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
     // category-split tensor-core levels hold fewer than 4 pairs per resident CTA
@@ -255,8 +256,8 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     CKE(cudaEventCreate(&e->ev_t0));
     CKE(cudaEventCreate(&e->ev_t1));
     const long long n = e->n, C = e->C, B = e->B, S = e->S;
-    // model arrays per mixture class: up to ncat classes on the mixed path (one otherwise)
-    const long long K = is_mixed(cfg) ? C : 1;
+    // model arrays per mixture class: up to ncat classes
+    const long long K = C;
     e->nmix = 1;
     e->cpc = (int)C;
     CKE(dalloc(e, &e->d_eval, K * n * 8));
@@ -409,10 +410,6 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
         set_error("null argument");
         return IQGPU_ERR_ARG;
     }
-    if (!is_mixed(&e->cfg)) {
-        set_error("mixture models run on the mixed-precision path (IQGPU_F32, IQGPU_TF32X3, IQGPU_BF16)");
-        return IQGPU_ERR_ARG;
-    }
     if (nmix < 1 || nmix > e->C || e->C % nmix != 0) {
         set_error("mixture: need 1 <= nmix <= ncat with ncat a multiple of nmix");
         return IQGPU_ERR_ARG;
@@ -426,14 +423,17 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
     CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_tip, tip_lh, S1 * K * n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_pi, state_freq, K * n * 8, cudaMemcpyHostToDevice));
-    std::vector<float> inv32(K * n * e->npad, 0.f);
-    for (size_t m = 0; m < K; m++)
-        for (size_t i = 0; i < n; i++)
-            for (size_t j = 0; j < n; j++) inv32[(m * n + i) * e->npad + j] = (float)inv_evec[(m * n + i) * n + j];
-    float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
-    CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
-    if (e->d_ivhl) {
+    const bool mixed = is_mixed(&e->cfg);
+    if (mixed) CK(cudaMemcpy(e->d_pi, state_freq, K * n * 8, cudaMemcpyHostToDevice));
+    if (mixed) {  // FP32 copies of every class's U^-1, after the op matrix blocks
+        std::vector<float> inv32(K * n * e->npad, 0.f);
+        for (size_t m = 0; m < K; m++)
+            for (size_t i = 0; i < n; i++)
+                for (size_t j = 0; j < n; j++) inv32[(m * n + i) * e->npad + j] = (float)inv_evec[(m * n + i) * n + j];
+        float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
+        CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
+    }
+    if (mixed && e->d_ivhl) {
         for (size_t m = 0; m < K; m++) CK(upload_hilo(e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n));
         CK(upload_hilo(e->d_tiphl, tip_lh, S1 * K * n));
     }

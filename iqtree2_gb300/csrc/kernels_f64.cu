@@ -20,10 +20,12 @@ namespace iqg {
 // per-op precompute: echild = U diag(exp(lambda r_c t)) and leaf lookup tables
 // (computePartialInfo, tree/phylokernelnew.h:895-1110)
 // ---------------------------------------------------------------------------
+// Mixtures: category c takes its class's eigen system (m = c / cpc) and the
+// class's eigen-space tip vectors tip_lh[s][m] (tree/phylokernelnew.h:908-918).
 __global__ void k_partial_info_f64(const OpDev *__restrict__ ops, double *__restrict__ opmats,
                                    const double *__restrict__ evec, const double *__restrict__ eval,
                                    const double *__restrict__ rates, const double *__restrict__ tip_lh,
-                                   int n, int C, int S) {
+                                   int n, int C, int S, int nmix, int cpc) {
     const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
     const OpDev op = ops[k];
     const int ref = op.child[ch];
@@ -35,23 +37,24 @@ __global__ void k_partial_info_f64(const OpDev *__restrict__ ops, double *__rest
     __shared__ double sexp[kMaxCat * kMaxStates];
     for (int t = threadIdx.x; t < C * n; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        sexp[t] = exp(eval[i] * (rates[c] * len));
+        sexp[t] = exp(eval[(c / cpc) * n + i] * (rates[c] * len));
     }
     __syncthreads();
+    const long long nn = (long long)n * n;
     if (z == 0) {
         for (long long t = threadIdx.x; t < CNN; t += blockDim.x) {
             const int c = (int)(t / (n * n)), x = (int)((t / n) % n), i = (int)(t % n);
-            echild[t] = evec[x * n + i] * sexp[c * n + i];
+            echild[t] = evec[(c / cpc) * nn + x * n + i] * sexp[c * n + i];
         }
     }
     if (ref >= 0) return;
     double *tab = base + 2 * CNN + (long long)ch * (S + 1) * B;
     const long long rows = (long long)S * B;
     for (long long t = (long long)z * blockDim.x + threadIdx.x; t < rows; t += (long long)Z * blockDim.x) {
-        const int s = (int)(t / B), r = (int)(t % B), c = r / n, x = r % n;
-        const double *T = tip_lh + (long long)s * n;
-        double acc = (evec[x * n] * sexp[c * n]) * T[0];
-        for (int i = 1; i < n; i++) acc = fma(evec[x * n + i] * sexp[c * n + i], T[i], acc);
+        const int s = (int)(t / B), r = (int)(t % B), c = r / n, x = r % n, m = c / cpc;
+        const double *T = tip_lh + ((long long)s * nmix + m) * n, *U = evec + m * nn;
+        double acc = (U[x * n] * sexp[c * n]) * T[0];
+        for (int i = 1; i < n; i++) acc = fma(U[x * n + i] * sexp[c * n + i], T[i], acc);
         tab[t] = acc;
     }
     if (z == 0)
@@ -202,7 +205,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
                 double out[NR];
 #pragma unroll
                 for (int x = 0; x < NR; x++) {
-                    out[x] = dot_reg<NR>(Ui + x * NR, tmp);
+                    out[x] = dot_reg<NR>(Ui + (c / P.cpc) * NR * NR + x * NR, tmp);
                     cmax = fmax(cmax, fabs(out[x]));
                 }
                 if (SAFE && check && cmax < kScaleThreshold) {
@@ -248,7 +251,8 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
                         const double t = stmp[j * kTPB + tid];
 #pragma unroll
                         for (int xx = 0; xx < XC; xx++)
-                            if (x0 + xx < n) acc[xx] = fma(__ldg(Ui + (x0 + xx) * n + j), t, acc[xx]);
+                            if (x0 + xx < n)
+                                acc[xx] = fma(__ldg(Ui + ((long long)(c / P.cpc) * n + x0 + xx) * n + j), t, acc[xx]);
                     }
 #pragma unroll
                     for (int xx = 0; xx < XC; xx++) {
@@ -279,7 +283,8 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
     const bool btip = P.b < 0;
     const double *pb = btip ? nullptr : P.partials + (long long)P.b * P.slot_stride + p;
     const uint8_t *sb = btip ? nullptr : P.scale + (long long)P.b * P.scale_stride + p;
-    const double *tipv = btip ? P.tip_lh + (long long)P.states[(long long)(-1 - P.b) * ld + p] * n : nullptr;
+    // a tip b: its state's eigen-space tip vector, per mixture class (tipv + class * n)
+    const double *tipv = btip ? P.tip_lh + (long long)P.states[(long long)(-1 - P.b) * ld + p] * P.nmix * n : nullptr;
     const bool valid = p < P.nptn;
 
     if constexpr (EPI == EPI_THETA) {
@@ -288,7 +293,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         for (int c = 0; c < C; c++)
             for (int x = 0; x < n; x++) {
                 const long long r = (long long)(c * n + x) * ld;
-                th[r] = (btip ? __ldg(tipv + x) : pb[r]) * pa[r];
+                th[r] = (btip ? __ldg(tipv + (c / P.cpc) * n + x) : pb[r]) * pa[r];
             }
         double bs;
         if (SAFE) {
@@ -315,7 +320,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         // branch lnL (tree/phylokernelnew.h:2641-3223)
         for (int t = tid; t < B; t += kTPB) {
             const int c = t / n, i = t % n;
-            sval[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+            sval[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
         }
         __syncthreads();
         double lh_cat[kMaxCat];
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
             double acc = 0.0;
             for (int i = 0; i < n; i++) {
                 const long long r = (long long)(c * n + i) * ld;
-                const double w = btip ? sval[c * n + i] * __ldg(tipv + i) : sval[c * n + i] * pb[r];
+                const double w = btip ? sval[c * n + i] * __ldg(tipv + (c / P.cpc) * n + i) : sval[c * n + i] * pb[r];
                 acc = fma(w, pa[r], acc);
             }
             lh_cat[c] = acc;
@@ -369,6 +374,7 @@ struct BufParams {
     long long ldp;
     const double *theta, *buffer_scale, *freq, *invar;
     const double *eval, *rates, *props;
+    int cpc;  // categories per mixture class (eval is [class][n])
     double len;
     double *pattern_lh;
     Reduce red;
@@ -382,7 +388,7 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
     const int n = P.n, C = P.ncat, B = n * C;
     for (int t = threadIdx.x; t < B; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        const double cof = P.eval[i] * P.rates[c];
+        const double cof = P.eval[(c / P.cpc) * n + i] * P.rates[c];
         const double val = exp(cof * P.len) * P.props[c];
         const double val1 = cof * val;
         v0[t] = val;
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(kTPB) k_from_buffer_f64(const BufParams P) {
     const int n = P.n, C = P.ncat, B = n * C;
     for (int t = threadIdx.x; t < B; t += blockDim.x) {
         const int c = t / n, i = t % n;
-        v0[t] = exp(P.eval[i] * (P.rates[c] * P.len)) * P.props[c];
+        v0[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
     }
     __syncthreads();
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -481,6 +487,8 @@ static TravParams trav_params(iqgpu_engine *e, int nops) {
     P.rates = e->d_rates;
     P.props = e->d_props;
     P.tip_lh = e->d_tip;
+    P.nmix = e->nmix;
+    P.cpc = e->cpc;
     P.freq = e->d_freq;
     P.invar = e->d_invar;
     P.states = e->d_states;
@@ -501,7 +509,7 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops) {
     if (nops <= 0) return IQGPU_OK;
     dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
     k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
-                                                 e->d_tip, e->n, e->C, e->S);
+                                                 e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "partial_info_f64");
 }
@@ -560,6 +568,7 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
     P.freq = e->d_freq;
     P.invar = e->d_invar;
     P.eval = e->d_eval;
+    P.cpc = e->cpc;
     P.rates = e->d_rates;
     P.props = e->d_props;
     P.len = len;

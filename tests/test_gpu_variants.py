@@ -205,27 +205,30 @@ def _mixture(data, nclass, ncat_rate, seed):
     return ds, models.profile_mixture(R, pis, w, 0.6, ncat_rate)
 
 
-@pytest.mark.parametrize("data,precision,nclass,ncat_rate", [("dna", engine.F32, 2, 2), ("dna", engine.F32, 3, 2),
-                                                             ("protein", engine.F32, 3, 2),
-                                                             ("protein", engine.TF32X3, 3, 2),
-                                                             ("protein", engine.TF32X3, 4, 1)])
-def test_mixture_lnl_and_derivatives(data, precision, nclass, ncat_rate):
-    """Profile mixtures on the mixed path (4-state kernel for 2 x 2
+@pytest.mark.parametrize("data,precision,nclass,ncat_rate,safe", [
+    ("dna", engine.F32, 2, 2, False), ("dna", engine.F32, 3, 2, False), ("protein", engine.F32, 3, 2, False),
+    ("protein", engine.TF32X3, 3, 2, False), ("protein", engine.TF32X3, 4, 1, False),
+    ("dna", engine.F64, 3, 2, False), ("protein", engine.F64, 3, 2, False), ("protein", engine.F64, 4, 1, True)])
+def test_mixture_lnl_and_derivatives(data, precision, nclass, ncat_rate, safe):
+    """Profile mixtures on every path (4-state kernels for 2 x 2
     categories, the generic CUDA-core and tensor-core kernels otherwise, one
-    fused mix-rate case): lnL and pattern lnL against the independent numpy
-    mixture pruning (1e-6 relative), the derivatives against its central
-    differences, the lnL from the theta buffer against it."""
+    fused mix-rate case; FP64 with each category in its class's eigen basis,
+    NORM and SAFE): lnL and pattern lnL against the independent numpy mixture
+    pruning (1e-10 relative for FP64, 1e-6 mixed), the derivatives against
+    its central differences, the lnL from the theta buffer against it."""
     import stdbasis
     ds, mix = _mixture(data, nclass, ncat_rate, 70 + nclass)
     want, pwant = stdbasis.tree_lnl_mixture(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa)
-    t = engine.GpuTree(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=precision)
+    f64 = precision == engine.F64
+    tol = 1e-10 if f64 else 1e-6
+    t = engine.GpuTree(mix, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=precision, safe=safe)
     lg, plh = t.compute_likelihood(want_pattern_lh=True)
-    assert rel(lg, want) < 1e-6, (lg, want)
-    np.testing.assert_allclose(plh, pwant, atol=1e-4)
+    assert rel(lg, want) < tol, (lg, want)
+    np.testing.assert_allclose(plh, pwant, atol=1e-8 if f64 else 1e-4)
 
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
     eng = engine.Engine(ds.nptn, mix.nstates, mix.ncat, ds.ntaxa, mix.state_unknown, topo.nslots, precision=precision,
-                        max_ops=topo.nslots)
+                        max_ops=topo.nslots, safe=safe)
     eng.set_model(mix)
     eng.set_patterns(ds.freq)
     eng.set_tip_states(ds.patterns)
@@ -246,15 +249,7 @@ def test_mixture_lnl_and_derivatives(data, precision, nclass, ncat_rate):
         floor = 1e-5 * float(ds.freq.sum())
         assert abs(df - fd1) <= 1e-4 * abs(fd1) + floor, (df, fd1)
         assert abs(ddf - fd2) <= 1e-2 * abs(fd2) + floor, (ddf, fd2)
-        assert rel(eng.lnl_from_buffer(x), l0) < 1e-6
-
-
-def test_mixture_refused_in_fp64():
-    ds, mix = _mixture("dna", 2, 2, 5)
-    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
-    eng = engine.Engine(ds.nptn, 4, mix.ncat, ds.ntaxa, mix.state_unknown, topo.nslots, max_ops=topo.nslots)
-    with pytest.raises(engine.EngineError):
-        eng.set_model(mix)
+        assert rel(eng.lnl_from_buffer(x), l0) < tol
 
 
 @pytest.mark.parametrize("precision", [engine.F64, engine.TF32X3])
