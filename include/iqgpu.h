@@ -190,8 +190,7 @@ int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
 int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const double *evec, const double *inv_evec,
                       const double *rates, const double *props, const double *tip_lh, const double *state_freq);
 /* Non-reversible model (ModelMarkov with is_reversible false: UNREST, NONREV,
- * Lie-Markov; model/modelmarkov.cpp:463-505, 732-756) on the mixed-precision
- * path. The partials stay in the standard basis (the reference's nonrev
+ * Lie-Markov; model/modelmarkov.cpp:463-505, 732-756) on every path. The partials stay in the standard basis (the reference's nonrev
  * kernels, tree/phylokernelnonrev.h); P(r_c t) = Re(V diag(exp(lambda r_c t))
  * V^-1) from the complex eigen system of the normalised rate matrix, each
  * array given as real and imaginary parts: ceval [n], cevec and cinv_evec
@@ -202,8 +201,10 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
  * unrooted tree (tree/phylokernelnonrev.h:1117-1130), all ones for a rooted
  * tree whose root leaf carries root_freq. Derivatives use r_c lambda and
  * (r_c lambda)^2 on the same eigen system (Q P and Q^2 P,
- * tree/phylokernelnonrev.h:628-660). FP64 engines, mixtures, +ASC and the
- * batched NNI / group entry points refuse non-reversible models. */
+ * tree/phylokernelnonrev.h:628-660). On FP64 engines the partials are
+ * standard-basis (the traversal's dad transform becomes the identity) with
+ * the reference's NORM / SAFE scale counts. Mixtures, +ASC and the batched
+ * NNI / group entry points refuse non-reversible models. */
 int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double *ceval_im, const double *cevec_re,
                            const double *cevec_im, const double *cinv_re, const double *cinv_im,
                            const double *rates, const double *props, const double *tip_vec,

@@ -182,6 +182,7 @@ int launch_from_buffer_mixed(iqgpu_engine *e, double len);
 // non-reversible models: branch lnL (derv false) or lnL and derivatives
 // (derv true) from the partials of the branch ends theta_a / theta_b
 int launch_branch_nonrev(iqgpu_engine *e, double len, bool derv);
+int launch_branch_nonrev64(iqgpu_engine *e, double len, bool derv);  // the same on FP64 engines
 
 // tensor-core pattern-node update (traverse_tc.cu)
 int tc_np(int npad);  // N of the MMA: npad padded to 32 or 64

@@ -75,14 +75,16 @@ static Sizes sizes(const iqgpu_config *c) {
         s.theta = B * s.Ppad * 4 + 2 * s.Ppad * (long long)sizeof(double) +
                   (n >= 16 ? C * (2 * n * n + 2 * (S + 1) * n) * 4 : 0) +  // + the hi/lo split of U^-1 and tips
                   (C - 1) * (n + 2 * n * n + (S + 2) * n) * 8 +             // + the other classes' model arrays
-                  (3 * n + 4 * n * n + (S + 1) * n) * 8 + 3 * C * n * npad * 4;  // + non-reversible model data
+                  (3 * n + 4 * n * n + (S + 1) * n) * 8 + 3 * C * n * npad * 8;  // + non-reversible model data
     } else {
         s.part = (long long)c->nslots * B * s.Ppad * (long long)sizeof(double);
         s.scale = (long long)c->nslots * (c->safe ? C : 1) * s.Ppad;
         s.op_stride = round_up(2 * C * n * n + 2 * (S + 1) * B, 4);
         s.opmats = (long long)c->max_ops * s.op_stride * (long long)sizeof(double);
         s.theta = B * s.Ppad * (long long)sizeof(double) + 2 * s.Ppad * (long long)sizeof(double) +
-                  (C - 1) * (n + 2 * n * n + (S + 1) * n) * 8;  // + the other mixture classes' model arrays
+                  (C - 1) * (n + 2 * n * n + (S + 1) * n) * 8 +  // + the other mixture classes' model arrays
+                  (3 * n + 4 * n * n + (S + 1) * n) * 8 + 3 * C * n * npad * 8 +  // + non-reversible model data
+                  C * n * 8;                                                     // + branch frequency weights
     }
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
     // category-split tensor-core levels hold fewer than 4 pairs per resident CTA
@@ -313,10 +315,10 @@ static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_byte
     e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
     CKE(dalloc(e, &e->d_red_out, kRedSlots * 8));
     CKE(dalloc(e, &e->d_asc, 3 * kMaxStates * 8));
-    if (is_mixed(cfg)) {
-        CKE(dalloc(e, &e->d_nr, (3 * e->n + 4LL * e->n * e->n + (long long)(S + 1) * e->n) * 8));
-        CKE(dalloc(e, &e->d_nrmats, 3LL * e->C * e->n * e->npad * 4));
-    }
+    // non-reversible model data ([3][C][n][npad] branch matrices: FP32 on the mixed path, FP64 [3][C][n][n] on FP64)
+    CKE(dalloc(e, &e->d_nr, (3 * e->n + 4LL * e->n * e->n + (long long)(S + 1) * e->n) * 8));
+    CKE(dalloc(e, &e->d_nrmats, 3LL * e->C * e->n * e->npad * 8));
+    if (!is_mixed(cfg)) CKE(dalloc(e, &e->d_pi, e->n * 8));  // branch weights of non-reversible models
     CKE(halloc(e, &e->h_ops, s.ops));
     CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
     CKE(halloc(e, &e->h_asc, 3 * kMaxStates * 8));
@@ -463,10 +465,6 @@ int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double
         set_error("null argument");
         return IQGPU_ERR_ARG;
     }
-    if (!is_mixed(&e->cfg)) {
-        set_error("non-reversible models run on the mixed-precision path (IQGPU_F32, IQGPU_TF32X3, IQGPU_BF16)");
-        return IQGPU_ERR_ARG;
-    }
     if (e->asc_n > 0) { set_error("+ASC is not available with non-reversible models"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
@@ -485,6 +483,11 @@ int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double
     CK(cudaMemcpy(e->d_nr, nr.data(), nr.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
+    if (!is_mixed(&e->cfg)) {  // FP64: standard-basis partials, the traversal's dad transform is the identity
+        std::vector<double> eye(nn, 0.0);
+        for (size_t i = 0; i < n; i++) eye[i * n + i] = 1.0;
+        CK(cudaMemcpy(e->d_inv, eye.data(), nn * 8, cudaMemcpyHostToDevice));
+    }
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
     e->nonrev = true;
@@ -498,7 +501,7 @@ int iqgpu_set_model_nonrev(iqgpu_engine *e, const double *ceval_re, const double
 
 int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq) {
     if (!e || !state_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
-    if (!is_mixed(&e->cfg)) return IQGPU_OK;  // the eigen-space FP64 path folds pi into U^-1
+    // the eigen-space FP64 path folds pi into U^-1; its non-reversible kernels weigh the branch by these
     CK(cudaSetDevice(e->dev));
     CK(cudaStreamSynchronize(e->st));
     CK(cudaMemcpy(e->d_pi, state_freq, (size_t)e->n * 8, cudaMemcpyHostToDevice));
@@ -791,8 +794,17 @@ static int lnl_common(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_
         return IQGPU_ERR_ARG;
     }
     CK(cudaSetDevice(e->dev));
-    if ((rc = upload_ops(e, ops, nops, true, b, len))) return rc;
-    if ((rc = traverse(e, nops, EPI_LNL, a, b, len))) return rc;
+    if (e->nonrev && !is_mixed(&e->cfg)) {  // FP64 non-reversible: traversal, then the branch kernel on both ends
+        if ((rc = upload_ops(e, ops, nops))) return rc;
+        if ((rc = traverse(e, nops, EPI_NONE, a, b, len))) return rc;
+        e->theta_valid = true;
+        e->theta_a = a;
+        e->theta_b = b;
+        if ((rc = launch_branch_nonrev64(e, len, false))) return rc;
+    } else {
+        if ((rc = upload_ops(e, ops, nops, true, b, len))) return rc;
+        if ((rc = traverse(e, nops, EPI_LNL, a, b, len))) return rc;
+    }
     if ((rc = fetch_result(e))) return rc;
     const double *r = e->h_red_out;
     *lnl = std::isfinite(r[0]) ? r[0] : r[1];
@@ -831,7 +843,7 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
         e->theta_a = a;
         e->theta_b = b;
     }
-    rc = e->nonrev ? launch_branch_nonrev(e, len, true)
+    rc = e->nonrev ? (is_mixed(&e->cfg) ? launch_branch_nonrev(e, len, true) : launch_branch_nonrev64(e, len, true))
                    : is_mixed(&e->cfg) ? launch_derv_mixed(e, len) : launch_derv_f64(e, len);
     if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;
@@ -864,7 +876,7 @@ int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
     if (!lnl) { set_error("null output"); return IQGPU_ERR_ARG; }
     if (!e->theta_valid) { set_error("no theta buffer: call iqgpu_likelihood_derv first"); return IQGPU_ERR_STATE; }
     CK(cudaSetDevice(e->dev));
-    rc = e->nonrev ? launch_branch_nonrev(e, len, false)
+    rc = e->nonrev ? (is_mixed(&e->cfg) ? launch_branch_nonrev(e, len, false) : launch_branch_nonrev64(e, len, false))
                    : is_mixed(&e->cfg) ? launch_from_buffer_mixed(e, len) : launch_from_buffer_f64(e, len);
     if (rc) return rc;
     if ((rc = fetch_result(e))) return rc;

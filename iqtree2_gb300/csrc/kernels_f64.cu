@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "engine.cuh"
+#include "nonrev.cuh"
 
 namespace iqg {
 
@@ -366,6 +367,143 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
 }
 
 // ---------------------------------------------------------------------------
+// non-reversible models on the FP64 path (tree/phylokernelnonrev.h): the
+// partials stay in the standard basis. echild is P(r_c t) itself (P^T for a
+// child reached against the edge direction) and the traversal runs with
+// U^-1 = I, so k_traverse_f64 computes the reference's nonrev update,
+// dad[x] = (P_L L)[x] (P_R R)[x], with its 2^-256 scaling rule unchanged.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_partial_info_nonrev64(const OpDev *__restrict__ ops,
+                                                               double *__restrict__ opmats,
+                                                               const double *__restrict__ nr,
+                                                               const double *__restrict__ rates, int n, int C, int S) {
+    extern __shared__ double nv64[];  // [n*n] P, [2n] exp scratch
+    const int k = blockIdx.x, ch = blockIdx.y, c = blockIdx.z;
+    const OpDev op = ops[k];
+    const NonrevModel m = nonrev_model(nr, n, S);
+    double *Pd = nv64, *ex = nv64 + n * n;
+    nonrev_matrix(m, n, rates[c], op.len[ch], 0, ex, Pd);
+    const bool tr = (op.flags >> ch) & 1, root = (op.flags >> (2 + ch)) & 1;
+    const long long CNN = (long long)C * n * n, B = (long long)n * C;
+    double *base = opmats + op.mat_off;
+    double *echild = base + ch * CNN + (long long)c * n * n;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int x = t / n, i = t % n;
+        echild[t] = tr ? Pd[i * n + x] : Pd[x * n + i];
+    }
+    if (op.child[ch] >= 0) return;
+    double *tab = base + 2 * CNN + (long long)ch * (S + 1) * B;
+    for (int t = threadIdx.x; t < (S + 1) * n; t += blockDim.x) {
+        const int st = t / n, x = t % n;
+        const double *v = root ? m.root : m.tipv + (long long)st * n;
+        double acc = 0.0;
+        for (int y = 0; y < n; y++) acc = fma(tr ? Pd[y * n + x] : Pd[x * n + y], v[y], acc);
+        tab[(long long)st * B + (long long)c * n + x] = acc;
+    }
+}
+
+// prop_c * (r_c lambda)^k-weighted P(r_c t), k = 0, 1, 2: FP64 [3][C][n][n]
+__global__ void __launch_bounds__(256) k_nonrev_branch_mats64(double *__restrict__ out, const double *__restrict__ nr,
+                                                              const double *__restrict__ rates,
+                                                              const double *__restrict__ props, double len, int n,
+                                                              int C, int S) {
+    extern __shared__ double nv64[];
+    const int c = blockIdx.x, k = blockIdx.y;
+    double *Pd = nv64, *ex = nv64 + n * n;
+    nonrev_matrix(nonrev_model(nr, n, S), n, rates[c], len, k, ex, Pd);
+    double *o = out + ((long long)k * C + c) * n * n;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) o[t] = props[c] * Pd[t];
+}
+
+// Branch lnL (and with DERV the Newton-Raphson sums) of a non-reversible model
+// from the two ends' FP64 partials: lh_k = sum_c sum_x w_x a[c][x] (M_k,c b_c)[x]
+// (tree/phylokernelnonrev.h:586-1056, 1062-1528), a the dad side, w the state
+// frequencies (unrooted) or ones (rooted); the scale counts as the reversible
+// branch lnL treats them (SAFE: categories one count above the minimum scaled
+// by 2^-256, more than one zeroed; NORM: the two ends' counts add).
+template <bool SAFE, bool DERV>
+__global__ void __launch_bounds__(kTPB) k_branch_nonrev64(const TravParams P, const double *__restrict__ mats,
+                                                          const double *__restrict__ tipv,
+                                                          const double *__restrict__ w) {
+    const int n = P.n, C = P.ncat;
+    const long long ld = P.ldp, CNN = (long long)C * n * n;
+    const long long p = (long long)blockIdx.x * kTPB + threadIdx.x;
+    double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+    if (p < P.nptn) {
+        const double *pa = P.partials + (long long)P.a * P.slot_stride + p;
+        const uint8_t *sa = P.scale + (long long)P.a * P.scale_stride + p;
+        const bool btip = P.b < 0;
+        const double *pb = btip ? nullptr : P.partials + (long long)P.b * P.slot_stride + p;
+        const uint8_t *sb = btip ? nullptr : P.scale + (long long)P.b * P.scale_stride + p;
+        const int sbst = btip ? P.states[(long long)(-1 - P.b) * ld + p] : 0;
+        double l0[kMaxCat], l1[kMaxCat], l2[kMaxCat];
+        for (int c = 0; c < C; c++) {
+            double bv[kMaxStates];
+            for (int y = 0; y < n; y++) bv[y] = btip ? tipv[(long long)sbst * n + y] : pb[(long long)(c * n + y) * ld];
+            double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+            for (int x = 0; x < n; x++) {
+                const double *m0 = mats + ((long long)c * n + x) * n;
+                double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+                for (int y = 0; y < n; y++) {
+                    w0 = fma(__ldg(m0 + y), bv[y], w0);
+                    if (DERV) {
+                        w1 = fma(__ldg(m0 + CNN + y), bv[y], w1);
+                        w2 = fma(__ldg(m0 + 2 * CNN + y), bv[y], w2);
+                    }
+                }
+                const double av = __ldg(w + x) * pa[(long long)(c * n + x) * ld];
+                h0 = fma(av, w0, h0);
+                if (DERV) {
+                    h1 = fma(av, w1, h1);
+                    h2 = fma(av, w2, h2);
+                }
+            }
+            l0[c] = h0;
+            l1[c] = h1;
+            l2[c] = h2;
+        }
+        double scale_count, lh = 0.0, d1 = 0.0, d2 = 0.0;
+        if (SAFE) {
+            unsigned sum[kMaxCat], mn = 1u << 30;
+            for (int c = 0; c < C; c++) {
+                sum[c] = ((unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld])) & 0xffu;
+                mn = min(mn, sum[c]);
+            }
+            for (int c = 0; c < C; c++) {
+                const double f = sum[c] == mn ? 1.0 : sum[c] == mn + 1 ? kScaleThreshold : 0.0;
+                lh += l0[c] * f;
+                d1 += l1[c] * f;
+                d2 += l2[c] * f;
+            }
+            scale_count = (double)mn;
+        } else {
+            for (int c = 0; c < C; c++) {
+                lh += l0[c];
+                d1 += l1[c];
+                d2 += l2[c];
+            }
+            scale_count = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));
+        }
+        lh = fabs(lh) + P.invar[p];
+        const double plh = log(lh) + scale_count * kLogScaleThreshold;
+        const double f = P.freq[p];
+        if (DERV) {
+            const double df_frac = d1 / lh, ddf_frac = d2 / lh;
+            const double tmp1 = df_frac * f, tmp2 = ddf_frac * f;
+            v[0] = tmp1;
+            v[1] = fma(-tmp1, df_frac, tmp2);
+            v[2] = plh * f;
+        } else {
+            P.pattern_lh[p] = plh;
+            v[0] = plh * f;
+            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;
+            v[2] = isfinite(plh) ? 0.0 : 1.0;
+        }
+    }
+    grid_reduce(v, P.red);
+}
+
+// ---------------------------------------------------------------------------
 // derivatives and lnL from the theta buffer
 // ---------------------------------------------------------------------------
 struct BufParams {
@@ -507,6 +645,13 @@ static TravParams trav_params(iqgpu_engine *e, int nops) {
 
 int launch_partial_info_f64(iqgpu_engine *e, int nops) {
     if (nops <= 0) return IQGPU_OK;
+    if (e->nonrev) {
+        const size_t smem = ((size_t)e->n * e->n + 2 * e->n) * 8;
+        k_partial_info_nonrev64<<<dim3(nops, 2, e->C), 256, smem, e->st>>>(e->d_ops, e->d_opmats, e->d_nr, e->d_rates,
+                                                                          e->n, e->C, e->S);
+        e->launches++;
+        return cuda_fail(cudaGetLastError(), "partial_info_nonrev64");
+    }
     dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
     k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
                                                  e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc);
@@ -591,6 +736,29 @@ int launch_from_buffer_f64(iqgpu_engine *e, double len) {
     k_from_buffer_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
     e->launches++;
     return cuda_fail(cudaGetLastError(), "from_buffer_f64");
+}
+
+int launch_branch_nonrev64(iqgpu_engine *e, double len, bool derv) {
+    const size_t smem = ((size_t)e->n * e->n + 2 * e->n) * 8;
+    double *mats = reinterpret_cast<double *>(e->d_nrmats);
+    k_nonrev_branch_mats64<<<dim3(e->C, derv ? 3 : 1), 256, smem, e->st>>>(mats, e->d_nr, e->d_rates, e->d_props, len,
+                                                                          e->n, e->C, e->S);
+    e->launches++;
+    int rc = cuda_fail(cudaGetLastError(), "nonrev_branch_mats64");
+    if (rc) return rc;
+    TravParams P = trav_params(e, 0);
+    P.a = e->theta_a;
+    P.b = e->theta_b;
+    const double *tipv = nonrev_model(e->d_nr, e->n, e->S).tipv;
+    if (e->cfg.safe) {
+        if (derv) k_branch_nonrev64<true, true><<<e->nblk, kTPB, 0, e->st>>>(P, mats, tipv, e->d_pi);
+        else k_branch_nonrev64<true, false><<<e->nblk, kTPB, 0, e->st>>>(P, mats, tipv, e->d_pi);
+    } else {
+        if (derv) k_branch_nonrev64<false, true><<<e->nblk, kTPB, 0, e->st>>>(P, mats, tipv, e->d_pi);
+        else k_branch_nonrev64<false, false><<<e->nblk, kTPB, 0, e->st>>>(P, mats, tipv, e->d_pi);
+    }
+    e->launches++;
+    return cuda_fail(cudaGetLastError(), "branch_nonrev64");
 }
 
 }  // namespace iqg

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "mixed.cuh"
+#include "nonrev.cuh"
 
 namespace iqg {
 
@@ -243,55 +244,6 @@ __global__ void __launch_bounds__(kTPB) k_from_buffer_mixed(const MixBufParams P
 // non-reversible models (tree/phylokernelnonrev.h; P(t) from the complex eigen
 // system as ModelMarkov::computeTransMatrixNonrev, model/modelmarkov.cpp:480-490)
 // ---------------------------------------------------------------------------
-struct NonrevModel {
-    const double *er, *ei, *vr, *vi, *wr, *wi, *root, *tipv;  // ceval, cevec, cinv_evec (re, im), root freq, tip vectors
-};
-__host__ __device__ inline NonrevModel nonrev_model(const double *nr, int n, int S) {
-    const long long nn = (long long)n * n;
-    NonrevModel m;
-    m.er = nr;
-    m.ei = nr + n;
-    m.vr = nr + 2 * n;
-    m.vi = m.vr + nn;
-    m.wr = m.vi + nn;
-    m.wi = m.wr + nn;
-    m.root = m.wi + nn;
-    m.tipv = m.root + n;
-    (void)S;
-    return m;
-}
-
-// out[x][y] = Re(sum_i V[x][i] (lambda_i r)^k exp(lambda_i r t) V^-1[i][y]) for
-// x, y < n, FP64, into shared memory (n*n doubles); e holds 2n doubles of scratch.
-__device__ void nonrev_matrix(const NonrevModel &m, int n, double r, double t, int k, double *e, double *out) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double a = m.er[i] * r, b = m.ei[i] * r;  // lambda_i r
-        const double g = exp(a * t);
-        double re = g * cos(b * t), im = g * sin(b * t);
-        for (int j = 0; j < k; j++) {  // times (lambda_i r)^k
-            const double nr = re * a - im * b, ni = re * b + im * a;
-            re = nr;
-            im = ni;
-        }
-        e[i] = re;
-        e[n + i] = im;
-    }
-    __syncthreads();
-    for (int t2 = threadIdx.x; t2 < n * n; t2 += blockDim.x) {
-        const int x = t2 / n, y = t2 % n;
-        double acc = 0.0;
-        for (int i = 0; i < n; i++) {
-            // (V[x][i] * E_i) * W[i][y], real part
-            const double pr = m.vr[x * n + i] * e[i] - m.vi[x * n + i] * e[n + i];
-            const double pi = m.vr[x * n + i] * e[n + i] + m.vi[x * n + i] * e[i];
-            acc = fma(pr, m.wr[i * n + y], acc);
-            acc = fma(-pi, m.wi[i * n + y], acc);
-        }
-        out[t2] = acc;
-    }
-    __syncthreads();
-}
-
 // Per-op P(t) blocks and leaf tables for a non-reversible model, in the layout
 // of k_partial_info_mixed: one CTA per (op, child, category). A child reached
 // against the edge direction takes P^T; the root leaf's rows are P . root

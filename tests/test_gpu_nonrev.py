@@ -13,8 +13,10 @@ the root leaf's rows are P(t)^T times the root frequencies (= the stationary
 frequencies); tree/phylokernelnew.h:932-963. Every branch then gives the
 same lnL, the rooted tree's.
 
-Tolerances, as for the mixed path: lnL 1e-6 relative; first and second
-derivatives 1e-4 / 1e-3 relative with an absolute floor of 1e-5 per site.
+Tolerances: mixed path lnL 1e-6 relative, first and second derivatives
+1e-4 / 1e-3 relative with an absolute floor of 1e-5 per site; FP64 path
+(standard-basis partials, U^-1 = I in the traversal, NORM and SAFE scaling)
+lnL 1e-10 relative, derivatives 1e-8 relative with a floor of 1e-9 per site.
 """
 import numpy as np
 import pytest
@@ -33,24 +35,29 @@ def _data(kind):
     return simulate.protein_lg_dataset(12, 600, 73), models.unrest_model(20, 74, 0.8)
 
 
-def _engine(ds, m, topo, precision):
+def _engine(ds, m, topo, precision, safe=False):
     return engine.Engine(ds.patterns.shape[1], m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
-                         precision=precision)
+                         precision=precision, safe=safe)
+
+
+def _tol(precision):
+    return 1e-10 if precision == engine.F64 else 1e-6
 
 
 def _internal_branches(topo, ds):
     return [(int(u), int(v)) for (u, v) in ds.edges if u >= ds.ntaxa and v >= ds.ntaxa]
 
 
-CASES = [("dna", engine.F32), ("protein", engine.F32), ("protein", engine.TF32X3)]
+CASES = [("dna", engine.F32, False), ("protein", engine.F32, False), ("protein", engine.TF32X3, False),
+         ("dna", engine.F64, False), ("protein", engine.F64, True)]
 
 
-@pytest.mark.parametrize("kind,precision", CASES)
-def test_nonrev_unrooted_lnl(kind, precision):
+@pytest.mark.parametrize("kind,precision,safe", CASES)
+def test_nonrev_unrooted_lnl(kind, precision, safe):
     ds, m = _data(kind)
     assert np.abs(m.ceval.imag).max() > 1e-3  # complex eigenvalues: the complex path is exercised
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
-    e = _engine(ds, m, topo, precision)
+    e = _engine(ds, m, topo, precision, safe)
     try:
         e.set_model(m)
         e.set_patterns(ds.freq)
@@ -64,7 +71,7 @@ def test_nonrev_unrooted_lnl(kind, precision):
                 ops = e.ops_array(topo.branch_ops(node, dad))
                 lg = e.compute_likelihood(ops, topo.ref(node, dad), topo.ref(dad, node), topo.edge_len(dad, node))
                 lo = stdbasis.branch_lnl_nonrev(m, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa, dad, node)
-                assert rel(lg, lo) < 1e-6, (dad, node, lg, lo)
+                assert rel(lg, lo) < _tol(precision), (dad, node, lg, lo)
                 values.append(lo)
         assert max(values) - min(values) > 1e-6 * abs(values[0])  # not root-invariant: the convention matters
     finally:
@@ -97,8 +104,8 @@ def _rooted_ops(topo, ds, parent, R, dad, node):
     return ops
 
 
-@pytest.mark.parametrize("kind,precision", CASES)
-def test_nonrev_rooted_every_branch(kind, precision):
+@pytest.mark.parametrize("kind,precision,safe", CASES)
+def test_nonrev_rooted_every_branch(kind, precision, safe):
     ds, m = _data(kind)
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
     R = ds.ntaxa - 1                 # the root leaf
@@ -117,7 +124,7 @@ def test_nonrev_rooted_every_branch(kind, precision):
     pat[R, :] = m.state_unknown      # the root leaf carries no data
     # the rooted tree's lnL: frequencies at the root, no data at R
     l_root = stdbasis.branch_lnl_nonrev(m, pat, ds.freq, ds.edges, ds.lengths, ds.ntaxa, r, R)
-    e = _engine(ds, m, topo, precision)
+    e = _engine(ds, m, topo, precision, safe)
     try:
         e.set_model_nonrev(m, rooted=True)
         e.set_patterns(ds.freq)
@@ -128,18 +135,20 @@ def test_nonrev_rooted_every_branch(kind, precision):
             ops = e.ops_array(_rooted_ops(topo, ds, parent, R, node, dad) +
                               _rooted_ops(topo, ds, parent, R, dad, node))
             lg = e.compute_likelihood(ops, topo.ref(node, dad), topo.ref(dad, node), topo.edge_len(dad, node))
-            assert rel(lg, l_root) < 1e-6, (dad, node, lg, l_root)
+            assert rel(lg, l_root) < _tol(precision), (dad, node, lg, l_root)
             checked += 1
         assert checked >= 3
     finally:
         e.close()
 
 
-@pytest.mark.parametrize("kind,precision", CASES)
-def test_nonrev_derivatives_and_from_buffer(kind, precision):
+@pytest.mark.parametrize("kind,precision,safe", CASES)
+def test_nonrev_derivatives_and_from_buffer(kind, precision, safe):
     ds, m = _data(kind)
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
-    e = _engine(ds, m, topo, precision)
+    e = _engine(ds, m, topo, precision, safe)
+    f64 = precision == engine.F64
+    r1, r2, floor = (1e-8, 1e-8, 1e-9) if f64 else (1e-4, 1e-3, 1e-5)
     try:
         e.set_model(m)
         e.set_patterns(ds.freq)
@@ -154,10 +163,10 @@ def test_nonrev_derivatives_and_from_buffer(kind, precision):
                 df, ddf = e.likelihood_derv(ops, a, b, t)
                 lo, d1, d2 = stdbasis.branch_lnl_nonrev(m, ds.patterns, ds.freq, ds.edges, ds.lengths, ds.ntaxa,
                                                         dad, node, blen=t, derivatives=True)
-                assert abs(df - d1) < 1e-4 * abs(d1) + 1e-5 * nsite, (t, df, d1)
-                assert abs(ddf - d2) < 1e-3 * abs(d2) + 1e-5 * nsite, (t, ddf, d2)
+                assert abs(df - d1) < r1 * abs(d1) + floor * nsite, (t, df, d1)
+                assert abs(ddf - d2) < r2 * abs(d2) + floor * nsite, (t, ddf, d2)
                 lb = e.lnl_from_buffer(t)
-                assert rel(lb, lo) < 1e-6, (t, lb, lo)
+                assert rel(lb, lo) < _tol(precision), (t, lb, lo)
     finally:
         e.close()
 
@@ -165,12 +174,6 @@ def test_nonrev_derivatives_and_from_buffer(kind, precision):
 def test_nonrev_refusals():
     ds, m = _data("dna")
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
-    e64 = _engine(ds, m, topo, engine.F64)
-    try:
-        with pytest.raises(engine.EngineError, match="mixed-precision"):
-            e64.set_model(m)
-    finally:
-        e64.close()
     e = _engine(ds, m, topo, engine.F32)
     try:
         e.set_model(m)
