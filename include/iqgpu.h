@@ -175,6 +175,17 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
  * points refuse +ASC engines (IQGPU_ERR_ARG); iqgpu_rell takes the corrected
  * pattern lnL from iqgpu_get_pattern_lh. */
 int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite);
+/* Holder's +ASC for variant sites with missing data (ASC_VARIANT_MISSING,
+ * alignment/alignment.cpp:4158-4180; tree/phylokernelnew.h:3175-3196 for the
+ * lnL, :2580-2617 for the derivatives): the first nobs patterns are the
+ * observed ones and the last nstates * nobs the unobserved ones with weight 0,
+ * block s holding, for observed pattern p, state s at every taxon where p has
+ * data and STATE_UNKNOWN elsewhere. Every pattern lnL drops by log(1 - P_p),
+ * P_p the sum of its unobserved patterns' likelihoods, the tree lnL by
+ * sum_p freq_p log(1 - P_p); the derivatives gain the matching terms.
+ * iqgpu_set_asc(e, 0, 0) switches it off. Refused with non-reversible models;
+ * the batched NNI, group and on-device RELL entry points refuse +ASC engines. */
+int iqgpu_set_asc_holder(iqgpu_engine *e, int32_t nobs);
 /* Mixture model (ModelMixture: profile mixtures such as C10-C60, LG4X, ...)
  * on every path: nmix classes, each with its own eigen system
  * and state frequencies; the ncat categories (a multiple of nmix) are class

@@ -101,6 +101,12 @@ struct iqgpu_engine {
     int asc_n;
     double asc_nsite, asc_lc;
     double *d_asc, *h_asc;
+    // +ASC Holder (missing data): asc_n = n * asc_nobs unobserved patterns,
+    // block s holding state s at every taxon each observed pattern has data
+    // for; d_asc_holder (cudaMalloc) takes their (lh, df, ddf) and two sums
+    bool asc_holder;
+    int asc_nobs;
+    double *d_asc_holder;
     bool theta_valid;
     int32_t theta_a, theta_b;
     // mixed-precision (FP32 standard-basis) state

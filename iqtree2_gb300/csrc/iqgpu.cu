@@ -156,6 +156,7 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
                         e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl, e->d_pair_cnt,
                         e->d_nr, e->d_nrmats};
+    if (e->d_asc_holder) cudaFree(e->d_asc_holder);  // cudaMalloc'd even in a region engine
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
@@ -768,8 +769,98 @@ int iqgpu_compute_partials(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
 // sum of the unobserved constant patterns' likelihoods (exp of their pattern
 // lnL, which carries their scaling), lnL -= nsite * log(1 - P_const)
 // (tree/phylokernelnew.h:3198-3222 and 3405-3420).
+// +ASC Holder (tree/phylokernelnew.h:3175-3196, 2580-2617): per observed
+// pattern p the unobserved patterns' likelihoods add up to P_p (block s of
+// the appended patterns, entry p); the pattern lnL drops by log(1 - P_p) and
+// the tree lnL by sum_p freq_p log(1 - P_p); the derivatives gain
+// sum_p freq_p d1_p / (1 - P_p) and sum_p freq_p (d2_p / (1 - P_p) + (d1_p /
+// (1 - P_p))^2). One CTA, a fixed order of additions: deterministic.
+constexpr int kHolderThreads = 1024;
+__device__ double holder_block_sum(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = kHolderThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kHolderThreads) k_asc_holder_lnl(double *plh, const double *freq, int nobs,
+                                                                   int nstates, double *out) {
+    __shared__ double sh[kHolderThreads];
+    double acc = 0.0, bad = 0.0;
+    for (int p = threadIdx.x; p < nobs; p += kHolderThreads) {
+        double c = 0.0;
+        for (int s = 0; s < nstates; s++) c += exp(plh[nobs + (long long)s * nobs + p]);
+        if (!(c < 1.0 && c >= 0.0)) bad += 1.0;
+        const double corr = log(1.0 - c);
+        plh[p] -= corr;
+        acc += freq[p] * corr;
+    }
+    acc = holder_block_sum(acc, sh);
+    bad = holder_block_sum(bad, sh);
+    if (threadIdx.x == 0) {
+        out[0] = acc;
+        out[1] = bad;
+    }
+}
+
+__global__ void __launch_bounds__(kHolderThreads) k_asc_holder_derv(const double *t, const double *freq, int nobs,
+                                                                    int nstates, double *out) {
+    __shared__ double sh[kHolderThreads];
+    double sdf = 0.0, sddf = 0.0;
+    for (int p = threadIdx.x; p < nobs; p += kHolderThreads) {
+        double c = 0.0, d1 = 0.0, d2 = 0.0;
+        for (int s = 0; s < nstates; s++) {
+            const double *o = t + 3 * ((long long)s * nobs + p);
+            c += o[0];
+            d1 += o[1];
+            d2 += o[2];
+        }
+        const double pv = 1.0 - c, df_frac = d1 / pv, ddf_frac = d2 / pv;
+        sdf += freq[p] * df_frac;
+        sddf += freq[p] * (ddf_frac + df_frac * df_frac);
+    }
+    sdf = holder_block_sum(sdf, sh);
+    sddf = holder_block_sum(sddf, sh);
+    if (threadIdx.x == 0) {
+        out[0] = sdf;
+        out[1] = sddf;
+    }
+}
+
+static int asc_holder_sums(iqgpu_engine *e, bool derv, double *r0, double *r1) {
+    double *out = e->d_asc_holder + 3LL * e->asc_n;
+    if (derv)
+        k_asc_holder_derv<<<1, kHolderThreads, 0, e->st>>>(e->d_asc_holder, e->d_freq, e->asc_nobs, e->n, out);
+    else
+        k_asc_holder_lnl<<<1, kHolderThreads, 0, e->st>>>(e->d_plh, e->d_freq, e->asc_nobs, e->n, out);
+    e->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e->h_asc, out, 16, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    *r0 = e->h_asc[0];
+    *r1 = e->h_asc[1];
+    return IQGPU_OK;
+}
+
 static int asc_lnl(iqgpu_engine *e, double *lnl) {
     if (e->asc_n <= 0) return IQGPU_OK;
+    if (e->asc_holder) {
+        double corr = 0.0, bad = 0.0;
+        int rc = asc_holder_sums(e, false, &corr, &bad);
+        if (rc) return rc;
+        if (bad != 0.0) {
+            set_error("+ASC (Holder): an observed pattern's unobserved patterns have probability outside [0, 1)");
+            return IQGPU_ERR_NONFINITE;
+        }
+        e->asc_lc = 0.0;  // the observed patterns' lnL were corrected on the device
+        *lnl -= corr;
+        return IQGPU_OK;
+    }
     CK(cudaMemcpyAsync(e->h_asc, e->d_plh + (e->P - e->asc_n), (size_t)e->asc_n * 8, cudaMemcpyDeviceToHost, e->st));
     CK(cudaStreamSynchronize(e->st));
     double pc = 0.0;
@@ -853,7 +944,12 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
         set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this");
         return IQGPU_ERR_NONFINITE;
     }
-    if (e->asc_n > 0) {  // Lewis +ASC (tree/phylokernelnew.h:2620-2628)
+    if (e->asc_n > 0 && e->asc_holder) {
+        double sdf = 0.0, sddf = 0.0;
+        if ((rc = asc_holder_sums(e, true, &sdf, &sddf))) return rc;
+        *df += sdf;
+        *ddf += sddf;
+    } else if (e->asc_n > 0) {  // Lewis +ASC (tree/phylokernelnew.h:2620-2628)
         CK(cudaMemcpyAsync(e->h_asc, e->d_asc, (size_t)e->asc_n * 24, cudaMemcpyDeviceToHost, e->st));
         CK(cudaStreamSynchronize(e->st));
         double lh = 0.0, d1 = 0.0, d2 = 0.0;
@@ -910,6 +1006,26 @@ int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite) {
     }
     e->asc_n = nconst;
     e->asc_nsite = nsite;
+    e->asc_lc = 0.0;
+    e->asc_holder = false;
+    return IQGPU_OK;
+}
+
+int iqgpu_set_asc_holder(iqgpu_engine *e, int32_t nobs) {
+    if (!e || nobs <= 0 || (long long)nobs * (e->n + 1) != e->P) {
+        set_error("+ASC (Holder): need nobs > 0 observed patterns followed by nstates * nobs unobserved ones");
+        return IQGPU_ERR_ARG;
+    }
+    if (e->nonrev) { set_error("+ASC is not available with non-reversible models"); return IQGPU_ERR_ARG; }
+    CK(cudaSetDevice(e->dev));
+    CK(cudaStreamSynchronize(e->st));
+    if (e->d_asc_holder) CK(cudaFree(e->d_asc_holder));
+    e->d_asc_holder = nullptr;
+    CK(cudaMalloc(&e->d_asc_holder, (3LL * e->n * nobs + 4) * 8));
+    e->asc_holder = true;
+    e->asc_nobs = nobs;
+    e->asc_n = e->n * nobs;
+    e->asc_nsite = 0.0;
     e->asc_lc = 0.0;
     return IQGPU_OK;
 }

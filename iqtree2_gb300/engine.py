@@ -100,6 +100,7 @@ def lib():
         "iqgpu_set_asc": ([vp, ct.c_int32, ct.c_double], ct.c_int),
         "iqgpu_set_mixture": ([vp, ct.c_int32] + [ct.c_void_p] * 7, ct.c_int),
         "iqgpu_set_model_nonrev": ([vp] + [ct.c_void_p] * 10, ct.c_int),
+        "iqgpu_set_asc_holder": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
         "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
@@ -233,6 +234,11 @@ class Engine:
         patterns (``models.asc_lewis_patterns``); lnL and derivatives are
         corrected with ``nsite`` sites. 0 switches it off."""
         _check(lib().iqgpu_set_asc(self.h, int(nconst), float(nsite)))
+
+    def set_asc_holder(self, nobs):
+        """+ASC (Holder, missing data): the first ``nobs`` patterns are observed,
+        the rest their unobserved patterns (``models.asc_holder_patterns``)."""
+        _check(lib().iqgpu_set_asc_holder(self.h, int(nobs)))
 
     def set_tip_states(self, patterns):
         s = np.ascontiguousarray(patterns, np.uint8)

@@ -162,6 +162,21 @@ def asc_lewis_patterns(patterns, freq, nstates, pi=None):
     return out, f, len(extra), float(np.asarray(freq).sum())
 
 
+def asc_holder_patterns(patterns, freq, nstates):
+    """Holder's +ASC for variant sites with missing data: append, after the
+    observed patterns, nstates blocks of unobserved patterns with weight 0,
+    block s holding for observed pattern p state s at every taxon where p has
+    a state below nstates and STATE_UNKNOWN elsewhere (ASC_VARIANT_MISSING,
+    alignment/alignment.cpp:4158-4180). Returns (patterns, freq, nobs)."""
+    su = STATE_UNKNOWN.get(nstates, nstates)
+    pat = np.asarray(patterns, np.uint8)
+    nobs = pat.shape[1]
+    known = pat < nstates
+    blocks = [np.where(known, np.uint8(s), np.uint8(su)) for s in range(nstates)]
+    return (np.ascontiguousarray(np.concatenate([pat] + blocks, axis=1)),
+            np.concatenate([np.asarray(freq, np.float64), np.zeros(nstates * nobs)]), nobs)
+
+
 def tip_vectors(nstates):
     """Standard-basis tip likelihood per alignment state, rows 0..STATE_UNKNOWN.
 

@@ -27,3 +27,14 @@ def test_op_flags_layout():
                                    (4, 3, 5, 0.3, 0.4)])
     assert arr["flags"].tolist() == [engine.OP_TRANSPOSE1 | engine.OP_ROOTLEAF1, 0]
     assert engine.OP_DTYPE.itemsize == 32
+
+
+def test_asc_holder_patterns_layout():
+    su = models.STATE_UNKNOWN[4]
+    pat = np.array([[0, 3, su], [2, su, 1], [su, 5, 1]], np.uint8)  # DNA; 5 is an ambiguity code
+    ext, freq, nobs = models.asc_holder_patterns(pat, np.array([2.0, 1.0, 3.0]), 4)
+    assert nobs == 3 and ext.shape == (3, 15) and freq.tolist() == [2.0, 1.0, 3.0] + [0.0] * 12
+    # block s = 2, observed pattern 0 (taxa 0 and 1 have data, taxon 2 is missing)
+    assert ext[:, 3 + 2 * 3 + 0].tolist() == [2, 2, su]
+    # ambiguity codes (>= nstates) count as missing, as in the reference
+    assert ext[:, 3 + 1 * 3 + 1].tolist() == [1, su, su]
