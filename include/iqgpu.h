@@ -171,6 +171,9 @@ int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
  * by log(1 - P_const) (tree/phylokernelnew.h:3198-3222, 3405-3420); the
  * derivative adds nsite * (d1/(1-P)) and nsite * (d2/(1-P) + (d1/(1-P))^2)
  * with d1, d2 the constant patterns' summed derivatives (:2620-2628).
+ * The same formula with the uninformative patterns as the unobserved ones is
+ * the correction for informative sites (ASC_INFORMATIVE, alignment/alignment.cpp:
+ * 4181-4192): nconst may be any count below the number of patterns.
  * nconst = 0 switches it off. The batched NNI, group and on-device RELL entry
  * points refuse +ASC engines (IQGPU_ERR_ARG); iqgpu_rell takes the corrected
  * pattern lnL from iqgpu_get_pattern_lh. */

@@ -106,7 +106,8 @@ struct iqgpu_engine {
     // for; d_asc_holder (cudaMalloc) takes their (lh, df, ddf) and two sums
     bool asc_holder;
     int asc_nobs;
-    double *d_asc_holder;
+    double *d_asc_holder;  // also the export buffer of Lewis corrections with more than n patterns
+    long long asc_cap;     // doubles in d_asc_holder
     bool theta_valid;
     int32_t theta_a, theta_b;
     // mixed-precision (FP32 standard-basis) state

@@ -832,6 +832,34 @@ __global__ void __launch_bounds__(kHolderThreads) k_asc_holder_derv(const double
     }
 }
 
+// out[v] = sum_i f(src[i * stride + v]) for v < nval, f = exp or the identity,
+// one CTA in a fixed order (the Lewis correction over any number of patterns)
+__global__ void __launch_bounds__(kHolderThreads) k_asc_sum(const double *src, int count, int stride, int nval,
+                                                            int expv, double *out) {
+    __shared__ double sh[kHolderThreads];
+    for (int v = 0; v < nval; v++) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < count; i += kHolderThreads) {
+            const double x = src[(long long)i * stride + v];
+            acc += expv ? exp(x) : x;
+        }
+        acc = holder_block_sum(acc, sh);
+        if (threadIdx.x == 0) out[v] = acc;
+    }
+}
+
+static int asc_lewis_sums(iqgpu_engine *e, bool derv, double *r) {
+    double *out = e->d_asc_holder ? e->d_asc_holder + (e->asc_cap - 4) : e->d_asc + 3 * kMaxStates - 3;
+    const double *src = derv ? (e->d_asc_holder ? e->d_asc_holder : e->d_asc) : e->d_plh + (e->P - e->asc_n);
+    k_asc_sum<<<1, kHolderThreads, 0, e->st>>>(src, e->asc_n, derv ? 3 : 1, derv ? 3 : 1, derv ? 0 : 1, out);
+    e->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e->h_asc, out, (derv ? 3 : 1) * 8, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    for (int v = 0; v < (derv ? 3 : 1); v++) r[v] = e->h_asc[v];
+    return IQGPU_OK;
+}
+
 static int asc_holder_sums(iqgpu_engine *e, bool derv, double *r0, double *r1) {
     double *out = e->d_asc_holder + 3LL * e->asc_n;
     if (derv)
@@ -861,10 +889,9 @@ static int asc_lnl(iqgpu_engine *e, double *lnl) {
         *lnl -= corr;
         return IQGPU_OK;
     }
-    CK(cudaMemcpyAsync(e->h_asc, e->d_plh + (e->P - e->asc_n), (size_t)e->asc_n * 8, cudaMemcpyDeviceToHost, e->st));
-    CK(cudaStreamSynchronize(e->st));
     double pc = 0.0;
-    for (int i = 0; i < e->asc_n; i++) pc += std::exp(e->h_asc[i]);
+    int rc = asc_lewis_sums(e, false, &pc);
+    if (rc) return rc;
     if (!(pc < 1.0 && pc >= 0.0)) {
         set_error("+ASC: the unobserved constant patterns' probability is outside [0, 1)");
         return IQGPU_ERR_NONFINITE;
@@ -950,14 +977,9 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
         *df += sdf;
         *ddf += sddf;
     } else if (e->asc_n > 0) {  // Lewis +ASC (tree/phylokernelnew.h:2620-2628)
-        CK(cudaMemcpyAsync(e->h_asc, e->d_asc, (size_t)e->asc_n * 24, cudaMemcpyDeviceToHost, e->st));
-        CK(cudaStreamSynchronize(e->st));
-        double lh = 0.0, d1 = 0.0, d2 = 0.0;
-        for (int i = 0; i < e->asc_n; i++) {
-            lh += e->h_asc[3 * i];
-            d1 += e->h_asc[3 * i + 1];
-            d2 += e->h_asc[3 * i + 2];
-        }
+        double s3[3];
+        if ((rc = asc_lewis_sums(e, true, s3))) return rc;
+        const double lh = s3[0], d1 = s3[1], d2 = s3[2];
         const double pv = 1.0 - lh, df_frac = d1 / pv, ddf_frac = d2 / pv;
         *df += e->asc_nsite * df_frac;
         *ddf += e->asc_nsite * (ddf_frac + df_frac * df_frac);
@@ -1000,9 +1022,20 @@ int iqgpu_set_asc(iqgpu_engine *e, int32_t nconst, double nsite) {
         set_error("+ASC is not available with non-reversible models");
         return IQGPU_ERR_ARG;
     }
-    if (!e || nconst < 0 || nconst > e->n || nconst >= e->P || !(nsite >= 0.0)) {
-        set_error("+ASC: need 0 <= nconst <= nstates, nconst < patterns and nsite >= 0");
+    if (!e || nconst < 0 || nconst >= e->P || !(nsite >= 0.0)) {
+        set_error("+ASC: need 0 <= nconst < patterns and nsite >= 0");
         return IQGPU_ERR_ARG;
+    }
+    // more unobserved patterns than the fixed export buffer takes (ASC_INFORMATIVE): a larger one
+    // (an existing buffer, from Holder's correction, is used whenever present, so it must fit too)
+    if ((3LL * nconst > 3LL * kMaxStates - 3 || e->d_asc_holder) && 3LL * nconst + 4 > e->asc_cap) {
+        CK(cudaSetDevice(e->dev));
+        CK(cudaStreamSynchronize(e->st));
+        if (e->d_asc_holder) CK(cudaFree(e->d_asc_holder));
+        e->d_asc_holder = nullptr;
+        e->asc_cap = 0;
+        CK(cudaMalloc(&e->d_asc_holder, (3LL * nconst + 4) * 8));
+        e->asc_cap = 3LL * nconst + 4;
     }
     e->asc_n = nconst;
     e->asc_nsite = nsite;
@@ -1021,7 +1054,9 @@ int iqgpu_set_asc_holder(iqgpu_engine *e, int32_t nobs) {
     CK(cudaStreamSynchronize(e->st));
     if (e->d_asc_holder) CK(cudaFree(e->d_asc_holder));
     e->d_asc_holder = nullptr;
+    e->asc_cap = 0;
     CK(cudaMalloc(&e->d_asc_holder, (3LL * e->n * nobs + 4) * 8));
+    e->asc_cap = 3LL * e->n * nobs + 4;
     e->asc_holder = true;
     e->asc_nobs = nobs;
     e->asc_n = e->n * nobs;

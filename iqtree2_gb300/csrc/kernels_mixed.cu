@@ -453,7 +453,7 @@ static MixBufParams mixbuf_params(iqgpu_engine *e, double len) {
     P.red.ticket = e->d_ticket;
     P.red.out = e->d_red_out;
     P.asc_first = (int)(e->P - e->asc_n);
-    P.asc_out = e->asc_holder ? e->d_asc_holder : e->d_asc;
+    P.asc_out = e->d_asc_holder ? e->d_asc_holder : e->d_asc;
     return P;
 }
 

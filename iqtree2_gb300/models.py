@@ -162,6 +162,31 @@ def asc_lewis_patterns(patterns, freq, nstates, pi=None):
     return out, f, len(extra), float(np.asarray(freq).sum())
 
 
+def asc_informative_patterns(ntaxa, nstates, limit=200000):
+    """Every uninformative pattern, the unobserved patterns of the +ASC
+    correction for informative sites (ASC_INFORMATIVE, Lewis's formula over
+    them; alignment/alignment.cpp:4104-4138, 4181-4192): for each repeat state
+    r and each subset T of the other states (in bitmask order) with |T| <
+    ntaxa - 1, or |T| = ntaxa - 1 when r = 0, every placement of T's states
+    (in order) on distinct taxa (taxa tuples in lexicographic order), all other
+    taxa in state r. Returns uint8 (ntaxa, count)."""
+    from itertools import permutations
+    out = []
+    for r in range(nstates):
+        rest = [s for s in range(nstates) if s != r]
+        for mask in range(1 << len(rest)):
+            T = [rest[i] for i in range(len(rest)) if mask & (1 << i)]
+            if not (len(T) < ntaxa - 1 or (len(T) == ntaxa - 1 and r == 0)):
+                continue
+            for pos in permutations(range(ntaxa), len(T)):
+                col = np.full(ntaxa, r, np.uint8)
+                col[list(pos)] = T
+                out.append(col)
+                if len(out) > limit:
+                    raise ValueError("too many uninformative patterns")
+    return np.ascontiguousarray(np.stack(out, axis=1))
+
+
 def asc_holder_patterns(patterns, freq, nstates):
     """Holder's +ASC for variant sites with missing data: append, after the
     observed patterns, nstates blocks of unobserved patterns with weight 0,

@@ -94,3 +94,52 @@ def test_asc_holder_argument_checks():
             engine.Group([e])           # +ASC engines cannot join a group
     finally:
         e.close()
+
+
+@pytest.mark.parametrize("precision", [engine.F64, engine.F32])
+def test_asc_informative(precision):
+    """+ASC for informative sites (ASC_INFORMATIVE): Lewis's formula over all
+    7,012 uninformative DNA patterns of 12 taxa, appended with weight 0;
+    lnL against the numpy pruning, derivatives against its central
+    differences."""
+    ds = simulate.dna_gtr_dataset(12, 800, 83)
+    m = ds.model
+    un = models.asc_informative_patterns(ds.ntaxa, m.nstates)
+    pat_ext = np.ascontiguousarray(np.concatenate([ds.patterns, un], axis=1))
+    freq_ext = np.concatenate([ds.freq, np.zeros(un.shape[1])])
+    nsite = float(ds.freq.sum())
+    nobs = ds.patterns.shape[1]
+    f64 = precision == engine.F64
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+
+    def want_at(lens):
+        _, plh = stdbasis.tree_lnl(m, pat_ext, freq_ext, ds.edges, lens, ds.ntaxa)
+        return float(plh[:nobs] @ ds.freq) - nsite * np.log(1.0 - np.exp(plh[nobs:]).sum())
+
+    e = engine.Engine(pat_ext.shape[1], m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                      precision=precision)
+    try:
+        e.set_model(m)
+        e.set_patterns(freq_ext)
+        e.set_tip_states(pat_ext)
+        e.set_asc(un.shape[1], nsite)
+        k = next(i for i, ed in enumerate(ds.edges) if min(ed) >= ds.ntaxa)
+        n1, n2 = map(int, ds.edges[k])
+        ops = e.ops_array(topo.ops_for(n1, n2, set()) + topo.ops_for(n2, n1, set()))
+        a, b = topo.ref(n1, n2), topo.ref(n2, n1)
+        got = e.compute_likelihood(ops, a, b, ds.lengths[k])
+        assert rel(got, want_at(ds.lengths)) < (1e-10 if f64 else 1e-6)
+        h = 1e-5
+        for x in (0.05, 0.3):
+            lens = [ds.lengths.copy() for _ in range(3)]
+            for L, d in zip(lens, (0.0, h, -h)):
+                L[k] = x + d
+            l0, lp, lm = (want_at(L) for L in lens)
+            fd1, fd2 = (lp - lm) / (2 * h), (lp - 2 * l0 + lm) / h ** 2
+            df, ddf = e.likelihood_derv(ops, a, b, x)
+            r1, floor = (1e-6, 1e-6) if f64 else (1e-4, 1e-5)
+            assert abs(df - fd1) <= r1 * abs(fd1) + floor * nsite, (df, fd1)
+            assert abs(ddf - fd2) <= 1e-2 * abs(fd2) + 1e-5 * nsite, (ddf, fd2)
+            assert rel(e.lnl_from_buffer(x), l0) < (1e-10 if f64 else 1e-6)
+    finally:
+        e.close()

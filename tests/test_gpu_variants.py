@@ -186,7 +186,7 @@ def test_asc_refused_by_batched_paths():
     with pytest.raises(engine.EngineError):
         engine.Group([eng])
     with pytest.raises(engine.EngineError):
-        eng.set_asc(99, nsite)  # more constant patterns than states
+        eng.set_asc(eng.nptn, nsite)  # no observed pattern left
 
 
 def _mixture(data, nclass, ncat_rate, seed):

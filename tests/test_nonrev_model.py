@@ -38,3 +38,12 @@ def test_asc_holder_patterns_layout():
     assert ext[:, 3 + 2 * 3 + 0].tolist() == [2, 2, su]
     # ambiguity codes (>= nstates) count as missing, as in the reference
     assert ext[:, 3 + 1 * 3 + 1].tolist() == [1, su, su]
+
+
+def test_asc_informative_patterns_are_uninformative_and_distinct():
+    p = models.asc_informative_patterns(6, 4)
+    cols = {tuple(c) for c in p.T}
+    assert len(cols) == p.shape[1]                        # no pattern twice
+    for c in p.T:                                         # at most one state occurs twice or more
+        counts = np.bincount(c, minlength=4)
+        assert (counts >= 2).sum() <= 1
