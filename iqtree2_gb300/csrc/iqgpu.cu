@@ -351,13 +351,13 @@ int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out) {
 
 // FP64 values as FP32 pairs hi = fl(v), lo = fl(v - hi) ([hi x count][lo x count]),
 // the split the double-float precompute multiplies with
-static cudaError_t upload_hilo(float *dst, const double *v, size_t count) {
+static cudaError_t upload_hilo(float *dst, const double *v, size_t count, cudaStream_t st) {
     std::vector<float> hl(2 * count);
     for (size_t i = 0; i < count; i++) {
         hl[i] = (float)v[i];
         hl[count + i] = (float)(v[i] - (double)hl[i]);
     }
-    return cudaMemcpy(dst, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice);
+    return cudaMemcpyAsync(dst, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice, st);
 }
 
 static void check_unit_tips(iqgpu_engine *e) {
@@ -372,12 +372,11 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     if (!e || !eval || !evec || !inv_evec || !rates || !props) { set_error("null argument"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
     const size_t n = e->n, C = e->C;
-    CK(cudaStreamSynchronize(e->st));
-    CK(cudaMemcpy(e->d_eval, eval, n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_evec, evec, n * n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_inv, inv_evec, n * n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_props, props, C * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(e->d_eval, eval, n * 8, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_evec, evec, n * n * 8, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_inv, inv_evec, n * n * 8, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_props, props, C * 8, cudaMemcpyHostToDevice, e->st));
     std::memcpy(e->h_eval, eval, n * 8);
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
@@ -389,8 +388,8 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
         for (size_t i = 0; i < n; i++)
             for (size_t j = 0; j < n; j++) inv32[i * e->npad + j] = (float)inv_evec[i * n + j];
         float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
-        CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
-        if (e->d_ivhl) CK(upload_hilo(e->d_ivhl, inv_evec, n * n));
+        CK(cudaMemcpyAsync(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice, e->st));
+        if (e->d_ivhl) CK(upload_hilo(e->d_ivhl, inv_evec, n * n, e->st));
     }
     e->have_model = true;
     e->theta_valid = false;
@@ -437,8 +436,8 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
         CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
     }
     if (mixed && e->d_ivhl) {
-        for (size_t m = 0; m < K; m++) CK(upload_hilo(e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n));
-        CK(upload_hilo(e->d_tiphl, tip_lh, S1 * K * n));
+        for (size_t m = 0; m < K; m++) CK(upload_hilo(e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n, e->st));
+        CK(upload_hilo(e->d_tiphl, tip_lh, S1 * K * n, e->st));
     }
     // leaf-table shortcut: every class's unambiguous tip vectors are columns of its U^-1
     bool unit = true;
@@ -504,8 +503,7 @@ int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq) {
     if (!e || !state_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
     // the eigen-space FP64 path folds pi into U^-1; its non-reversible kernels weigh the branch by these
     CK(cudaSetDevice(e->dev));
-    CK(cudaStreamSynchronize(e->st));
-    CK(cudaMemcpy(e->d_pi, state_freq, (size_t)e->n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(e->d_pi, state_freq, (size_t)e->n * 8, cudaMemcpyHostToDevice, e->st));
     e->have_pi = true;
     return IQGPU_OK;
 }
@@ -517,9 +515,8 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
         return IQGPU_ERR_STATE;
     }
     CK(cudaSetDevice(e->dev));
-    CK(cudaStreamSynchronize(e->st));
-    CK(cudaMemcpy(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice));
-    if (e->d_tiphl) CK(upload_hilo(e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n));
+    CK(cudaMemcpyAsync(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice, e->st));
+    if (e->d_tiphl) CK(upload_hilo(e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n, e->st));
     std::memcpy(e->h_tipv, tip_lh, (size_t)e->n * e->n * 8);
     e->have_tips = true;
     check_unit_tips(e);
@@ -529,10 +526,9 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
 int iqgpu_set_patterns(iqgpu_engine *e, const double *ptn_freq, const double *ptn_invar) {
     if (!e || !ptn_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
-    CK(cudaStreamSynchronize(e->st));
-    CK(cudaMemcpy(e->d_freq, ptn_freq, (size_t)e->P * 8, cudaMemcpyHostToDevice));
-    if (ptn_invar) CK(cudaMemcpy(e->d_invar, ptn_invar, (size_t)e->P * 8, cudaMemcpyHostToDevice));
-    else CK(cudaMemset(e->d_invar, 0, (size_t)e->Ppad * 8));
+    CK(cudaMemcpyAsync(e->d_freq, ptn_freq, (size_t)e->P * 8, cudaMemcpyHostToDevice, e->st));
+    if (ptn_invar) CK(cudaMemcpyAsync(e->d_invar, ptn_invar, (size_t)e->P * 8, cudaMemcpyHostToDevice, e->st));
+    else CK(cudaMemsetAsync(e->d_invar, 0, (size_t)e->Ppad * 8, e->st));
     e->have_patterns = true;
     return IQGPU_OK;
 }
