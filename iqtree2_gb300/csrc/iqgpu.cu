@@ -554,10 +554,10 @@ __global__ void k_check_states(const uint4 *__restrict__ st, long long n16, unsi
 int iqgpu_set_tip_states(iqgpu_engine *e, const uint8_t *states) {
     if (!e || !states) { set_error("null argument"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
-    CK(cudaStreamSynchronize(e->st));
     e->have_states = false;
-    CK(cudaMemcpy2D(e->d_states, (size_t)e->Ppad, states, (size_t)e->P, (size_t)e->P, (size_t)e->cfg.ntaxa,
-                    cudaMemcpyHostToDevice));
+    // stream-ordered: after any traversal still reading the previous states
+    CK(cudaMemcpy2DAsync(e->d_states, (size_t)e->Ppad, states, (size_t)e->P, (size_t)e->P, (size_t)e->cfg.ntaxa,
+                         cudaMemcpyHostToDevice, e->st));
     // the range check runs on the uploaded copy (a byte loop over the host
     // array would cost more than the whole likelihood evaluation)
     int *bad = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 56);
