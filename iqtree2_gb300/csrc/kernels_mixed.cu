@@ -97,7 +97,7 @@ __device__ __forceinline__ void df_split(double v, float &h, float &l) {
 // L1. Each output is a double-float dot product of length n, rounded once to
 // FP32 at the end. GB300 runs FP64 FMAs ~60x slower than FP32; the result is
 // stored in FP32, so the 44-bit double-float sums lose nothing that is kept.
-constexpr int kPiRows = 16;
+constexpr int kPiRows = 8;
 __global__ void __launch_bounds__(256) k_partial_info_df(const OpDev *__restrict__ ops, float *__restrict__ opmats,
                                                          long long op_stride, const double *__restrict__ evec,
                                                          const double *__restrict__ eval,
