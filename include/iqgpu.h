@@ -70,7 +70,9 @@ typedef struct {
     int32_t ntaxa;         /* leaves */
     int32_t state_unknown; /* aln->STATE_UNKNOWN, <= 255 */
     int32_t nslots;        /* partial-likelihood slots to reserve in HBM */
-    int32_t safe;          /* 1 = SAFE (scale count per pattern x category), 0 = NORM */
+    int32_t safe;          /* 1 = SAFE (scale count per pattern x category), 0 = NORM; the engine
+                              turns SAFE on by the reference's rule unless
+                              IQGPU_FLAG_SAFE_AS_GIVEN (see below) */
     int32_t precision;     /* IQGPU_F64 ... */
     int32_t device;        /* CUDA device ordinal */
     int32_t max_ops;       /* largest traversal the engine must accept (>= ntaxa) */
@@ -82,6 +84,13 @@ typedef struct {
  * block entry twice when nstates is odd and N is even (codon +G4). Off by
  * default: the engine then returns the exact derivative of lnL. */
 #define IQGPU_FLAG_REF_TRIPLE_TAIL 1
+/* The reference picks SAFE scaling by itself (PhyloTree::setLikelihoodKernel,
+ * tree/phylotreesse.cpp:95-96): with -safe, for trees of 2000 taxa or more
+ * (params->numseq_safe_scaling, utils/tools.cpp:1262) and for every model
+ * whose state count is not 4 or 20 (codon, binary, morphology). The engine
+ * applies the same rule to cfg.safe at creation (iqgpu_get_config returns
+ * the result); this flag takes cfg.safe as given instead. */
+#define IQGPU_FLAG_SAFE_AS_GIVEN 2
 
 /* One TraversalInfo entry (tree/phylotree.h:320-333): compute the partial of
  * dad_slot from two children with their branch lengths. flags is 0 for

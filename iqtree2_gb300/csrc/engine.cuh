@@ -20,6 +20,9 @@ constexpr int kTPB = 128;        // threads (= patterns) per CTA in the pattern-
 constexpr int kMaxStates = 64;
 constexpr int kPairCounters = 8192;  // (op, tile) pairs of one category-split tensor-core level
 constexpr int kMaxCat = 16;
+// params->numseq_safe_scaling default (utils/tools.cpp:1262): from this many
+// taxa on, the reference switches to SAFE scaling
+constexpr int kSafeScalingTaxa = 2000;
 
 // Device copy of one traversal entry plus the offset of its per-op matrices.
 struct OpDev {

@@ -47,6 +47,20 @@ static int check_config(const iqgpu_config *c) {
     return IQGPU_OK;
 }
 
+// The reference's kernel choice (PhyloTree::setLikelihoodKernel,
+// tree/phylotreesse.cpp:95-96): SAFE scaling when asked for (-safe), when the
+// tree has params->numseq_safe_scaling (2000) taxa or more, and whenever the
+// model has other than 4 or 20 states. IQGPU_FLAG_SAFE_AS_GIVEN takes cfg.safe
+// as it is.
+static iqgpu_config normalized(const iqgpu_config *c) {
+    iqgpu_config r = *c;
+    if (!(c->flags & IQGPU_FLAG_SAFE_AS_GIVEN) &&
+        (c->ntaxa >= kSafeScalingTaxa || (c->nstates != 4 && c->nstates != 20)))
+        r.safe = 1;
+    r.safe = r.safe ? 1 : 0;
+    return r;
+}
+
 static bool is_mixed(const iqgpu_config *c) { return c->precision != IQGPU_F64; }
 // tensor-core contraction (split TF32 or BF16): 20- and 61-state models (any
 // 16 <= n <= 64); smaller state spaces stay on the FP32 CUDA-core kernels
@@ -118,7 +132,8 @@ int iqgpu_memory_required(const iqgpu_config *cfg, size_t *bytes) {
     int rc = check_config(cfg);
     if (rc) return rc;
     if (!bytes) { set_error("null output"); return IQGPU_ERR_ARG; }
-    *bytes = (size_t)sizes(cfg).total;
+    const iqgpu_config eff = normalized(cfg);
+    *bytes = (size_t)sizes(&eff).total;
     return IQGPU_OK;
 }
 
@@ -187,9 +202,11 @@ int iqgpu_create_in(const iqgpu_config *cfg, void *dev_mem, size_t bytes, iqgpu_
     return create_engine(cfg, dev_mem, bytes, out);
 }
 
-static int create_engine(const iqgpu_config *cfg, void *dev_mem, size_t dev_bytes, iqgpu_engine **out) {
-    int rc = check_config(cfg);
+static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_bytes, iqgpu_engine **out) {
+    int rc = check_config(cfg_in);
     if (rc) return rc;
+    const iqgpu_config cfg_eff = normalized(cfg_in);
+    const iqgpu_config *cfg = &cfg_eff;
     if (!out) { set_error("null output"); return IQGPU_ERR_ARG; }
     *out = nullptr;
     int ndev = 0;

@@ -35,6 +35,9 @@ class Config(ct.Structure):
 
 
 FLAG_REF_TRIPLE_TAIL = 1
+# take cfg.safe as given instead of the reference's SAFE rule (SAFE for
+# nstates not in {4, 20} and for 2000 taxa or more, tree/phylotreesse.cpp:95-96)
+FLAG_SAFE_AS_GIVEN = 2
 
 
 class Op(ct.Structure):
@@ -162,7 +165,9 @@ class Engine:
         _check(lib().iqgpu_create(ct.byref(self.cfg), ct.byref(h)))
         self.h = h
         self.nptn, self.nstates, self.ncat, self.ntaxa = int(nptn), int(nstates), int(ncat), int(ntaxa)
-        self.safe = bool(safe)
+        eff = Config()
+        _check(lib().iqgpu_get_config(self.h, ct.byref(eff)))
+        self.safe = bool(eff.safe)  # after the reference's SAFE rule
         self.precision = int(precision)
 
     @property

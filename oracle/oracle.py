@@ -49,7 +49,7 @@ def lib():
         L.orc_tree_num_updates.restype = ct.c_longlong
         L.orc_tree_get_partial.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, dp, u8p]
         L.orc_tree_derv.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_double, dp, dp]
-        L.orc_tree_lnl_branch.argtypes = [ct.c_void_p, ct.c_int, ct.c_int]
+        L.orc_tree_lnl_branch.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, dp]
         L.orc_tree_lnl_branch.restype = ct.c_double
         _lib = L
     return _lib
@@ -158,8 +158,10 @@ class OracleTree:
             raise ValueError("not a branch")
         return df.value, ddf.value
 
-    def lnl_branch(self, node, dad):
-        return lib().orc_tree_lnl_branch(self.h, node, dad)
+    def lnl_branch(self, node, dad, want_pattern_lh=False):
+        plh = np.zeros(self.m.nptn) if want_pattern_lh else None
+        v = lib().orc_tree_lnl_branch(self.h, node, dad, _dp(plh) if plh is not None else None)
+        return (v, plh) if want_pattern_lh else v
 
     def partial(self, node, nbr):
         """Partial of directed branch node->nbr in the reference layout [ptn][c][x]."""

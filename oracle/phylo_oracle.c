@@ -1,8 +1,13 @@
 /*
  * CPU FP64 oracle -- see phylo_oracle.h. TEST INFRASTRUCTURE ONLY.
  *
- * Parity unpinned against the reference (no buildable reference, no golden
- * vectors in its tests); pinned by analytic known-answer tests.
+ * Pinned to the reference: tests/test_ref_kernels.py compiles IQ-TREE 2's own
+ * kernel templates (tree/phylokernelnew.h, one-lane Vec1d kernels) into
+ * oracle/_ref/ and checks that this file reproduces them BIT FOR BIT (every
+ * partial and scale count, branch lnL, pattern lnL, derivatives), NORM and
+ * SAFE, on seeded fixtures, on a tree that underflows 2^-256 and on the
+ * reference's own test alignments; tests/golden/ref_*.npz keep the
+ * reference's outputs for machines without a reference checkout.
  *
  * Function-by-function restatement of IQ-TREE 2 (paths relative to the
  * iqtree2 source root):
@@ -18,10 +23,14 @@
  *   optimize_all_branches   tree/phylotree.cpp:2698-2774, computeBestTraversal :2689
  *   farthest leaf, preorder tree/mtree.cpp:3040-3082
  *   clear_reverse           tree/phylonode.cpp:22-33
- * The summation helpers keep the reference's accumulator split
- * (dotProductDualVec :214-314, productVecMat :449-567, dotProductVec,
- * dotProduct3Vec :737-793, dotProductTriple :666-725, sumVec :44-70) so the
- * oracle rounds the way the reference's one-lane build does.
+ * The summation helpers restate the reference's vector helpers as its
+ * one-lane build compiles them (JAMES_VERSION dotProductVec :83-126,
+ * dotProductDualVec :214-314, productVecMat :449-567, dotProduct3Vec
+ * :737-793, dotProductTriple :666-725, sumVec :44-70), with the one-lane
+ * mul_add as a separately rounded multiply and add; the file is compiled with
+ * -ffp-contract=off. Sums over patterns split across OpenMP threads differ
+ * from the reference's packet split by rounding only; with one thread they
+ * are the reference's.
  */
 #include "phylo_oracle.h"
 
@@ -33,59 +42,147 @@
 #endif
 
 /* ------------------------------------------------------------------ */
-/* summation helpers (one-lane restatements)                            */
+/* summation helpers: the reference's vector helpers on one lane        */
 /* ------------------------------------------------------------------ */
 
+/* The one-lane vector class of the reference (vectorclass/vectorf64.h:
+ * 339-351) multiplies and adds with two roundings; this file is compiled with
+ * -ffp-contract=off so the compiler fuses nothing either. */
+static inline double mul_add(double a, double b, double c) { return a * b + c; }
+static inline double nmul_add(double a, double b, double c) { return c - a * b; }
+
+/* dotProductVec as compiled (JAMES_VERSION, tree/phylokernelnew.h:83-126):
+ * four accumulators over A[0..N-cruft), the N%4 tail added into the first
+ * accumulators in turn, then (X+v1)+(v2+v3); N == 4 and N < 4 have their own
+ * forms. */
 static double dot_vec(const double *A, const double *B, int N) {
+    if (N == 4) return (A[0] * B[0] + A[1] * B[1]) + (A[2] * B[2] + A[3] * B[3]);
+    const int cruft = N & 3;
+    if (N == cruft) {
+        double X = 0.0;
+        for (int i = 0; i < cruft; i++) X = mul_add(A[i], B[i], X);
+        return X;
+    }
+    double X = A[0] * B[0], v1 = A[1] * B[1], v2 = A[2] * B[2], v3 = A[3] * B[3];
+    int i = 4;
+    for (; i < N - cruft; i += 4) {
+        X = mul_add(A[i], B[i], X);
+        v1 = mul_add(A[i + 1], B[i + 1], v1);
+        v2 = mul_add(A[i + 2], B[i + 2], v2);
+        v3 = mul_add(A[i + 3], B[i + 3], v3);
+    }
+    if (cruft > 0) {
+        X = mul_add(A[i], B[i], X);
+        if (cruft > 1) {
+            v1 = mul_add(A[i + 1], B[i + 1], v1);
+            if (cruft > 2) v2 = mul_add(A[i + 2], B[i + 2], v2);
+        }
+    }
+    return (X + v1) + (v2 + v3);
+}
+
+/* X = (A.B) * (C.D), dotProductDualVec (tree/phylokernelnew.h:214-314). The
+ * second factor of the N%4 = 0 and 1 forms is summed ((CD0+CD1)+CD2)+CD3. */
+static double dot_dual(const double *A, const double *B, const double *C, const double *D, int N) {
     switch (N) {
-    case 1: return A[0] * B[0];
-    case 2: return fma(A[1], B[1], A[0] * B[0]);
-    case 3: return fma(A[2], B[2], fma(A[1], B[1], A[0] * B[0]));
-    case 4: return fma(A[1], B[1], A[0] * B[0]) + fma(A[3], B[3], A[2] * B[2]);
+    case 1: return (A[0] * B[0]) * (C[0] * D[0]);
+    case 2: return mul_add(A[1], B[1], A[0] * B[0]) * mul_add(C[1], D[1], C[0] * D[0]);
+    case 3:
+        return mul_add(A[2], B[2], mul_add(A[1], B[1], A[0] * B[0])) *
+               mul_add(C[2], D[2], mul_add(C[1], D[1], C[0] * D[0]));
+    case 4:
+        return (mul_add(A[1], B[1], A[0] * B[0]) + mul_add(A[3], B[3], A[2] * B[2])) *
+               (mul_add(C[1], D[1], C[0] * D[0]) + mul_add(C[3], D[3], C[2] * D[2]));
     default: break;
     }
-    double V[4];
+    double AB[4], CD[4];
     int i, j;
     switch (N % 4) {
     case 0:
-        for (j = 0; j < 4; j++) V[j] = A[j] * B[j];
+        for (j = 0; j < 4; j++) { AB[j] = A[j] * B[j]; CD[j] = C[j] * D[j]; }
         for (i = 4; i < N; i += 4)
-            for (j = 0; j < 4; j++) V[j] = fma(A[i + j], B[i + j], V[j]);
-        return (V[0] + V[1]) + (V[2] + V[3]);
+            for (j = 0; j < 4; j++) {
+                AB[j] = mul_add(A[i + j], B[i + j], AB[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
+            }
+        return ((AB[0] + AB[1]) + (AB[2] + AB[3])) * (((CD[0] + CD[1]) + CD[2]) + CD[3]);
     case 1:
-        for (j = 0; j < 4; j++) V[j] = A[j] * B[j];
+        for (j = 0; j < 4; j++) { AB[j] = A[j] * B[j]; CD[j] = C[j] * D[j]; }
         for (i = 4; i < N - 1; i += 4)
-            for (j = 0; j < 4; j++) V[j] = fma(A[i + j], B[i + j], V[j]);
-        return fma(A[N - 1], B[N - 1], (V[0] + V[1]) + (V[2] + V[3]));
+            for (j = 0; j < 4; j++) {
+                AB[j] = mul_add(A[i + j], B[i + j], AB[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
+            }
+        return mul_add(A[N - 1], B[N - 1], (AB[0] + AB[1]) + (AB[2] + AB[3])) *
+               mul_add(C[N - 1], D[N - 1], ((CD[0] + CD[1]) + CD[2]) + CD[3]);
     case 2:
-        for (j = 0; j < 2; j++) V[j] = A[j] * B[j];
+        for (j = 0; j < 2; j++) { AB[j] = A[j] * B[j]; CD[j] = C[j] * D[j]; }
         for (i = 2; i < N; i += 2)
-            for (j = 0; j < 2; j++) V[j] = fma(A[i + j], B[i + j], V[j]);
-        return V[0] + V[1];
+            for (j = 0; j < 2; j++) {
+                AB[j] = mul_add(A[i + j], B[i + j], AB[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
+            }
+        return (AB[0] + AB[1]) * (CD[0] + CD[1]);
     default:
-        for (j = 0; j < 2; j++) V[j] = A[j] * B[j];
+        for (j = 0; j < 2; j++) { AB[j] = A[j] * B[j]; CD[j] = C[j] * D[j]; }
         for (i = 2; i < N - 1; i += 2)
-            for (j = 0; j < 2; j++) V[j] = fma(A[i + j], B[i + j], V[j]);
-        return fma(A[N - 1], B[N - 1], V[0] + V[1]);
+            for (j = 0; j < 2; j++) {
+                AB[j] = mul_add(A[i + j], B[i + j], AB[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
+            }
+        return mul_add(A[N - 1], B[N - 1], AB[0] + AB[1]) * mul_add(C[N - 1], D[N - 1], CD[0] + CD[1]);
     }
 }
 
-/* X = (A.B) * (C.D) */
-static double dot_dual(const double *A, const double *B, const double *C, const double *D, int N) {
-    return dot_vec(A, B, N) * dot_vec(C, D, N);
+/* One row of productVecMat (tree/phylokernelnew.h:449-567): sum_j A[j]*M[j]
+ * with the reference's per-N unrolling. */
+static double vec_mat_row(const double *A, const double *M, int N) {
+    switch (N) {
+    case 1: return A[0] * M[0];
+    case 2: return mul_add(A[1], M[1], A[0] * M[0]);
+    case 3: return mul_add(A[2], M[2], mul_add(A[1], M[1], A[0] * M[0]));
+    case 4: return mul_add(A[1], M[1], A[0] * M[0]) + mul_add(A[3], M[3], A[2] * M[2]);
+    default: break;
+    }
+    double V[4];
+    int x, j;
+    switch (N % 4) {
+    case 0:
+        for (j = 0; j < 4; j++) V[j] = A[j] * M[j];
+        for (x = 4; x < N; x += 4)
+            for (j = 0; j < 4; j++) V[j] = mul_add(A[x + j], M[x + j], V[j]);
+        return (V[0] + V[1]) + (V[2] + V[3]);
+    case 1:
+        for (j = 0; j < 4; j++) V[j] = A[j] * M[j];
+        for (x = 4; x < N - 1; x += 4)
+            for (j = 0; j < 4; j++) V[j] = mul_add(A[x + j], M[x + j], V[j]);
+        return mul_add(A[N - 1], M[N - 1], (V[0] + V[1]) + (V[2] + V[3]));
+    case 2:
+        for (j = 0; j < 2; j++) V[j] = A[j] * M[j];
+        for (x = 2; x < N; x += 2)
+            for (j = 0; j < 2; j++) V[j] = mul_add(A[x + j], M[x + j], V[j]);
+        return V[0] + V[1];
+    default:
+        for (j = 0; j < 2; j++) V[j] = A[j] * M[j];
+        for (x = 2; x < N - 1; x += 2)
+            for (j = 0; j < 2; j++) V[j] = mul_add(A[x + j], M[x + j], V[j]);
+        return mul_add(A[N - 1], M[N - 1], V[0] + V[1]);
+    }
 }
 
-/* X[i] = sum_j A[j] * M[i*N+j]; returns updated running max |X|. */
+/* X[i] = sum_j A[j] * M[i*N+j]; returns the updated running max |X|
+ * (productVecMat with Xmax, tree/phylokernelnew.h:449-567). */
 static double prod_vec_mat(const double *A, const double *M, double *X, int N, double xmax) {
     for (int i = 0; i < N; i++) {
-        X[i] = dot_vec(A, M + (size_t)i * N, N);
+        X[i] = vec_mat_row(A, M + (size_t)i * N, N);
         double a = fabs(X[i]);
         if (a > xmax) xmax = a;
     }
     return xmax;
 }
 
-/* X = sum A[i]*B[i]*C[i] */
+/* X = sum A[i]*B[i]*C[i], dotProduct3Vec (tree/phylokernelnew.h:737-793):
+ * no special form for N <= 4. */
 static double dot3(const double *A, const double *B, const double *C, int N) {
     double V[4];
     int i, j;
@@ -93,27 +190,29 @@ static double dot3(const double *A, const double *B, const double *C, int N) {
     case 0:
         for (j = 0; j < 4; j++) V[j] = A[j] * B[j] * C[j];
         for (i = 4; i < N; i += 4)
-            for (j = 0; j < 4; j++) V[j] = fma(A[i + j] * B[i + j], C[i + j], V[j]);
+            for (j = 0; j < 4; j++) V[j] = mul_add(A[i + j] * B[i + j], C[i + j], V[j]);
         return (V[0] + V[1]) + (V[2] + V[3]);
     case 1:
         for (j = 0; j < 4; j++) V[j] = A[j] * B[j] * C[j];
         for (i = 4; i < N - 1; i += 4)
-            for (j = 0; j < 4; j++) V[j] = fma(A[i + j] * B[i + j], C[i + j], V[j]);
-        return fma(A[N - 1] * B[N - 1], C[N - 1], (V[0] + V[1]) + (V[2] + V[3]));
+            for (j = 0; j < 4; j++) V[j] = mul_add(A[i + j] * B[i + j], C[i + j], V[j]);
+        return mul_add(A[N - 1] * B[N - 1], C[N - 1], (V[0] + V[1]) + (V[2] + V[3]));
     case 2:
         for (j = 0; j < 2; j++) V[j] = A[j] * B[j] * C[j];
         for (i = 2; i < N; i += 2)
-            for (j = 0; j < 2; j++) V[j] = fma(A[i + j] * B[i + j], C[i + j], V[j]);
+            for (j = 0; j < 2; j++) V[j] = mul_add(A[i + j] * B[i + j], C[i + j], V[j]);
         return V[0] + V[1];
     default:
         for (j = 0; j < 2; j++) V[j] = A[j] * B[j] * C[j];
         for (i = 2; i < N - 1; i += 2)
-            for (j = 0; j < 2; j++) V[j] = fma(A[i + j] * B[i + j], C[i + j], V[j]);
-        return fma(A[N - 1] * B[N - 1], C[N - 1], V[0] + V[1]);
+            for (j = 0; j < 2; j++) V[j] = mul_add(A[i + j] * B[i + j], C[i + j], V[j]);
+        return mul_add(A[N - 1] * B[N - 1], C[N - 1], V[0] + V[1]);
     }
 }
 
-/* (X,Y,Z) = (A.D, B.D, C.D) over N = block entries; nstates parity picks the split. */
+/* (X,Y,Z) = (A.D, B.D, C.D) over N = block entries, dotProductTriple
+ * (tree/phylokernelnew.h:666-725) with ADD = false; the parity of
+ * `nstates` picks the two-accumulator form, as in the reference. */
 static void dot_triple(const double *A, const double *B, const double *C, const double *D,
                        int N, int nstates, double *X, double *Y, double *Z) {
     double AD[2], BD[2], CD[2];
@@ -126,9 +225,9 @@ static void dot_triple(const double *A, const double *B, const double *C, const 
     if ((nstates & 1) == 0) {
         for (i = 2; i < N; i += 2)
             for (j = 0; j < 2; j++) {
-                AD[j] = fma(A[i + j], D[i + j], AD[j]);
-                BD[j] = fma(B[i + j], D[i + j], BD[j]);
-                CD[j] = fma(C[i + j], D[i + j], CD[j]);
+                AD[j] = mul_add(A[i + j], D[i + j], AD[j]);
+                BD[j] = mul_add(B[i + j], D[i + j], BD[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
             }
         *X = AD[0] + AD[1];
         *Y = BD[0] + BD[1];
@@ -136,13 +235,13 @@ static void dot_triple(const double *A, const double *B, const double *C, const 
     } else {
         for (i = 2; i < N - 1; i += 2)
             for (j = 0; j < 2; j++) {
-                AD[j] = fma(A[i + j], D[i + j], AD[j]);
-                BD[j] = fma(B[i + j], D[i + j], BD[j]);
-                CD[j] = fma(C[i + j], D[i + j], CD[j]);
+                AD[j] = mul_add(A[i + j], D[i + j], AD[j]);
+                BD[j] = mul_add(B[i + j], D[i + j], BD[j]);
+                CD[j] = mul_add(C[i + j], D[i + j], CD[j]);
             }
-        *X = fma(A[N - 1], D[N - 1], AD[0] + AD[1]);
-        *Y = fma(B[N - 1], D[N - 1], BD[0] + BD[1]);
-        *Z = fma(C[N - 1], D[N - 1], CD[0] + CD[1]);
+        *X = mul_add(A[N - 1], D[N - 1], AD[0] + AD[1]);
+        *Y = mul_add(B[N - 1], D[N - 1], BD[0] + BD[1]);
+        *Z = mul_add(C[N - 1], D[N - 1], CD[0] + CD[1]);
     }
 }
 
@@ -190,13 +289,21 @@ static void orc_echild(const orc_model *m, double len, double *echild) {
     }
 }
 
+/* A[0]*B[0] + A[1]*B[1] + ..., left to right (computePartialInfo's one-lane
+ * leaf-table sum, tree/phylokernelnew.h:1037-1046) */
+static double seq_dot(const double *A, const double *B, int N) {
+    double v = A[0] * B[0];
+    for (int i = 1; i < N; i++) v = mul_add(A[i], B[i], v);
+    return v;
+}
+
 /* leaf[s][c][x] = sum_i echild[c][x][i]*tip_lh[s][i]; unknown state row = 1.0 */
 static void orc_leaf_table(const orc_model *m, const double *echild, double *leaf) {
     int n = m->nstates, B = n * m->ncat, S = m->state_unknown;
     for (int s = 0; s < S; s++)
         for (int c = 0; c < m->ncat; c++)
             for (int x = 0; x < n; x++)
-                leaf[(size_t)s * B + c * n + x] = dot_vec(echild + ((size_t)c * n + x) * n, m->tip_lh + (size_t)s * n, n);
+                leaf[(size_t)s * B + c * n + x] = seq_dot(echild + ((size_t)c * n + x) * n, m->tip_lh + (size_t)s * n, n);
     for (int k = 0; k < B; k++) leaf[(size_t)S * B + k] = 1.0;
 }
 
@@ -424,7 +531,7 @@ double orc_branch_lnl(const orc_model *m, const double *partials, const uint8_t 
             }
             lh = log(lh) + sc;
             plh[ptn] = lh;
-            acc = fma(lh, m->ptn_freq[ptn], acc);
+            acc = mul_add(lh, m->ptn_freq[ptn], acc);
         }
         thread_sum[tid] = acc;
         thread_const[tid] = pconst;
@@ -563,7 +670,7 @@ void orc_derv(const orc_model *m, const double *theta, const double *buffer_scal
             double freq = m->ptn_freq[ptn];
             double tmp1 = df_frac * freq, tmp2 = ddf_frac * freq;
             my_df += tmp1;
-            my_ddf += fma(-tmp1, df_frac, tmp2);
+            my_ddf += nmul_add(tmp1, df_frac, tmp2);
         }
         tdf[tid] = my_df;
         tddf[tid] = my_ddf;
@@ -618,7 +725,9 @@ double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double
             }
             lh = log(fabs(lh)) + buffer_scale[ptn];
             plh[ptn] = lh;
-            acc = fma(lh, m->ptn_freq[ptn], acc);
+            /* the reference adds each pattern's term on its own
+             * (tree/phylokernelnew.h:3376-3392) */
+            acc += mul_add(lh, m->ptn_freq[ptn], 0.0);
         }
         tsum[tid] = acc;
         tconst[tid] = pconst;
@@ -973,4 +1082,6 @@ int orc_tree_derv(orc_tree *t, int node1, int node2, double len, double *df, dou
     return 0;
 }
 
-double orc_tree_lnl_branch(orc_tree *t, int node, int dad) { return lnl_branch(t, node, dad, NULL); }
+double orc_tree_lnl_branch(orc_tree *t, int node, int dad, double *pattern_lh) {
+    return lnl_branch(t, node, dad, pattern_lh);
+}

@@ -13,12 +13,14 @@
  * B = n*ncat, in eigen space; scale counts are uint8, one per pattern (NORM)
  * or per pattern x category (SAFE).
  *
- * Parity status: the reference cannot be built here (it needs Eigen3,
- * Boost and cmake-generated headers), and its test suite holds no golden
- * vectors for this path, so this oracle is "parity unpinned" against the
- * reference itself. It is pinned by analytic known-answer tests instead
- * (closed-form two-taxon JC69, zero-length star trees, P(t) row sums) and by
- * an independent standard-basis pruning written in numpy.
+ * Parity status: pinned to the reference's own compiled kernels. The whole
+ * reference does not build here (Eigen3, Boost, cmake-generated headers), but
+ * its kernel templates do: oracle/ref/ compiles tree/phylokernelnew.h against
+ * a stand-in PhyloTree environment into oracle/_ref/, and the tests require
+ * this oracle (one thread) to reproduce those kernels bit for bit. It is also
+ * checked against analytic known-answer tests (closed-form two-taxon JC69,
+ * zero-length star trees, P(t) row sums) and an independent standard-basis
+ * pruning written in numpy.
  */
 #ifndef IQ_PHYLO_ORACLE_H
 #define IQ_PHYLO_ORACLE_H
@@ -114,7 +116,8 @@ int orc_tree_get_partial(orc_tree *t, int node, int nbr, double *partial, uint8_
  * sets that branch's length and rebuilds theta. Returns 0 or -1 if not a branch. */
 int orc_tree_derv(orc_tree *t, int node1, int node2, double len, double *df, double *ddf);
 /* lnL on the branch node-dad (computeLikelihoodBranch with dad_branch = dad->node). */
-double orc_tree_lnl_branch(orc_tree *t, int node, int dad);
+/* computeLikelihoodBranch(dad->node, dad); pattern_lh (nptn) may be NULL */
+double orc_tree_lnl_branch(orc_tree *t, int node, int dad, double *pattern_lh);
 
 #ifdef __cplusplus
 }

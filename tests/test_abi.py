@@ -37,3 +37,18 @@ def test_create_without_gpu_reports_no_device():
         pytest.skip("a GPU is present")
     assert rc == 7  # IQGPU_ERR_NODEV
     assert b"device" in engine.lib().iqgpu_last_error()
+
+
+def test_reference_safe_rule_in_memory_sizing():
+    """The engine applies the reference's SAFE rule (tree/phylotreesse.cpp:95-96)
+    at configuration: a 61-state FP64 engine keeps one scale count per pattern
+    x category even when NORM is asked for, unless IQGPU_FLAG_SAFE_AS_GIVEN."""
+    kw = dict(nptn=10000, nstates=61, ncat=4, ntaxa=40, state_unknown=61, nslots=114)
+    norm, safe = engine.Engine.memory_required(safe=0, **kw), engine.Engine.memory_required(safe=1, **kw)
+    assert norm == safe
+    given = engine.Engine.memory_required(safe=0, flags=engine.FLAG_SAFE_AS_GIVEN, **kw)
+    assert safe - given >= 114 * 3 * 10000  # the per-category counts
+    kw20 = dict(kw, nstates=20, state_unknown=23)
+    assert engine.Engine.memory_required(safe=0, **kw20) < engine.Engine.memory_required(safe=1, **kw20)
+    kw_big = dict(kw20, ntaxa=2000, nslots=5994, nptn=64)
+    assert engine.Engine.memory_required(safe=0, **kw_big) == engine.Engine.memory_required(safe=1, **kw_big)

@@ -22,7 +22,10 @@ PARTIAL_RTOL = 1e-10
 
 
 def _gpu_tree(g, safe):
-    return engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe)
+    # kernel-level parity: NORM and SAFE exactly as asked (the reference's
+    # automatic SAFE rule is tested on its own below)
+    return engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe,
+                          flags=engine.FLAG_SAFE_AS_GIVEN)
 
 
 @pytest.mark.parametrize("name", ["dna16", "prot12", "codon8"])
@@ -53,7 +56,8 @@ def test_kernel_level_partials(oracle_mod, name, safe):
     g = load_golden(name)
     topo = Topology(g.edges, g.lengths, g.ntaxa)
     eng = engine.Engine(g.patterns.shape[1], g.model.nstates, g.model.ncat, g.ntaxa, g.model.state_unknown,
-                        topo.nslots, safe=safe, max_ops=topo.nslots)
+                        topo.nslots, safe=safe, max_ops=topo.nslots,
+                        flags=engine.FLAG_SAFE_AS_GIVEN)
     eng.set_model(g.model)
     eng.set_patterns(g.freq)
     eng.set_tip_states(g.patterns)
@@ -78,7 +82,8 @@ def test_derivatives_and_from_buffer(oracle_mod, name, safe):
     g = load_golden(name)
     topo = Topology(g.edges, g.lengths, g.ntaxa)
     eng = engine.Engine(g.patterns.shape[1], g.model.nstates, g.model.ncat, g.ntaxa, g.model.state_unknown,
-                        topo.nslots, safe=safe, max_ops=topo.nslots)
+                        topo.nslots, safe=safe, max_ops=topo.nslots,
+                        flags=engine.FLAG_SAFE_AS_GIVEN)
     eng.set_model(g.model)
     eng.set_patterns(g.freq)
     eng.set_tip_states(g.patterns)
@@ -125,7 +130,8 @@ def test_scaling_counts_identical(oracle_mod, safe):
                simulate.dna_gtr_dataset(300, 200, 5, mean_bl=0.5)):
         topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
         eng = engine.Engine(ds.nptn, ds.model.nstates, ds.model.ncat, ds.ntaxa, ds.model.state_unknown,
-                            topo.nslots, safe=safe, max_ops=topo.nslots)
+                            topo.nslots, safe=safe, max_ops=topo.nslots,
+                        flags=engine.FLAG_SAFE_AS_GIVEN)
         eng.set_model(ds.model)
         eng.set_patterns(ds.freq)
         eng.set_tip_states(ds.patterns)
@@ -222,3 +228,23 @@ def test_reference_triple_tail_flag(oracle_mod):
         odf, oddf = orc.derv(n1, n2, 0.02)
         assert abs(df - odf) <= 1e-9 * max(1.0, abs(odf))
         assert abs(ddf - oddf) <= 1e-9 * max(1.0, abs(oddf))
+
+
+def test_reference_safe_rule():
+    """The engine picks SAFE as PhyloTree::setLikelihoodKernel does
+    (tree/phylotreesse.cpp:95-96): always for state counts other than 4 and
+    20 (codon), from 2000 taxa on, and when asked; NORM otherwise. The flag
+    IQGPU_FLAG_SAFE_AS_GIVEN keeps the caller's choice."""
+    g = load_golden("codon8")
+    t = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
+    assert t.engine.safe
+    topo = Topology(g.edges, g.lengths, g.ntaxa)
+    _, s = t.engine.partial(0)
+    assert s.shape == (g.patterns.shape[1], g.model.ncat)  # one count per pattern x category
+    e = engine.Engine(g.patterns.shape[1], 61, 4, g.ntaxa, 61, topo.nslots, flags=engine.FLAG_SAFE_AS_GIVEN)
+    assert not e.safe
+    for n, ntaxa, want in ((4, 16, False), (20, 16, False), (20, 16, True), (4, 2000, True), (20, 2500, True),
+                           (2, 16, True)):
+        asked = want and ntaxa < 2000 and n in (4, 20)
+        e = engine.Engine(64, n, 4, ntaxa, n if n > 4 else 18, 4, safe=asked, max_ops=4)
+        assert e.safe == want, (n, ntaxa)
