@@ -1,10 +1,10 @@
 /*
  * iqgpu -- GB300 (sm_103a) Felsenstein-pruning likelihood engine, C ABI.
  *
- * This is the drop-in boundary for IQ-TREE 2's likelihood kernels. A
- * PhyloTree shim binds these entry points in place of
- * the function pointers that PhyloTree::setLikelihoodKernel installs
- * (tree/phylotreesse.cpp:91-199):
+ * This is the drop-in boundary for IQ-TREE 2's likelihood kernels. The
+ * PhyloTree binding in iqtree2_gb300/shim/phylotreegb300.cpp binds these entry
+ * points in place of the function pointers that PhyloTree::setLikelihoodKernel
+ * installs (tree/phylotreesse.cpp:91-199):
  *
  *   computePartialLikelihoodPointer      -> iqgpu_compute_partials
  *   computeLikelihoodBranchPointer       -> iqgpu_branch_lnl / iqgpu_compute_likelihood
@@ -110,6 +110,16 @@ typedef struct {
 #define IQGPU_OP_TRANSPOSE1 2
 #define IQGPU_OP_ROOTLEAF0 4
 #define IQGPU_OP_ROOTLEAF1 8
+/* Multifurcating nodes (node->degree() > 3, tree/phylokernelnew.h:1407-1631):
+ * a dad with k > 2 children is given as ceil(k/2) consecutive records with the
+ * same dad_slot, two children each, every record but the last flagged
+ * IQGPU_OP_MORE; when k is odd the last record's child[1] is IQGPU_NO_CHILD.
+ * Children keep the neighbour order of the node (the order of the products).
+ * Reversible models; the FP64 drop-in follows the reference's multifurcating
+ * update (products of the children's eigen-space sums, the 2^-256 check after
+ * every child, one U^-1 transform at the end). */
+#define IQGPU_OP_MORE 16
+#define IQGPU_NO_CHILD ((int32_t)0x80000000)
 
 typedef struct iqgpu_engine iqgpu_engine;
 typedef struct iqgpu_tree iqgpu_tree;

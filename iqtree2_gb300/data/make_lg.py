@@ -27,7 +27,9 @@ def extract(src_root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python make_lg.py <iqtree2 source tree>")
+    root = sys.argv[1]
     nums = extract(root)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lg.dat")
     with open(out, "w") as f:
