@@ -407,6 +407,12 @@ int iqgpu_derv_noalloc(const double *theta_dev, const double *buffer_scale_dev, 
 /* edges[2*k], edges[2*k+1]: endpoints of branch k; leaves are 0..ntaxa-1,
  * internal nodes ntaxa..2*ntaxa-3; a node's neighbour order is edge order. */
 int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out);
+/* The same for a tree with multifurcating nodes (degree 3 to 32): nedge edges
+ * (ntaxa .. 2*ntaxa-3), internal nodes ntaxa..nedge; the engine needs a slot
+ * per directed internal partial. FP64 engines (multifurcating updates follow
+ * the reference's, tree/phylokernelnew.h:1407-1631). */
+int iqgpu_tree_create_n(iqgpu_engine *e, int32_t nedge, const int32_t *edges, const double *lengths,
+                        iqgpu_tree **out);
 int iqgpu_tree_destroy(iqgpu_tree *t);
 /* PhyloTree::computeLikelihood (tree/phylotree.cpp:1233-1280). pattern_lh may be NULL. */
 int iqgpu_tree_compute_likelihood(iqgpu_tree *t, double *lnl, double *pattern_lh);

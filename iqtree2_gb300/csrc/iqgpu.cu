@@ -627,20 +627,40 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
     if (nops == 0 && !extra) return IQGPU_OK;
     // the previous upload must have left the staging buffer
     CK(cudaStreamSynchronize(e->st));
+    bool in_group = false;  // inside the records of a multifurcating node
     for (int k = 0; k < nops; k++) {
         const iqgpu_op &o = ops[k];
-        if (o.dad_slot < 0 || o.dad_slot >= e->cfg.nslots || check_ref(e, o.child[0]) || check_ref(e, o.child[1]) ||
-            o.child[0] == o.dad_slot || o.child[1] == o.dad_slot || !(o.len[0] >= 0.0) || !(o.len[1] >= 0.0)) {
+        const bool more = (o.flags & IQGPU_OP_MORE) != 0;
+        // an absent second child closes a multifurcating node with an odd child count
+        const bool absent1 = o.child[1] == IQGPU_NO_CHILD && in_group && !more;
+        if (o.dad_slot < 0 || o.dad_slot >= e->cfg.nslots || check_ref(e, o.child[0]) ||
+            (!absent1 && check_ref(e, o.child[1])) || o.child[0] == o.dad_slot || o.child[1] == o.dad_slot ||
+            !(o.len[0] >= 0.0) || !(o.len[1] >= 0.0)) {
             set_error("bad traversal entry " + std::to_string(k));
             return IQGPU_ERR_ARG;
         }
-        if (o.flags & ~(IQGPU_OP_TRANSPOSE0 | IQGPU_OP_TRANSPOSE1 | IQGPU_OP_ROOTLEAF0 | IQGPU_OP_ROOTLEAF1) ||
-            (o.flags && !e->nonrev) || ((o.flags & IQGPU_OP_ROOTLEAF0) && o.child[0] >= 0) ||
-            ((o.flags & IQGPU_OP_ROOTLEAF1) && o.child[1] >= 0)) {
+        if (in_group && o.dad_slot != ops[k - 1].dad_slot) {
+            set_error("traversal entry " + std::to_string(k) +
+                      ": the records of a multifurcating node must share their dad slot");
+            return IQGPU_ERR_ARG;
+        }
+        if ((more || in_group) && (is_mixed(&e->cfg) || e->nonrev)) {
+            set_error("multifurcating nodes (IQGPU_OP_MORE) run on FP64 engines with reversible models");
+            return IQGPU_ERR_ARG;
+        }
+        const int dir = o.flags & ~IQGPU_OP_MORE;
+        if (dir & ~(IQGPU_OP_TRANSPOSE0 | IQGPU_OP_TRANSPOSE1 | IQGPU_OP_ROOTLEAF0 | IQGPU_OP_ROOTLEAF1) ||
+            (dir && !e->nonrev) || ((dir & IQGPU_OP_ROOTLEAF0) && o.child[0] >= 0) ||
+            ((dir & IQGPU_OP_ROOTLEAF1) && o.child[1] >= 0)) {
             set_error("bad flags in traversal entry " + std::to_string(k) +
                       " (non-reversible models only; root-leaf flags on tip children only)");
             return IQGPU_ERR_ARG;
         }
+        in_group = more;
+    }
+    if (in_group) {
+        set_error("the last traversal entry is flagged IQGPU_OP_MORE");
+        return IQGPU_ERR_ARG;
     }
     // Mixed engines take the ops in tree-level order (a valid post-order: every
     // child is produced in a lower level), so that a level-synchronous launch

@@ -30,6 +30,7 @@ __global__ void k_partial_info_f64(const OpDev *__restrict__ ops, double *__rest
     const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
     const OpDev op = ops[k];
     const int ref = op.child[ch];
+    if (ref == IQGPU_NO_CHILD) return;  // odd child count of a multifurcating node
     const double len = op.len[ch];
     const long long CNN = (long long)C * n * n;
     const int B = n * C;
@@ -132,6 +133,112 @@ __device__ void grid_reduce(double (&v)[kRedSlots], const Reduce &red) {
 }
 
 // ---------------------------------------------------------------------------
+// multifurcating node (tree/phylokernelnew.h:1407-1631): one record of its
+// op group. The dad's column of its own slot holds the running product of the
+// children's contributions (this thread's pattern only); the first record
+// sets it to one and the scale counts to zero, every child multiplies in
+// (a tip as its leaf-table row, an internal child as the left-to-right sums
+// echild[c][x][.].child[c][.] and its scale counts added), the 2^-256 check
+// follows every child (per category in SAFE, over the block in NORM), and the
+// last record transforms the product with U^-1, with no check after.
+// ---------------------------------------------------------------------------
+template <int NT, bool SAFE>
+__device__ __forceinline__ void multi_record(const TravParams &P, const OpDev &op, bool first, bool last,
+                                             long long p, double invar, double *stmp) {
+    constexpr bool REG = (NT != 0 && NT <= 20);
+    constexpr int NR = REG ? NT : 1;
+    const int n = NT ? NT : P.n;
+    const int C = P.ncat, B = n * C, S = P.state_unknown, tid = threadIdx.x;
+    const long long ld = P.ldp;
+    const long long CNN = (long long)C * n * n, SB = (long long)(S + 1) * B;
+    double *acc = P.partials + (long long)op.dad_slot * P.slot_stride + p;
+    uint8_t *sd = P.scale + (long long)op.dad_slot * P.scale_stride + p;
+    if (first) {
+        for (int r = 0; r < B; r++) acc[(long long)r * ld] = 1.0;
+        if (SAFE) {
+            for (int c = 0; c < C; c++) sd[c * ld] = 0;
+        } else {
+            sd[0] = 0;
+        }
+    }
+    for (int ch = 0; ch < 2; ch++) {
+        const int ref = op.child[ch];
+        if (ref == IQGPU_NO_CHILD) continue;
+        const double *E = P.opmats + op.mat_off + ch * CNN;
+        if (ref < 0) {
+            const double *T = P.opmats + op.mat_off + 2 * CNN + ch * SB +
+                              (long long)P.states[(long long)(-1 - ref) * ld + p] * B;
+            for (int r = 0; r < B; r++) acc[(long long)r * ld] *= __ldg(T + r);
+        } else {
+            const double *Cp = P.partials + (long long)ref * P.slot_stride + p;
+            const uint8_t *sc = P.scale + (long long)ref * P.scale_stride + p;
+            if (!SAFE) sd[0] = (uint8_t)(sd[0] + sc[0]);
+            for (int c = 0; c < C; c++) {
+                if (SAFE) sd[c * ld] = (uint8_t)(sd[c * ld] + sc[c * ld]);
+                if constexpr (REG) {
+                    double v[NR];
+#pragma unroll
+                    for (int i = 0; i < NR; i++) v[i] = Cp[(long long)(c * NR + i) * ld];
+#pragma unroll
+                    for (int x = 0; x < NR; x++) {
+                        const double *e = E + (long long)(c * NR + x) * NR;
+                        double y = __ldg(e) * v[0];
+#pragma unroll
+                        for (int i = 1; i < NR; i++) y = fma(__ldg(e + i), v[i], y);
+                        acc[(long long)(c * NR + x) * ld] *= y;
+                    }
+                } else {
+                    for (int i = 0; i < n; i++) stmp[i * kTPB + tid] = Cp[(long long)(c * n + i) * ld];
+                    for (int x = 0; x < n; x++) {
+                        const double *e = E + (long long)(c * n + x) * n;
+                        double y = __ldg(e) * stmp[tid];
+                        for (int i = 1; i < n; i++) y = fma(__ldg(e + i), stmp[i * kTPB + tid], y);
+                        acc[(long long)(c * n + x) * ld] *= y;
+                    }
+                }
+            }
+        }
+        if (invar != 0.0) continue;
+        if (SAFE) {
+            for (int c = 0; c < C; c++) {
+                double m = 0.0;
+                for (int x = 0; x < n; x++) m = fmax(m, fabs(acc[(long long)(c * n + x) * ld]));
+                if (m < kScaleThreshold) {
+                    for (int x = 0; x < n; x++) acc[(long long)(c * n + x) * ld] *= kTwoPow256;
+                    sd[c * ld] += 1;
+                }
+            }
+        } else {
+            double m = 0.0;
+            for (int r = 0; r < B; r++) m = fmax(m, fabs(acc[(long long)r * ld]));
+            if (m < kScaleThreshold) {
+                for (int r = 0; r < B; r++) acc[(long long)r * ld] *= kTwoPow256;
+                sd[0] += 1;
+            }
+        }
+    }
+    if (!last) return;
+    const double *__restrict__ Ui = P.inv_evec;
+    for (int c = 0; c < C; c++) {
+        const double *U = Ui + (long long)(c / P.cpc) * n * n;
+        if constexpr (REG) {
+            double t[NR];
+#pragma unroll
+            for (int x = 0; x < NR; x++) t[x] = acc[(long long)(c * NR + x) * ld];
+#pragma unroll
+            for (int x = 0; x < NR; x++) acc[(long long)(c * NR + x) * ld] = dot_reg<NR>(U + x * NR, t);
+        } else {
+            for (int j = 0; j < n; j++) stmp[j * kTPB + tid] = acc[(long long)(c * n + j) * ld];
+            for (int x = 0; x < n; x++) {
+                double a = 0.0;
+                for (int j = 0; j < n; j++) a = fma(__ldg(U + (long long)x * n + j), stmp[j * kTPB + tid], a);
+                acc[(long long)(c * n + x) * ld] = a;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // traversal kernel
 // ---------------------------------------------------------------------------
 template <int NT, bool SAFE, int EPI>
@@ -152,8 +259,15 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
     const long long SB = (long long)(S + 1) * B;
     const double *__restrict__ Ui = P.inv_evec;
 
+    bool in_group = false;  // inside the records of a multifurcating node
     for (int k = 0; k < P.nops; ++k) {
         const OpDev op = P.ops[k];
+        const bool more = (op.flags & IQGPU_OP_MORE) != 0;
+        if (more || in_group) {
+            multi_record<NT, SAFE>(P, op, !in_group, !more, p, invar, stmp);
+            in_group = more;
+            continue;
+        }
         int lref = op.child[0], rref = op.child[1];
         const double *eL = P.opmats + op.mat_off, *eR = eL + CNN;
         const double *tL = eL + 2 * CNN, *tR = tL + SB;

@@ -27,13 +27,16 @@ namespace iqg {
 void set_error(const std::string &msg);
 }
 
+// largest node degree (a multifurcating node of degree d has d - 1 children)
+constexpr int kMaxDeg = 32;
+
 struct iqgpu_tree {
     iqgpu_engine *e;
     int64_t nptn;
     int ntaxa, nnode, nedge;
     std::vector<int> deg;
-    std::vector<int> nbr, edge, slot;  // [node*3 + j]
-    std::vector<uint8_t> computed;     // [node*3 + j]: partial of node->nbr valid
+    std::vector<int> nbr, edge, slot;  // [node*kMaxDeg + j]
+    std::vector<uint8_t> computed;     // [node*kMaxDeg + j]: partial of node->nbr valid
     std::vector<double> len;
     std::vector<int> height;
     std::vector<iqgpu_op> ops;
@@ -46,29 +49,42 @@ struct iqgpu_tree {
     bool leaf(int u) const { return u < ntaxa; }
     int idx(int u, int v) const {
         for (int j = 0; j < deg[u]; j++)
-            if (nbr[u * 3 + j] == v) return j;
+            if (nbr[u * kMaxDeg + j] == v) return j;
         return -1;
     }
-    int ref(int dad, int node) const { return leaf(node) ? -1 - node : slot[dad * 3 + idx(dad, node)]; }
-    double &blen(int u, int v) { return len[edge[u * 3 + idx(u, v)]]; }
+    int ref(int dad, int node) const { return leaf(node) ? -1 - node : slot[dad * kMaxDeg + idx(dad, node)]; }
+    double &blen(int u, int v) { return len[edge[u * kMaxDeg + idx(u, v)]]; }
 
+    // post-order list of stale partials (tree/phylotree.cpp:5918-6028); a node
+    // with more than two children becomes consecutive records flagged
+    // IQGPU_OP_MORE (two children each, IQGPU_NO_CHILD closing an odd count)
     void traverse(int dad, int node) {
         const int j = idx(dad, node);
-        if (leaf(node) || computed[dad * 3 + j]) return;
-        iqgpu_op op;
-        std::memset(&op, 0, sizeof(op));
+        if (leaf(node) || computed[dad * kMaxDeg + j]) return;
+        int kids[kMaxDeg];
+        double kl[kMaxDeg];
         int k = 0;
         for (int q = 0; q < deg[node]; q++) {
-            const int ch = nbr[node * 3 + q];
+            const int ch = nbr[node * kMaxDeg + q];
             if (ch == dad) continue;
             traverse(node, ch);
-            op.child[k] = ref(node, ch);
-            op.len[k] = len[edge[node * 3 + q]];
+            kids[k] = ref(node, ch);
+            kl[k] = len[edge[node * kMaxDeg + q]];
             k++;
         }
-        op.dad_slot = slot[dad * 3 + j];
-        computed[dad * 3 + j] = 1;
-        ops.push_back(op);
+        const int dslot = slot[dad * kMaxDeg + j];
+        for (int i = 0; i < k; i += 2) {
+            iqgpu_op op;
+            std::memset(&op, 0, sizeof(op));
+            op.dad_slot = dslot;
+            op.child[0] = kids[i];
+            op.len[0] = kl[i];
+            op.child[1] = i + 1 < k ? kids[i + 1] : IQGPU_NO_CHILD;
+            op.len[1] = i + 1 < k ? kl[i + 1] : 0.0;
+            op.flags = i + 2 < k ? IQGPU_OP_MORE : 0;
+            ops.push_back(op);
+        }
+        computed[dad * kMaxDeg + j] = 1;
     }
     void collect(int node, int dad) {
         ops.clear();
@@ -80,7 +96,7 @@ struct iqgpu_tree {
         int res = -1;
         height[node] = 0;
         for (int q = 0; q < deg[node]; q++) {
-            const int ch = nbr[node * 3 + q];
+            const int ch = nbr[node * kMaxDeg + q];
             if (ch == dad) continue;
             const int lf = farthest_leaf(ch, node);
             if (height[node] < height[ch] + 1) {
@@ -92,16 +108,16 @@ struct iqgpu_tree {
     }
     void clear_reverse(int node, int dad) {
         for (int q = 0; q < deg[node]; q++) {
-            const int x = nbr[node * 3 + q];
+            const int x = nbr[node * kMaxDeg + q];
             if (x == dad) continue;
-            computed[x * 3 + idx(x, node)] = 0;
+            computed[x * kMaxDeg + idx(x, node)] = 0;
             clear_reverse(x, node);
         }
     }
     void preorder(int node, int dad, std::vector<int> &n1, std::vector<int> &n2) {
         if (dad >= 0) { n1.push_back(node); n2.push_back(dad); }
-        int order[3], d = deg[node];
-        for (int q = 0; q < d; q++) order[q] = nbr[node * 3 + q];
+        int order[kMaxDeg], d = deg[node];
+        for (int q = 0; q < d; q++) order[q] = nbr[node * kMaxDeg + q];
         for (int i = 0; i < d; i++)
             for (int k = i + 1; k < d; k++)
                 if (height[order[i]] > height[order[k]]) std::swap(order[i], order[k]);
@@ -183,57 +199,73 @@ int minimize_newton(iqgpu_tree *t, double x1, double xguess, double x2, double x
 
 extern "C" {
 
-int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out) {
+int iqgpu_tree_create_n(iqgpu_engine *e, int32_t nedge, const int32_t *edges, const double *lengths,
+                        iqgpu_tree **out) {
     if (!e || !edges || !lengths || !out) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
     *out = nullptr;
     iqgpu_config cfgv;
     int rc0 = iqgpu_get_config(e, &cfgv);
     if (rc0) return rc0;
     const iqgpu_config *cfg = &cfgv;
+    if (nedge < cfg->ntaxa || nedge > 2 * cfg->ntaxa - 3) {
+        iqg::set_error("an unrooted tree on ntaxa leaves has between ntaxa and 2*ntaxa-3 edges");
+        return IQGPU_ERR_ARG;
+    }
     iqgpu_tree *t = new iqgpu_tree();
     t->e = e;
     t->nptn = cfg->nptn;
     t->ntaxa = cfg->ntaxa;
-    t->nnode = 2 * t->ntaxa - 2;
-    t->nedge = 2 * t->ntaxa - 3;
-    if (cfg->nslots < 3 * (t->ntaxa - 2) || cfg->max_ops < 2 * t->ntaxa) {
-        delete t;
-        iqg::set_error("engine needs nslots >= 3*(ntaxa-2) and max_ops >= 2*ntaxa for a tree");
-        return IQGPU_ERR_ARG;
-    }
+    t->nedge = nedge;
+    t->nnode = nedge + 1;  // a tree
     t->deg.assign(t->nnode, 0);
-    t->nbr.assign(t->nnode * 3, -1);
-    t->edge.assign(t->nnode * 3, -1);
-    t->slot.assign(t->nnode * 3, -1);
-    t->computed.assign(t->nnode * 3, 0);
+    t->nbr.assign((size_t)t->nnode * kMaxDeg, -1);
+    t->edge.assign((size_t)t->nnode * kMaxDeg, -1);
+    t->slot.assign((size_t)t->nnode * kMaxDeg, -1);
+    t->computed.assign((size_t)t->nnode * kMaxDeg, 0);
     t->height.assign(t->nnode, 0);
     t->len.assign(lengths, lengths + t->nedge);
     for (int k = 0; k < t->nedge; k++) {
         const int u = edges[2 * k], v = edges[2 * k + 1];
-        if (u < 0 || v < 0 || u >= t->nnode || v >= t->nnode || u == v || t->deg[u] >= 3 || t->deg[v] >= 3 ||
-            !(lengths[k] >= 0.0)) {
+        if (u < 0 || v < 0 || u >= t->nnode || v >= t->nnode || u == v || t->deg[u] >= kMaxDeg ||
+            t->deg[v] >= kMaxDeg || !(lengths[k] >= 0.0)) {
             delete t;
-            iqg::set_error("edge list is not an unrooted binary tree on 2*ntaxa-2 nodes");
+            iqg::set_error("edge list is not an unrooted tree on nedge+1 nodes (node degree <= 32)");
             return IQGPU_ERR_ARG;
         }
-        t->nbr[u * 3 + t->deg[u]] = v;
-        t->edge[u * 3 + t->deg[u]++] = k;
-        t->nbr[v * 3 + t->deg[v]] = u;
-        t->edge[v * 3 + t->deg[v]++] = k;
+        t->nbr[u * kMaxDeg + t->deg[u]] = v;
+        t->edge[u * kMaxDeg + t->deg[u]++] = k;
+        t->nbr[v * kMaxDeg + t->deg[v]] = u;
+        t->edge[v * kMaxDeg + t->deg[v]++] = k;
     }
     for (int u = 0; u < t->nnode; u++) {
-        if ((t->leaf(u) && t->deg[u] != 1) || (!t->leaf(u) && t->deg[u] != 3)) {
+        if ((t->leaf(u) && t->deg[u] != 1) || (!t->leaf(u) && t->deg[u] < 3)) {
             delete t;
-            iqg::set_error("leaves need degree 1 and internal nodes degree 3");
+            iqg::set_error("leaves need degree 1 and internal nodes degree 3 or more");
             return IQGPU_ERR_ARG;
         }
     }
     int ns = 0;
     for (int u = 0; u < t->nnode; u++)
         for (int j = 0; j < t->deg[u]; j++)
-            if (!t->leaf(t->nbr[u * 3 + j])) t->slot[u * 3 + j] = ns++;
+            if (!t->leaf(t->nbr[u * kMaxDeg + j])) t->slot[u * kMaxDeg + j] = ns++;
+    if (cfg->nslots < ns || cfg->max_ops < 2 * t->ntaxa) {
+        delete t;
+        iqg::set_error("engine needs nslots >= " + std::to_string(ns) + " (one per directed internal partial; " +
+                       "3*(ntaxa-2) for a binary tree) and max_ops >= 2*ntaxa");
+        return IQGPU_ERR_ARG;
+    }
     *out = t;
     return IQGPU_OK;
+}
+
+int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out) {
+    iqgpu_config cfg;
+    int rc = e ? iqgpu_get_config(e, &cfg) : IQGPU_ERR_ARG;
+    if (rc) {
+        if (!e) iqg::set_error("null argument");
+        return rc;
+    }
+    return iqgpu_tree_create_n(e, 2 * cfg.ntaxa - 3, edges, lengths, out);
 }
 
 int iqgpu_tree_destroy(iqgpu_tree *t) {
@@ -246,7 +278,7 @@ int iqgpu_tree_compute_likelihood(iqgpu_tree *t, double *lnl, double *pattern_lh
     if (t->cur1 < 0) {
         const int lf = t->farthest_leaf(0, -1);  // root is taxon 0, a leaf
         t->cur1 = lf;
-        t->cur2 = t->nbr[lf * 3];
+        t->cur2 = t->nbr[lf * kMaxDeg];
     }
     int rc = lnl_branch(t, t->cur2, t->cur1, lnl);
     if (rc) return rc;

@@ -48,6 +48,10 @@ class Op(ct.Structure):
 # iqgpu_op flags (non-reversible models): transpose P for a child reached
 # against the edge direction; a tip child that is the root leaf
 OP_TRANSPOSE0, OP_TRANSPOSE1, OP_ROOTLEAF0, OP_ROOTLEAF1 = 1, 2, 4, 8
+# multifurcating nodes: records of one node after the first carry on its
+# child list (OP_MORE on every record but the last; NO_CHILD pads an odd count)
+OP_MORE = 16
+NO_CHILD = -(2 ** 31)
 OP_DTYPE = np.dtype([("dad_slot", np.int32), ("child", np.int32, (2,)), ("flags", np.int32),
                      ("len", np.float64, (2,))])
 assert OP_DTYPE.itemsize == ct.sizeof(Op) == 32
@@ -119,6 +123,7 @@ def lib():
         "iqgpu_set_boot_weights": ([vp, ct.POINTER(ct.c_float), ct.c_int32], ct.c_int),
         "iqgpu_rell": ([vp, _DP, ct.c_int32, _DP], ct.c_int),
         "iqgpu_tree_create": ([vp, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
+        "iqgpu_tree_create_n": ([vp, ct.c_int32, _I32P, _DP, ct.POINTER(vp)], ct.c_int),
         "iqgpu_tree_destroy": ([vp], ct.c_int),
         "iqgpu_tree_compute_likelihood": ([vp, _DP, _DP], ct.c_int),
         "iqgpu_tree_optimize_one_branch": ([vp, ct.c_int32, ct.c_int32, ct.c_int32], ct.c_int),
@@ -427,7 +432,7 @@ class GpuTree:
         the unobserved constant patterns (``models.asc_lewis_patterns``)."""
         ntaxa = patterns.shape[0]
         self.ntaxa = ntaxa
-        self.nedge = 2 * ntaxa - 3
+        self.nedge = len(edges)  # 2*ntaxa-3, fewer with multifurcating nodes
         self.engine = Engine(patterns.shape[1], model.nstates, model.ncat, ntaxa, model.state_unknown,
                              3 * (ntaxa - 2), safe=safe, precision=precision, device=device,
                              max_ops=2 * ntaxa, flags=flags)
@@ -438,8 +443,8 @@ class GpuTree:
             self.engine.set_asc(*asc)
         self.edges = np.ascontiguousarray(edges, np.int32)
         h = ct.c_void_p()
-        _check(lib().iqgpu_tree_create(self.engine.h, self.edges.ctypes.data_as(_I32P),
-                                       _dp(np.ascontiguousarray(lengths, np.float64)), ct.byref(h)))
+        _check(lib().iqgpu_tree_create_n(self.engine.h, self.nedge, self.edges.ctypes.data_as(_I32P),
+                                         _dp(np.ascontiguousarray(lengths, np.float64)), ct.byref(h)))
         self.h = h
 
     def close(self):

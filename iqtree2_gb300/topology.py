@@ -7,10 +7,14 @@ referenced as -1 - v.
 import numpy as np
 
 
+NO_CHILD = -(2 ** 31)  # absent second child of a multifurcating node's last record
+OP_MORE = 16           # more records of the same multifurcating node follow
+
+
 class Topology:
     def __init__(self, edges, lengths, ntaxa):
         self.ntaxa = ntaxa
-        self.nnode = 2 * ntaxa - 2
+        self.nnode = int(np.max(edges)) + 1
         self.adj = [[] for _ in range(self.nnode)]
         for k, (u, v) in enumerate(edges):
             self.adj[int(u)].append((int(v), k))
@@ -37,8 +41,23 @@ class Topology:
             kids = [(c, k) for (c, k) in self.adj[n] if c != d]
             for (c, _) in kids:
                 rec(n, c)
-            (c0, k0), (c1, k1) = kids
-            ops.append((self.slot[(d, n)], self.ref(n, c0), self.ref(n, c1), self.lengths[k0], self.lengths[k1]))
+            # two children per record; a multifurcating node continues over
+            # records flagged OP_MORE (tree/phylokernelnew.h:1407-1631)
+            if len(kids) == 2:
+                (c0, k0), (c1, k1) = kids
+                ops.append((self.slot[(d, n)], self.ref(n, c0), self.ref(n, c1), self.lengths[k0],
+                            self.lengths[k1]))
+            else:
+                for i in range(0, len(kids), 2):
+                    c0, k0 = kids[i]
+                    last = i + 2 >= len(kids)
+                    if i + 1 < len(kids):
+                        c1, k1 = kids[i + 1]
+                        r1, l1 = self.ref(n, c1), self.lengths[k1]
+                    else:
+                        r1, l1 = NO_CHILD, 0.0
+                    ops.append((self.slot[(d, n)], self.ref(n, c0), r1, self.lengths[k0], l1,
+                                0 if last else OP_MORE))
             done.add((d, n))
 
         rec(dad, node)
@@ -95,3 +114,36 @@ class Topology:
             arr.append((tuple(subs), (first_scratch + 2 * k, first_scratch + 2 * k + 1), tuple(lens),
                         self.edge_len(u, v)))
         return arr
+
+
+def collapse_edges(edges, lengths, ntaxa, collapse):
+    """Contract the internal edges listed in ``collapse`` (edge indices): their
+    end nodes merge, so nodes of degree 4, 5, ... (polytomies) appear.
+    Returns (edges, lengths, nnode) with internal nodes renumbered ntaxa..;
+    neighbour order follows the remaining edges' order."""
+    edges = [(int(u), int(v)) for (u, v) in edges]
+    parent = {}
+
+    def find(x):
+        while parent.get(x, x) != x:
+            x = parent[x]
+        return x
+
+    for k in collapse:
+        u, v = edges[k]
+        if u < ntaxa or v < ntaxa:
+            raise ValueError("only internal edges can be collapsed")
+        a, b = find(u), find(v)
+        if a != b:
+            parent[max(a, b)] = min(a, b)
+    keep = [k for k in range(len(edges)) if k not in set(collapse)]
+    label = {}
+    out_e, out_l = [], []
+    for k in keep:
+        u, v = find(edges[k][0]), find(edges[k][1])
+        for w in (u, v):
+            if w >= ntaxa and w not in label:
+                label[w] = ntaxa + len(label)
+        out_e.append((label.get(u, u), label.get(v, v)))
+        out_l.append(float(lengths[k]))
+    return np.asarray(out_e, np.int32), np.asarray(out_l), ntaxa + len(label)

@@ -34,7 +34,7 @@ def lib():
         L.orc_derv.argtypes = [ct.c_void_p, dp, dp, ct.c_double, dp, dp, ct.c_int]
         L.orc_lnl_from_buffer.argtypes = [ct.c_void_p, dp, dp, ct.c_double, dp, ct.c_int]
         L.orc_lnl_from_buffer.restype = ct.c_double
-        L.orc_tree_new.argtypes = [ct.c_void_p, ip, dp, ct.c_int]
+        L.orc_tree_new.argtypes = [ct.c_void_p, ip, ct.c_int, dp, ct.c_int]
         L.orc_tree_new.restype = ct.c_void_p
         L.orc_tree_free.argtypes = [ct.c_void_p]
         L.orc_tree_compute_likelihood.argtypes = [ct.c_void_p, dp]
@@ -115,8 +115,10 @@ class OracleTree:
         self.edges = np.ascontiguousarray(edges, np.int32)
         self.nedge = len(self.edges)
         L = lib()
-        self.h = L.orc_tree_new(self.m.ptr, self.edges.ctypes.data_as(ct.POINTER(ct.c_int)),
+        self.h = L.orc_tree_new(self.m.ptr, self.edges.ctypes.data_as(ct.POINTER(ct.c_int)), self.nedge,
                                 _dp(np.ascontiguousarray(lengths, np.float64)), int(nthreads))
+        if not self.h:
+            raise ValueError("tree node degree above ORC_MAX_DEG")
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -49,6 +49,9 @@
  * 339-351) multiplies and adds with two roundings; this file is compiled with
  * -ffp-contract=off so the compiler fuses nothing either. */
 static inline double mul_add(double a, double b, double c) { return a * b + c; }
+/* the one-lane max (std::max order: the second argument only if larger) */
+static inline double fmax_ref(double a, double b) { return a < b ? b : a; }
+#define ORC_MAX_BLOCK (64 * 16)
 static inline double nmul_add(double a, double b, double c) { return c - a * b; }
 
 /* dotProductVec as compiled (JAMES_VERSION, tree/phylokernelnew.h:83-126):
@@ -414,10 +417,89 @@ static void orc_compute_one(const orc_model *m, double *partials, uint8_t *scale
     free(leafR);
 }
 
+/* Multifurcating node, nchild > 2 (tree/phylokernelnew.h:1407-1631, the
+ * non-site-model branch): the running product of the children's contributions
+ * in neighbour order, each child's internal partial entering as the left-to-
+ * right sum echild[c][x][.].child[c][.] and a tip child as its leaf-table row;
+ * the 2^-256 check (per category in SAFE, whole block in NORM) after every
+ * child on the product; one U^-1 transform at the end with no check after. */
+static void orc_compute_multi(const orc_model *m, double *partials, uint8_t *scale, const orc_op *op, int nth) {
+    const int n = m->nstates, C = m->ncat, B = n * C, S = m->state_unknown, k = op->nchild;
+    const int safe = m->safe;
+    const size_t pstride = (size_t)m->nptn * B;
+    const size_t sstride = (size_t)m->nptn * (safe ? C : 1);
+    double *ech[ORC_MAX_DEG - 1], *leaf[ORC_MAX_DEG - 1];
+    for (int ch = 0; ch < k; ch++) {
+        ech[ch] = malloc(sizeof(double) * (size_t)C * n * n);
+        orc_echild(m, op->len[ch], ech[ch]);
+        leaf[ch] = NULL;
+        if (op->child[ch] < 0) {
+            leaf[ch] = malloc(sizeof(double) * (size_t)(S + 1) * B);
+            orc_leaf_table(m, ech[ch], leaf[ch]);
+        }
+    }
+    double *dad = partials + (size_t)op->dad_slot * pstride;
+    uint8_t *sdad = scale + (size_t)op->dad_slot * sstride;
+    const int nptn = m->nptn;
+
+#pragma omp parallel for schedule(static) num_threads(nth)
+    for (int ptn = 0; ptn < nptn; ptn++) {
+        double all[ORC_MAX_BLOCK];
+        uint8_t *sd = safe ? sdad + (size_t)ptn * C : sdad + ptn;
+        for (int i = 0; i < B; i++) all[i] = 1.0;
+        memset(sd, 0, safe ? C : 1);
+        for (int ch = 0; ch < k; ch++) {
+            const int ref = op->child[ch];
+            if (ref < 0) {
+                const double *tl = leaf[ch] + (size_t)tip_state(m, -1 - ref, ptn) * B;
+                for (int i = 0; i < B; i++) all[i] *= tl[i];
+            } else {
+                const double *pc = partials + (size_t)ref * pstride + (size_t)ptn * B;
+                const uint8_t *sc = scale + (size_t)ref * sstride;
+                if (!safe) sd[0] = (uint8_t)(sd[0] + sc[ptn]);
+                for (int c = 0; c < C; c++) {
+                    if (safe) sd[c] = (uint8_t)(sd[c] + sc[(size_t)ptn * C + c]);
+                    for (int x = 0; x < n; x++) {
+                        const double *e = ech[ch] + ((size_t)c * n + x) * n;
+                        all[c * n + x] *= seq_dot(e, pc + c * n, n);
+                    }
+                }
+            }
+            if (m->ptn_invar[ptn] != 0.0) continue;
+            if (safe) {
+                for (int c = 0; c < C; c++) {
+                    double lh_max = 0.0;
+                    for (int x = 0; x < n; x++) lh_max = fmax_ref(lh_max, fabs(all[c * n + x]));
+                    if (lh_max < ORC_SCALING_THRESHOLD) {
+                        for (int x = 0; x < n; x++) all[c * n + x] = ldexp(all[c * n + x], ORC_SCALING_THRESHOLD_EXP);
+                        sd[c] += 1;
+                    }
+                }
+            } else {
+                double lh_max = 0.0;
+                for (int i = 0; i < B; i++) lh_max = fmax_ref(lh_max, fabs(all[i]));
+                if (lh_max < ORC_SCALING_THRESHOLD) {
+                    for (int i = 0; i < B; i++) all[i] = ldexp(all[i], ORC_SCALING_THRESHOLD_EXP);
+                    sd[0] += 1;
+                }
+            }
+        }
+        double *pd = dad + (size_t)ptn * B;
+        for (int c = 0; c < C; c++) prod_vec_mat(all + c * n, m->inv_evec, pd + c * n, n, 0.0);
+    }
+    for (int ch = 0; ch < k; ch++) {
+        free(ech[ch]);
+        free(leaf[ch]);
+    }
+}
+
 void orc_compute_partials(const orc_model *m, double *partials, uint8_t *scale,
                           const orc_op *ops, int nops, int nthreads) {
     int nth = num_threads(nthreads);
-    for (int k = 0; k < nops; k++) orc_compute_one(m, partials, scale, &ops[k], nth);
+    for (int k = 0; k < nops; k++) {
+        if (ops[k].nchild > 2) orc_compute_multi(m, partials, scale, &ops[k], nth);
+        else orc_compute_one(m, partials, scale, &ops[k], nth);
+    }
 }
 
 /* ------------------------------------------------------------------ */
@@ -760,10 +842,10 @@ struct orc_tree {
     orc_model m;
     int ntaxa, nnode, nedge, nth;
     int *deg;          /* [nnode] */
-    int (*nbr)[3];     /* neighbour node */
-    int (*edge)[3];    /* edge id of that neighbour */
-    int (*slot)[3];    /* slot of directed partial node->nbr (nbr internal), else -1 */
-    uint8_t (*computed)[3];
+    int (*nbr)[ORC_MAX_DEG];     /* neighbour node */
+    int (*edge)[ORC_MAX_DEG];    /* edge id of that neighbour */
+    int (*slot)[ORC_MAX_DEG];    /* slot of directed partial node->nbr (nbr internal), else -1 */
+    uint8_t (*computed)[ORC_MAX_DEG];
     double *lengths;   /* [nedge] */
     double *partials;
     uint8_t *scale;
@@ -786,12 +868,14 @@ static int nbr_index(const orc_tree *t, int node, int nb) {
 
 static int is_leaf(const orc_tree *t, int node) { return node < t->ntaxa; }
 
-orc_tree *orc_tree_new(const orc_model *m, const int *edges, const double *lengths, int nthreads) {
+orc_tree *orc_tree_new(const orc_model *m, const int *edges, int nedge, const double *lengths, int nthreads) {
     orc_tree *t = calloc(1, sizeof(orc_tree));
     t->m = *m;
     t->ntaxa = m->ntaxa;
-    t->nnode = 2 * m->ntaxa - 2;
-    t->nedge = 2 * m->ntaxa - 3;
+    t->nedge = nedge;
+    t->nnode = 0;
+    for (int k = 0; k < 2 * nedge; k++)
+        if (edges[k] + 1 > t->nnode) t->nnode = edges[k] + 1;
     t->nth = num_threads(nthreads);
     t->deg = calloc(t->nnode, sizeof(int));
     t->nbr = calloc(t->nnode, sizeof(*t->nbr));
@@ -802,12 +886,13 @@ orc_tree *orc_tree_new(const orc_model *m, const int *edges, const double *lengt
     memcpy(t->lengths, lengths, sizeof(double) * t->nedge);
     for (int k = 0; k < t->nedge; k++) {
         int u = edges[2 * k], v = edges[2 * k + 1];
+        if (t->deg[u] >= ORC_MAX_DEG || t->deg[v] >= ORC_MAX_DEG) { orc_tree_free(t); return NULL; }
         t->nbr[u][t->deg[u]] = v; t->edge[u][t->deg[u]++] = k;
         t->nbr[v][t->deg[v]] = u; t->edge[v][t->deg[v]++] = k;
     }
     int ns = 0;
     for (int u = 0; u < t->nnode; u++)
-        for (int j = 0; j < 3; j++)
+        for (int j = 0; j < ORC_MAX_DEG; j++)
             t->slot[u][j] = (j < t->deg[u] && !is_leaf(t, t->nbr[u][j])) ? ns++ : -1;
     const int B = m->nstates * m->ncat;
     t->partials = malloc(sizeof(double) * (size_t)ns * m->nptn * B);
@@ -860,6 +945,7 @@ static void traverse(orc_tree *t, int dad, int node) {
         op.len[k] = t->lengths[t->edge[node][q]];
         k++;
     }
+    op.nchild = k;
     op.dad_slot = t->slot[dad][j];
     t->computed[dad][j] = 1;
     t->ops[t->nops++] = op;
@@ -1010,7 +1096,7 @@ int orc_tree_optimize_one_branch(orc_tree *t, int node1, int node2, int max_nr_s
 
 static void preorder(orc_tree *t, int node, int dad, int *nodes, int *nodes2, int *cnt) {
     if (dad >= 0) { nodes[*cnt] = node; nodes2[*cnt] = dad; (*cnt)++; }
-    int order[3], d = t->deg[node];
+    int order[ORC_MAX_DEG], d = t->deg[node];
     for (int q = 0; q < d; q++) order[q] = t->nbr[node][q];
     for (int i = 0; i < d; i++)
         for (int k = i + 1; k < d; k++)

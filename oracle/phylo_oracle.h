@@ -60,11 +60,18 @@ typedef struct {
     double asc_nsite;
 } orc_model;
 
-/* A reference to a directed partial: >= 0 is a slot, < 0 is tip taxon (-1-ref). */
+/* Largest node degree of a tree (a multifurcating node of degree d has d-1
+ * children in a traversal). */
+#define ORC_MAX_DEG 32
+
+/* A reference to a directed partial: >= 0 is a slot, < 0 is tip taxon
+ * (-1-ref). An op has nchild >= 2 children in the node's neighbour order;
+ * nchild > 2 is a multifurcating node (tree/phylokernelnew.h:1407-1631). */
 typedef struct {
     int dad_slot;
-    int child[2];
-    double len[2];
+    int nchild;
+    int child[ORC_MAX_DEG - 1];
+    double len[ORC_MAX_DEG - 1];
 } orc_op;
 
 /* Partial update for a traversal list (computePartialLikelihoodGenericSIMD). */
@@ -95,7 +102,10 @@ double orc_lnl_from_buffer(const orc_model *m, const double *theta, const double
 /* ---- tree-level drivers (PhyloTree restatement) ---- */
 typedef struct orc_tree orc_tree;
 
-orc_tree *orc_tree_new(const orc_model *m, const int *edges, const double *lengths, int nthreads);
+/* nedge edges edges[2k], edges[2k+1]; leaves are 0..ntaxa-1, internal nodes
+ * any ids above (2*ntaxa-3 edges for a binary tree, fewer with multifurcating
+ * nodes); a node's neighbour order is edge order. */
+orc_tree *orc_tree_new(const orc_model *m, const int *edges, int nedge, const double *lengths, int nthreads);
 void orc_tree_free(orc_tree *t);
 double orc_tree_compute_likelihood(orc_tree *t, double *pattern_lh);
 /* optimizeOneBranch on the branch between node1 and node2. Returns 0 or -1 on NR failure. */

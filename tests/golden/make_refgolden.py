@@ -11,6 +11,9 @@ kernels) on
 * ``underflow150``: a seeded 150-taxon protein alignment on a long-branch
   tree whose partials fall below 2^-256, so NORM and SAFE scale counts are
   exercised,
+* ``example_polytomy`` and ``underflow150_polytomy``: the same with internal
+  edges contracted, so multifurcating nodes (degree 4 and more) run the
+  reference's multifurcating update,
 
 and writes ``ref_<name>.npz`` here: the inputs (patterns, weights, tree,
 the model's eigen arrays) and the reference kernels' outputs (branch lnL on
@@ -32,7 +35,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.dirname(HERE)):
     sys.path.insert(0, p)
 
-from iqtree2_gb300 import simulate  # noqa: E402
+from iqtree2_gb300 import simulate, topology  # noqa: E402
 import refdata  # noqa: E402
 import refkernels  # noqa: E402
 
@@ -46,6 +49,18 @@ def underflow150():
     return SimpleNamespace(name="underflow150", patterns=ds.patterns, freq=ds.freq, edges=np.asarray(ds.edges),
                            lengths=np.asarray(ds.lengths, np.float64), model=ds.model, ntaxa=ds.ntaxa,
                            nsites=int(round(float(np.sum(ds.freq)))))
+
+
+def polytomy(d, ncollapse, name):
+    """d with ncollapse internal edges contracted: nodes of degree 4 and more
+    (the reference's multifurcating update, tree/phylokernelnew.h:1407-1631)."""
+    from types import SimpleNamespace
+    internal = [k for k, (u, v) in enumerate(d.edges) if min(int(u), int(v)) >= d.ntaxa]
+    rng = np.random.default_rng(5)
+    pick = sorted(rng.choice(internal, size=ncollapse, replace=False).tolist())
+    e2, l2, _ = topology.collapse_edges(d.edges, d.lengths, d.ntaxa, pick)
+    return SimpleNamespace(name=name, patterns=d.patterns, freq=d.freq, edges=e2, lengths=l2, model=d.model,
+                           ntaxa=d.ntaxa, nsites=d.nsites)
 
 
 def branches(d):
@@ -108,6 +123,7 @@ def main():
         raise SystemExit("no reference checkout (pass its path or set IQTREE_REFERENCE)")
     os.environ["IQTREE_REFERENCE"] = ref
     sets = [refdata.load(name, ref) for name in refdata.REF_ALIGNMENTS] + [underflow150()]
+    sets += [polytomy(sets[0], 10, "example_polytomy"), polytomy(sets[3], 25, "underflow150_polytomy")]
     for d in sets:
         out = run(d)
         np.savez_compressed(os.path.join(HERE, f"ref_{d.name}.npz"), **out)

@@ -33,7 +33,8 @@ def rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-REF_FIXTURES = ["example", "d59_8", "prot_M126_27_269", "underflow150"]
+REF_FIXTURES = ["example", "d59_8", "prot_M126_27_269", "underflow150", "example_polytomy",
+                "underflow150_polytomy"]
 
 
 def load_ref_golden(name):

@@ -141,3 +141,26 @@ def test_committed_fixtures_match_reference(oracle_mod):
     r = refkernels.RefTree(m.model, m.patterns, m.freq, m.edges, m.lengths)
     node, dad = _oriented(m.edges, m.ntaxa)[0]
     assert r.branch_lnl(node, dad) == float(d["lnl_norm"][0])
+
+
+@pytest.mark.parametrize("name", ["dna16", "prot12", "codon8"])
+@pytest.mark.parametrize("safe", [False, True])
+def test_oracle_bit_exact_on_multifurcating_trees(oracle_mod, name, safe):
+    """Internal edges contracted to nodes of degree 4 to 6: the reference's
+    multifurcating update (tree/phylokernelnew.h:1407-1631)."""
+    from iqtree2_gb300 import topology
+    g = load_golden(name)
+    internal = [k for k, (u, v) in enumerate(g.edges) if min(u, v) >= g.ntaxa]
+    e2, l2, _ = topology.collapse_edges(g.edges, g.lengths, g.ntaxa, internal[:3])
+    assert np.bincount(e2.ravel()).max() >= 4
+    _check_bit_exact(oracle_mod, g.model, g.patterns, g.freq, e2, l2, safe,
+                     codon_tail=(g.model.nstates % 2 == 1))
+
+
+@pytest.mark.parametrize("safe", [False, True])
+def test_oracle_bit_exact_multifurcating_underflow(oracle_mod, safe):
+    from iqtree2_gb300 import topology
+    ds = simulate.protein_lg_dataset(150, 40, 11, mean_bl=0.5)
+    internal = [k for k, (u, v) in enumerate(ds.edges) if min(u, v) >= ds.ntaxa]
+    e2, l2, _ = topology.collapse_edges(ds.edges, ds.lengths, ds.ntaxa, internal[::6])
+    _check_bit_exact(oracle_mod, ds.model, ds.patterns, ds.freq, e2, l2, safe, derv_edges=[0, 9])
