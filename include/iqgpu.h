@@ -29,6 +29,12 @@
  * concurrently from different threads (PhyloSuperTree calls partitions from
  * OpenMP threads, tree/phylosupertree.cpp:716-723).
  *
+ * Host inputs. The setters (iqgpu_set_model, iqgpu_set_state_freq,
+ * iqgpu_set_tip_partials, iqgpu_set_patterns, ...) take a copy of the
+ * caller's arrays before they return and send it in stream order, so a
+ * caller may overwrite or free its buffers at once (pinned memory included)
+ * while the engine's stream is still busy.
+ *
  * Partial references. A directed partial (the reference's PhyloNeighbor
  * partial_lh: the subtree at `node` seen from `dad`) is named by an int32:
  * r >= 0 is an HBM slot, r < 0 is tip taxon (-1 - r).

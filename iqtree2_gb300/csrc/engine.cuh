@@ -164,6 +164,13 @@ struct iqgpu_engine {
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;
+    // host inputs of the setters go through engine-owned staging (pinned unless
+    // the engine lives in a caller's region): two halves used in turn, a half
+    // refilled only after the copies that read it last have run (its event)
+    char *h_stage[2];
+    size_t stage_cap, stage_used;
+    int stage_cur;
+    cudaEvent_t stage_ev[2];
     // stream ownership and kernel timing
     cudaStream_t own_st;
     cudaEvent_t ev_t0, ev_t1;

@@ -177,13 +177,19 @@ static void free_engine(iqgpu_engine *e) {
             if (p) cudaFree(p);
         if (e->h_ops) cudaFreeHost(e->h_ops);
         if (e->h_red_out) cudaFreeHost(e->h_red_out);
+        for (char *h : e->h_stage)
+            if (h) cudaFreeHost(h);
         if (e->h_asc) cudaFreeHost(e->h_asc);
     } else {
         std::free(e->h_ops);
         std::free(e->h_red_out);
+        std::free(e->h_stage[0]);
+        std::free(e->h_stage[1]);
         std::free(e->h_asc);
     }
     std::free(e->level_off);
+    for (cudaEvent_t ev : e->stage_ev)
+        if (ev) cudaEventDestroy(ev);
     if (e->ev_t0) cudaEventDestroy(e->ev_t0);
     if (e->ev_t1) cudaEventDestroy(e->ev_t1);
     if (e->own_st) cudaStreamDestroy(e->own_st);
@@ -340,6 +346,15 @@ static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_b
     CKE(halloc(e, &e->h_ops, s.ops));
     CKE(halloc(e, &e->h_red_out, kRedSlots * 8 + 16));
     CKE(halloc(e, &e->h_asc, 3 * kMaxStates * 8));
+    // setter staging: the largest single setter payload (pattern weights, or
+    // the model arrays) per half
+    e->stage_cap = (size_t)std::max<long long>(2 * e->Ppad * 8, (n + 2 * n * n + 2 * C + (S + 2) * n) * 8 + 1024);
+    CKE(halloc(e, &e->h_stage[0], (long long)e->stage_cap));
+    CKE(halloc(e, &e->h_stage[1], (long long)e->stage_cap));
+    CKE(cudaEventCreateWithFlags(&e->stage_ev[0], cudaEventDisableTiming));
+    CKE(cudaEventCreateWithFlags(&e->stage_ev[1], cudaEventDisableTiming));
+    CKE(cudaEventRecord(e->stage_ev[0], e->st));
+    CKE(cudaEventRecord(e->stage_ev[1], e->st));
     CKE(cudaMemsetAsync(e->d_ticket, 0, 64, e->st));
     CKE(cudaMemsetAsync(e->d_freq, 0, e->Ppad * 8, e->st));
     CKE(cudaMemsetAsync(e->d_invar, 0, e->Ppad * 8, e->st));
@@ -384,16 +399,39 @@ static void check_unit_tips(iqgpu_engine *e) {
             if (e->h_tipv[s * e->n + i] != e->h_inv[i * e->n + s]) { e->unit_tips = false; break; }
 }
 
+// Setter uploads: the caller's arrays are copied into a staging half and
+// sent from there, in stream order, so a setter returns before its copy runs
+// and the caller may overwrite or free its buffer at once (pinned or not).
+static cudaError_t stage_begin(iqgpu_engine *e) {
+    e->stage_cur ^= 1;
+    e->stage_used = 0;
+    return cudaEventSynchronize(e->stage_ev[e->stage_cur]);  // the half's previous copies have run
+}
+static cudaError_t stage_copy(iqgpu_engine *e, void *dst, const void *src, size_t bytes) {
+    const size_t off = (e->stage_used + 255) & ~(size_t)255;
+    if (off + bytes > e->stage_cap) {  // larger than a half: copy through the driver, then wait for it
+        cudaError_t err = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->st);
+        return err != cudaSuccess ? err : cudaStreamSynchronize(e->st);
+    }
+    char *h = e->h_stage[e->stage_cur] + off;
+    std::memcpy(h, src, bytes);
+    e->stage_used = off + bytes;
+    return cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, e->st);
+}
+static cudaError_t stage_end(iqgpu_engine *e) { return cudaEventRecord(e->stage_ev[e->stage_cur], e->st); }
+
 int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
                     const double *rates, const double *props) {
     if (!e || !eval || !evec || !inv_evec || !rates || !props) { set_error("null argument"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
     const size_t n = e->n, C = e->C;
-    CK(cudaMemcpyAsync(e->d_eval, eval, n * 8, cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->d_evec, evec, n * n * 8, cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->d_inv, inv_evec, n * n * 8, cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->d_rates, rates, C * 8, cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->d_props, props, C * 8, cudaMemcpyHostToDevice, e->st));
+    CK(stage_begin(e));
+    CK(stage_copy(e, e->d_eval, eval, n * 8));
+    CK(stage_copy(e, e->d_evec, evec, n * n * 8));
+    CK(stage_copy(e, e->d_inv, inv_evec, n * n * 8));
+    CK(stage_copy(e, e->d_rates, rates, C * 8));
+    CK(stage_copy(e, e->d_props, props, C * 8));
+    CK(stage_end(e));
     std::memcpy(e->h_eval, eval, n * 8);
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
@@ -520,7 +558,9 @@ int iqgpu_set_state_freq(iqgpu_engine *e, const double *state_freq) {
     if (!e || !state_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
     // the eigen-space FP64 path folds pi into U^-1; its non-reversible kernels weigh the branch by these
     CK(cudaSetDevice(e->dev));
-    CK(cudaMemcpyAsync(e->d_pi, state_freq, (size_t)e->n * 8, cudaMemcpyHostToDevice, e->st));
+    CK(stage_begin(e));
+    CK(stage_copy(e, e->d_pi, state_freq, (size_t)e->n * 8));
+    CK(stage_end(e));
     e->have_pi = true;
     return IQGPU_OK;
 }
@@ -532,7 +572,9 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
         return IQGPU_ERR_STATE;
     }
     CK(cudaSetDevice(e->dev));
-    CK(cudaMemcpyAsync(e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8, cudaMemcpyHostToDevice, e->st));
+    CK(stage_begin(e));
+    CK(stage_copy(e, e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8));
+    CK(stage_end(e));
     if (e->d_tiphl) CK(upload_hilo(e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n, e->st));
     std::memcpy(e->h_tipv, tip_lh, (size_t)e->n * e->n * 8);
     e->have_tips = true;
@@ -543,9 +585,11 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
 int iqgpu_set_patterns(iqgpu_engine *e, const double *ptn_freq, const double *ptn_invar) {
     if (!e || !ptn_freq) { set_error("null argument"); return IQGPU_ERR_ARG; }
     CK(cudaSetDevice(e->dev));
-    CK(cudaMemcpyAsync(e->d_freq, ptn_freq, (size_t)e->P * 8, cudaMemcpyHostToDevice, e->st));
-    if (ptn_invar) CK(cudaMemcpyAsync(e->d_invar, ptn_invar, (size_t)e->P * 8, cudaMemcpyHostToDevice, e->st));
+    CK(stage_begin(e));
+    CK(stage_copy(e, e->d_freq, ptn_freq, (size_t)e->P * 8));
+    if (ptn_invar) CK(stage_copy(e, e->d_invar, ptn_invar, (size_t)e->P * 8));
     else CK(cudaMemsetAsync(e->d_invar, 0, (size_t)e->Ppad * 8, e->st));
+    CK(stage_end(e));
     e->have_patterns = true;
     return IQGPU_OK;
 }
