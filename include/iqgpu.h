@@ -391,19 +391,25 @@ int iqgpu_simulate(int32_t ntaxa, int64_t nsites, int32_t nstates, int32_t ncat,
 /* No counterpart in the reference. For callers that may not allocate device
  * memory when they need a derivative (GPU memory owned by a pool they must
  * not bypass, a pipeline that cannot afford the device synchronisation of
- * cudaMalloc/cudaFree, or only borrowed device buffers at hand): the same
- * FP64 derivative sums as iqgpu_likelihood_derv, from a theta buffer the
+ * cudaMalloc/cudaFree, or only borrowed device buffers at hand): the FP64
+ * derivative sums of iqgpu_likelihood_derv for reversible single-class
+ * models (one eigen system; no mixture classes, no +ASC terms, and the exact
+ * sum rather than IQGPU_FLAG_REF_TRIPLE_TAIL's), from a theta buffer the
  * caller owns. All pointers ending in _dev are device memory:
  * theta_dev[B][ldp] (B = nstates*ncat, eigen space, row c*nstates+x),
  * buffer_scale_dev/freq_dev/invar_dev[nptn]; eval/rates/props are host
- * arrays. out_dev receives {df, ddf, lnl}. The kernel runs on cuda_stream
- * (NULL = legacy default stream); nothing is allocated or freed. Its only
- * scratch is a static device array sized for at most 524,288 patterns; larger
- * nptn is rejected with IQGPU_ERR_ARG. Every call on a device shares that
- * array, so calls whose kernels overlap on the GPU race: serialise them (one
- * stream, or events). The first call on each device resolves the array's
- * device address (set-up that must not happen inside a stream capture), so
- * make one call on each device before capturing. */
+ * arrays. out_dev receives {df, ddf, lnl}: the sums of lnL's first and
+ * second derivatives in the branch length and lnL itself at len. The kernel
+ * runs on cuda_stream (NULL = legacy default stream); nothing is allocated or
+ * freed. Its only scratch is a static device array sized for at most 524,288
+ * patterns; larger nptn is rejected with IQGPU_ERR_ARG. Every call on a
+ * device shares that array, so calls whose kernels overlap on the GPU race:
+ * serialise them (one stream, or events). The first call on each device
+ * resolves the array's device address (set-up that must not happen inside a
+ * stream capture), so make one call on each device before capturing. The
+ * address is kept for the life of the process: after cudaDeviceReset on a
+ * device, the next call there would use a stale address, so do not reset a
+ * device between calls. */
 int iqgpu_derv_noalloc(const double *theta_dev, const double *buffer_scale_dev, const double *freq_dev,
                        const double *invar_dev, int32_t nptn, int64_t ldp, int32_t nstates, int32_t ncat,
                        const double *eval, const double *rates, const double *props, double len,

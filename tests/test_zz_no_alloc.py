@@ -42,6 +42,7 @@ def test_noalloc_derivative_matches_engine(oracle_mod):
     lengths = (0.03, 0.4)
     want = [eng.likelihood_derv(ops, a, b, lengths[0]),
             eng.likelihood_derv([], a, b, lengths[1], theta_computed=True)]
+    want_lnl = [eng.lnl_from_buffer(length) for length in lengths]  # lnL at each length, same theta
 
     # the caller's own buffers: theta = node o dad in eigen space, NORM scale offset
     orc = oracle_mod.OracleTree(m, g.patterns, g.freq, g.edges, g.lengths)
@@ -66,10 +67,11 @@ def test_noalloc_derivative_matches_engine(oracle_mod):
             rv.ctypes.data_as(dp), pv.ctypes.data_as(dp), length, ct.c_void_p(t_out.data_ptr()),
             ct.c_void_p(stream.cuda_stream))
         assert rc == 0, engine.lib().iqgpu_last_error()
-        df, ddf, _ = t_out.cpu().numpy()
+        df, ddf, lnl = t_out.cpu().numpy()
         wdf, wddf = want[k]
         assert abs(df - wdf) <= 1e-9 * max(1.0, abs(wdf))
         assert abs(ddf - wddf) <= 1e-9 * max(1.0, abs(wddf))
+        assert abs(lnl - want_lnl[k]) <= 1e-9 * abs(want_lnl[k])
 
 
 def test_noalloc_rejects_oversized_input():
