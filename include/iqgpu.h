@@ -292,6 +292,14 @@ int iqgpu_set_stages(iqgpu_engine *e, int32_t stages);
  * split evenly. Chosen by the autotuner; results do not depend on it. */
 int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
+/* Failure detection (no counterpart in the reference, whose kernels cannot
+ * wait on each other): the number of polls after which a wait on another
+ * CTA's progress -- the dataflow schedule's producer flags -- gives up; the
+ * launch then stops, the call returns IQGPU_ERR_TIMEOUT and the engine stays
+ * usable (its next call runs normally). 0 restores the built-in limit (about
+ * seconds). Waits for the engine's own TMA copies and MMAs keep a fixed
+ * limit. */
+int iqgpu_set_wait_limit(iqgpu_engine *e, uint32_t polls);
 /* Kernel launches issued by this engine so far (all entry points). */
 int iqgpu_get_launches(iqgpu_engine *e, int64_t *launches);
 

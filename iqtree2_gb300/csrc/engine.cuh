@@ -171,6 +171,8 @@ struct iqgpu_engine {
     size_t stage_cap, stage_used;
     int stage_cur;
     cudaEvent_t stage_ev[2];
+    // limit of the waits on other CTAs' progress (0 = the built-in ~seconds)
+    unsigned wait_polls;
     // stream ownership and kernel timing
     cudaStream_t own_st;
     cudaEvent_t ev_t0, ev_t1;

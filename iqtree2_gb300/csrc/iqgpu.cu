@@ -1239,6 +1239,12 @@ int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
     return IQGPU_OK;
 }
 
+int iqgpu_set_wait_limit(iqgpu_engine *e, uint32_t polls) {
+    if (!e) { set_error("null engine"); return IQGPU_ERR_ARG; }
+    e->wait_polls = polls;
+    return IQGPU_OK;
+}
+
 int iqgpu_set_stages(iqgpu_engine *e, int32_t stages) {
     if (!e || !(stages == 0 || (stages >= 2 && stages <= 4))) {
         set_error("stages must be 0, 2, 3 or 4");

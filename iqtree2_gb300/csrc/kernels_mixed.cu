@@ -403,6 +403,7 @@ MixParams mix_params(iqgpu_engine *e, int nops) {
     P.red.ticket = e->d_ticket;
     P.red.out = e->d_red_out;
     P.status = e->d_status;
+    P.wait_polls = e->wait_polls ? e->wait_polls : kWaitPolls;
     P.branch_op = nops;
     return P;
 }

@@ -44,6 +44,7 @@ struct MixParams {
     double *buffer_scale;
     Reduce red;
     int *status;            // set to a nonzero code when a bounded wait gives up
+    unsigned wait_polls;    // polls of a wait on another CTA's progress (dataflow producer flags)
     int branch_op;          // op block holding the evaluated branch's matrices (= total ops)
 };
 

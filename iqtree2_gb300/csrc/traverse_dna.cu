@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kDnaTile) k_flow_dna(const MixParams P, unsign
                     const unsigned *f = done + (long long)prod[j] * ntiles + t;
                     unsigned polls = 0;
                     while (ld_acquire(f) != epoch) {
-                        if (++polls >= kWaitPolls || *(volatile int *)P.status != 0) { ok = 0; break; }
+                        if (++polls >= P.wait_polls || *(volatile int *)P.status != 0) { ok = 0; break; }
                     }
                 }
                 if (!ok) atomicExch(P.status, kStatusTimeout);

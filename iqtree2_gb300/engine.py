@@ -109,6 +109,7 @@ def lib():
         "iqgpu_set_model_nonrev": ([vp] + [ct.c_void_p] * 10, ct.c_int),
         "iqgpu_set_asc_holder": ([vp, ct.c_int32], ct.c_int),
         "iqgpu_set_stages": ([vp, ct.c_int32], ct.c_int),
+        "iqgpu_set_wait_limit": ([vp, ct.c_uint32], ct.c_int),
         "iqgpu_group_create": ([ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_void_p)], ct.c_int),
         "iqgpu_group_prepare": ([vp, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p], ct.c_int),
         "iqgpu_group_set_lengths": ([vp, ct.c_void_p, ct.c_void_p], ct.c_int),

@@ -159,11 +159,13 @@ Kernels pick_kernels(int kind, bool safe, int nstates) {
 template <class T> struct Aligned {
     T *p = nullptr;
     size_t n = 0;
-    void alloc(size_t count) {
+    // zeroed unless `lazy` (partials and scale counts: written before they are
+    // read, so pages of slots a traversal never touches are never committed)
+    void alloc(size_t count, bool lazy = false) {
         release();
         n = count;
         p = aligned_alloc<T>(count ? count : 1);
-        memset(p, 0, sizeof(T) * (count ? count : 1));
+        if (!lazy) memset(p, 0, sizeof(T) * (count ? count : 1));
     }
     void release() {
         if (p) free(p);
@@ -358,8 +360,8 @@ int iqref_set_tree(iqref *r, int nedges, const int *edges, const double *lengths
         size_t k = 0;
         for (auto &nei : r->neis) {
             if (nei->node->isLeaf()) continue;
-            r->partials[k].alloc((size_t)r->nptn_pad * block);
-            r->scales[k].alloc(scale_n);
+            r->partials[k].alloc((size_t)r->nptn_pad * block, true);
+            r->scales[k].alloc(scale_n, true);
             nei->partial_lh = r->partials[k].p;
             nei->scale_num = r->scales[k].p;
             k++;
