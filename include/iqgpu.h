@@ -277,8 +277,10 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * other kernels run fused); 3 = as 1, with the warp-specialised tensor-core
  * kernel (a copy/MMA issuer warp beside four worker warps; other kernels run
  * as 1); 4 = as 1, with the tensor-core kernel that keeps operand A in tensor
- * memory (20-state models in IQGPU_TF32X3; others run as 3). Results do not
- * depend on it. */
+ * memory (20-state models in IQGPU_TF32X3; others run as 3); 5 = as 3, and
+ * the narrow levels of models up to 32 padded states run as (tile, op,
+ * category) items on the tensor cores, as 61-state models always do, instead
+ * of on the CUDA-core tail. Results do not depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots

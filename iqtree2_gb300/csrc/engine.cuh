@@ -156,6 +156,7 @@ struct iqgpu_engine {
     int tc_kpieces;           // K pieces per stage (0/1 = whole K, 2 = halves)
     bool tc_ws;               // level schedule on the warp-specialised tensor-core kernel
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
+    bool tc_split;            // category-split items on narrow levels for <= 32 padded states too (schedule 5)
     float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs
     int nmix, cpc;            // mixture classes; categories per class (category c belongs to class c / cpc)
     float *d_cmax;            // category-split levels: per (op, category, pattern) maxima

@@ -1231,11 +1231,12 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
 }
 
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
-    if (!e || schedule < 0 || schedule > 4) { set_error("schedule must be 0 .. 4"); return IQGPU_ERR_ARG; }
+    if (!e || schedule < 0 || schedule > 5) { set_error("schedule must be 0 .. 5"); return IQGPU_ERR_ARG; }
     e->level_sync = schedule == 1 || schedule >= 3;
     e->flow = schedule == 2;
-    e->tc_ws = schedule == 3;
+    e->tc_ws = schedule == 3 || schedule == 5;
     e->tc_tm = schedule == 4;
+    e->tc_split = schedule == 5;
     return IQGPU_OK;
 }
 

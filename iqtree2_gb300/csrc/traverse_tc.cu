@@ -1229,19 +1229,20 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     const size_t smem = tc_smem_bytes(T, NSTAGE);
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF, false>;
-    auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, NP == 64>;
+    auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, true>;
+    const bool split_ok = NP == 64 || e->tc_split;  // 61 states always; fewer states with schedule 5
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err == cudaSuccess && ws)
         err = cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err == cudaSuccess && ws && NP == 64)
+    if (err == cudaSuccess && ws && split_ok)
         err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // the whole unified L1/shared array as shared memory: residency is set by shared memory
     if (err == cudaSuccess)
         err = ws ? cudaFuncSetAttribute(kern_ws, cudaFuncAttributePreferredSharedMemoryCarveout, 100)
                  : cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (err == cudaSuccess && ws && NP == 64)
+    if (err == cudaSuccess && ws && split_ok)
         err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
@@ -1274,7 +1275,7 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     // triples, each pair's chain of stages cut into ncat independent ones
     // (61 states only: a 20-state item is 8 short stages and the narrow levels
     // run faster on the CUDA-core tail than split plus the fix-up launch)
-    const bool can_split = ws && NP == 64 && e->d_cmax != nullptr;
+    const bool can_split = ws && split_ok && e->d_cmax != nullptr;
     int lt = e->nlevels;
     if (NP == 32)
         for (int l = 0; l < e->nlevels; l++)

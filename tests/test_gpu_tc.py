@@ -142,8 +142,9 @@ def test_tc_level_kernels_protein(oracle_mod):
     narrow levels go to the CUDA-core tail); the partials of levels 1-3, which
     every schedule computes on the tensor cores (operand A in shared or in
     tensor memory), bit-identical; the A-in-tensor-memory kernel
-    deterministic. (Category-split items are checked bit for bit by the codon
-    case of test_tc_schedules_agree_and_match_cuda_cores.)"""
+    deterministic; schedule 5 runs the narrow levels as category-split items
+    (bit-identical partials on the levels every schedule puts on the tensor
+    cores)."""
     ds = simulate.protein_lg_dataset(100, 20000, 35)
     topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
     leaf, nb = 0, topo.adj[0][0][0]
@@ -156,7 +157,7 @@ def test_tc_level_kernels_protein(oracle_mod):
     assert len(check) >= 20
     eng = _engine(ds, topo)
     got, launches, parts = {}, {}, {}
-    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0)]:
+    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0), (0, 5, 2, 1)]:
         autotune.apply(eng, cand)
         l0 = eng.launches()
         got[cand] = eng.compute_likelihood(ops, a, b, length)
