@@ -67,6 +67,7 @@ struct TravParams {
     double *theta;             // THETA
     double *buffer_scale;      // THETA
     Reduce red;
+    int cat_split;             // 1: this launch's CTA (x, y) computes category y only (SAFE op walks)
 };
 
 enum Epilogue { EPI_NONE = 0, EPI_LNL = 1, EPI_THETA = 2 };
@@ -157,6 +158,8 @@ struct iqgpu_engine {
     bool tc_ws;               // level schedule on the warp-specialised tensor-core kernel
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
     bool tc_split;            // category-split items on narrow levels for <= 32 padded states too (schedule 5)
+    bool has_multi;           // the uploaded op list holds multifurcating records (IQGPU_OP_MORE)
+    int sms;                  // multiprocessors of the engine's device
     float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs
     int nmix, cpc;            // mixture classes; categories per class (category c belongs to class c / cpc)
     float *d_cmax;            // category-split levels: per (op, category, pattern) maxima

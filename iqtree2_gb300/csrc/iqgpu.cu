@@ -259,6 +259,8 @@ static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_b
     e->P = cfg->nptn;
     e->Ppad = s.Ppad;
     e->nblk = (int)(s.Ppad / kTPB);
+    if (cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess || e->sms < 1)
+        e->sms = 1;
     e->op_stride = s.op_stride;
     e->level_off = static_cast<int *>(std::malloc(sizeof(int) * ((size_t)cfg->max_ops + 2)));
     if (!e->level_off) {
@@ -706,6 +708,8 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         set_error("the last traversal entry is flagged IQGPU_OP_MORE");
         return IQGPU_ERR_ARG;
     }
+    e->has_multi = false;
+    for (int k = 0; k < nops && !e->has_multi; k++) e->has_multi = (ops[k].flags & IQGPU_OP_MORE) != 0;
     // Mixed engines take the ops in tree-level order (a valid post-order: every
     // child is produced in a lower level), so that a level-synchronous launch
     // can run each level's independent ops together.

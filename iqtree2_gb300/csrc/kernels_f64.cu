@@ -258,6 +258,9 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
     const long long CNN = (long long)C * n * n;
     const long long SB = (long long)(S + 1) * B;
     const double *__restrict__ Ui = P.inv_evec;
+    // SAFE walks with few pattern tiles: one category per CTA (its scale counts
+    // and checks involve no other category); otherwise every category
+    const int c_lo = P.cat_split ? (int)blockIdx.y : 0, c_hi = P.cat_split ? (int)blockIdx.y + 1 : C;
 
     bool in_group = false;  // inside the records of a multifurcating node
     for (int k = 0; k < P.nops; ++k) {
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         const double *tr = rint ? nullptr : tR + (long long)P.states[(long long)(-1 - rref) * ld + p] * B;
         // scale counts of the dad: 0 (tip-tip), copy (tip-internal), sum (internal-internal)
         if (SAFE) {
-            for (int c = 0; c < C; c++) {
+            for (int c = c_lo; c < c_hi; c++) {
                 unsigned s = 0;
                 if (lint) s += P.scale[(long long)lref * P.scale_stride + c * ld + p];
                 if (rint) s += P.scale[(long long)rref * P.scale_stride + c * ld + p];
@@ -299,7 +302,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         }
         const bool check = (lint || rint) && invar == 0.0;  // tip-tip never scales
         double lh_max = 0.0;
-        for (int c = 0; c < C; c++) {
+        for (int c = c_lo; c < c_hi; c++) {
             double cmax = 0.0;
             if constexpr (REG) {
                 double lv[NR], rv[NR], tmp[NR];
@@ -748,6 +751,7 @@ static TravParams trav_params(iqgpu_engine *e, int nops) {
     P.scale = e->d_scale;
     P.a = P.b = 0;
     P.len = 0.0;
+    P.cat_split = 0;
     P.pattern_lh = e->d_plh;
     P.theta = e->d_theta;
     P.buffer_scale = e->d_bscale;
@@ -775,6 +779,7 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops) {
 
 template <int NT, bool SAFE, int EPI>
 static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
+    const dim3 grid(e->nblk, P.cat_split ? e->C : 1);
     constexpr bool REG = (NT != 0 && NT <= 20);
     size_t smem = (REG ? 0 : (size_t)kMaxStates * kTPB * sizeof(double)) +
                   (EPI == EPI_LNL ? (size_t)kMaxCat * kMaxStates * sizeof(double) : 0);
@@ -783,7 +788,7 @@ static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "traverse_f64 smem attribute");
     }
-    kern<<<e->nblk, kTPB, smem, e->st>>>(P);
+    kern<<<grid, kTPB, smem, e->st>>>(P);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "traverse_f64");
 }
@@ -808,6 +813,15 @@ int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b
     P.b = b;
     P.len = len;
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    // SAFE op walks over too few pattern tiles to fill the GPU (codon, short
+    // alignments): one CTA per (tile, category), then the epilogue on its own
+    if (e->cfg.safe && !e->nonrev && !e->has_multi && nops > 0 && e->C > 1 && e->nblk < 2 * e->sms) {
+        P.cat_split = 1;
+        int rc = dispatch_safe<EPI_NONE>(e, P);
+        if (rc || epi == EPI_NONE) return rc;
+        P.cat_split = 0;
+        P.nops = 0;
+    }
     switch (epi) {
     case EPI_NONE: return dispatch_safe<EPI_NONE>(e, P);
     case EPI_LNL: return dispatch_safe<EPI_LNL>(e, P);
