@@ -356,7 +356,8 @@ typedef struct {
 typedef struct {
     int64_t id;
     int32_t status;             /* IQGPU_OK, IQGPU_ERR_OOM if refused, ... */
-    int32_t pad;
+    int32_t slots;              /* partial slots of the job's engine; fewer than the tree's
+                                   3*(ntaxa-2) directed partials means they were recycled */
     double lnl_initial, lnl;    /* before and after branch optimisation */
     double t_submit, t_start, t_end;  /* seconds since the server started */
     int64_t bytes;              /* HBM the job's engine held */
@@ -377,8 +378,12 @@ typedef struct iqgpu_server iqgpu_server;
 
 /* Reserve the arena and start the scheduler. Jobs are admitted in arrival
  * order when a worker slot (max_active) is free and their engine fits in the
- * arena's free space; a job larger than the arena is refused (IQGPU_ERR_OOM).
- * Admitted jobs run concurrently, each on its own stream. */
+ * arena's free space. A job whose partials do not fit in half the arena gets
+ * an engine with fewer partial slots than its tree has directed partials,
+ * recycled least-recently-used first and recomputed when needed (the
+ * reference's LM_MEM_SAVE, tree/memslot.h:44-74, tree/phylotree.cpp:967-1027);
+ * a job that does not fit even then is refused (IQGPU_ERR_OOM). Admitted
+ * jobs run concurrently, each on its own stream. */
 int iqgpu_server_create(const iqgpu_server_config *cfg, iqgpu_server **out);
 /* Queue a job (precision IQGPU_F64 or IQGPU_F32); returns its id at once. */
 int iqgpu_server_submit(iqgpu_server *s, const iqgpu_job *job, int32_t precision, int64_t *id);

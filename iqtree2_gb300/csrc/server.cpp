@@ -14,6 +14,7 @@
 // depend on what else is running.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -244,7 +245,26 @@ int iqgpu_server_submit(iqgpu_server *s, const iqgpu_job *job, int32_t precision
     size_t bytes = 0;
     int rc = iqgpu_memory_required(&c, &bytes);
     if (rc) return rc;
+    if (bytes > s->arena.total / 2) {
+        // slot recycling: as many partial slots as half the arena holds, at
+        // least the ones pinned along a root path (larger subtrees first)
+        iqgpu_config c1 = c;
+        size_t b1 = 0, b2 = 0;
+        c1.nslots = 1;
+        if ((rc = iqgpu_memory_required(&c1, &b1))) return rc;
+        c1.nslots = 2;
+        if ((rc = iqgpu_memory_required(&c1, &b2))) return rc;
+        const size_t per = b2 - b1, base = b1 - per, target = s->arena.total / 2;
+        int lg = 1;
+        while ((1 << lg) < T) lg++;
+        const long long fit = target > base ? (long long)((target - base) / per) : 0;
+        if (fit >= 2 * lg + 4) {
+            c.nslots = (int32_t)std::min<long long>(fit, c.nslots);
+            if ((rc = iqgpu_memory_required(&c, &bytes))) return rc;
+        }
+    }
     j->bytes = bytes;
+    j->res.slots = c.nslots;
     j->opt_iterations = job->opt_iterations;
     j->tolerance = job->tolerance > 0 ? job->tolerance : 1e-3;
     j->eval.assign(job->eval, job->eval + n);

@@ -16,6 +16,7 @@
 // Every directed partial of an internal subtree owns one HBM slot (three per
 // internal node), so a branch-length change only recomputes the partials it
 // invalidates, as with the reference's per-neighbour partial_lh buffers.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -35,16 +36,35 @@ struct iqgpu_tree {
     int64_t nptn;
     int ntaxa, nnode, nedge;
     std::vector<int> deg;
-    std::vector<int> nbr, edge, slot;  // [node*kMaxDeg + j]
-    std::vector<uint8_t> computed;     // [node*kMaxDeg + j]: partial of node->nbr valid
+    std::vector<int> nbr, edge;        // [node*kMaxDeg + j]
+    std::vector<uint8_t> computed;     // [node*kMaxDeg + j]: partial of node->nbr valid (and resident)
     std::vector<double> len;
     std::vector<int> height;
-    std::vector<iqgpu_op> ops;
+    std::vector<iqgpu_op> ops;         // records not yet executed
     int64_t nupdates = 0;
     double min_bl = 1e-6, max_bl = 10.0;
     int cur1 = -1, cur2 = -1;  // current_it: cur1 -> cur2
     bool theta_computed = false;
     int last_rc = IQGPU_OK;
+
+    // HBM slots. A tree may have more directed internal partials than its
+    // engine has slots (a job larger than its memory): partials then share the
+    // slots least-recently-used first, as MemSlotVector does under LM_MEM_SAVE
+    // (tree/memslot.h:44-74, tree/phylotree.cpp:967-1027), and are recomputed
+    // when needed again. A slot is never reassigned while an op that is not
+    // yet executed reads or writes it (pending) or an op that is not yet built
+    // will read it (pins); subtrees are walked larger first, so only about
+    // log2(ntaxa) partials are pinned at once.
+    int nslots = 0;
+    std::vector<int> slot_of;          // [node*kMaxDeg + j]: slot holding that partial, or -1
+    std::vector<int> owner;            // [slot]: the directed partial it holds, or -1
+    std::vector<int64_t> stamp;        // [slot]: last use
+    std::vector<int> pins;             // [slot]
+    std::vector<uint8_t> pending;      // [slot]
+    std::vector<int> free_slots;
+    std::vector<int> leaves;           // [node*kMaxDeg + j]: leaves behind that directed edge (0 = not yet known)
+    int64_t tick = 0;
+    int walk_rc = IQGPU_OK;
 
     bool leaf(int u) const { return u < ntaxa; }
     int idx(int u, int v) const {
@@ -52,44 +72,116 @@ struct iqgpu_tree {
             if (nbr[u * kMaxDeg + j] == v) return j;
         return -1;
     }
-    int ref(int dad, int node) const { return leaf(node) ? -1 - node : slot[dad * kMaxDeg + idx(dad, node)]; }
     double &blen(int u, int v) { return len[edge[u * kMaxDeg + idx(u, v)]]; }
-
-    // post-order list of stale partials (tree/phylotree.cpp:5918-6028); a node
-    // with more than two children becomes consecutive records flagged
-    // IQGPU_OP_MORE (two children each, IQGPU_NO_CHILD closing an odd count)
-    void traverse(int dad, int node) {
-        const int j = idx(dad, node);
-        if (leaf(node) || computed[dad * kMaxDeg + j]) return;
-        int kids[kMaxDeg];
-        double kl[kMaxDeg];
-        int k = 0;
-        for (int q = 0; q < deg[node]; q++) {
-            const int ch = nbr[node * kMaxDeg + q];
-            if (ch == dad) continue;
-            traverse(node, ch);
-            kids[k] = ref(node, ch);
-            kl[k] = len[edge[node * kMaxDeg + q]];
-            k++;
+    int leaves_behind(int dad, int node) {
+        if (leaf(node)) return 1;
+        int &c = leaves[dad * kMaxDeg + idx(dad, node)];
+        if (c == 0)
+            for (int q = 0; q < deg[node]; q++)
+                if (nbr[node * kMaxDeg + q] != dad) c += leaves_behind(node, nbr[node * kMaxDeg + q]);
+        return c;
+    }
+    void evict(int s) {
+        if (owner[s] >= 0) {
+            computed[owner[s]] = 0;
+            slot_of[owner[s]] = -1;
+            owner[s] = -1;
         }
-        const int dslot = slot[dad * kMaxDeg + j];
+    }
+    int take_slot(int d) {
+        if (slot_of[d] >= 0) return slot_of[d];
+        int s = -1;
+        if (!free_slots.empty()) {
+            s = free_slots.back();
+            free_slots.pop_back();
+        } else {
+            for (int k = 0; k < nslots; k++)
+                if (pins[k] == 0 && !pending[k] && (s < 0 || stamp[k] < stamp[s])) s = k;
+            if (s < 0) return -1;
+            evict(s);
+        }
+        owner[s] = d;
+        slot_of[d] = s;
+        return s;
+    }
+    int flush() {
+        if (ops.empty()) return IQGPU_OK;
+        const int rc = iqgpu_compute_partials(e, ops.data(), (int32_t)ops.size());
+        nupdates += (int64_t)ops.size() * nptn;
+        settled(rc);
+        return rc;
+    }
+    void unpin(int ref) {
+        if (ref >= 0 && pins[ref] > 0) pins[ref]--;
+    }
+    void settled(int rc) {  // the evaluation launch executed the pending records (or failed)
+        ops.clear();
+        std::fill(pending.begin(), pending.end(), 0);
+        if (rc) std::fill(computed.begin(), computed.end(), 0);  // nothing of a failed launch is valid
+    }
+
+    // post-order list of stale partials (tree/phylotree.cpp:5918-6028); returns
+    // the partial of node seen from dad (a slot, pinned for the caller, or a
+    // tip). A node with more than two children becomes consecutive records
+    // flagged IQGPU_OP_MORE (two children each, IQGPU_NO_CHILD closing an odd
+    // count); children keep the neighbour order in the records.
+    int traverse(int dad, int node) {
+        if (leaf(node)) return -1 - node;
+        const int d = dad * kMaxDeg + idx(dad, node);
+        if (computed[d]) {
+            const int s = slot_of[d];
+            pins[s]++;
+            stamp[s] = ++tick;
+            return s;
+        }
+        int kid_q[kMaxDeg], order[kMaxDeg], refs[kMaxDeg];
+        int k = 0;
+        for (int q = 0; q < deg[node]; q++)
+            if (nbr[node * kMaxDeg + q] != dad) kid_q[k++] = q;
+        for (int i = 0; i < k; i++) order[i] = i;
+        std::stable_sort(order, order + k, [&](int x, int y) {
+            return leaves_behind(node, nbr[node * kMaxDeg + kid_q[x]]) > leaves_behind(node, nbr[node * kMaxDeg + kid_q[y]]);
+        });
+        for (int i = 0; i < k; i++) refs[order[i]] = traverse(node, nbr[node * kMaxDeg + kid_q[order[i]]]);
+        if (walk_rc) return 0;
+        int s = take_slot(d);
+        if (s < 0) {
+            if ((walk_rc = flush())) return 0;
+            s = take_slot(d);
+        }
+        if (s < 0) {
+            iqg::set_error("too few partial slots for this tree (every slot holds a partial still needed)");
+            walk_rc = IQGPU_ERR_OOM;
+            return 0;
+        }
         for (int i = 0; i < k; i += 2) {
             iqgpu_op op;
             std::memset(&op, 0, sizeof(op));
-            op.dad_slot = dslot;
-            op.child[0] = kids[i];
-            op.len[0] = kl[i];
-            op.child[1] = i + 1 < k ? kids[i + 1] : IQGPU_NO_CHILD;
-            op.len[1] = i + 1 < k ? kl[i + 1] : 0.0;
+            op.dad_slot = s;
+            op.child[0] = refs[i];
+            op.len[0] = len[edge[node * kMaxDeg + kid_q[i]]];
+            op.child[1] = i + 1 < k ? refs[i + 1] : IQGPU_NO_CHILD;
+            op.len[1] = i + 1 < k ? len[edge[node * kMaxDeg + kid_q[i + 1]]] : 0.0;
             op.flags = i + 2 < k ? IQGPU_OP_MORE : 0;
             ops.push_back(op);
         }
-        computed[dad * kMaxDeg + j] = 1;
+        for (int i = 0; i < k; i++)
+            if (refs[i] >= 0) {
+                unpin(refs[i]);
+                pending[refs[i]] = 1;
+            }
+        pending[s] = 1;
+        stamp[s] = ++tick;
+        computed[d] = 1;
+        pins[s]++;
+        return s;
     }
-    void collect(int node, int dad) {
-        ops.clear();
-        traverse(dad, node);
-        traverse(node, dad);
+    // both partials of branch dad-node, pinned until the branch is evaluated
+    int collect(int node, int dad, int *a, int *b) {
+        walk_rc = IQGPU_OK;
+        *a = traverse(dad, node); /* dad_branch: dad -> node */
+        *b = traverse(node, dad); /* node_branch: node -> dad */
+        return walk_rc;
     }
     int farthest_leaf(int node, int dad) {
         if (dad >= 0 && leaf(node)) { height[node] = 0; return node; }
@@ -110,7 +202,7 @@ struct iqgpu_tree {
         for (int q = 0; q < deg[node]; q++) {
             const int x = nbr[node * kMaxDeg + q];
             if (x == dad) continue;
-            computed[x * kMaxDeg + idx(x, node)] = 0;
+            computed[x * kMaxDeg + idx(x, node)] = 0;  // stale; its slot is reused when it is recomputed
             clear_reverse(x, node);
         }
     }
@@ -133,10 +225,13 @@ int64_t nptn_of(const iqgpu_tree *t) { return t->nptn; }
 // computeLikelihoodBranch(dad_branch = dad->node, dad)
 int lnl_branch(iqgpu_tree *t, int node, int dad, double *lnl) {
     if (t->leaf(node)) std::swap(node, dad);
-    t->collect(node, dad);
-    const int rc = iqgpu_compute_likelihood(t->e, t->ops.data(), (int32_t)t->ops.size(), t->ref(dad, node),
-                                            t->ref(node, dad), t->blen(node, dad), lnl);
+    int a, b;
+    int rc = t->collect(node, dad, &a, &b);
+    if (!rc) rc = iqgpu_compute_likelihood(t->e, t->ops.data(), (int32_t)t->ops.size(), a, b, t->blen(node, dad), lnl);
     t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+    t->settled(rc);
+    t->unpin(a);
+    t->unpin(b);
     return rc;
 }
 
@@ -146,12 +241,17 @@ int func_derv(iqgpu_tree *t, double value, double *f, double *df) {
     t->blen(n1, n2) = value;
     int node = n2, dad = n1;
     if (t->leaf(node)) std::swap(node, dad);
-    t->collect(node, dad);
+    int a, b;
+    int rc = t->collect(node, dad, &a, &b);
     double d1 = 0.0, d2 = 0.0;
-    const int rc = iqgpu_likelihood_derv(t->e, t->ops.data(), (int32_t)t->ops.size(), t->ref(dad, node),
-                                         t->ref(node, dad), value, t->theta_computed ? 1 : 0, &d1, &d2);
-    if (rc) return rc;
+    if (!rc)
+        rc = iqgpu_likelihood_derv(t->e, t->ops.data(), (int32_t)t->ops.size(), a, b, value,
+                                   t->theta_computed ? 1 : 0, &d1, &d2);
     t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+    t->settled(rc);
+    t->unpin(a);
+    t->unpin(b);
+    if (rc) return rc;
     t->theta_computed = true;
     *f = -d1;
     *df = -d2;
@@ -220,7 +320,8 @@ int iqgpu_tree_create_n(iqgpu_engine *e, int32_t nedge, const int32_t *edges, co
     t->deg.assign(t->nnode, 0);
     t->nbr.assign((size_t)t->nnode * kMaxDeg, -1);
     t->edge.assign((size_t)t->nnode * kMaxDeg, -1);
-    t->slot.assign((size_t)t->nnode * kMaxDeg, -1);
+    t->slot_of.assign((size_t)t->nnode * kMaxDeg, -1);
+    t->leaves.assign((size_t)t->nnode * kMaxDeg, 0);
     t->computed.assign((size_t)t->nnode * kMaxDeg, 0);
     t->height.assign(t->nnode, 0);
     t->len.assign(lengths, lengths + t->nedge);
@@ -244,16 +345,27 @@ int iqgpu_tree_create_n(iqgpu_engine *e, int32_t nedge, const int32_t *edges, co
             return IQGPU_ERR_ARG;
         }
     }
-    int ns = 0;
+    int ns = 0;  // directed internal partials
     for (int u = 0; u < t->nnode; u++)
         for (int j = 0; j < t->deg[u]; j++)
-            if (!t->leaf(t->nbr[u * kMaxDeg + j])) t->slot[u * kMaxDeg + j] = ns++;
-    if (cfg->nslots < ns || cfg->max_ops < 2 * t->ntaxa) {
+            if (!t->leaf(t->nbr[u * kMaxDeg + j])) ns++;
+    // fewer slots than partials: recycling; it needs the partials pinned along
+    // one root path (larger subtrees first: about log2(ntaxa)) plus the branch
+    int lg = 1;
+    while ((1 << lg) < t->ntaxa) lg++;
+    const int min_slots = std::min(ns, 2 * lg + 4);
+    if (cfg->nslots < min_slots || cfg->max_ops < 2 * t->ntaxa) {
         delete t;
-        iqg::set_error("engine needs nslots >= " + std::to_string(ns) + " (one per directed internal partial; " +
-                       "3*(ntaxa-2) for a binary tree) and max_ops >= 2*ntaxa");
+        iqg::set_error("engine needs nslots >= " + std::to_string(min_slots) + " (" + std::to_string(ns) +
+                       " for every directed internal partial at once) and max_ops >= 2*ntaxa");
         return IQGPU_ERR_ARG;
     }
+    t->nslots = std::min(cfg->nslots, ns);
+    t->owner.assign(t->nslots, -1);
+    t->stamp.assign(t->nslots, 0);
+    t->pins.assign(t->nslots, 0);
+    t->pending.assign(t->nslots, 0);
+    for (int k = t->nslots - 1; k >= 0; k--) t->free_slots.push_back(k);
     *out = t;
     return IQGPU_OK;
 }

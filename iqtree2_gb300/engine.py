@@ -428,14 +428,17 @@ class GpuTree:
     """PhyloTree drivers on the GPU engine (one engine per tree)."""
 
     def __init__(self, model, patterns, freq, edges, lengths, safe=False, precision=F64, device=0, invar=None,
-                 flags=0, asc=None):
+                 flags=0, asc=None, slots=None):
         """asc=(nconst, nsite): +ASC (Lewis) with the last nconst patterns as
-        the unobserved constant patterns (``models.asc_lewis_patterns``)."""
+        the unobserved constant patterns (``models.asc_lewis_patterns``).
+        slots: partial slots of the engine (default one per directed internal
+        partial, 3*(ntaxa-2)); fewer are recycled and partials recomputed as
+        needed (the reference's LM_MEM_SAVE)."""
         ntaxa = patterns.shape[0]
         self.ntaxa = ntaxa
         self.nedge = len(edges)  # 2*ntaxa-3, fewer with multifurcating nodes
         self.engine = Engine(patterns.shape[1], model.nstates, model.ncat, ntaxa, model.state_unknown,
-                             3 * (ntaxa - 2), safe=safe, precision=precision, device=device,
+                             slots or 3 * (ntaxa - 2), safe=safe, precision=precision, device=device,
                              max_ops=2 * ntaxa, flags=flags)
         self.engine.set_model(model)
         self.engine.set_patterns(freq, invar)

@@ -29,7 +29,7 @@ class Job(ct.Structure):
 
 
 class JobResult(ct.Structure):
-    _fields_ = [("id", ct.c_int64), ("status", ct.c_int32), ("pad", ct.c_int32), ("lnl_initial", ct.c_double),
+    _fields_ = [("id", ct.c_int64), ("status", ct.c_int32), ("slots", ct.c_int32), ("lnl_initial", ct.c_double),
                 ("lnl", ct.c_double), ("t_submit", ct.c_double), ("t_start", ct.c_double), ("t_end", ct.c_double),
                 ("bytes", ct.c_int64), ("error", ct.c_char * 128)]
 
@@ -89,8 +89,8 @@ class Server:
         lengths = np.zeros(nedge) if nedge else None
         engine._check(self.L.iqgpu_server_wait(self.h, jid, ct.byref(r),
                                                lengths.ctypes.data_as(_DP) if lengths is not None else None))
-        out = {k: getattr(r, k) for k in ("id", "status", "lnl_initial", "lnl", "t_submit", "t_start", "t_end",
-                                           "bytes")}
+        out = {k: getattr(r, k) for k in ("id", "status", "slots", "lnl_initial", "lnl", "t_submit", "t_start",
+                                           "t_end", "bytes")}
         out["error"] = r.error.decode()
         if lengths is not None:
             out["lengths"] = lengths
