@@ -779,41 +779,58 @@ def run_batched(args):
 
 
 def run_serve(args):
-    """Serving: seeded Poisson stream (mean --rate req/s) of lnL + one round of
-    branch optimisation; 70% DNA GTR+G4 / 30% protein LG+G4, taxa log-U[8, max],
-    sites log-U[500, max]; inputs simulated on the device, generation untimed.
-    Reports p50/p99 latency (completion - arrival) and throughput per precision."""
+    """Serving: seeded stream of lnL + one round of branch optimisation jobs;
+    70% DNA GTR+G4 / 30% protein LG+G4, taxa log-U[8, max], sites log-U[500,
+    max]; inputs simulated on the device, generation untimed. Two regimes per
+    precision: the specified Poisson rate (--rate, 200/s: far above what one
+    GPU completes, so latency is mostly queueing of a burst) on the first
+    --requests jobs, and a steady state below capacity (--steady-requests jobs
+    at --steady-rate for the mixed path, --steady-requests-fp64 at
+    --steady-rate-fp64 for FP64), where p99 is a tail of a stationary queue.
+    Reports p50/p99 latency (completion - arrival) and throughput."""
     from iqtree2_gb300 import engine, serving
     rng = np.random.default_rng(args.seed)
+    njobs = max(args.requests, args.steady_requests, args.steady_requests_fp64)
     jobs = []
-    for k in range(args.requests):
+    t_gen = time.perf_counter()
+    for k in range(njobs):
         kind = "dna" if rng.random() < 0.7 else "protein"
         taxa = int(round(np.exp(rng.uniform(np.log(8), np.log(args.max_taxa)))))
         sites = int(round(np.exp(rng.uniform(np.log(500), np.log(args.max_sites)))))
         jobs.append(simulate.serving_dataset(kind, max(taxa, 4), sites, int(rng.integers(1 << 30))))
-    out = {"metric": "serve latency (completion - arrival)", "unit": "s", "requests": len(jobs),
-           "rate_per_s": args.rate, "data": "synthetic (device-simulated, seeded)",
-           "config": {"workload": f"Poisson {args.rate}/s, 70% DNA GTR+G4 / 30% LG+G4, taxa log-U[8,{args.max_taxa}], "
+    t_gen = time.perf_counter() - t_gen
+    out = {"metric": "serve latency (completion - arrival)", "unit": "s", "data": "synthetic (device-simulated, seeded)",
+           "config": {"workload": f"70% DNA GTR+G4 / 30% LG+G4, taxa log-U[8,{args.max_taxa}], "
                                   f"sites log-U[500,{args.max_sites}], lnL + 1 round of branch NR",
-                      "max_active": args.max_active}}
+                      "max_active": args.max_active, "jobs_generated": njobs, "generation_s": t_gen}}
     lnl = {}
-    for name, prec in (("mixed_f32", engine.F32), ("fp64", engine.F64)):
-        if name == "fp64" and args.no_fp64_serve:
-            continue
+
+    def run(name, prec, rate, n):
         srv = serving.Server(max_active=args.max_active)
-        res, wall = serving.poisson_stream(srv, jobs, args.rate, args.seed, precision=prec)
+        res, wall = serving.poisson_stream(srv, jobs[:n], rate, args.seed, precision=prec)
         st = srv.stats()
         srv.close()
         ok = [r for r in res if r["status"] == 0]
         lat = np.array([r["latency"] for r in ok])
-        upd = sum((r["ntaxa"] - 2) * r["nptn"] for r in ok)
-        lnl[name] = {r["id"]: r["lnl_initial"] for r in ok}
-        out[name] = {"p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
-                     "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
-                     "throughput_jobs_per_s": len(ok) / wall, "wall_s": wall, "completed": len(ok),
-                     "refused": st["refused"], "peak_active": st["peak_active"],
-                     "peak_hbm_gb": st["peak_bytes"] / 1e9, "arena_gb": st["arena_bytes"] / 1e9,
-                     "full_traversal_updates": upd}
+        qw = np.array([r["queue_wait"] for r in ok])
+        lnl.setdefault(name, {}).update({r["id"] - res[0]["id"]: r["lnl_initial"] for r in ok})
+        return {"rate_per_s": rate, "requests": n, "completed": len(ok), "refused": st["refused"],
+                "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                "p50_queue_wait_s": float(np.percentile(qw, 50)) if len(qw) else None,
+                "throughput_jobs_per_s": len(ok) / wall, "wall_s": wall, "peak_active": st["peak_active"],
+                "peak_hbm_gb": st["peak_bytes"] / 1e9, "arena_gb": st["arena_bytes"] / 1e9,
+                "recycled_slot_jobs": sum(1 for r in ok if r["slots"] < 3 * (r["ntaxa"] - 2)),
+                "full_traversal_updates": sum((r["ntaxa"] - 2) * r["nptn"] for r in ok)}
+
+    for name, prec in (("mixed_f32", engine.F32), ("fp64", engine.F64)):
+        if name == "fp64" and args.no_fp64_serve:
+            continue
+        out[name] = {"burst": run(name, prec, args.rate, args.requests)}
+        steady = (args.steady_rate, args.steady_requests) if prec == engine.F32 else \
+            (args.steady_rate_fp64, args.steady_requests_fp64)
+        if steady[1] > 0:
+            out[name]["steady"] = run(name, prec, *steady)
     if "fp64" in lnl:
         common = set(lnl["fp64"]) & set(lnl["mixed_f32"])
         out["lnl_max_rel_err_mixed_vs_fp64"] = max(
@@ -837,6 +854,10 @@ def main():
     ap.add_argument("--max-active", type=int, default=16)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--no-fp64-serve", action="store_true")
+    ap.add_argument("--steady-rate", type=float, default=12.0)
+    ap.add_argument("--steady-requests", type=int, default=500)
+    ap.add_argument("--steady-rate-fp64", type=float, default=3.5)
+    ap.add_argument("--steady-requests-fp64", type=int, default=200)
     ap.add_argument("--config", default=None,
                     help="fixed traversal configuration instead of the autotuner, as the autotuner labels it "
                          "(tile/schedule[/sD][/kP], e.g. 0/level/s2/k1)")
