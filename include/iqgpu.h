@@ -184,6 +184,30 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
                           double len, int32_t theta_computed, double *df, double *ddf);
 /* computeLikelihoodFromBufferPointer (tree/phylokernelnew.h:3232-3428). */
 int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl);
+/* Optimization::minimizeNewton (utils/optimization.cpp:422-499) of one branch
+ * length, with computeFuncDerv (tree/phylotree.cpp:2529-2536: f = -df,
+ * df = -ddf) as its function, run as one device kernel: the traversal
+ * (when theta_computed is 0, as for iqgpu_likelihood_derv) and every Newton or
+ * bisection step happen on the GPU, and the host waits once. x1/xguess/x2/
+ * xacc/max_nr_step mean what they mean to minimizeNewton; *optx receives its
+ * return value, *d2l its d2l output (the last second-derivative value of
+ * computeFuncDerv), *last_len the length of the last derivative evaluation
+ * (where the reference leaves the branch: computeLikelihoodFromBuffer after
+ * minimizeNewton reads it) and *steps the iterations taken; d2l, last_len
+ * and steps may be NULL. Errors as the
+ * reference's: IQGPU_ERR_NONFINITE for a non-finite NORM derivative,
+ * IQGPU_ERR_NEWTON for "Wrong computeFuncDerv" or the iteration limit.
+ * Reversible FP64 engines without +ASC whose theta buffer holds at most
+ * IQGPU_NEWTON_MAX_ENTRIES doubles (patterns x states x categories); other
+ * engines return IQGPU_ERR_ARG before doing anything, and callers iterate
+ * iqgpu_likelihood_derv on the host as minimizeNewton does. The theta buffer
+ * stays valid for iqgpu_lnl_from_buffer at any length afterwards. */
+#define IQGPU_NEWTON_MAX_ENTRIES (1 << 20)
+/* *supported = 1 when iqgpu_newton_branch serves this engine, else 0. */
+int iqgpu_newton_supported(iqgpu_engine *e, int32_t *supported);
+int iqgpu_newton_branch(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b,
+                        int32_t theta_computed, double x1, double xguess, double x2, double xacc,
+                        int32_t max_nr_step, double *optx, double *d2l, double *last_len, int32_t *steps);
 /* Per-pattern lnL of the last branch/from-buffer evaluation (_pattern_lh);
  * with +ASC the observed patterns carry the correction term. */
 int iqgpu_get_pattern_lh(iqgpu_engine *e, double *out);
@@ -280,7 +304,13 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * memory (20-state models in IQGPU_TF32X3; others run as 3); 5 = as 3, and
  * the narrow levels of models up to 32 padded states run as (tile, op,
  * category) items on the tensor cores, as 61-state models always do, instead
- * of on the CUDA-core tail. Results do not depend on it. */
+ * of on the CUDA-core tail; 6 = dataflow on the tensor cores: leading
+ * tip-tip levels as in 1, then every other op in one persistent launch of
+ * (tile, op, category) items handed out in level order, each item's copies
+ * issued once the items writing its children are done (bounded waits; the
+ * level form of 5 when the traversal has more (op, tile) pairs than the
+ * engine's pair counters; other kernels run as 3). Results do not depend on
+ * it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots
@@ -454,6 +484,10 @@ int iqgpu_tree_set_lengths(iqgpu_tree *t, const double *lengths);
 int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl);
 /* Pattern-node updates executed so far (throughput accounting). */
 int iqgpu_tree_num_updates(iqgpu_tree *t, int64_t *updates);
+/* Where optimizeOneBranch runs minimizeNewton: on the device through
+ * iqgpu_newton_branch (on = 1, the default; engines it does not serve keep the
+ * host loop) or on the host, one iqgpu_likelihood_derv per step (on = 0). */
+int iqgpu_tree_set_device_newton(iqgpu_tree *t, int32_t on);
 
 /* ---- partitions: one graph launch over several engines ------------------- */
 /* Replaces the OpenMP loop of PhyloSuperTree::computeLikelihood

@@ -19,6 +19,7 @@ constexpr double kTwoPow256 = 1.157920892373161954235709850086879078532699846656
 constexpr int kTPB = 128;        // threads (= patterns) per CTA in the pattern-tile kernels
 constexpr int kMaxStates = 64;
 constexpr int kPairCounters = 8192;  // (op, tile) pairs of one category-split tensor-core level
+constexpr int kFlowWindowOps = 32;   // ops of one dataflow tensor-core launch (pair counters and maxima)
 constexpr int kMaxCat = 16;
 // params->numseq_safe_scaling default (utils/tools.cpp:1262): from this many
 // taxa on, the reference switches to SAFE scaling
@@ -158,6 +159,7 @@ struct iqgpu_engine {
     bool tc_ws;               // level schedule on the warp-specialised tensor-core kernel
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
     bool tc_split;            // category-split items on narrow levels for <= 32 padded states too (schedule 5)
+    bool tc_flow;             // dataflow schedule on the warp-specialised tensor-core kernel (schedule 6)
     bool has_multi;           // the uploaded op list holds multifurcating records (IQGPU_OP_MORE)
     int sms;                  // multiprocessors of the engine's device
     float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs
@@ -165,6 +167,7 @@ struct iqgpu_engine {
     float *d_cmax;            // category-split levels: per (op, category, pattern) maxima
     size_t cmax_bytes;
     unsigned *d_pair_cnt;     // category-split levels: arrivals per (op, tile) pair, re-armed to 0
+    long long pair_cap;       // counters in d_pair_cnt
     // caller-provided device memory (iqgpu_create_in): buffers are carved from it
     char *arena_base;
     size_t arena_size, arena_used;
@@ -194,6 +197,8 @@ int cuda_fail(cudaError_t e, const char *what);
 int launch_partial_info_f64(iqgpu_engine *e, int nops);
 int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_f64(iqgpu_engine *e, double len);
+int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, double xacc, int max_steps,
+                      double *out_dev);
 int launch_from_buffer_f64(iqgpu_engine *e, double len);
 
 // mixed-precision launchers (kernels_mixed.cu); op index nops holds the

@@ -27,7 +27,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 static long long round_up(long long v, long long g) { return (v + g - 1) / g * g; }
 
 struct Sizes {
-    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, flow, cmax, total, op_stride;
+    long long Ppad, part, scale, states, ops, opmats, theta, red, tcb, flow, cmax, pairs, total, op_stride;
 };
 
 static int check_config(const iqgpu_config *c) {
@@ -102,12 +102,15 @@ static Sizes sizes(const iqgpu_config *c) {
     }
     s.tcb = uses_tc(c) ? (long long)(c->max_ops + 1) * tcb_stride(c) * 4 : 0;
     // category-split tensor-core levels hold fewer than 4 pairs per resident CTA
-    // (<= 4 per SM): nl * Ppad < 16 * SMs * 128 patterns, SMs <= 160
-    s.cmax = uses_tc(c) ? 16LL * 160 * 128 * C * 4 + kPairCounters * 4 : 0;
+    // (<= 4 per SM): nl * Ppad < 16 * SMs * 128 patterns, SMs <= 160; the
+    // dataflow schedule runs windows of up to kFlowWindowOps ops
+    s.cmax = uses_tc(c) ? std::max(16LL * 160 * 128, (long long)kFlowWindowOps * s.Ppad) * C * 4 : 0;
+    s.pairs = uses_tc(c) ? std::max<long long>(kPairCounters, (long long)kFlowWindowOps * (s.Ppad / 128)) : 0;
     s.flow = is_mixed(c) ? (long long)(c->max_ops + 1) * (s.Ppad / 128) * 4 : 0;
     // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
     s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
     s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + s.cmax +
+              s.pairs * 4 +
               2 * s.Ppad * 8 +
               3 * kMaxStates * 8 +
               (n + 2 * n * n + 2 * C + (S + 1) * n) * 8 + 32 * 256;  // + alignment of ~30 buffers
@@ -323,8 +326,9 @@ static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_b
             CKE(dalloc(e, &e->d_tcb, s.tcb));
             CKE(dalloc(e, &e->d_cmax, s.cmax));
             e->cmax_bytes = (size_t)s.cmax;
-            CKE(dalloc(e, &e->d_pair_cnt, kPairCounters * 4));
-            CKE(cudaMemsetAsync(e->d_pair_cnt, 0, kPairCounters * 4, e->st));
+            CKE(dalloc(e, &e->d_pair_cnt, s.pairs * 4));
+            CKE(cudaMemsetAsync(e->d_pair_cnt, 0, s.pairs * 4, e->st));
+            e->pair_cap = s.pairs;
         }
     } else {
         CKE(dalloc(e, &e->d_part, s.part));
@@ -786,6 +790,14 @@ int stage_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch, i
 }
 }  // namespace iqg
 
+namespace iqg {
+// the engines iqgpu_newton_branch serves
+bool newton_on_device(const iqgpu_engine *e) {
+    return e && !is_mixed(&e->cfg) && !e->nonrev && e->asc_n == 0 &&
+           (long long)e->P * e->n * e->C <= IQGPU_NEWTON_MAX_ENTRIES;
+}
+}  // namespace iqg
+
 extern "C" {
 
 // Fold the last timed traversal into the running total.
@@ -823,7 +835,7 @@ static int check_status(iqgpu_engine *e) {
     CK(cudaStreamSynchronize(e->st));
     if (*h_status != 0) {
         CK(cudaMemsetAsync(e->d_status, 0, 4, e->st));
-        if (e->d_pair_cnt) CK(cudaMemsetAsync(e->d_pair_cnt, 0, kPairCounters * 4, e->st));  // partial arrivals
+        if (e->d_pair_cnt) CK(cudaMemsetAsync(e->d_pair_cnt, 0, (size_t)e->pair_cap * 4, e->st));  // partial arrivals
         set_error("a device-side wait gave up (TMA copy not completed); results of that launch are invalid");
         return IQGPU_ERR_TIMEOUT;
     }
@@ -1069,6 +1081,60 @@ int iqgpu_likelihood_derv(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, in
     return IQGPU_OK;
 }
 
+int iqgpu_newton_supported(iqgpu_engine *e, int32_t *supported) {
+    if (!e || !supported) { set_error("null argument"); return IQGPU_ERR_ARG; }
+    *supported = iqg::newton_on_device(e) ? 1 : 0;
+    return IQGPU_OK;
+}
+
+int iqgpu_newton_branch(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b,
+                        int32_t theta_computed, double x1, double xguess, double x2, double xacc,
+                        int32_t max_nr_step, double *optx, double *d2l, double *last_len, int32_t *steps) {
+    int rc = ready(e);
+    if (rc) return rc;
+    if (!optx) { set_error("null output"); return IQGPU_ERR_ARG; }
+    if (!iqg::newton_on_device(e)) {
+        set_error("device Newton-Raphson: reversible FP64 engines without +ASC and at most "
+                  "IQGPU_NEWTON_MAX_ENTRIES theta entries");
+        return IQGPU_ERR_ARG;
+    }
+    if (!std::isfinite(x1) || !std::isfinite(x2) || !std::isfinite(xguess) || !std::isfinite(xacc) || x1 < 0.0) {
+        set_error("bad Newton-Raphson bounds");
+        return IQGPU_ERR_ARG;
+    }
+    if (a < 0) std::swap(a, b);
+    if (a < 0 || check_ref(e, a) || check_ref(e, b) || a == b) {
+        set_error("bad branch");
+        return IQGPU_ERR_ARG;
+    }
+    CK(cudaSetDevice(e->dev));
+    if (!theta_computed || !e->theta_valid || e->theta_a != a || e->theta_b != b) {
+        if (theta_computed && (!e->theta_valid || e->theta_a != a || e->theta_b != b)) {
+            set_error("theta_computed set but the buffer holds another branch");
+            return IQGPU_ERR_STATE;
+        }
+        if ((rc = upload_ops(e, ops, nops))) return rc;
+        const double len0 = xguess < x1 ? x1 : (xguess > x2 ? x2 : xguess);
+        if ((rc = traverse(e, nops, EPI_THETA, a, b, len0))) return rc;
+        e->theta_valid = true;
+        e->theta_a = a;
+        e->theta_b = b;
+    }
+    if ((rc = launch_newton_f64(e, x1, xguess, x2, xacc, max_nr_step, e->d_red_out))) return rc;
+    if ((rc = fetch_result(e))) return rc;
+    const double *r = e->h_red_out;  // {optx, status + 16 * steps, d2l, last length}
+    const int status = (int)r[1] & 15;
+    if (steps) *steps = (int32_t)(r[1] / 16.0);
+    if (d2l) *d2l = r[2];
+    if (last_len) *last_len = r[3];
+    switch (status) {
+    case 0: *optx = r[0]; return IQGPU_OK;
+    case 1: set_error("Numerical underflow (lh-derivative); the SAFE kernel avoids this"); return IQGPU_ERR_NONFINITE;
+    case 2: set_error("Wrong computeFuncDerv"); return IQGPU_ERR_NEWTON;
+    default: set_error("Maximum number of iterations exceeded in minimizeNewton"); return IQGPU_ERR_NEWTON;
+    }
+}
+
 int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
     int rc = ready(e);
     if (rc) return rc;
@@ -1235,12 +1301,13 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
 }
 
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
-    if (!e || schedule < 0 || schedule > 5) { set_error("schedule must be 0 .. 5"); return IQGPU_ERR_ARG; }
+    if (!e || schedule < 0 || schedule > 6) { set_error("schedule must be 0 .. 6"); return IQGPU_ERR_ARG; }
     e->level_sync = schedule == 1 || schedule >= 3;
     e->flow = schedule == 2;
-    e->tc_ws = schedule == 3 || schedule == 5;
+    e->tc_ws = schedule == 3 || schedule >= 5;
     e->tc_tm = schedule == 4;
-    e->tc_split = schedule == 5;
+    e->tc_split = schedule >= 5;
+    e->tc_flow = schedule == 6;
     return IQGPU_OK;
 }
 

@@ -690,6 +690,165 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
     grid_reduce(r, P.red);
 }
 
+// ---------------------------------------------------------------------------
+// Optimization::minimizeNewton (utils/optimization.cpp:422-499) over
+// computeFuncDerv (tree/phylotree.cpp:2529-2536) on the device, for pattern
+// counts a few SMs cover: one thread-block cluster of up to 8 CTAs. Every
+// step, each CTA sums the per-pattern derivative terms of k_derv_f64 over its
+// interleaved share of the resident theta buffer and reduces them in a fixed
+// order; a cluster barrier publishes the CTA sums (double-buffered by step
+// parity in shared memory), and every thread adds them from distributed
+// shared memory in rank order. All threads of all CTAs then hold the same f
+// and df and take the same safeguarded step, so a branch costs one launch and
+// one host wait instead of one of each per step. (GB300's FP64 rate is a few
+// FMAs per clock per SM, so one CTA alone would take ~10 us per step on 600
+// DNA patterns; eight take about a microsecond.)
+// out: {optx, status + 16 * steps, d2l, last evaluated length}; status 0 ok,
+// 1 non-finite NORM derivative, 2 the reference's "Wrong computeFuncDerv",
+// 3 too many iterations.
+// ---------------------------------------------------------------------------
+constexpr int kNewtonThreads = 512;
+constexpr int kNewtonMaxCluster = 8;
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ double2 ld_dsmem_f64x2(const double2 *local, unsigned rank) {
+    unsigned addr = (unsigned)__cvta_generic_to_shared(local), raddr;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(raddr) : "r"(addr), "r"(rank));
+    double2 v;
+    asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(raddr) : "memory");
+    return v;
+}
+
+__device__ void newton_derv(const BufParams &P, double len, double *v0, double *v1, double *v2, double *red,
+                            double2 *part, int step, unsigned rank, unsigned nrank, bool safe, double *f, double *df) {
+    const int n = P.n, C = P.ncat, B = n * C, tid = threadIdx.x;
+    __syncthreads();  // this CTA's readers of v0..v2 and red for the previous step are done
+    for (int t = tid; t < B; t += blockDim.x) {
+        const int c = t / n, i = t % n;
+        const double cof = P.eval[(c / P.cpc) * n + i] * P.rates[c];
+        const double val = exp(cof * len) * P.props[c];
+        const double val1 = cof * val;
+        v0[t] = val;
+        v1[t] = val1;
+        v2[t] = cof * val1;
+    }
+    __syncthreads();
+    double s1 = 0.0, s2 = 0.0;
+    const long long stride = (long long)nrank * blockDim.x;
+    for (long long p = (long long)rank * blockDim.x + tid; p < P.nptn; p += stride) {
+        const double *th = P.theta + p;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
+        int k = 0;
+        for (; k + 1 < B; k += 2) {
+            const double t0 = th[(long long)k * P.ldp], t1 = th[(long long)(k + 1) * P.ldp];
+            a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
+            b0 = fma(v0[k + 1], t1, b0); b1 = fma(v1[k + 1], t1, b1); b2 = fma(v2[k + 1], t1, b2);
+        }
+        if (k < B) {
+            const double t0 = th[(long long)k * P.ldp];
+            a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
+        }
+        if (P.tail_dup) {
+            const double t0 = th[(long long)(B - 1) * P.ldp];
+            a0 = fma(v0[B - 1], t0, a0); a1 = fma(v1[B - 1], t0, a1); a2 = fma(v2[B - 1], t0, a2);
+        }
+        const double lh = fabs(a0 + b0) + P.invar[p];
+        const double inv = 1.0 / lh;
+        const double df_frac = (a1 + b1) * inv, ddf_frac = (a2 + b2) * inv;
+        const double fq = P.freq[p];
+        const double tmp1 = df_frac * fq, tmp2 = ddf_frac * fq;
+        s1 += tmp1;
+        s2 += fma(-tmp1, df_frac, tmp2);
+    }
+    // fixed-order reduction: warps by shuffles, warp sums in order, CTA sums in rank order
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+    }
+    if ((tid & 31) == 0) {
+        red[2 * (tid >> 5)] = s1;
+        red[2 * (tid >> 5) + 1] = s2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t1 = 0.0, t2 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            t1 += red[2 * w];
+            t2 += red[2 * w + 1];
+        }
+        part[step & 1] = make_double2(t1, t2);
+    }
+    // publishes part[step & 1] of every CTA; part[(step + 1) & 1] is rewritten
+    // only after the next barrier, which every CTA reaches after reading this one
+    cluster_sync_all();
+    double t1 = 0.0, t2 = 0.0;
+    for (unsigned q = 0; q < nrank; q++) {
+        const double2 v = ld_dsmem_f64x2(part + (step & 1), q);
+        t1 += v.x;
+        t2 += v.y;
+    }
+    if (!isfinite(t1) && safe) t1 = t2 = 0.0;  // tree/phylokernelnew.h:2629-2632
+    *f = -t1;  // computeFuncDerv returns the negated sums
+    *df = -t2;
+}
+
+__global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParams P, double x1, double xguess,
+                                                                double x2, double xacc, int max_steps, int safe,
+                                                                double *out) {
+    __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
+    __shared__ double red[2 * (kNewtonThreads / 32)];
+    __shared__ double2 part[2];
+    unsigned rank, nrank;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(nrank));
+    double f, df, dx, temp, xh, xl, rts, rts_old, xlast;
+    int status = 0, steps = 0, step = 0;
+    rts = xguess;
+    if (rts < x1) rts = x1;
+    if (rts > x2) rts = x2;
+    xlast = rts;
+    newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df);
+    if (!isfinite(f)) status = safe ? 2 : 1;
+    else if (!isfinite(df)) status = 2;
+    else if (!(df >= 0.0 && fabs(f) < xacc)) {
+        if (f < 0.0) { xl = rts; xh = x2; } else { xh = rts; xl = x1; }
+        dx = fabs(xh - xl);
+        status = 3;
+        for (int j = 1; j <= max_steps; j++) {
+            steps = j;
+            rts_old = rts;
+            if ((df <= 0.0) || (((rts - xh) * df - f) * ((rts - xl) * df - f) >= 0.0)) {
+                dx = 0.5 * (xh - xl);
+                rts = xl + dx;
+                if (xl == rts) { status = 0; break; }
+            } else {
+                dx = f / df;
+                temp = rts;
+                rts -= dx;
+                if (temp == rts) { status = 0; break; }
+            }
+            if (fabs(dx) < xacc || (j == max_steps)) { rts = rts_old; status = 0; break; }
+            xlast = rts;
+            newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df);
+            if (!isfinite(f)) { status = safe ? 2 : 1; break; }
+            if (!isfinite(df)) { status = 2; break; }
+            if (df > 0.0 && fabs(f) < xacc) { status = 0; break; }
+            if (f < 0.0) xl = rts;
+            else if (f > 0.0) xh = rts;
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        out[0] = rts;
+        out[1] = (double)(status + 16 * steps);
+        out[2] = df;  // d2l: minimizeNewton leaves it at the latest df
+        out[3] = xlast;
+    }
+    cluster_sync_all();  // no CTA leaves while another may still read its shared memory
+}
+
 // (tree/phylokernelnew.h:3232-3428)
 __global__ void __launch_bounds__(kTPB) k_from_buffer_f64(const BufParams P) {
     __shared__ double v0[kMaxCat * kMaxStates];
@@ -852,6 +1011,30 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
     P.asc_first = (int)(e->P - e->asc_n);
     P.asc_out = e->d_asc_holder ? e->d_asc_holder : e->d_asc;
     return P;
+}
+
+int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, double xacc, int max_steps,
+                      double *out_dev) {
+    // one cluster, one CTA per 256 patterns up to 8 (the portable cluster size)
+    const int q = (int)std::min<long long>(kNewtonMaxCluster, std::max<long long>(1, (e->P + 255) / 256));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)q);
+    cfg.blockDim = dim3(kNewtonThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = e->st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)q;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const BufParams P = buf_params(e, 0.0);
+    const int safe = e->cfg.safe ? 1 : 0;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, k_newton_f64, P, x1, xguess, x2, xacc, max_steps, safe, out_dev);
+    e->launches++;
+    if (err != cudaSuccess) return cuda_fail(err, "newton_f64");
+    return cuda_fail(cudaGetLastError(), "newton_f64");
 }
 
 int launch_derv_f64(iqgpu_engine *e, double len) {

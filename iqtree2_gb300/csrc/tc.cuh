@@ -201,6 +201,14 @@ __device__ __forceinline__ void st_release_cta(unsigned *p, unsigned v) {
     asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v)
                  : "memory");
 }
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// generic-proxy writes acquired from other CTAs, ordered before this thread's
+// later TMA (async-proxy) reads of global memory
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 __device__ __forceinline__ unsigned ld_acquire_cta(const unsigned *p) {
     unsigned v;
     asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];"

@@ -81,6 +81,7 @@ struct TcItem {
     int k, tile, dad, lref, rref, lch;  // lch: original child index of the left side (after the tip-left swap)
     int cat;                            // the item's one rate category (category-split items), else -1
     bool lint, rint;
+    int prod0, prod1;                   // dataflow: uploaded-list index of the op writing each child, or -1
 };
 
 constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged in shared memory
@@ -91,11 +92,20 @@ constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged i
 // Category-split (csplit): (tile, op, category) triples, the categories of a
 // pair on adjacent CTAs; the last of them to finish applies the rescale.
 __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc,
-                                          bool csplit = false) {
+                                          bool csplit = false, int flow_id = -1) {
     const MixParams &P = T.M;
     TcItem it;
     it.cat = -1;
-    if (fused) {
+    it.prod0 = it.prod1 = -1;
+    if (flow_id >= 0) {  // dataflow ticket: (op, tile, category) in level order
+        it.cat = flow_id % P.ncat;
+        const int i = flow_id / P.ncat;
+        it.tile = i % T.ntiles;
+        it.k = op0 + i / T.ntiles;
+        const OpDev &od = P.ops[it.k];
+        it.prod0 = od.prod0;
+        it.prod1 = od.prod1;
+    } else if (fused) {
         it.k = j;
         it.tile = blockIdx.x;
     } else {
@@ -456,10 +466,26 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 // category's per-pattern maximum in cmax[(op - op0) * ncat + c][pattern]; the
 // item that completes a (tile, op) pair applies the rescale and writes the
 // exponents.
-template <int NP, int NSTAGE, bool BF, bool CSPLIT>
+//
+// FLOW (dataflow schedule, category-split items): one launch for the ops
+// [op0, op0 + nl) of several levels. The issuer takes (op, tile, category)
+// items from a global ticket in level order and passes their ids to the
+// workers through a shared-memory FIFO; it issues an item's copies once the
+// (op, tile) pairs writing its internal children have raised their flags in
+// flow_done (polled without blocking, so the MMAs of earlier items keep
+// going), and the workers acquire the same flags before reading the
+// children's exponents. The item that completes a pair raises the pair's
+// flag after its rescale. Tickets go only to running CTAs in increasing
+// order and every producer has a smaller ticket, so every wait ends whatever
+// the residency; the waits are bounded all the same.
+constexpr int kFlowFifo = 8;  // item ids between the issuer and the workers
+
+template <int NP, int NSTAGE, bool BF, bool CSPLIT, bool FLOW = false>
 __global__ void __launch_bounds__(kTcRows + 32, 4)
     k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl,
-                     float *__restrict__ cmax_out, unsigned *__restrict__ pair_cnt) {
+                     float *__restrict__ cmax_out, unsigned *__restrict__ pair_cnt,
+                     unsigned *__restrict__ flow_done, unsigned *__restrict__ ticket, const unsigned epoch) {
+    static_assert(!FLOW || CSPLIT, "the dataflow schedule runs category-split items");
     constexpr bool csplit = CSPLIT;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
@@ -481,6 +507,9 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     __shared__ unsigned tmem_base_s, epi_done, abort_flag;
     __shared__ bool s_last;
     __shared__ int4 opc[kTcOpCache];
+    __shared__ int fifo_id[kFlowFifo];
+    __shared__ unsigned fifo_seq[kFlowFifo], fifo_taken;
+    const int flow_first = op0 + P.op_base;  // producers below it finished before this launch
     unsigned char *const tc_smem = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
     auto slot_at = [&](int s) { return tc_smem + s * T.slot_bytes; };
 
@@ -504,6 +533,8 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
         mbar_init(&ebar[1], 1);
         epi_done = 0;
         abort_flag = 0;
+        for (int i = 0; i < kFlowFifo; i++) fifo_seq[i] = 0;
+        fifo_taken = 0;
         fence_mbar_init();
     }
     if (warp == 0) {
@@ -516,7 +547,137 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     tc_fence_after();
     const unsigned tmem = tmem_base_s;
 
-    if (!worker) {
+    // producers' flags of an item, polled once each (issuer) or waited for (workers)
+    auto flow_ready = [&](const TcItem &it) -> bool {
+        const int pr[2] = {it.prod0, it.prod1};
+        for (int q = 0; q < 2; q++)
+            if (pr[q] >= flow_first && ld_acquire_gpu(flow_done + (long long)pr[q] * T.ntiles + it.tile) != epoch)
+                return false;
+        return true;
+    };
+    auto flow_wait = [&](const TcItem &it) -> bool {
+        const int pr[2] = {it.prod0, it.prod1};
+        for (int q = 0; q < 2; q++) {
+            if (pr[q] < flow_first) continue;
+            const unsigned *f = flow_done + (long long)pr[q] * T.ntiles + it.tile;
+            unsigned polls = 0;
+            while (ld_acquire_gpu(f) != epoch)
+                if (++polls >= P.wait_polls || *(volatile unsigned *)&abort_flag || *(volatile int *)P.status != 0)
+                    return false;
+        }
+        return true;
+    };
+    if (!worker && FLOW) {
+        // ---------------- issuer, dataflow ----------------
+        if ((tid & 31) == 0) {
+            TcItem fit[kFlowFifo];
+            bool fready[kFlowFifo];
+            int nf = 0;  // items taken
+            bool exhausted = false;
+            int ti = 0, ts = 0, issued = 0;  // copy cursor
+            int mi = 0, ms = 0, mdone = 0;   // MMA cursor
+            unsigned idle = 0;
+            auto push = [&](int id) {
+                fifo_id[nf % kFlowFifo] = id;
+                st_release_cta(&fifo_seq[nf % kFlowFifo], (unsigned)(nf + 1));
+            };
+            for (;;) {
+                bool progress = false;
+                // copies: as far ahead as the ring allows, in item order, each item once its producers are done
+                while (issued < mdone + NSTAGE) {
+                    const int s = issued % NSTAGE;
+                    if (issued >= NSTAGE && !mbar_test(&mmab[s], (unsigned)((issued / NSTAGE - 1) & 1))) break;
+                    if (ti == nf) {  // take the next ticket once the workers have read the FIFO entry it reuses
+                        // (and never over an item the MMA cursor has not passed)
+                        if (exhausted || nf - mi >= kFlowFifo || nf - (int)ld_acquire_cta(&fifo_taken) >= kFlowFifo)
+                            break;
+                        const int id = (int)atomicAdd(ticket, 1u);
+                        if (id >= total) {
+                            exhausted = true;
+                            push(-1);
+                            break;
+                        }
+                        fit[nf % kFlowFifo] = tc_item(T, 0, false, op0, opc, true, id);
+                        fready[nf % kFlowFifo] = false;
+                        push(id);
+                        nf++;
+                        progress = true;
+                    }
+                    const TcItem &tit = fit[ti % kFlowFifo];
+                    const int nst = tc_nstages(tit, C, ksplit);
+                    if (nst == 0) {  // tip-tip item: the workers alone
+                        ti++;
+                        ts = 0;
+                        continue;
+                    }
+                    if (!fready[ti % kFlowFifo]) {
+                        if (!flow_ready(tit)) break;
+                        fence_proxy_async_global();
+                        fready[ti % kFlowFifo] = true;
+                    }
+                    int c, side, kh;
+                    tc_stage(tit, ts, ksplit, c, side, kh);
+                    const int child = side == 0 ? tit.lref : tit.rref;
+                    unsigned char *slot = slot_at(s);
+                    mbar_expect_tx(&full[s], stage_tx);
+                    tma_load_3d(slot, &tmA, 0, c * kq + kh * kqs, child * T.groups_per_slot + tit.tile * 16,
+                                &full[s]);
+                    const int ch = side == 0 ? tit.lch : 1 - tit.lch;
+                    const float *bsrc = T.tcb + (long long)tit.k * T.tcb_stride +
+                                        (long long)((ch * C + c) * ksplit + kh) * T.b_stage;
+                    tma_load_1d(slot + T.b_off, bsrc, (unsigned)T.b_total, &full[s]);
+                    issued++;
+                    if (++ts >= nst) {
+                        ti++;
+                        ts = 0;
+                    }
+                    progress = true;
+                }
+                // MMAs of the next converted stage, once its accumulator buffer is free
+                while (mi < ti && tc_nstages(fit[mi % kFlowFifo], C, ksplit) == 0) {
+                    mi++;
+                    ms = 0;
+                }
+                if (mdone < issued) {
+                    const TcItem &mit = fit[mi % kFlowFifo];
+                    const int s = mdone % NSTAGE;
+                    int c, side, kh;
+                    tc_stage(mit, ms, ksplit, c, side, kh);
+                    const int per = (int)mit.lint + (int)mit.rint;
+                    const int g = mi;
+                    const bool first = ms == 0, last = ms == per * ksplit - 1;
+                    if (mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
+                        (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
+                        tc_fence_after();
+                        const unsigned d = tmem + (unsigned)((g & 1) * 2 * NP + side * NP);
+                        tc_stage_mmas<NP, BF>(T, d, slot_at(s), kh);
+                        mma_commit(&mmab[s]);
+                        if (last) mma_commit(&ebar[g & 1]);
+                        mdone++;
+                        if (++ms >= per * ksplit) {
+                            mi++;
+                            ms = 0;
+                        }
+                        progress = true;
+                    }
+                }
+                if (exhausted && ti >= nf && mdone == issued) break;
+                if (progress) {
+                    idle = 0;
+                } else if (__nanosleep(64), ++idle >= kWaitPolls / 16 || *(volatile unsigned *)&abort_flag) {
+                    if (idle >= kWaitPolls / 16) {
+                        atomicExch(&abort_flag, 1u);
+                        atomicExch(P.status, kStatusTimeout);
+                    }
+                    break;
+                }
+            }
+            for (int i = mdone; i < issued; i++) mbar_wait(&full[i % NSTAGE], (unsigned)((i / NSTAGE) & 1), kWaitPolls);
+            if (mdone > 0)
+                mbar_wait(&mmab[(mdone - 1) % NSTAGE], (unsigned)(((mdone - 1) / NSTAGE) & 1), kWaitPolls);
+        }
+        __syncwarp();
+    } else if (!worker) {
         // ---------------- issuer ----------------
         if ((tid & 31) == 0 && nitems > 0) {
             int ti = 0, ts = 0, issued = 0;  // copy cursor: item, stage within item, stages issued
@@ -639,13 +800,44 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
             if (r == 0) st_release_cta(&epi_done, (unsigned)(g + 1));
             return true;
         };
-        for (int j = 0; j < nitems && !abort; j++) {
-            const TcItem it = tc_item(T, j, false, op0, opc, csplit);
+        for (int j = 0; (FLOW || j < nitems) && !abort; j++) {
+            TcItem it;
+            if constexpr (FLOW) {
+                // the next item id from the issuer, then the producers' flags
+                const int e = j % kFlowFifo;
+                unsigned polls = 0;
+                bool ok = true;
+                while (ld_acquire_cta(&fifo_seq[e]) != (unsigned)(j + 1))
+                    if (*(volatile unsigned *)&abort_flag || ++polls >= kWaitPolls) {
+                        ok = false;
+                        break;
+                    }
+                const int id = ok ? fifo_id[e] : -1;
+                if (bar_or_part(kTcRows, !ok)) {
+                    abort = true;
+                    break;
+                }
+                if (id < 0) break;
+                it = tc_item(T, 0, false, op0, opc, true, id);
+                const bool dep_ok = r != 0 || flow_wait(it);
+                if (bar_or_part(kTcRows, !dep_ok)) {  // also: every worker has read the FIFO entry
+                    abort = true;
+                    break;
+                }
+                if (r == 0) st_release_cta(&fifo_taken, (unsigned)(j + 1));
+            } else {
+                it = tc_item(T, j, false, op0, opc, csplit);
+            }
             const long long p = (long long)it.tile * kTcRows + r;
             const int sl = it.lint ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
             const int sr = it.rint ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
-            const int e_in = (it.lint ? P.expo[(long long)it.lref * ld + p] : 0) +
-                             (it.rint ? P.expo[(long long)it.rref * ld + p] : 0);
+            // (dataflow: written in this launch by other CTAs, read through L2)
+            const int e_in = (it.lint ? (FLOW ? __ldcg(P.expo + (long long)it.lref * ld + p)
+                                              : P.expo[(long long)it.lref * ld + p])
+                                      : 0) +
+                             (it.rint ? (FLOW ? __ldcg(P.expo + (long long)it.rref * ld + p)
+                                              : P.expo[(long long)it.rref * ld + p])
+                                      : 0);
             const int per = (int)it.lint + (int)it.rint;
             const float *TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
             float *dad = P.part + (long long)it.dad * P.slot_floats;
@@ -719,6 +911,11 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     }
                     P.expo[(long long)it.dad * ld + p] = e_in - sh;
                     if (r == 0) pair_cnt[pair] = 0u;  // re-armed for the next level and evaluation
+                    if constexpr (FLOW) {  // the pair is complete: raise its flag
+                        __threadfence();
+                        bar_sync_part(kTcRows);
+                        if (r == 0) atomicExch(flow_done + (long long)(it.k + P.op_base) * T.ntiles + it.tile, epoch);
+                    }
                 }
                 continue;
             }
@@ -1230,6 +1427,7 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF, false>;
     auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, true>;
+    auto kern_flow = k_traverse_tc_ws<NP, NSTAGE, BF, true, true>;
     const bool split_ok = NP == 64 || e->tc_split;  // 61 states always; fewer states with schedule 5
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
@@ -1244,6 +1442,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
                  : cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err == cudaSuccess && ws && split_ok)
         err = cudaFuncSetAttribute(kern_ws_cs, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err == cudaSuccess && ws && split_ok && e->tc_flow)
+        err = cudaFuncSetAttribute(kern_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess && ws && split_ok && e->tc_flow)
+        err = cudaFuncSetAttribute(kern_flow, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
     // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
@@ -1276,6 +1478,43 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     // (61 states only: a 20-state item is 8 short stages and the narrow levels
     // run faster on the CUDA-core tail than split plus the fix-up launch)
     const bool can_split = ws && split_ok && e->d_cmax != nullptr;
+    if (can_split && e->tc_flow && e->d_flow_done) {
+        // Dataflow: leading levels of tip-tip ops as store streams, then every
+        // other op in one launch of category-split items (no CUDA-core tail)
+        int l = 0;
+        for (; l < e->nlevels; l++) {
+            const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+            if (nl > 0 && !level_all_tiptip(e, op0, nl)) break;
+        }
+        const int op_first = l < e->nlevels ? e->level_off[l] : M.nops;
+        const int nflow = M.nops - op_first;
+        const long long ntiles = T.ntiles;
+        // ops per launch: as many as the pair counters and the maxima hold
+        const long long window = std::min<long long>(e->pair_cap / ntiles,
+                                                     (long long)(e->cmax_bytes / ((size_t)e->C * e->Ppad * 4)));
+        if (window >= 1) {
+            for (int q = 0; q < l; q++) {
+                const int op0 = e->level_off[q], nl = e->level_off[q + 1] - op0;
+                if (nl > 0 && (rc = launch_tiptip_level(e, M, op0, nl))) return rc;
+            }
+            *rest = M.nops;
+            if (nflow <= 0) return IQGPU_OK;
+            err = cudaMemsetAsync(e->d_flow_done, 0, (size_t)(M.op_base + M.nops) * ntiles * 4, e->st);
+            if (err != cudaSuccess) return cuda_fail(err, "flow flag reset");
+            for (int w0 = op_first; w0 < M.nops; w0 += (int)window) {
+                const int nw = (int)std::min<long long>(window, M.nops - w0);
+                if ((err = cudaMemsetAsync(e->d_flow_ticket, 0, 4, e->st)) != cudaSuccess)
+                    return cuda_fail(err, "flow ticket reset");
+                const long long items = (long long)nw * ntiles * e->C;
+                const int grid = (int)std::min<long long>(items, resident);
+                kern_flow<<<grid, nthr, smem, e->st>>>(tm, T, w0, nw, e->d_cmax, e->d_pair_cnt, e->d_flow_done,
+                                                       e->d_flow_ticket, 1u);
+                e->launches++;
+                if ((err = cudaGetLastError()) != cudaSuccess) return cuda_fail(err, "traverse_tc flow");
+            }
+            return IQGPU_OK;
+        }
+    }
     int lt = e->nlevels;
     if (NP == 32)
         for (int l = 0; l < e->nlevels; l++)
@@ -1301,13 +1540,13 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
             continue;
         }
         const long long items = (long long)T.ntiles * nl;
-        const bool cs = can_split && items < 4 * resident && items <= kPairCounters &&
+        const bool cs = can_split && items < 4 * resident && items <= e->pair_cap &&
                         (size_t)nl * e->C * (size_t)e->Ppad * sizeof(float) <= e->cmax_bytes;
         const int grid = (int)std::min<long long>(items * (cs ? e->C : 1), resident);
         if (ws && cs)
-            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt);
+            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt, nullptr, nullptr, 1u);
         else if (ws)
-            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt);
+            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt, nullptr, nullptr, 1u);
         else
             kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
         e->launches++;

@@ -26,6 +26,7 @@
 
 namespace iqg {
 void set_error(const std::string &msg);
+bool newton_on_device(const iqgpu_engine *e);
 }
 
 // largest node degree (a multifurcating node of degree d has d - 1 children)
@@ -45,6 +46,7 @@ struct iqgpu_tree {
     double min_bl = 1e-6, max_bl = 10.0;
     int cur1 = -1, cur2 = -1;  // current_it: cur1 -> cur2
     bool theta_computed = false;
+    bool device_newton = true;  // minimizeNewton through iqgpu_newton_branch where the engine serves it
     int last_rc = IQGPU_OK;
 
     // HBM slots. A tree may have more directed internal partials than its
@@ -295,6 +297,28 @@ int minimize_newton(iqgpu_tree *t, double x1, double xguess, double x2, double x
     return IQGPU_ERR_NEWTON;
 }
 
+// minimizeNewton as one device kernel (iqgpu_newton_branch): the same
+// control flow, with one host wait per branch instead of one per step
+int minimize_newton_device(iqgpu_tree *t, double x1, double xguess, double x2, double xacc, int max_nr_step,
+                           double *out) {
+    int node = t->cur2, dad = t->cur1;
+    if (t->leaf(node)) std::swap(node, dad);
+    int a, b;
+    double last = xguess;
+    int rc = t->collect(node, dad, &a, &b);
+    if (!rc)
+        rc = iqgpu_newton_branch(t->e, t->ops.data(), (int32_t)t->ops.size(), a, b, t->theta_computed ? 1 : 0, x1,
+                                 xguess, x2, xacc, max_nr_step, out, nullptr, &last, nullptr);
+    t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+    t->settled(rc);
+    t->unpin(a);
+    t->unpin(b);
+    if (rc) return rc;
+    t->theta_computed = true;
+    t->blen(t->cur1, t->cur2) = last;  // the branch holds the last evaluated length, as after computeFuncDerv
+    return IQGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -408,11 +432,14 @@ int iqgpu_tree_optimize_one_branch(iqgpu_tree *t, int32_t node1, int32_t node2, 
     const double current_len = t->blen(node1, node2);
     t->theta_computed = false;
     double optx = current_len;
-    int rc = minimize_newton(t, t->min_bl, current_len, t->max_bl, t->min_bl, max_nr_step, &optx);
+    int rc = t->device_newton && iqg::newton_on_device(t->e)
+                 ? minimize_newton_device(t, t->min_bl, current_len, t->max_bl, t->min_bl, max_nr_step, &optx)
+                 : minimize_newton(t, t->min_bl, current_len, t->max_bl, t->min_bl, max_nr_step, &optx);
     if (rc) return rc;
     if (optx > t->max_bl * 0.95) {
+        // at the length of the last derivative evaluation, as the reference
+        // (current_it->length, tree/phylotree.cpp:2619-2621)
         double opt_lh, orig_lh;
-        t->blen(node1, node2) = optx;
         if ((rc = from_buffer(t, &opt_lh))) return rc;
         t->blen(node1, node2) = current_len;
         if ((rc = from_buffer(t, &orig_lh))) return rc;
@@ -479,6 +506,12 @@ int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl) {
     if (!t || !(min_bl > 0.0) || !(max_bl > min_bl)) { iqg::set_error("bad bounds"); return IQGPU_ERR_ARG; }
     t->min_bl = min_bl;
     t->max_bl = max_bl;
+    return IQGPU_OK;
+}
+
+int iqgpu_tree_set_device_newton(iqgpu_tree *t, int32_t on) {
+    if (!t) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
+    t->device_newton = on != 0;
     return IQGPU_OK;
 }
 

@@ -95,6 +95,9 @@ def lib():
         "iqgpu_likelihood_derv": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_int32, _DP, _DP],
                                   ct.c_int),
         "iqgpu_lnl_from_buffer": ([vp, ct.c_double, _DP], ct.c_int),
+        "iqgpu_newton_supported": ([vp, _I32P], ct.c_int),
+        "iqgpu_newton_branch": ([vp, vp, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double,
+                                 ct.c_double, ct.c_double, ct.c_int32, _DP, _DP, _DP, _I32P], ct.c_int),
         "iqgpu_get_pattern_lh": ([vp, _DP], ct.c_int),
         "iqgpu_get_partial": ([vp, ct.c_int32, _DP, _U8P], ct.c_int),
         "iqgpu_get_exponent": ([vp, ct.c_int32, _I32P], ct.c_int),
@@ -133,6 +136,7 @@ def lib():
         "iqgpu_tree_set_lengths": ([vp, _DP], ct.c_int),
         "iqgpu_tree_set_bounds": ([vp, ct.c_double, ct.c_double], ct.c_int),
         "iqgpu_tree_num_updates": ([vp, ct.POINTER(ct.c_int64)], ct.c_int),
+        "iqgpu_tree_set_device_newton": ([vp, ct.c_int32], ct.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -286,6 +290,23 @@ class Engine:
         _check(lib().iqgpu_likelihood_derv(self.h, arr.ctypes.data, len(arr), a, b, length,
                                            int(theta_computed), ct.byref(df), ct.byref(ddf)))
         return df.value, ddf.value
+
+    def newton_supported(self):
+        out = ct.c_int32()
+        _check(lib().iqgpu_newton_supported(self.h, ct.byref(out)))
+        return bool(out.value)
+
+    def newton_branch(self, ops, a, b, x1, xguess, x2, xacc, max_nr_step=100, theta_computed=False, full=False):
+        """minimizeNewton of one branch on the device: (optx, iterations);
+        with full=True also its d2l output and the last evaluated length."""
+        arr = ops if isinstance(ops, np.ndarray) else self.ops_array(ops)
+        out, d2l, last, steps = ct.c_double(), ct.c_double(), ct.c_double(), ct.c_int32()
+        _check(lib().iqgpu_newton_branch(self.h, arr.ctypes.data, len(arr), a, b, int(theta_computed), x1, xguess,
+                                         x2, xacc, max_nr_step, ct.byref(out), ct.byref(d2l), ct.byref(last),
+                                         ct.byref(steps)))
+        if full:
+            return out.value, steps.value, d2l.value, last.value
+        return out.value, steps.value
 
     def lnl_from_buffer(self, length):
         out = ct.c_double()
@@ -488,6 +509,9 @@ class GpuTree:
 
     def set_bounds(self, min_bl, max_bl):
         _check(lib().iqgpu_tree_set_bounds(self.h, min_bl, max_bl))
+
+    def set_device_newton(self, on):
+        _check(lib().iqgpu_tree_set_device_newton(self.h, int(bool(on))))
 
     def num_updates(self):
         out = ct.c_int64()

@@ -293,6 +293,39 @@ void PhyloTree::computeLikelihoodDervGB300(PhyloNeighbor *dad_branch, PhyloNode 
     theta_computed = true;
 }
 
+/* Optimization::minimizeNewton (utils/optimization.cpp:422-499) over
+   computeFuncDerv (tree/phylotree.cpp:2529-2536) for the current branch of
+   optimizeOneBranch (:2611), as one device kernel: the traversal and every
+   Newton or bisection step run on the GPU with one host wait. Leaves the
+   branch at the last evaluated length, as computeFuncDerv does. False when
+   the engine keeps the host loop (mixed precision, non-reversible, +ASC,
+   theta buffers above IQGPU_NEWTON_MAX_ENTRIES, super trees, mixlen). */
+bool PhyloTree::minimizeNewtonGB300(double x1, double xguess, double x2, double xacc, double &d2l, int maxNRStep,
+                                    double &optx) {
+    int32_t supported = 0;
+    if (!gpu_engine || isSuperTree() || getMixlen() > 1) return false;
+    gpuCheck(iqgpu_newton_supported(gpu_engine, &supported), "Newton-Raphson");
+    if (!supported) return false;
+    syncInputsGB300();
+    PhyloNeighbor *dad_branch = current_it, *node_branch = current_it_back;
+    PhyloNode *dad = (PhyloNode *)current_it_back->node, *node = (PhyloNode *)current_it->node;
+    if (node->isLeaf()) {
+        std::swap(node, dad);
+        std::swap(dad_branch, node_branch);
+    }
+    vector<iqgpu_op> ops;
+    if (!theta_computed) traversalOpsGB300(dad_branch, dad, ops);
+    double last = xguess;
+    gpuCheck(iqgpu_newton_branch(gpu_engine, ops.data(), (int32_t)ops.size(), gpuRef(dad_branch),
+                                 gpuRef(node_branch), theta_computed ? 1 : 0, x1, xguess, x2, xacc, maxNRStep, &optx,
+                                 &d2l, &last, nullptr),
+             "Newton-Raphson");
+    theta_computed = true;
+    current_it->length = last;
+    current_it_back->length = last;
+    return true;
+}
+
 double PhyloTree::computeLikelihoodFromBufferGB300() {
     double lnl = 0.0;
     gpuCheck(iqgpu_lnl_from_buffer(gpu_engine, current_it->length, &lnl), "lnL from buffer");

@@ -1080,7 +1080,8 @@ int orc_tree_optimize_one_branch(orc_tree *t, int node1, int node2, int max_nr_s
     double optx = minimize_newton(t, t->min_bl, current_len, t->max_bl, t->min_bl, max_nr_step, &status);
     if (status) return -1;
     if (optx > t->max_bl * 0.95) {
-        t->lengths[e] = optx;
+        /* at the length of the last derivative evaluation, as the reference
+           (current_it->length, tree/phylotree.cpp:2619-2621) */
         double opt_lh = lnl_from_buffer(t);
         t->lengths[e] = current_len;
         double orig_lh = lnl_from_buffer(t);

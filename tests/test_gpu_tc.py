@@ -98,9 +98,11 @@ def test_tc_schedules_agree_and_match_cuda_cores(oracle_mod, kind):
     internal-internal ops. Codon (no CUDA-core tail: every level of every
     schedule on the tensor cores, the warp-specialised kernel with
     category-split items): all schedules and ring depths bit-identical.
-    Protein: schedules differ in which narrow levels go to the CUDA-core tail,
-    so they agree within 1e-7. The CUDA-core FP32 kernel within the mixed
-    tolerance."""
+    Protein: schedules differ in which narrow levels go to the CUDA-core tail
+    (FP32) rather than the split-TF32 tensor cores (the dataflow schedule puts
+    every level on the tensor cores; split TF32 is ~1.5e-7 from FP64 at
+    worst), so they agree within 3e-7. The CUDA-core FP32 kernel within the
+    mixed tolerance."""
     ds = (simulate.protein_lg_dataset(40, 1500, 31) if kind == "protein"
           else simulate.codon_gy94_dataset(16, 700, 32))
     topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
@@ -118,7 +120,7 @@ def test_tc_schedules_agree_and_match_cuda_cores(oracle_mod, kind):
     if kind == "codon":
         assert len(vals) == 1, got  # same per-op arithmetic in every schedule and ring depth
     else:
-        assert max(vals) - min(vals) <= 1e-7 * abs(min(vals)), got
+        assert max(vals) - min(vals) <= 3e-7 * abs(min(vals)), got
     cc = _engine(ds, topo, engine.F32)
     assert rel(cc.compute_likelihood(ops, a, b, length), vals.pop()) < LNL_RTOL
 
@@ -138,7 +140,7 @@ def test_tc_level_kernels_protein(oracle_mod):
     launch the tensor-core level kernels (single-issuer, warp-specialised and
     A-in-tensor-memory), with tip-internal and internal-internal items mixed
     in one launch and a ragged last tile. Every candidate within 1e-6 of the
-    FP64 oracle and within 1e-7 of the others (schedules may differ in which
+    FP64 oracle and within 3e-7 of the others (schedules may differ in which
     narrow levels go to the CUDA-core tail); the partials of levels 1-3, which
     every schedule computes on the tensor cores (operand A in shared or in
     tensor memory), bit-identical; the A-in-tensor-memory kernel
@@ -157,7 +159,7 @@ def test_tc_level_kernels_protein(oracle_mod):
     assert len(check) >= 20
     eng = _engine(ds, topo)
     got, launches, parts = {}, {}, {}
-    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0), (0, 5, 2, 1)]:
+    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0), (0, 5, 2, 1), (0, 6, 2, 1)]:
         autotune.apply(eng, cand)
         l0 = eng.launches()
         got[cand] = eng.compute_likelihood(ops, a, b, length)
@@ -171,10 +173,72 @@ def test_tc_level_kernels_protein(oracle_mod):
         for x, y in zip(pl, ref):
             np.testing.assert_array_equal(x, y, err_msg=str(cand))
     base = got[(0, 1, 2, 1)]
-    assert all(rel(v, base) < 1e-7 for v in got.values()), got
+    assert all(rel(v, base) < 3e-7 for v in got.values()), got
     autotune.apply(eng, (0, 4, 0, 0))
     again = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
     assert again == [got[(0, 4, 0, 0)]] * 3
+
+
+@pytest.mark.parametrize("kind", ["codon", "protein"])
+def test_tc_dataflow_schedule(oracle_mod, kind):
+    """Schedule 6 (one persistent launch of (tile, op, category) items, each
+    waiting for the items writing its children): partials, exponents and lnL
+    bit-identical to the level schedule of category-split items (same per-item
+    arithmetic), deterministic over repeated runs, and the lnL within 1e-6 of
+    the FP64 oracle; also on a partial traversal (the ops below one internal
+    branch after a length change, so some children come from earlier
+    traversals). Protein 100 x 20,000: more (op, tile) pairs than one launch's
+    counters hold, so the ops run in several windows."""
+    ds = (simulate.codon_gy94_dataset(40, 3000, 36) if kind == "codon"
+          else simulate.protein_lg_dataset(100, 20000, 35))
+    topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops_l = topo.branch_ops(nb, leaf)
+    ops = engine.Engine.ops_array(ops_l)
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    eng = _engine(ds, topo)
+    res = {}
+    for cand in [(0, 5, 2, 1), (0, 6, 2, 1), (0, 6, 3, 1)]:
+        autotune.apply(eng, cand)
+        l0 = eng.launches()
+        lnl = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
+        nl = (eng.launches() - l0) // 3
+        assert lnl == [lnl[0]] * 3, (cand, lnl)
+        res[cand] = (lnl[0], nl, [(eng.partial(op[0])[0], eng.exponent(op[0])) for op in ops_l[::7]])
+        assert rel(lnl[0], want) < LNL_RTOL, (cand, lnl[0], want)
+    print({c: (v[0], v[1]) for c, v in res.items()}, "oracle", want)
+    ref = res[(0, 5, 2, 1)]
+    if kind == "codon":  # every op on category-split items in both schedules
+        for cand in [(0, 6, 2, 1), (0, 6, 3, 1)]:
+            assert res[cand][0] == ref[0], cand
+            for (p1, e1), (p2, e2) in zip(res[cand][2], ref[2]):
+                np.testing.assert_array_equal(p1, p2)
+                np.testing.assert_array_equal(e1, e2)
+        assert res[(0, 6, 2, 1)][1] < ref[1]  # fewer launches than one per level
+    else:  # schedule 5 puts the narrowest levels on other kernels: agreement to rounding
+        assert abs(res[(0, 6, 2, 1)][0] - ref[0]) <= 1e-7 * abs(ref[0])
+    # the tree driver on schedule 6: after a length change only the stale
+    # partials are recomputed (children from earlier traversals, tip-tip ops
+    # inside the dataflow launch), then branch-length optimisation
+    t = engine.GpuTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=engine.TF32X3)
+    autotune.apply(t.engine, (0, 6, 2, 1))
+    o = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
+    lens = ds.lengths.copy()
+    internal = [i for i, (u, v) in enumerate(ds.edges) if min(u, v) >= ds.ntaxa]
+    for i in internal[::3]:
+        lens[i] *= 1.7
+    t.set_lengths(lens)
+    o.set_lengths(lens)
+    lg, lo = t.compute_likelihood(), o.compute_likelihood()
+    assert rel(lg, lo) < LNL_RTOL, (lg, lo)
+    if kind == "codon":
+        n1, n2 = (int(x) for x in ds.edges[internal[0]])
+        t.optimize_one_branch(n1, n2)
+        o.optimize_one_branch(n1, n2)
+        np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-4)
+        assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
 
 
 def test_tc_deep_tree_exponents(oracle_mod):
@@ -257,7 +321,14 @@ def test_bf16_schedules_agree(oracle_mod, kind):
     for cand in autotune.candidates(eng):
         autotune.apply(eng, cand)
         got[cand] = eng.compute_likelihood(ops, a, b, length)
-    assert len(set(got.values())) == 1, got
-    err = rel(next(iter(got.values())), want)
-    print(f"{kind}: bf16 lnL rel err {err:.2e}")
-    assert err < BF16_LNL_RTOL
+    # codon: every schedule runs every op on the tensor cores, bit-identical.
+    # protein: the dataflow schedule (6) also runs the narrow tail there (BF16
+    # operands) where the others use FP32 CUDA cores: identical within each group
+    groups = ([got] if kind == "codon" else
+              [{c: v for c, v in got.items() if c[1] == 6}, {c: v for c, v in got.items() if c[1] != 6}])
+    for grp in groups:
+        assert len(set(grp.values())) == 1, grp
+    for v in set(got.values()):
+        err = rel(v, want)
+        print(f"{kind}: bf16 lnL rel err {err:.2e}")
+        assert err < BF16_LNL_RTOL
