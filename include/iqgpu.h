@@ -123,7 +123,9 @@ typedef struct {
  * Children keep the neighbour order of the node (the order of the products).
  * Reversible models; the FP64 drop-in follows the reference's multifurcating
  * update (products of the children's eigen-space sums, the 2^-256 check after
- * every child, one U^-1 transform at the end). */
+ * every child, one U^-1 transform at the end); mixed-precision engines run
+ * such traversals on their fused CUDA-core kernel (a running product rescaled
+ * by powers of two after every record). */
 #define IQGPU_OP_MORE 16
 #define IQGPU_NO_CHILD ((int32_t)0x80000000)
 
@@ -202,7 +204,7 @@ int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl);
  * engines return IQGPU_ERR_ARG before doing anything, and callers iterate
  * iqgpu_likelihood_derv on the host as minimizeNewton does. The theta buffer
  * stays valid for iqgpu_lnl_from_buffer at any length afterwards. */
-#define IQGPU_NEWTON_MAX_ENTRIES (1 << 20)
+#define IQGPU_NEWTON_MAX_ENTRIES (1 << 18)
 /* *supported = 1 when iqgpu_newton_branch serves this engine, else 0. */
 int iqgpu_newton_supported(iqgpu_engine *e, int32_t *supported);
 int iqgpu_newton_branch(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int32_t a, int32_t b,
@@ -466,8 +468,8 @@ int iqgpu_derv_noalloc(const double *theta_dev, const double *buffer_scale_dev, 
 int iqgpu_tree_create(iqgpu_engine *e, const int32_t *edges, const double *lengths, iqgpu_tree **out);
 /* The same for a tree with multifurcating nodes (degree 3 to 32): nedge edges
  * (ntaxa .. 2*ntaxa-3), internal nodes ntaxa..nedge; the engine needs a slot
- * per directed internal partial. FP64 engines (multifurcating updates follow
- * the reference's, tree/phylokernelnew.h:1407-1631). */
+ * per directed internal partial (multifurcating updates follow the
+ * reference's, tree/phylokernelnew.h:1407-1631). */
 int iqgpu_tree_create_n(iqgpu_engine *e, int32_t nedge, const int32_t *edges, const double *lengths,
                         iqgpu_tree **out);
 int iqgpu_tree_destroy(iqgpu_tree *t);

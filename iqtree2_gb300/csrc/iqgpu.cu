@@ -694,8 +694,8 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
                       ": the records of a multifurcating node must share their dad slot");
             return IQGPU_ERR_ARG;
         }
-        if ((more || in_group) && (is_mixed(&e->cfg) || e->nonrev)) {
-            set_error("multifurcating nodes (IQGPU_OP_MORE) run on FP64 engines with reversible models");
+        if ((more || in_group) && e->nonrev) {
+            set_error("multifurcating nodes (IQGPU_OP_MORE) run with reversible models");
             return IQGPU_ERR_ARG;
         }
         const int dir = o.flags & ~IQGPU_OP_MORE;
@@ -723,12 +723,17 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
     if (is_mixed(&e->cfg) && nops > 0) {
         std::vector<int> producer_level(e->cfg.nslots, 0);  // level of the op writing each slot in this list
         int maxl = 0;
-        for (int k = 0; k < nops; k++) {
+        for (int k = 0, g0 = 0; k < nops; k++) {
             int l = 1;
             for (int j = 0; j < 2; j++)
                 if (ops[k].child[j] >= 0) l = std::max(l, producer_level[ops[k].child[j]] + 1);
             level[k] = l;
-            producer_level[ops[k].dad_slot] = l;
+            if (k > g0) l = std::max(l, level[k - 1]);  // the records of a multifurcating node share one level
+            for (int j = g0; j <= k; j++) level[j] = l;
+            if (!(ops[k].flags & IQGPU_OP_MORE)) {
+                producer_level[ops[k].dad_slot] = l;
+                g0 = k + 1;
+            }
             maxl = std::max(maxl, l);
         }
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return level[x] < level[y]; });

@@ -188,11 +188,11 @@ __device__ __forceinline__ void multi_record(const TravParams &P, const OpDev &o
                         acc[(long long)(c * NR + x) * ld] *= y;
                     }
                 } else {
-                    for (int i = 0; i < n; i++) stmp[i * kTPB + tid] = Cp[(long long)(c * n + i) * ld];
+                    for (int i = 0; i < n; i++) stmp[i * blockDim.x + tid] = Cp[(long long)(c * n + i) * ld];
                     for (int x = 0; x < n; x++) {
                         const double *e = E + (long long)(c * n + x) * n;
                         double y = __ldg(e) * stmp[tid];
-                        for (int i = 1; i < n; i++) y = fma(__ldg(e + i), stmp[i * kTPB + tid], y);
+                        for (int i = 1; i < n; i++) y = fma(__ldg(e + i), stmp[i * blockDim.x + tid], y);
                         acc[(long long)(c * n + x) * ld] *= y;
                     }
                 }
@@ -228,10 +228,10 @@ __device__ __forceinline__ void multi_record(const TravParams &P, const OpDev &o
 #pragma unroll
             for (int x = 0; x < NR; x++) acc[(long long)(c * NR + x) * ld] = dot_reg<NR>(U + x * NR, t);
         } else {
-            for (int j = 0; j < n; j++) stmp[j * kTPB + tid] = acc[(long long)(c * n + j) * ld];
+            for (int j = 0; j < n; j++) stmp[j * blockDim.x + tid] = acc[(long long)(c * n + j) * ld];
             for (int x = 0; x < n; x++) {
                 double a = 0.0;
-                for (int j = 0; j < n; j++) a = fma(__ldg(U + (long long)x * n + j), stmp[j * kTPB + tid], a);
+                for (int j = 0; j < n; j++) a = fma(__ldg(U + (long long)x * n + j), stmp[j * blockDim.x + tid], a);
                 acc[(long long)(c * n + x) * ld] = a;
             }
         }
@@ -249,11 +249,11 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
     const int n = NT ? NT : P.n;
     const int C = P.ncat, B = n * C, S = P.state_unknown;
     const int tid = threadIdx.x;
-    const long long p = (long long)blockIdx.x * kTPB + tid;
+    const long long p = (long long)blockIdx.x * blockDim.x + tid;
     const long long ld = P.ldp;
     extern __shared__ double smem[];
-    double *stmp = smem;                                     // !REG: [n][kTPB]
-    double *sval = smem + (REG ? 0 : (long long)kMaxStates * kTPB);  // EPI_LNL: [B]
+    double *stmp = smem;                                          // !REG: [n][blockDim.x]
+    double *sval = smem + (REG ? 0 : (long long)kMaxStates * blockDim.x);  // EPI_LNL: [B]
     const double invar = P.invar[p];
     const long long CNN = (long long)C * n * n;
     const long long SB = (long long)(S + 1) * B;
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
                         if (x0 + xx < n) {
                             const double yl = lint ? al[xx] : __ldg(tl + c * n + x0 + xx);
                             const double yr = rint ? ar[xx] : __ldg(tr + c * n + x0 + xx);
-                            stmp[(x0 + xx) * kTPB + tid] = yl * yr;
+                            stmp[(x0 + xx) * blockDim.x + tid] = yl * yr;
                         }
                     }
                 }
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
 #pragma unroll
                     for (int xx = 0; xx < XC; xx++) acc[xx] = 0.0;
                     for (int j = 0; j < n; j++) {
-                        const double t = stmp[j * kTPB + tid];
+                        const double t = stmp[j * blockDim.x + tid];
 #pragma unroll
                         for (int xx = 0; xx < XC; xx++)
                             if (x0 + xx < n)
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         return;
     } else {
         // branch lnL (tree/phylokernelnew.h:2641-3223)
-        for (int t = tid; t < B; t += kTPB) {
+        for (int t = tid; t < B; t += blockDim.x) {
             const int c = t / n, i = t % n;
             sval[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
         }
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(kTPB) k_branch_nonrev64(const TravParams P, co
                                                           const double *__restrict__ w) {
     const int n = P.n, C = P.ncat;
     const long long ld = P.ldp, CNN = (long long)C * n * n;
-    const long long p = (long long)blockIdx.x * kTPB + threadIdx.x;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
     if (p < P.nptn) {
         const double *pa = P.partials + (long long)P.a * P.slot_stride + p;
@@ -700,14 +700,14 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
 // parity in shared memory), and every thread adds them from distributed
 // shared memory in rank order. All threads of all CTAs then hold the same f
 // and df and take the same safeguarded step, so a branch costs one launch and
-// one host wait instead of one of each per step. (GB300's FP64 rate is a few
-// FMAs per clock per SM, so one CTA alone would take ~10 us per step on 600
-// DNA patterns; eight take about a microsecond.)
+// one host wait instead of one of each per step. (GB300 issues a few FP64
+// FMAs per clock per SM, so the CTAs take contiguous chunks of the patterns:
+// one CTA alone would take ~10 us per step on 600 DNA patterns.)
 // out: {optx, status + 16 * steps, d2l, last evaluated length}; status 0 ok,
 // 1 non-finite NORM derivative, 2 the reference's "Wrong computeFuncDerv",
 // 3 too many iterations.
 // ---------------------------------------------------------------------------
-constexpr int kNewtonThreads = 512;
+constexpr int kNewtonThreads = 256;
 constexpr int kNewtonMaxCluster = 8;
 
 __device__ __forceinline__ void cluster_sync_all() {
@@ -736,8 +736,10 @@ __device__ void newton_derv(const BufParams &P, double len, double *v0, double *
     }
     __syncthreads();
     double s1 = 0.0, s2 = 0.0;
-    const long long stride = (long long)nrank * blockDim.x;
-    for (long long p = (long long)rank * blockDim.x + tid; p < P.nptn; p += stride) {
+    // contiguous chunks of whole warps per CTA, so every CTA of the cluster has patterns
+    const long long chunk = (((long long)P.nptn + nrank - 1) / nrank + 31) / 32 * 32;
+    const long long p_end = min((long long)P.nptn, (long long)(rank + 1) * chunk);
+    for (long long p = rank * chunk + tid; p < p_end; p += blockDim.x) {
         const double *th = P.theta + p;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
         int k = 0;
@@ -936,18 +938,26 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops) {
     return cuda_fail(cudaGetLastError(), "partial_info_f64");
 }
 
+// Patterns per CTA of the FP64 pattern-tile kernels: 128, or one warp's 32
+// when 128-pattern tiles would leave most SMs idle (short alignments: GB300
+// issues only a few FP64 FMAs per clock per SM, so these kernels run at the
+// FP64 rate of the SMs they occupy). Per-pattern arithmetic is the same; the
+// grid reduction groups the CTA sums differently.
+static int f64_tpb(const iqgpu_engine *e) { return e->nblk < e->sms ? 32 : kTPB; }
+
 template <int NT, bool SAFE, int EPI>
 static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
-    const dim3 grid(e->nblk, P.cat_split ? e->C : 1);
+    const int tpb = f64_tpb(e);
+    const dim3 grid((unsigned)(e->Ppad / tpb), P.cat_split ? e->C : 1);
     constexpr bool REG = (NT != 0 && NT <= 20);
-    size_t smem = (REG ? 0 : (size_t)kMaxStates * kTPB * sizeof(double)) +
+    size_t smem = (REG ? 0 : (size_t)kMaxStates * tpb * sizeof(double)) +
                   (EPI == EPI_LNL ? (size_t)kMaxCat * kMaxStates * sizeof(double) : 0);
     auto kern = k_traverse_f64<NT, SAFE, EPI>;
     if (smem > 48 * 1024) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "traverse_f64 smem attribute");
     }
-    kern<<<grid, kTPB, smem, e->st>>>(P);
+    kern<<<grid, tpb, smem, e->st>>>(P);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "traverse_f64");
 }
@@ -1015,8 +1025,8 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
 
 int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, double xacc, int max_steps,
                       double *out_dev) {
-    // one cluster, one CTA per 256 patterns up to 8 (the portable cluster size)
-    const int q = (int)std::min<long long>(kNewtonMaxCluster, std::max<long long>(1, (e->P + 255) / 256));
+    // one cluster, one CTA per 32 patterns up to 8 (the portable cluster size)
+    const int q = (int)std::min<long long>(kNewtonMaxCluster, std::max<long long>(1, (e->P + 31) / 32));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)q);
     cfg.blockDim = dim3(kNewtonThreads);
@@ -1038,13 +1048,13 @@ int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, doub
 }
 
 int launch_derv_f64(iqgpu_engine *e, double len) {
-    k_derv_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    k_derv_f64<<<(unsigned)(e->Ppad / f64_tpb(e)), f64_tpb(e), 0, e->st>>>(buf_params(e, len));
     e->launches++;
     return cuda_fail(cudaGetLastError(), "derv_f64");
 }
 
 int launch_from_buffer_f64(iqgpu_engine *e, double len) {
-    k_from_buffer_f64<<<e->nblk, kTPB, 0, e->st>>>(buf_params(e, len));
+    k_from_buffer_f64<<<(unsigned)(e->Ppad / f64_tpb(e)), f64_tpb(e), 0, e->st>>>(buf_params(e, len));
     e->launches++;
     return cuda_fail(cudaGetLastError(), "from_buffer_f64");
 }

@@ -70,9 +70,16 @@ __device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float 
     const long long TB = (long long)(S + 1) * C * npad;
     const OpDev op = P.ops[k];
     int lref = op.child[0], rref = op.child[1];
+    // Multifurcating node (tree/phylokernelnew.h:1407-1631): consecutive records
+    // flagged IQGPU_OP_MORE share the dad; a continuation multiplies its
+    // children into the dad's running product, each record rescaling it
+    // (exact powers of two, exponents accumulate); an odd child count ends
+    // with an absent second child.
+    const bool cont = k > 0 && (P.ops[k - 1].flags & IQGPU_OP_MORE);
+    const bool rnone = rref == IQGPU_NO_CHILD;
     const float *gbase = P.opmats + (long long)k * P.op_stride;
     const float *PL = sP, *PR = sP + PM, *TL = gbase + 2 * PM, *TR = TL + TB;
-    if (lref >= 0 && rref < 0) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
+    if (lref >= 0 && rref < 0 && !rnone) {  // the tip goes on the left (tree/phylokernelnew.h:1390-1400)
         int t = lref; lref = rref; rref = t;
         const float *q = PL; PL = PR; PR = q;
         q = TL; TL = TR; TR = q;
@@ -82,7 +89,8 @@ __device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float 
     const float *Lp = lint ? P.part + (long long)lref * P.slot_floats + pbase : nullptr;
     const float *Rp = rint ? P.part + (long long)rref * P.slot_floats + pbase : nullptr;
     const float *tl = lint ? nullptr : TL + (long long)P.states[(long long)(-1 - lref) * ld + p] * C * npad + c * npad;
-    const float *tr = rint ? nullptr : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad + c * npad;
+    const float *tr = (rint || rnone) ? nullptr
+                                      : TR + (long long)P.states[(long long)(-1 - rref) * ld + p] * C * npad + c * npad;
     const float *PLc = PL + (long long)c * n * npad, *PRc = PR + (long long)c * n * npad;
     float cmax = 0.f;
     float4 out[NQ ? NQ : 1];
@@ -99,14 +107,17 @@ __device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float 
 #pragma unroll
         for (int q = 0; q < NQ; q++) {
             float o[4];
+            const float4 d4 = cont ? *reinterpret_cast<const float4 *>(dad + q * 32) : make_float4(1.f, 1.f, 1.f, 1.f);
+            const float dv[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int x = 4 * q + j;
                 float v = 0.f;
                 if (x < n) {
                     const float yl = lint ? row_dot_s<NQ>(PLc + x * npad, lv) : __ldg(tl + x);
-                    const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : __ldg(tr + x);
+                    const float yr = rint ? row_dot_s<NQ>(PRc + x * npad, rv) : (rnone ? 1.f : __ldg(tr + x));
                     v = yl * yr;
+                    if (cont) v *= dv[j];
                 }
                 o[j] = v;
                 cmax = fmaxf(cmax, v);
@@ -133,14 +144,19 @@ __device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float 
 #pragma unroll
             for (int j = 0; j < XC; j += 4) {
                 float o[4];
+                float dv[4] = {1.f, 1.f, 1.f, 1.f};
+                if (cont && x0 + j < npad) {
+                    const float4 d4 = *reinterpret_cast<const float4 *>(dad + ((x0 + j) >> 2) * 32);
+                    dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
+                }
 #pragma unroll
                 for (int jj = 0; jj < 4; jj++) {
                     const int x = x0 + j + jj;
                     float v = 0.f;
                     if (x < n) {
                         const float yl = lint ? al[j + jj] : __ldg(tl + x);
-                        const float yr = rint ? ar[j + jj] : __ldg(tr + x);
-                        v = yl * yr;
+                        const float yr = rint ? ar[j + jj] : (rnone ? 1.f : __ldg(tr + x));
+                        v = yl * yr * dv[jj];
                     }
                     o[jj] = v;
                     cmax = fmaxf(cmax, v);
@@ -179,7 +195,8 @@ __device__ __forceinline__ void mixed_op(const MixParams &P, int k, const float 
     }
     if (c == 0) {
         // exponents are read and written by the category-0 thread of the pattern only
-        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0);
+        const int e = (lint ? P.expo[(long long)lref * ld + p] : 0) + (rint ? P.expo[(long long)rref * ld + p] : 0) +
+                      (cont ? P.expo[(long long)op.dad_slot * ld + p] : 0);
         P.expo[(long long)op.dad_slot * ld + p] = e - sh;
     }
 }
@@ -834,12 +851,31 @@ static int fused_rest(iqgpu_engine *e, MixParams P, int rest) {
     }
 }
 
+template <int EPI>
+static int launch_fused_any(iqgpu_engine *e, const MixParams &P) {
+    switch (e->npad) {
+    case 4: return launch_mix_t<1, EPI>(e, P);
+    case 20: return launch_mix_t<5, EPI>(e, P);
+    default: return launch_mix_t<0, EPI>(e, P);
+    }
+}
+
 int launch_traverse_mixed(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len) {
     MixParams P = mix_params(e, nops);
     P.a = a;
     P.b = b;
     P.len = len;
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
+    if (e->has_multi) {
+        // multifurcating records share their dad: the fused CUDA-core kernel walks
+        // them in order per pattern (the level and tensor-core schedules would
+        // run them side by side)
+        switch (epi) {
+        case EPI_NONE: return launch_fused_any<EPI_NONE>(e, P);
+        case EPI_LNL: return launch_fused_any<EPI_LNL>(e, P);
+        default: return launch_fused_any<EPI_THETA>(e, P);
+        }
+    }
     if (e->tc) {
         int rest = nops;
         int rc = launch_traverse_tc(e, P, &rest);

@@ -5,8 +5,9 @@ partial within 1e-10 of each pattern's largest entry and scale counts
 identical to the oracle (itself bit-exact with the reference's compiled
 multifurcating kernel), NORM and SAFE, including a 150-taxon case whose
 partials underflow 2^-256; branch lnL 1e-10 relative, derivatives 1e-9,
-the tree drivers (iqgpu_tree_create_n) within the Newton-Raphson tolerance.
-Mixed-precision engines refuse multifurcating records (IQGPU_ERR_ARG).
+the tree drivers (iqgpu_tree_create_n) within the Newton-Raphson tolerance;
+the mixed-precision paths (FP32 and split TF32 engines, whose multifurcating
+records run on the fused CUDA-core kernel) within their tolerances.
 """
 import numpy as np
 import pytest
@@ -92,15 +93,62 @@ def test_multifurcating_tree_drivers(oracle_mod, name):
     np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-5)
 
 
-def test_mixed_engines_refuse_multifurcating_records():
-    g = load_golden("prot12")
-    edges, lengths = _collapsed(g, lambda internal: internal[:2])
+@pytest.mark.parametrize("name", ["dna16", "prot12", "codon8"])
+@pytest.mark.parametrize("precision", [engine.F32, engine.TF32X3])
+def test_mixed_multifurcating_match_oracle(oracle_mod, name, precision):
+    """The mixed paths on multifurcating nodes: every partial (standard basis,
+    exponents applied) within 1e-5 of each pattern's largest entry, branch lnL
+    within 1e-6, derivatives within the mixed tolerances of the tensor-core
+    tests, the tree drivers within 1e-6 after branch optimisation."""
+    g = load_golden(name)
+    edges, lengths = _collapsed(g, lambda internal: internal[:3])
+    assert np.bincount(np.asarray(edges).ravel()).max() >= 4
     topo = Topology(edges, lengths, g.ntaxa)
-    eng = engine.Engine(g.patterns.shape[1], 20, g.model.ncat, g.ntaxa, 23, topo.nslots, precision=engine.F32,
-                        max_ops=2 * topo.nslots)
+    eng = engine.Engine(g.patterns.shape[1], g.model.nstates, g.model.ncat, g.ntaxa, g.model.state_unknown,
+                        topo.nslots, precision=precision, max_ops=2 * topo.nslots + 8)
     eng.set_model(g.model)
     eng.set_patterns(g.freq)
     eng.set_tip_states(g.patterns)
-    with pytest.raises(engine.EngineError) as ei:
-        eng.compute_partials(topo.all_partials_ops())
-    assert ei.value.code == 1
+    eng.compute_partials(topo.all_partials_ops())
+    orc = oracle_mod.OracleTree(g.model, g.patterns, g.freq, edges, lengths)
+    n, C = g.model.nstates, g.model.ncat
+    for (u, v), slot in topo.slot.items():
+        gp, _ = eng.partial(slot)
+        op, _ = orc.partial(u, v)
+        std = np.einsum("xi,pci->pcx", g.model.evec, op.reshape(-1, C, n)).reshape(op.shape)
+        gn = gp / np.abs(gp).max(axis=1, keepdims=True)
+        on = std / np.abs(std).max(axis=1, keepdims=True)
+        assert np.max(np.abs(gn - on)) < 1e-5, (u, v)
+    for (u, v) in edges[:6]:
+        u, v = int(u), int(v)
+        node, dad = (v, u) if v >= g.ntaxa else (u, v)
+        lg = eng.branch_lnl(topo.ref(dad, node), topo.ref(node, dad), topo.edge_len(node, dad))
+        assert rel(lg, orc.lnl_branch(node, dad)) < 1e-6, (u, v)
+    internal = [(int(u), int(v)) for (u, v) in edges if min(int(u), int(v)) >= g.ntaxa][:2]
+    for (n1, n2) in internal:
+        orc2 = oracle_mod.OracleTree(g.model, g.patterns, g.freq, edges, lengths)
+        ops = topo.branch_ops(n2, n1)
+        df, ddf = eng.likelihood_derv(ops, topo.ref(n1, n2), topo.ref(n2, n1), 0.07)
+        odf, oddf = orc2.derv(n1, n2, 0.07)
+        assert abs(df - odf) <= 1e-4 * abs(odf) + 1e-3 and abs(ddf - oddf) <= 1e-3 * abs(oddf) + 1e-3
+    t = engine.GpuTree(g.model, g.patterns, g.freq, edges, lengths, precision=precision)
+    o = oracle_mod.OracleTree(g.model, g.patterns, g.freq, edges, lengths)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < 1e-6
+    lg, lo = t.optimize_all_branches(), o.optimize_all_branches()
+    assert rel(lg, lo) < 1e-6
+    np.testing.assert_allclose(t.lengths(), o.lengths(), atol=1e-4)
+
+
+def test_mixed_multifurcating_underflow():
+    """150 taxa, long branches: partials that underflow FP32 many times over
+    carry the per-pattern exponents through multifurcating nodes (lnL within
+    1e-6 of the FP64 drop-in)."""
+    ds = simulate.protein_lg_dataset(150, 400, 11, mean_bl=0.5)
+    from types import SimpleNamespace
+    g = SimpleNamespace(model=ds.model, patterns=ds.patterns, freq=ds.freq, edges=ds.edges, lengths=ds.lengths,
+                        ntaxa=ds.ntaxa)
+    edges, lengths = _collapsed(g, lambda internal: internal[::6])
+    want = engine.GpuTree(g.model, g.patterns, g.freq, edges, lengths, safe=True).compute_likelihood()
+    for precision in (engine.F32, engine.TF32X3):
+        got = engine.GpuTree(g.model, g.patterns, g.freq, edges, lengths, precision=precision).compute_likelihood()
+        assert rel(got, want) < 1e-6, (precision, got, want)

@@ -10,7 +10,7 @@ pattern lnL, the scale counts of the largest partial identical, its values
 within 1e-10 of each pattern's largest entry, derivatives within 1e-9 and the
 lnL from the theta buffer within 1e-10, NORM and SAFE, on binary trees
 and on trees with multifurcating nodes. The mixed paths (FP32, split TF32
-for protein) match the reference's lnL within 1e-6 on the binary trees.
+for protein) match the reference's lnL within 1e-6, polytomies included.
 """
 import numpy as np
 import pytest
@@ -70,8 +70,6 @@ def test_tree_drivers_and_mixed_paths_match_reference(name):
     ref = float(g.d["lnl_norm"][0])
     t = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths)
     assert rel(t.compute_likelihood(), ref) < 1e-10
-    if "polytomy" in name:  # multifurcating nodes run on FP64 engines only
-        return
     precisions = [engine.F32] + ([engine.TF32X3] if g.model.nstates == 20 else [])
     for prec in precisions:
         tm = engine.GpuTree(g.model, g.patterns, g.freq, g.edges, g.lengths, precision=prec)
