@@ -311,8 +311,9 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * (tile, op, category) items handed out in level order, each item's copies
  * issued once the items writing its children are done (bounded waits; the
  * level form of 5 when the traversal has more (op, tile) pairs than the
- * engine's pair counters; other kernels run as 3). Results do not depend on
- * it. */
+ * engine's pair counters; other kernels run as 3); 7 = as 6 with whole
+ * (tile, op) items (every category of the pair in one item). Results do not
+ * depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots

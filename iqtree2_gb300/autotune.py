@@ -27,14 +27,16 @@ def candidates(eng):
     operand A in tensor memory (20 states, split TF32), 5 = as 3 with
     category-split items on the narrow levels (up to 32 padded states),
     6 = dataflow on the tensor cores (one launch of category-split items,
-    each waiting for the items writing its children)."""
+    each waiting for the items writing its children), 7 = as 6 with whole
+    (op, tile) items."""
     if getattr(eng, "tensor_cores", False):  # one CTA = 128 patterns (the MMA's M)
         npad = (eng.nstates + 3) // 4 * 4
         pieces = (1, 2) if (npad > 32 and npad % 16 == 0) else (1,)
         out = [(0, sched, st, kp) for sched in (0, 1, 3) for st in (2, 3, 4) for kp in pieces]
         if npad <= 32:  # category-split narrow levels on the tensor cores
             out += [(0, 5, st, 1) for st in (2, 3)]
-        out += [(0, 6, st, kp) for st in (2, 3) for kp in pieces]  # dataflow
+        out += [(0, 6, st, kp) for st in (2, 3) for kp in pieces]  # dataflow, category-split items
+        out += [(0, 7, 2, kp) for kp in pieces]  # dataflow, whole (op, tile) items
         if npad == 20 and getattr(eng, "precision", 0) == 2:  # split TF32
             out.append((0, 4, 0, 0))
         return out
@@ -50,7 +52,7 @@ def candidates(eng):
 
 def label(cand):
     tile, sched, stages, kp = cand
-    return (f"{tile}/{('fused', 'level', 'flow', 'level-ws', 'level-tm', 'level-wsc', 'flow-tc')[sched]}" +
+    return (f"{tile}/{('fused', 'level', 'flow', 'level-ws', 'level-tm', 'level-wsc', 'flow-tc', 'flow-tcw')[sched]}" +
             (f"/s{stages}" if stages else "") +
             (f"/k{kp}" if kp else ""))
 

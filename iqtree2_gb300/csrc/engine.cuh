@@ -160,6 +160,7 @@ struct iqgpu_engine {
     bool tc_tm;               // level schedule on the A-in-tensor-memory kernel (20 states, split TF32)
     bool tc_split;            // category-split items on narrow levels for <= 32 padded states too (schedule 5)
     bool tc_flow;             // dataflow schedule on the warp-specialised tensor-core kernel (schedule 6)
+    bool tc_flow_whole;       // as tc_flow, with whole (op, tile) items (schedule 7)
     bool has_multi;           // the uploaded op list holds multifurcating records (IQGPU_OP_MORE)
     int sms;                  // multiprocessors of the engine's device
     float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs

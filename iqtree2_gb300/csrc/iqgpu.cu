@@ -107,8 +107,9 @@ static Sizes sizes(const iqgpu_config *c) {
     s.cmax = uses_tc(c) ? std::max(16LL * 160 * 128, (long long)kFlowWindowOps * s.Ppad) * C * 4 : 0;
     s.pairs = uses_tc(c) ? std::max<long long>(kPairCounters, (long long)kFlowWindowOps * (s.Ppad / 128)) : 0;
     s.flow = is_mixed(c) ? (long long)(c->max_ops + 1) * (s.Ppad / 128) * 4 : 0;
-    // one partial-sum row per CTA; the smallest pattern tile of any kernel is 32
-    s.red = (s.Ppad / 32) * kRedSlots * (long long)sizeof(double) + 64;
+    // one partial-sum row per CTA; the smallest pattern tile of any kernel is 4
+    // (the FP64 lane kernel: 128 threads, up to 32 lanes per pattern)
+    s.red = (s.Ppad / 4) * kRedSlots * (long long)sizeof(double) + 64;
     s.total = s.part + s.scale + s.states + s.ops + s.opmats + s.theta + s.red + s.tcb + s.flow + s.cmax +
               s.pairs * 4 +
               2 * s.Ppad * 8 +
@@ -339,7 +340,7 @@ static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_b
     CKE(dalloc(e, &e->d_theta, is_mixed(cfg) ? 8 : B * e->Ppad * 8));
     CKE(dalloc(e, &e->d_bscale, e->Ppad * 8));
     CKE(dalloc(e, &e->d_plh, e->Ppad * 8));
-    CKE(dalloc(e, &e->d_red_partials, (e->Ppad / 32) * kRedSlots * 8));
+    CKE(dalloc(e, &e->d_red_partials, (size_t)s.red));  // one row per CTA of the smallest pattern tile
     CKE(dalloc(e, &e->d_ticket, 64));  // ticket at byte 0, status word at 32, flow ticket at 48, state check at 56
     e->d_status = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_ticket) + 32);
     e->d_flow_ticket = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(e->d_ticket) + 48);
@@ -1306,13 +1307,14 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
 }
 
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
-    if (!e || schedule < 0 || schedule > 6) { set_error("schedule must be 0 .. 6"); return IQGPU_ERR_ARG; }
+    if (!e || schedule < 0 || schedule > 7) { set_error("schedule must be 0 .. 7"); return IQGPU_ERR_ARG; }
     e->level_sync = schedule == 1 || schedule >= 3;
     e->flow = schedule == 2;
     e->tc_ws = schedule == 3 || schedule >= 5;
     e->tc_tm = schedule == 4;
-    e->tc_split = schedule >= 5;
+    e->tc_split = schedule == 5 || schedule == 6;
     e->tc_flow = schedule == 6;
+    e->tc_flow_whole = schedule == 7;
     return IQGPU_OK;
 }
 

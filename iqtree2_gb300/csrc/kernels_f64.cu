@@ -238,6 +238,108 @@ __device__ __forceinline__ void multi_record(const TravParams &P, const OpDev &o
     }
 }
 
+// Branch epilogue of a traversal for pattern p (theta, or the branch lnL and
+// its grid sums). Every thread of the CTA calls it (the lnL form has a CTA
+// barrier and the grid reduction); threads with on = false hold no pattern.
+template <int NT, bool SAFE, int EPI>
+__device__ __forceinline__ void f64_epilogue(const TravParams &P, long long p, double invar, double *sval, bool on) {
+    const int n = NT ? NT : P.n;
+    const int C = P.ncat, B = n * C;
+    const int tid = threadIdx.x;
+    const long long ld = P.ldp;
+    // ---- epilogue on the branch (a, b): a is internal (dad_branch), b is node_branch or a tip
+    const double *pa = P.partials + (long long)P.a * P.slot_stride + p;
+    const uint8_t *sa = P.scale + (long long)P.a * P.scale_stride + p;
+    const bool btip = P.b < 0;
+    const double *pb = btip ? nullptr : P.partials + (long long)P.b * P.slot_stride + p;
+    const uint8_t *sb = btip ? nullptr : P.scale + (long long)P.b * P.scale_stride + p;
+    // a tip b: its state's eigen-space tip vector, per mixture class (tipv + class * n)
+    const double *tipv = btip ? P.tip_lh + (long long)P.states[(long long)(-1 - P.b) * ld + p] * P.nmix * n : nullptr;
+    const bool valid = on && p < P.nptn;
+
+    if constexpr (EPI == EPI_THETA) {
+        if (!on) return;
+        // theta = node o dad and per-pattern scale offset (tree/phylokernelnew.h:2048-2231)
+        double *th = P.theta + p;
+        for (int c = 0; c < C; c++)
+            for (int x = 0; x < n; x++) {
+                const long long r = (long long)(c * n + x) * ld;
+                th[r] = (btip ? __ldg(tipv + (c / P.cpc) * n + x) : pb[r]) * pa[r];
+            }
+        double bs;
+        if (SAFE) {
+            unsigned sum[kMaxCat], mn = 1u << 30;
+            for (int c = 0; c < C; c++) {
+                sum[c] = (unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld]);
+                sum[c] &= 0xffu;  // UBYTE arithmetic
+                mn = min(mn, sum[c]);
+            }
+            for (int c = 0; c < C; c++) {
+                if (sum[c] == mn + 1) {
+                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] *= kScaleThreshold;
+                } else if (sum[c] > mn + 1) {
+                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] = 0.0;
+                }
+            }
+            bs = (double)mn;
+        } else {
+            bs = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+        }
+        P.buffer_scale[p] = bs * kLogScaleThreshold;
+        return;
+    } else {
+        // branch lnL (tree/phylokernelnew.h:2641-3223)
+        for (int t = tid; t < B; t += blockDim.x) {
+            const int c = t / n, i = t % n;
+            sval[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
+        }
+        __syncthreads();
+        // threads without a pattern add zeros; every thread reaches the one
+        // grid_reduce below (its warp shuffles and barriers need the whole CTA)
+        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
+        if (on) {
+            double lh_cat[kMaxCat];
+            double lh = 0.0;
+            for (int c = 0; c < C; c++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) {
+                    const long long r = (long long)(c * n + i) * ld;
+                    const double w = btip ? sval[c * n + i] * __ldg(tipv + (c / P.cpc) * n + i) : sval[c * n + i] * pb[r];
+                    acc = fma(w, pa[r], acc);
+                }
+                lh_cat[c] = acc;
+                if (!SAFE) lh += acc;
+            }
+            double scale_count;
+            if (SAFE) {
+                unsigned sum[kMaxCat], mn = 1u << 30;
+                for (int c = 0; c < C; c++) {
+                    sum[c] = ((unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld])) & 0xffu;
+                    mn = min(mn, sum[c]);
+                }
+                for (int c = 0; c < C; c++) {
+                    if (sum[c] == mn + 1) lh_cat[c] *= kScaleThreshold;
+                    else if (sum[c] > mn + 1) lh_cat[c] = 0.0;
+                    lh += lh_cat[c];
+                }
+                scale_count = (double)mn;
+            } else {
+                scale_count = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+            }
+            lh = fabs(lh) + invar;
+            const double plh = log(lh) + scale_count * kLogScaleThreshold;
+            P.pattern_lh[p] = plh;
+            if (valid) {
+                const double f = P.freq[p];
+                v[0] = plh * f;
+                v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;  // underflow fix-up sum
+                v[2] = isfinite(plh) ? 0.0 : 1.0;
+            }
+        }
+        grid_reduce(v, P.red);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // traversal kernel
 // ---------------------------------------------------------------------------
@@ -393,93 +495,91 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
         }
     }
 
-    if constexpr (EPI == EPI_NONE) return;
+    if constexpr (EPI != EPI_NONE) f64_epilogue<NT, SAFE, EPI>(P, p, invar, sval, true);
+}
 
-    // ---- epilogue on the branch (a, b): a is internal (dad_branch), b is node_branch or a tip
-    const double *pa = P.partials + (long long)P.a * P.slot_stride + p;
-    const uint8_t *sa = P.scale + (long long)P.a * P.scale_stride + p;
-    const bool btip = P.b < 0;
-    const double *pb = btip ? nullptr : P.partials + (long long)P.b * P.slot_stride + p;
-    const uint8_t *sb = btip ? nullptr : P.scale + (long long)P.b * P.scale_stride + p;
-    // a tip b: its state's eigen-space tip vector, per mixture class (tipv + class * n)
-    const double *tipv = btip ? P.tip_lh + (long long)P.states[(long long)(-1 - P.b) * ld + p] * P.nmix * n : nullptr;
-    const bool valid = p < P.nptn;
-
-    if constexpr (EPI == EPI_THETA) {
-        // theta = node o dad and per-pattern scale offset (tree/phylokernelnew.h:2048-2231)
-        double *th = P.theta + p;
-        for (int c = 0; c < C; c++)
-            for (int x = 0; x < n; x++) {
-                const long long r = (long long)(c * n + x) * ld;
-                th[r] = (btip ? __ldg(tipv + (c / P.cpc) * n + x) : pb[r]) * pa[r];
-            }
-        double bs;
-        if (SAFE) {
-            unsigned sum[kMaxCat], mn = 1u << 30;
-            for (int c = 0; c < C; c++) {
-                sum[c] = (unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld]);
-                sum[c] &= 0xffu;  // UBYTE arithmetic
-                mn = min(mn, sum[c]);
-            }
-            for (int c = 0; c < C; c++) {
-                if (sum[c] == mn + 1) {
-                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] *= kScaleThreshold;
-                } else if (sum[c] > mn + 1) {
-                    for (int x = 0; x < n; x++) th[(long long)(c * n + x) * ld] = 0.0;
-                }
-            }
-            bs = (double)mn;
-        } else {
-            bs = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+// ---------------------------------------------------------------------------
+// Short alignments on the FP64 path, 4-state models with n * ncat <= 32: G
+// lanes per pattern (the power of two >= 4 * ncat), one per (category, state)
+// entry. GB300 issues only a few FP64 FMAs per clock per SM, so a pattern per
+// thread leaves a DNA alignment of a few hundred patterns on a handful of SMs
+// and serialises each thread's whole op chain; here the same work spreads over
+// G times the warps. A lane reads its own entry of each child, the category's
+// four entries come from the neighbouring lanes by shuffles, and every sum is
+// formed in the order of k_traverse_f64's register path (dot_reg<4>), the
+// checks and scale counts as there, so partials, scale counts and lnL are
+// identical to it. Binary records only (multifurcating traversals and
+// category-split walks stay on k_traverse_f64); the epilogue is
+// k_traverse_f64's, run by the pattern's first lane.
+// ---------------------------------------------------------------------------
+template <bool SAFE, int EPI, int G>
+__global__ void __launch_bounds__(128) k_traverse_f64_lanes(const TravParams P) {
+    constexpr int n = 4;
+    static_assert(G >= 4 && G <= 32 && (G & (G - 1)) == 0, "lanes per pattern");
+    __shared__ double sval[kMaxCat * kMaxStates];
+    const int C = P.ncat, B = n * C;
+    const int lane = threadIdx.x & 31, r = lane & (G - 1), base = lane & ~(G - 1);
+    const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const bool act = r < B;
+    const int c = act ? r / n : 0, x = r % n;
+    const long long ld = P.ldp;
+    const double invar = P.invar[p];
+    const long long CNN = (long long)C * n * n;
+    const long long SB = (long long)(P.state_unknown + 1) * B;
+    const double *Ui = P.inv_evec + ((long long)(c / P.cpc) * n + x) * n;
+    const int src = base + c * n;  // this category's first lane
+    for (int k = 0; k < P.nops; ++k) {
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const double *eL = P.opmats + op.mat_off, *eR = eL + CNN;
+        const double *tL = eL + 2 * CNN, *tR = tL + SB;
+        if (lref >= 0 && rref < 0) {  // put the tip on the left (tree/phylokernelnew.h:1390-1400)
+            int t = lref; lref = rref; rref = t;
+            const double *q = eL; eL = eR; eR = q;
+            q = tL; tL = tR; tR = q;
         }
-        P.buffer_scale[p] = bs * kLogScaleThreshold;
-        return;
-    } else {
-        // branch lnL (tree/phylokernelnew.h:2641-3223)
-        for (int t = tid; t < B; t += blockDim.x) {
-            const int c = t / n, i = t % n;
-            sval[t] = exp(P.eval[(c / P.cpc) * n + i] * (P.rates[c] * P.len)) * P.props[c];
+        const bool lint = lref >= 0, rint = rref >= 0;
+        // scale counts of the dad: 0 (tip-tip), copy (tip-internal), sum (internal-internal)
+        const long long so = SAFE ? (long long)c * ld + p : p;
+        unsigned sc = 0;
+        if (lint) sc += P.scale[(long long)lref * P.scale_stride + so];
+        if (rint) sc += P.scale[(long long)rref * P.scale_stride + so];
+        const double lv = (lint && act) ? P.partials[(long long)lref * P.slot_stride + (long long)r * ld + p] : 0.0;
+        const double rv = (rint && act) ? P.partials[(long long)rref * P.slot_stride + (long long)r * ld + p] : 0.0;
+        double l4[n], r4[n];
+#pragma unroll
+        for (int i = 0; i < n; i++) {
+            l4[i] = __shfl_sync(0xffffffffu, lv, src + i);
+            r4[i] = __shfl_sync(0xffffffffu, rv, src + i);
         }
-        __syncthreads();
-        double lh_cat[kMaxCat];
-        double lh = 0.0;
-        for (int c = 0; c < C; c++) {
-            double acc = 0.0;
-            for (int i = 0; i < n; i++) {
-                const long long r = (long long)(c * n + i) * ld;
-                const double w = btip ? sval[c * n + i] * __ldg(tipv + (c / P.cpc) * n + i) : sval[c * n + i] * pb[r];
-                acc = fma(w, pa[r], acc);
-            }
-            lh_cat[c] = acc;
-            if (!SAFE) lh += acc;
+        double tmp = 0.0;
+        if (act) {
+            const long long row = (long long)(c * n + x) * n;
+            const double yl = lint ? dot_reg<n>(eL + row, l4)
+                                   : __ldg(tL + (long long)P.states[(long long)(-1 - lref) * ld + p] * B + c * n + x);
+            const double yr = rint ? dot_reg<n>(eR + row, r4)
+                                   : __ldg(tR + (long long)P.states[(long long)(-1 - rref) * ld + p] * B + c * n + x);
+            tmp = yl * yr;
         }
-        double scale_count;
-        if (SAFE) {
-            unsigned sum[kMaxCat], mn = 1u << 30;
-            for (int c = 0; c < C; c++) {
-                sum[c] = ((unsigned)sa[c * ld] + (btip ? 0u : (unsigned)sb[c * ld])) & 0xffu;
-                mn = min(mn, sum[c]);
-            }
-            for (int c = 0; c < C; c++) {
-                if (sum[c] == mn + 1) lh_cat[c] *= kScaleThreshold;
-                else if (sum[c] > mn + 1) lh_cat[c] = 0.0;
-                lh += lh_cat[c];
-            }
-            scale_count = (double)mn;
-        } else {
-            scale_count = (double)((unsigned)sa[0] + (btip ? 0u : (unsigned)sb[0]));  // NORM sums do not wrap
+        double t4[n];
+#pragma unroll
+        for (int i = 0; i < n; i++) t4[i] = __shfl_sync(0xffffffffu, tmp, src + i);
+        double out = act ? dot_reg<n>(Ui, t4) : 0.0;
+        const bool check = (lint || rint) && invar == 0.0;  // tip-tip never scales
+        // the category's (SAFE) or the pattern's (NORM) largest |entry|, NaN ignored as fmax does
+        double m = fmax(0.0, fabs(out));
+#pragma unroll
+        for (int off = 1; off < (SAFE ? n : G); off <<= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+        if (check && m < kScaleThreshold) {
+            out *= kTwoPow256;
+            sc += 1;
         }
-        lh = fabs(lh) + invar;
-        const double plh = log(lh) + scale_count * kLogScaleThreshold;
-        P.pattern_lh[p] = plh;
-        double v[kRedSlots] = {0.0, 0.0, 0.0, 0.0};
-        if (valid) {
-            const double f = P.freq[p];
-            v[0] = plh * f;
-            v[1] = (isfinite(plh) ? plh : 4.0 * kLogScaleThreshold) * f;  // underflow fix-up sum
-            v[2] = isfinite(plh) ? 0.0 : 1.0;
-        }
-        grid_reduce(v, P.red);
+        if (act) P.partials[(long long)op.dad_slot * P.slot_stride + (long long)r * ld + p] = out;
+        if (SAFE ? (act && x == 0) : r == 0) P.scale[(long long)op.dad_slot * P.scale_stride + so] = (uint8_t)sc;
+    }
+    if constexpr (EPI != EPI_NONE) {
+        __syncwarp();  // the pattern's entries, written by its lanes, are visible to its first lane
+        f64_epilogue<n, SAFE, EPI>(P, p, invar, sval, r == 0);
     }
 }
 
@@ -962,8 +1062,28 @@ static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
     return cuda_fail(cudaGetLastError(), "traverse_f64");
 }
 
+// 4-state models on short alignments: the lane kernel (see above)
+template <bool SAFE, int EPI, int G>
+static int launch_lanes_t(iqgpu_engine *e, const TravParams &P) {
+    k_traverse_f64_lanes<SAFE, EPI, G><<<(unsigned)(e->Ppad * G / 128), 128, 0, e->st>>>(P);
+    e->launches++;
+    return cuda_fail(cudaGetLastError(), "traverse_f64_lanes");
+}
+
+static bool use_lanes(const iqgpu_engine *e, const TravParams &P) {
+    return e->n == 4 && e->C <= 8 && !e->nonrev && !e->has_multi && !P.cat_split && e->nblk < e->sms;
+}
+
 template <bool SAFE, int EPI>
 static int dispatch_n(iqgpu_engine *e, const TravParams &P) {
+    if (use_lanes(e, P)) {
+        switch (e->C) {
+        case 1: return launch_lanes_t<SAFE, EPI, 4>(e, P);
+        case 2: return launch_lanes_t<SAFE, EPI, 8>(e, P);
+        case 3: case 4: return launch_lanes_t<SAFE, EPI, 16>(e, P);
+        default: return launch_lanes_t<SAFE, EPI, 32>(e, P);
+        }
+    }
     switch (e->n) {
     case 4: return launch_trav_t<4, SAFE, EPI>(e, P);
     case 20: return launch_trav_t<20, SAFE, EPI>(e, P);

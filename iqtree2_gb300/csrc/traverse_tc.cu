@@ -97,9 +97,9 @@ __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, 
     TcItem it;
     it.cat = -1;
     it.prod0 = it.prod1 = -1;
-    if (flow_id >= 0) {  // dataflow ticket: (op, tile, category) in level order
-        it.cat = flow_id % P.ncat;
-        const int i = flow_id / P.ncat;
+    if (flow_id >= 0) {  // dataflow ticket: (op, tile[, category]) in level order
+        if (csplit) it.cat = flow_id % P.ncat;
+        const int i = csplit ? flow_id / P.ncat : flow_id;
         it.tile = i % T.ntiles;
         it.k = op0 + i / T.ntiles;
         const OpDev &od = P.ops[it.k];
@@ -467,15 +467,15 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 // item that completes a (tile, op) pair applies the rescale and writes the
 // exponents.
 //
-// FLOW (dataflow schedule, category-split items): one launch for the ops
-// [op0, op0 + nl) of several levels. The issuer takes (op, tile, category)
-// items from a global ticket in level order and passes their ids to the
+// FLOW (dataflow schedule): one launch for the ops [op0, op0 + nl) of several
+// levels. The issuer takes (op, tile, category) items (CSPLIT) or whole
+// (op, tile) items from a global ticket in level order and passes their ids to the
 // workers through a shared-memory FIFO; it issues an item's copies once the
 // (op, tile) pairs writing its internal children have raised their flags in
 // flow_done (polled without blocking, so the MMAs of earlier items keep
 // going), and the workers acquire the same flags before reading the
 // children's exponents. The item that completes a pair raises the pair's
-// flag after its rescale. Tickets go only to running CTAs in increasing
+// flag after its rescale (a whole item raises it after its own). Tickets go only to running CTAs in increasing
 // order and every producer has a smaller ticket, so every wait ends whatever
 // the residency; the waits are bounded all the same.
 constexpr int kFlowFifo = 8;  // item ids between the issuer and the workers
@@ -485,7 +485,6 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl,
                      float *__restrict__ cmax_out, unsigned *__restrict__ pair_cnt,
                      unsigned *__restrict__ flow_done, unsigned *__restrict__ ticket, const unsigned epoch) {
-    static_assert(!FLOW || CSPLIT, "the dataflow schedule runs category-split items");
     constexpr bool csplit = CSPLIT;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
@@ -597,7 +596,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                             push(-1);
                             break;
                         }
-                        fit[nf % kFlowFifo] = tc_item(T, 0, false, op0, opc, true, id);
+                        fit[nf % kFlowFifo] = tc_item(T, 0, false, op0, opc, csplit, id);
                         fready[nf % kFlowFifo] = false;
                         push(id);
                         nf++;
@@ -644,8 +643,9 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     int c, side, kh;
                     tc_stage(mit, ms, ksplit, c, side, kh);
                     const int per = (int)mit.lint + (int)mit.rint;
-                    const int g = mi;
-                    const bool first = ms == 0, last = ms == per * ksplit - 1;
+                    const int sk = ms % (per * ksplit);
+                    const int g = mi * CI + (csplit ? 0 : c);
+                    const bool first = sk == 0, last = sk == per * ksplit - 1;
                     if (mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
                         (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
                         tc_fence_after();
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                         mma_commit(&mmab[s]);
                         if (last) mma_commit(&ebar[g & 1]);
                         mdone++;
-                        if (++ms >= per * ksplit) {
+                        if (++ms >= tc_nstages(mit, C, ksplit)) {
                             mi++;
                             ms = 0;
                         }
@@ -818,7 +818,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     break;
                 }
                 if (id < 0) break;
-                it = tc_item(T, 0, false, op0, opc, true, id);
+                it = tc_item(T, 0, false, op0, opc, csplit, id);
                 const bool dep_ok = r != 0 || flow_wait(it);
                 if (bar_or_part(kTcRows, !dep_ok)) {  // also: every worker has read the FIFO entry
                     abort = true;
@@ -933,6 +933,11 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                 }
             }
             P.expo[(long long)it.dad * ld + p] = e_in - sh;
+            if constexpr (FLOW) {  // the (op, tile) item is complete: raise its flag
+                __threadfence();
+                bar_sync_part(kTcRows);
+                if (r == 0) atomicExch(flow_done + (long long)(it.k + P.op_base) * T.ntiles + it.tile, epoch);
+            }
         }
         if (abort && r == 0) {
             atomicExch(&abort_flag, 1u);
@@ -1428,6 +1433,7 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF, false>;
     auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, true>;
     auto kern_flow = k_traverse_tc_ws<NP, NSTAGE, BF, true, true>;
+    auto kern_flow_whole = k_traverse_tc_ws<NP, NSTAGE, BF, false, true>;
     const bool split_ok = NP == 64 || e->tc_split;  // 61 states always; fewer states with schedule 5
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
     const int nthr = ws ? kTcRows + 32 : kTcRows;
@@ -1446,6 +1452,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
         err = cudaFuncSetAttribute(kern_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err == cudaSuccess && ws && split_ok && e->tc_flow)
         err = cudaFuncSetAttribute(kern_flow, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err == cudaSuccess && ws && e->tc_flow_whole)
+        err = cudaFuncSetAttribute(kern_flow_whole, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess && ws && e->tc_flow_whole)
+        err = cudaFuncSetAttribute(kern_flow_whole, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc smem attribute");
     // Residency per SM: bounded by shared memory (dynamic + static + the per-CTA
     // reserve) and by tensor memory (512 columns, 4 * NP per CTA).
@@ -1478,6 +1488,29 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     // (61 states only: a 20-state item is 8 short stages and the narrow levels
     // run faster on the CUDA-core tail than split plus the fix-up launch)
     const bool can_split = ws && split_ok && e->d_cmax != nullptr;
+    if (ws && e->tc_flow_whole && e->d_flow_done) {
+        // Dataflow over whole (op, tile) items: leading tip-tip levels as store
+        // streams, then every other op in one launch
+        int l = 0;
+        for (; l < e->nlevels; l++) {
+            const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+            if (nl > 0 && !level_all_tiptip(e, op0, nl)) break;
+            if (nl > 0 && (rc = launch_tiptip_level(e, M, op0, nl))) return rc;
+        }
+        const int op_first = l < e->nlevels ? e->level_off[l] : M.nops;
+        const int nflow = M.nops - op_first;
+        *rest = M.nops;
+        if (nflow <= 0) return IQGPU_OK;
+        const long long ntiles = T.ntiles;
+        err = cudaMemsetAsync(e->d_flow_done, 0, (size_t)(M.op_base + M.nops) * ntiles * 4, e->st);
+        if (err == cudaSuccess) err = cudaMemsetAsync(e->d_flow_ticket, 0, 4, e->st);
+        if (err != cudaSuccess) return cuda_fail(err, "flow flag reset");
+        const int grid = (int)std::min<long long>((long long)nflow * ntiles, resident);
+        kern_flow_whole<<<grid, nthr, smem, e->st>>>(tm, T, op_first, nflow, e->d_cmax, e->d_pair_cnt, e->d_flow_done,
+                                                     e->d_flow_ticket, 1u);
+        e->launches++;
+        return cuda_fail(cudaGetLastError(), "traverse_tc flow");
+    }
     if (can_split && e->tc_flow && e->d_flow_done) {
         // Dataflow: leading levels of tip-tip ops as store streams, then every
         // other op in one launch of category-split items (no CUDA-core tail)
