@@ -59,7 +59,7 @@ PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_BYTES = {
     "protein": (2583.1e6, "profiles/k_traverse_tc_ws_protein100x50k.md"),
     "dna-large": (2219.6e6, "profiles/k_level_dna_dna200x100k.md"),
-    "codon": (418.7e6, "profiles/k_traverse_tc_ws_codon40x10k.md"),
+    "codon": (438.3e6, "profiles/k_traverse_tc_ws_flow_codon40x10k.md"),  # the tuned dataflow schedule
 }
 
 
@@ -89,8 +89,14 @@ def kernel_name(use_tc, n, tile, bf16=False):
         depth = next((int(t[1:]) for t in tile.split("/") if t.startswith("s")), 2)
         if "/level-tm" in tile and not bf16:
             return "k_traverse_tc_tm"
+        np_ = 64 if n > 32 else 32
+        bf = 'true' if bf16 else 'false'
+        if "/flow-tcw" in tile:  # dataflow, whole (op, tile) items
+            return f"k_traverse_tc_ws<{np_},{depth},{bf},false,true>"
+        if "/flow-tc" in tile:  # dataflow, category-split items
+            return f"k_traverse_tc_ws<{np_},{depth},{bf},true,true>"
         name = "k_traverse_tc_ws" if "/level-ws" in tile else "k_traverse_tc"
-        return f"{name}<{64 if n > 32 else 32},{depth},{'true' if bf16 else 'false'}>"
+        return f"{name}<{np_},{depth},{bf}>"
     if tile.startswith("1/"):
         return "k_level_dna" if "/level" in tile else "k_traverse_dna<LNL>"
     nq = {4: 1, 20: 5}.get((n + 3) // 4 * 4, 0)
@@ -490,10 +496,11 @@ def branch_optimisation_dna16(args):
             "speedup": c_s / g_s,
             "optimisations_per_s": 1.0 / g_s, "pattern_node_updates_per_run": gpu_updates,
             "lnl": {"gpu_fp64": g_lnl, "cpu": c_lnl, "rel_err": abs(g_lnl - c_lnl) / abs(c_lnl)},
-            "note": "GPU: host drivers (csrc/tree.cpp) over the FP64 kernels, minimizeNewton as one device "
-                    "kernel per branch (iqgpu_newton_branch; gpu_fp64_host_newton_ms: the host loop, one launch "
-                    "and read-back per derivative); CPU: the C restatement of the same drivers and kernels, one "
-                    "thread (the alignment has ~600 patterns)"}
+            "note": "GPU: host drivers (csrc/tree.cpp) over the FP64 kernels (the lane kernel for this short "
+                    "4-state alignment), minimizeNewton as one thread-block-cluster kernel per branch "
+                    "(iqgpu_newton_branch; gpu_fp64_host_newton_ms: the host loop, one launch and read-back per "
+                    "derivative); CPU: the C restatement of the same drivers and kernels, one thread (the "
+                    "alignment has ~600 patterns)"}
 
 
 def run_ours(args):
@@ -851,7 +858,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="protein", choices=sorted(WORKLOADS))
-    ap.add_argument("--mode", default="headline", choices=["headline", "serve", "batched"])
+    ap.add_argument("--mode", default="headline", choices=["headline", "serve", "batched", "branchopt"])
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--max-taxa", type=int, default=2000)
@@ -861,8 +868,8 @@ def main():
     ap.add_argument("--no-fp64-serve", action="store_true")
     ap.add_argument("--steady-rate", type=float, default=12.0)
     ap.add_argument("--steady-requests", type=int, default=500)
-    ap.add_argument("--steady-rate-fp64", type=float, default=3.5)
-    ap.add_argument("--steady-requests-fp64", type=int, default=200)
+    ap.add_argument("--steady-rate-fp64", type=float, default=0.8)  # FP64 completes ~1.2 of these jobs/s
+    ap.add_argument("--steady-requests-fp64", type=int, default=120)
     ap.add_argument("--config", default=None,
                     help="fixed traversal configuration instead of the autotuner, as the autotuner labels it "
                          "(tile/schedule[/sD][/kP], e.g. 0/level/s2/k1)")
@@ -877,6 +884,8 @@ def main():
         run_serve(args)
     elif args.mode == "batched":
         run_batched(args)
+    elif args.mode == "branchopt":  # the DNA 16 x 1,000 all-branch optimisation alone
+        print(json.dumps({"mode": "branchopt", **branch_optimisation_dna16(args)}))
     elif args.impl == "reference":
         run_reference(args)
     else:

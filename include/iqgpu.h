@@ -33,7 +33,9 @@
  * iqgpu_set_tip_partials, iqgpu_set_patterns, ...) take a copy of the
  * caller's arrays before they return and send it in stream order, so a
  * caller may overwrite or free its buffers at once (pinned memory included)
- * while the engine's stream is still busy.
+ * while the engine's stream is still busy. (Arrays of 16 KB or more in
+ * page-locked memory are copied to the device from where they are, and the
+ * setter returns once that copy has run.)
  *
  * Partial references. A directed partial (the reference's PhyloNeighbor
  * partial_lh: the subtree at `node` seen from `dad`) is named by an int32:

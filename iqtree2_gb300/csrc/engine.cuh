@@ -178,6 +178,7 @@ struct iqgpu_engine {
     char *h_stage[2];
     size_t stage_cap, stage_used;
     int stage_cur;
+    bool stage_direct;        // a copy of this setter reads the caller's page-locked buffer directly
     cudaEvent_t stage_ev[2];
     // limit of the waits on other CTAs' progress (0 = the built-in ~seconds)
     unsigned wait_polls;

@@ -412,7 +412,16 @@ static void check_unit_tips(iqgpu_engine *e) {
 static cudaError_t stage_begin(iqgpu_engine *e) {
     e->stage_cur ^= 1;
     e->stage_used = 0;
+    e->stage_direct = false;
     return cudaEventSynchronize(e->stage_ev[e->stage_cur]);  // the half's previous copies have run
+}
+static bool page_locked(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory on older runtimes reports an error: clear it
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
 }
 static cudaError_t stage_copy(iqgpu_engine *e, void *dst, const void *src, size_t bytes) {
     const size_t off = (e->stage_used + 255) & ~(size_t)255;
@@ -420,12 +429,22 @@ static cudaError_t stage_copy(iqgpu_engine *e, void *dst, const void *src, size_
         cudaError_t err = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->st);
         return err != cudaSuccess ? err : cudaStreamSynchronize(e->st);
     }
+    if (bytes >= 16384 && page_locked(src)) {
+        // page-locked caller buffer: copied from where it is, and stage_end waits
+        // for it before the setter returns (no host copy of large arrays)
+        e->stage_direct = true;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->st);
+    }
     char *h = e->h_stage[e->stage_cur] + off;
     std::memcpy(h, src, bytes);
     e->stage_used = off + bytes;
     return cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, e->st);
 }
-static cudaError_t stage_end(iqgpu_engine *e) { return cudaEventRecord(e->stage_ev[e->stage_cur], e->st); }
+static cudaError_t stage_end(iqgpu_engine *e) {
+    cudaError_t err = cudaEventRecord(e->stage_ev[e->stage_cur], e->st);
+    if (err == cudaSuccess && e->stage_direct) err = cudaEventSynchronize(e->stage_ev[e->stage_cur]);
+    return err;
+}
 
 int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, const double *inv_evec,
                     const double *rates, const double *props) {

@@ -1,8 +1,9 @@
 """Setters copy the caller's arrays before they return.
 
 iqgpu_set_patterns / set_model / set_state_freq / set_tip_partials queue
-their copies in stream order (they do not wait for the stream), so the data
-goes through engine-owned staging first: a caller may overwrite or free its
+their copies in stream order, so the data goes through engine-owned staging
+first, or, from a page-locked buffer of 16 KB or more, is copied from where it
+is and the setter waits for that copy: a caller may overwrite or free its
 buffer as soon as the setter returns, pinned memory included (IQ-TREE
 reweights ptn_freq in place for every bootstrap replicate). The test keeps
 the stream busy with a traversal, passes pinned buffers, overwrites them at
