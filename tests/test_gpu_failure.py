@@ -1,10 +1,11 @@
 """Failure paths, made on the host or by a bounded wait that runs out.
 
-* A wait on another CTA's progress (the dataflow schedule's producer flags)
-  that gives up: with the per-engine limit set to one poll the launch stops,
-  the call returns IQGPU_ERR_TIMEOUT, and the same engine then computes the
-  right likelihood. No GPU fault is involved: every wait is bounded and a CTA
-  that gives up returns.
+* A wait on another CTA's progress (the producer flags of the 4-state
+  dataflow kernel and of the tensor-core dataflow schedules) that gives up:
+  with the per-engine limit set to one poll the launch stops, the call
+  returns IQGPU_ERR_TIMEOUT, and the same engine then computes the right
+  likelihood. No GPU fault is involved: every wait is bounded and a CTA that
+  gives up drains what it has in flight and returns.
 * IQGPU_ERR_NONFINITE, the reference's outError "Numerical underflow
   (lh-derivative) ... -safe" (tree/phylokernelnew.h:2577-2578): a pattern
   whose likelihood is exactly zero (a tip vector of zeros) makes the NORM
@@ -51,6 +52,37 @@ def test_dataflow_wait_gives_up_and_engine_stays_usable():
         assert "gave up" in str(ei.value)
         engine._check(engine.lib().iqgpu_set_wait_limit(eng.h, 0))
         assert eng.compute_likelihood(ops, *args) == want  # deterministic reductions: bit for bit
+
+
+@pytest.mark.parametrize("schedule", [6, 7])
+def test_tensor_core_dataflow_wait_gives_up_and_engine_stays_usable(schedule):
+    """The tensor-core dataflow schedules (6: category-split items, 7: whole
+    items) with a one-poll limit on their producer-flag waits: the workers of
+    an item whose producers are not done stop at the item boundary, the issuer
+    drains its copies and MMAs and frees its tensor memory, the launch reports
+    IQGPU_ERR_TIMEOUT, and the same engine then computes the lnL bit for bit."""
+    from iqtree2_gb300 import autotune
+    ds = simulate.codon_gy94_dataset(40, 3000, 36)
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    m = ds.model
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                        precision=engine.TF32X3, max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    autotune.apply(eng, (0, schedule, 2, 1))
+    u0, v0 = next((int(u), int(v)) for (u, v) in ds.edges if 0 in (int(u), int(v)))
+    nb = u0 + v0
+    ops = topo.branch_ops(nb, 0)
+    args = (topo.ref(0, nb), topo.ref(nb, 0), topo.edge_len(0, nb))
+    want = eng.compute_likelihood(ops, *args)
+    for _ in range(2):
+        engine._check(engine.lib().iqgpu_set_wait_limit(eng.h, 1))
+        with pytest.raises(engine.EngineError) as ei:
+            eng.compute_likelihood(ops, *args)
+        assert ei.value.code == TIMEOUT
+        engine._check(engine.lib().iqgpu_set_wait_limit(eng.h, 0))
+        assert eng.compute_likelihood(ops, *args) == want
 
 
 def _zero_tip_model(g):
