@@ -602,7 +602,8 @@ def run_ours(args):
         "fp64_path": None if r64 is None else {
             "value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
             "ms_per_step": r64["elapsed_ms"] / max(3, args.steps // 4),
-            "kernel": f"k_traverse_f64<{m.nstates},NORM,LNL>",
+            "kernel": ("k_traverse_f64_wide<NORM,LNL>" if m.nstates == 20 and m.ncat <= 4
+                       else f"k_traverse_f64<{m.nstates},NORM,LNL>"),
             "hbm_frac": b64 / r64["kern_avg_s"] / 1e9 / peaks["hbm_gbs"],
             "fp64_tflops": f64 / r64["kern_avg_s"] / 1e12, "fp64_peak_tflops": fp64_peak,
             "fp64_peak_source": "cuBLAS DGEMM 6144^3 measured in this run",

@@ -584,6 +584,153 @@ __global__ void __launch_bounds__(128) k_traverse_f64_lanes(const TravParams P) 
 }
 
 // ---------------------------------------------------------------------------
+// 20-state models on the FP64 drop-in, wide form: a CTA of 20 warps over 32
+// patterns, warp x computing state x of every category (lane = pattern, so
+// every global access is coalesced). k_traverse_f64's register form holds all
+// of a pattern's entries in one thread (254 registers, 8 warps per SM), and its
+// chains of dependent FP64 FMAs leave GB300's FP64 pipe about a third busy.
+// Here a CTA stages the children's entries in shared memory once per op and
+// each thread forms its entries' sums in dot_reg<20>'s order (four
+// accumulators, the same products, maxima and 2^-256 checks), so partials,
+// scale counts and lnL are identical to the register form. Binary records
+// only; the epilogue is k_traverse_f64's, run by warp 0.
+// ---------------------------------------------------------------------------
+constexpr int kWideN = 20, kWideP = 32, kWideMaxCat = 4;
+
+// dot_reg<20> with the row and the vector (stride kWideP) in shared memory
+__device__ __forceinline__ double dot_wide(const double *row, const double *v) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+    for (int i = 0; i < kWideN; i += 4) {
+        a0 = fma(row[i], v[i * kWideP], a0);
+        a1 = fma(row[i + 1], v[(i + 1) * kWideP], a1);
+        a2 = fma(row[i + 2], v[(i + 2) * kWideP], a2);
+        a3 = fma(row[i + 3], v[(i + 3) * kWideP], a3);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+
+template <bool SAFE, int EPI>
+__global__ void __launch_bounds__(kWideN * kWideP, 2) k_traverse_f64_wide(const TravParams P) {
+    constexpr int n = kWideN;
+    // [C][n][32] left entries, then the products; [C][n][32] right entries, then
+    // |entries|; [C][n][n] echild left, echild right, U^-1 of each category's class
+    extern __shared__ double wsm[];
+    __shared__ double sval[kMaxCat * kMaxStates];
+    __shared__ double scmax[kWideMaxCat][kWideP];  // per category and pattern: the largest |entry|
+    const int C = P.ncat, B = n * C;
+    const int lane = threadIdx.x & 31, x = threadIdx.x >> 5;
+    const long long p = (long long)blockIdx.x * kWideP + lane;
+    const long long ld = P.ldp;
+    const int CN32 = C * n * kWideP, CNN = C * n * n;
+    double *sL = wsm, *sR = wsm + CN32, *sM = sR;
+    double *sEL = wsm + 2 * CN32, *sER = sEL + CNN, *sU = sER + CNN;
+    const double invar = P.invar[p];
+    const long long SB = (long long)(P.state_unknown + 1) * B;
+    for (int t = threadIdx.x; t < CNN; t += blockDim.x) {  // U^-1 rows per category, once
+        const int c = t / (n * n), r = t % (n * n);
+        sU[t] = P.inv_evec[(long long)(c / P.cpc) * n * n + r];
+    }
+    for (int k = 0; k < P.nops; ++k) {
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const double *eL = P.opmats + op.mat_off, *eR = eL + CNN;
+        const double *tL = eL + 2 * CNN, *tR = tL + SB;
+        if (lref >= 0 && rref < 0) {  // put the tip on the left (tree/phylokernelnew.h:1390-1400)
+            int t = lref; lref = rref; rref = t;
+            const double *q = eL; eL = eR; eR = q;
+            q = tL; tL = tR; tR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        __syncthreads();  // the previous op's readers of the shared arrays are done
+        for (int c = 0; c < C; c++) {
+            const long long r = (long long)(c * n + x) * ld + p;
+            if (lint) sL[(c * n + x) * kWideP + lane] = P.partials[(long long)lref * P.slot_stride + r];
+            if (rint) sR[(c * n + x) * kWideP + lane] = P.partials[(long long)rref * P.slot_stride + r];
+        }
+        for (int t = threadIdx.x; t < CNN; t += blockDim.x) {
+            if (lint) sEL[t] = __ldg(eL + t);
+            if (rint) sER[t] = __ldg(eR + t);
+        }
+        __syncthreads();
+        const double *tl = lint ? nullptr : tL + (long long)P.states[(long long)(-1 - lref) * ld + p] * B;
+        const double *tr = rint ? nullptr : tR + (long long)P.states[(long long)(-1 - rref) * ld + p] * B;
+        double tmp[kWideMaxCat];
+#pragma unroll
+        for (int c = 0; c < kWideMaxCat; c++) {
+            if (c >= C) break;
+            const int row = (c * n + x) * n;
+            const double yl = lint ? dot_wide(sEL + row, sL + c * n * kWideP + lane) : __ldg(tl + c * n + x);
+            const double yr = rint ? dot_wide(sER + row, sR + c * n * kWideP + lane) : __ldg(tr + c * n + x);
+            tmp[c] = yl * yr;
+        }
+        __syncthreads();  // every read of the children's entries is done: sL takes the products
+#pragma unroll
+        for (int c = 0; c < kWideMaxCat; c++) {
+            if (c >= C) break;
+            sL[(c * n + x) * kWideP + lane] = tmp[c];
+        }
+        __syncthreads();
+        double out[kWideMaxCat];
+#pragma unroll
+        for (int c = 0; c < kWideMaxCat; c++) {
+            if (c >= C) break;
+            out[c] = dot_wide(sU + (c * n + x) * n, sL + c * n * kWideP + lane);
+            sM[(c * n + x) * kWideP + lane] = fabs(out[c]);
+        }
+        __syncthreads();
+        if (x < C) {  // warp c: category c's largest |entry| per pattern, in state order as the register form
+            double cmax = 0.0;
+            for (int xx = 0; xx < n; xx++) cmax = fmax(cmax, sM[(x * n + xx) * kWideP + lane]);
+            scmax[x][lane] = cmax;
+        }
+        __syncthreads();
+        // the category maxima (SAFE), their maximum (NORM)
+        const bool check = (lint || rint) && invar == 0.0;  // tip-tip never scales
+        double lh_max = 0.0;
+        bool scaled[kWideMaxCat];
+#pragma unroll
+        for (int c = 0; c < kWideMaxCat; c++) {
+            scaled[c] = false;
+            if (c >= C) break;
+            const double cmax = scmax[c][lane];
+            if (SAFE && check && cmax < kScaleThreshold) {
+                out[c] *= kTwoPow256;
+                scaled[c] = true;
+            }
+            lh_max = fmax(lh_max, cmax);
+        }
+        const bool scale_all = !SAFE && check && lh_max < kScaleThreshold;
+        double *dad = P.partials + (long long)op.dad_slot * P.slot_stride + p;
+#pragma unroll
+        for (int c = 0; c < kWideMaxCat; c++) {
+            if (c >= C) break;
+            dad[(long long)(c * n + x) * ld] = scale_all ? out[c] * kTwoPow256 : out[c];
+        }
+        if (x == 0) {  // scale counts: 0 (tip-tip), copy (tip-internal), sum (internal-internal), + this op's
+            uint8_t *sdad = P.scale + (long long)op.dad_slot * P.scale_stride + p;
+            if (SAFE) {
+                for (int c = 0; c < C; c++) {
+                    unsigned sc = 0;
+                    if (lint) sc += P.scale[(long long)lref * P.scale_stride + (long long)c * ld + p];
+                    if (rint) sc += P.scale[(long long)rref * P.scale_stride + (long long)c * ld + p];
+                    sdad[(long long)c * ld] = (uint8_t)(sc + (scaled[c] ? 1u : 0u));
+                }
+            } else {
+                unsigned sc = 0;
+                if (lint) sc += P.scale[(long long)lref * P.scale_stride + p];
+                if (rint) sc += P.scale[(long long)rref * P.scale_stride + p];
+                sdad[0] = (uint8_t)(sc + (scale_all ? 1u : 0u));
+            }
+        }
+    }
+    if constexpr (EPI != EPI_NONE) {
+        __syncthreads();  // the last op's entries, written by every warp, are visible to warp 0
+        f64_epilogue<kWideN, SAFE, EPI>(P, p, invar, sval, x == 0);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // non-reversible models on the FP64 path (tree/phylokernelnonrev.h): the
 // partials stay in the standard basis. echild is P(r_c t) itself (P^T for a
 // child reached against the edge direction) and the traversal runs with
@@ -1074,8 +1221,27 @@ static bool use_lanes(const iqgpu_engine *e, const TravParams &P) {
     return e->n == 4 && e->C <= 8 && !e->nonrev && !e->has_multi && !P.cat_split && e->nblk < e->sms;
 }
 
+// 20-state models: the wide kernel (see above)
+template <bool SAFE, int EPI>
+static int launch_wide_t(iqgpu_engine *e, const TravParams &P) {
+    const size_t smem = ((size_t)2 * e->C * kWideN * kWideP + (size_t)3 * e->C * kWideN * kWideN) * sizeof(double);
+    auto kern = k_traverse_f64_wide<SAFE, EPI>;
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_f64_wide smem attribute");
+    }
+    kern<<<(unsigned)(e->Ppad / kWideP), kWideN * kWideP, smem, e->st>>>(P);
+    e->launches++;
+    return cuda_fail(cudaGetLastError(), "traverse_f64_wide");
+}
+
+static bool use_wide(const iqgpu_engine *e, const TravParams &P) {
+    return e->n == kWideN && e->C <= kWideMaxCat && !e->nonrev && !e->has_multi && !P.cat_split;
+}
+
 template <bool SAFE, int EPI>
 static int dispatch_n(iqgpu_engine *e, const TravParams &P) {
+    if (use_wide(e, P)) return launch_wide_t<SAFE, EPI>(e, P);
     if (use_lanes(e, P)) {
         switch (e->C) {
         case 1: return launch_lanes_t<SAFE, EPI, 4>(e, P);
