@@ -1217,6 +1217,8 @@ static int launch_lanes_t(iqgpu_engine *e, const TravParams &P) {
     return cuda_fail(cudaGetLastError(), "traverse_f64_lanes");
 }
 
+// (at full size, 87,306 DNA patterns, the lane kernel measured 16.1 ms per
+// evaluation against 13.7 ms for the pattern kernel: it is for short alignments)
 static bool use_lanes(const iqgpu_engine *e, const TravParams &P) {
     return e->n == 4 && e->C <= 8 && !e->nonrev && !e->has_multi && !P.cat_split && e->nblk < e->sms;
 }
