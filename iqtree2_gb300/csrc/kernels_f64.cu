@@ -731,6 +731,115 @@ __global__ void __launch_bounds__(kWideN * kWideP, 2) k_traverse_f64_wide(const 
 }
 
 // ---------------------------------------------------------------------------
+// SAFE walks for large state counts (codon: 21..64 states), one category per
+// CTA: SAFE checks the 2^-256 threshold per category, so a category's update
+// needs nothing from the others. A CTA of 16 warps over 32 patterns (lane =
+// pattern); warp w computes states w, w + 16, w + 32, w + 48 of category
+// blockIdx.y. Per op the CTA stages the category's child entries and both
+// echild blocks in shared memory (U^-1 of the category's class once per
+// launch), and each entry's sums run in the generic register-free path's
+// order (one accumulator, i = 0 .. n-1), with its maximum, check and scale
+// counts, so partials and scale counts are identical to it. The generic path
+// kept a pattern's whole category in one thread (6 warps per SM on codon 40 x
+// 10,000); here each of those sums has a thread of its own. Binary records
+// only; the epilogue runs as its own launch afterwards.
+// ---------------------------------------------------------------------------
+constexpr int kCatWarps = 16, kCatP = 32, kCatMaxN = 64, kCatPer = kCatMaxN / kCatWarps;
+
+__device__ __forceinline__ double dot_seq(const double *row, const double *v, int n) {
+    double a = 0.0;
+    for (int i = 0; i < n; i++) a = fma(row[i], v[i * kCatP], a);
+    return a;
+}
+
+__global__ void __launch_bounds__(kCatWarps * kCatP, 1) k_traverse_f64_cat(const TravParams P) {
+    // [n][32] left entries, then the products; [n][32] right entries; [n][n]
+    // echild left, echild right, U^-1 of the category's class
+    extern __shared__ double csm[];
+    __shared__ double scm[kCatWarps][kCatP];
+    const int n = P.n, C = P.ncat, B = n * C, c = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long p = (long long)blockIdx.x * kCatP + lane;
+    const long long ld = P.ldp;
+    const int N32 = n * kCatP, NN = n * n;
+    double *sL = csm, *sR = csm + N32, *sEL = csm + 2 * N32, *sER = sEL + NN, *sU = sER + NN;
+    const double invar = P.invar[p];
+    const long long CNN = (long long)C * n * n;
+    const long long SB = (long long)(P.state_unknown + 1) * B;
+    for (int t = threadIdx.x; t < NN; t += blockDim.x) sU[t] = P.inv_evec[(long long)(c / P.cpc) * NN + t];
+    for (int k = 0; k < P.nops; ++k) {
+        const OpDev op = P.ops[k];
+        int lref = op.child[0], rref = op.child[1];
+        const double *eL = P.opmats + op.mat_off, *eR = eL + CNN;
+        const double *tL = eL + 2 * CNN, *tR = tL + SB;
+        if (lref >= 0 && rref < 0) {  // put the tip on the left (tree/phylokernelnew.h:1390-1400)
+            int t = lref; lref = rref; rref = t;
+            const double *q = eL; eL = eR; eR = q;
+            q = tL; tL = tR; tR = q;
+        }
+        const bool lint = lref >= 0, rint = rref >= 0;
+        __syncthreads();  // the previous op's readers of the shared arrays are done
+        for (int j = 0; j < kCatPer; j++) {
+            const int x = w + j * kCatWarps;
+            if (x >= n) break;
+            const long long r = (long long)(c * n + x) * ld + p;
+            if (lint) sL[x * kCatP + lane] = P.partials[(long long)lref * P.slot_stride + r];
+            if (rint) sR[x * kCatP + lane] = P.partials[(long long)rref * P.slot_stride + r];
+        }
+        for (int t = threadIdx.x; t < NN; t += blockDim.x) {
+            if (lint) sEL[t] = __ldg(eL + (long long)c * NN + t);
+            if (rint) sER[t] = __ldg(eR + (long long)c * NN + t);
+        }
+        __syncthreads();
+        const double *tl = lint ? nullptr : tL + (long long)P.states[(long long)(-1 - lref) * ld + p] * B + c * n;
+        const double *tr = rint ? nullptr : tR + (long long)P.states[(long long)(-1 - rref) * ld + p] * B + c * n;
+        double v[kCatPer];
+#pragma unroll
+        for (int j = 0; j < kCatPer; j++) {
+            const int x = w + j * kCatWarps;
+            v[j] = 0.0;
+            if (x >= n) continue;
+            const double yl = lint ? dot_seq(sEL + x * n, sL + lane, n) : __ldg(tl + x);
+            const double yr = rint ? dot_seq(sER + x * n, sR + lane, n) : __ldg(tr + x);
+            v[j] = yl * yr;
+        }
+        __syncthreads();  // every read of the children's entries is done: sL takes the products
+#pragma unroll
+        for (int j = 0; j < kCatPer; j++) {
+            const int x = w + j * kCatWarps;
+            if (x < n) sL[x * kCatP + lane] = v[j];
+        }
+        __syncthreads();
+        double m = 0.0;
+#pragma unroll
+        for (int j = 0; j < kCatPer; j++) {
+            const int x = w + j * kCatWarps;
+            if (x >= n) continue;
+            v[j] = dot_seq(sU + x * n, sL + lane, n);
+            m = fmax(m, fabs(v[j]));
+        }
+        scm[w][lane] = m;
+        __syncthreads();
+        double cmax = 0.0;  // the category's largest |entry| for this pattern
+        for (int ww = 0; ww < kCatWarps; ww++) cmax = fmax(cmax, scm[ww][lane]);
+        const bool check = (lint || rint) && invar == 0.0;  // tip-tip never scales
+        const bool scaled = check && cmax < kScaleThreshold;
+        double *dad = P.partials + (long long)op.dad_slot * P.slot_stride + p;
+#pragma unroll
+        for (int j = 0; j < kCatPer; j++) {
+            const int x = w + j * kCatWarps;
+            if (x < n) dad[(long long)(c * n + x) * ld] = scaled ? v[j] * kTwoPow256 : v[j];
+        }
+        if (w == 0) {  // this category's scale count: the children's (uint8 sum) plus this op's
+            unsigned sc = 0;
+            if (lint) sc += P.scale[(long long)lref * P.scale_stride + (long long)c * ld + p];
+            if (rint) sc += P.scale[(long long)rref * P.scale_stride + (long long)c * ld + p];
+            P.scale[(long long)op.dad_slot * P.scale_stride + (long long)c * ld + p] = (uint8_t)(sc + (scaled ? 1u : 0u));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // non-reversible models on the FP64 path (tree/phylokernelnonrev.h): the
 // partials stay in the standard basis. echild is P(r_c t) itself (P^T for a
 // child reached against the edge direction) and the traversal runs with
@@ -1272,7 +1381,18 @@ int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b
     if (nops == 0 && epi == EPI_NONE) return IQGPU_OK;
     // SAFE op walks over too few pattern tiles to fill the GPU (codon, short
     // alignments): one CTA per (tile, category), then the epilogue on its own
-    if (e->cfg.safe && !e->nonrev && !e->has_multi && nops > 0 && e->C > 1 && e->nblk < 2 * e->sms) {
+    // Large state counts in SAFE: the per-category kernel for the walk, any size
+    if (e->cfg.safe && !e->nonrev && !e->has_multi && nops > 0 && e->n > 20 && e->n <= kCatMaxN) {
+        const size_t smem = ((size_t)2 * e->n * kCatP + (size_t)3 * e->n * e->n) * sizeof(double);
+        cudaError_t err = cudaFuncSetAttribute(k_traverse_f64_cat, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_f64_cat smem attribute");
+        k_traverse_f64_cat<<<dim3((unsigned)(e->Ppad / kCatP), e->C), kCatWarps * kCatP, smem, e->st>>>(P);
+        e->launches++;
+        if ((err = cudaGetLastError()) != cudaSuccess) return cuda_fail(err, "traverse_f64_cat");
+        if (epi == EPI_NONE) return IQGPU_OK;
+        P.nops = 0;
+    } else if (e->cfg.safe && !e->nonrev && !e->has_multi && nops > 0 && e->C > 1 && e->nblk < 2 * e->sms) {
         P.cat_split = 1;
         int rc = dispatch_safe<EPI_NONE>(e, P);
         if (rc || epi == EPI_NONE) return rc;
