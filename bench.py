@@ -603,6 +603,7 @@ def run_ours(args):
             "value": updates_per_step * max(3, args.steps // 4) / (r64["elapsed_ms"] / 1e3),
             "ms_per_step": r64["elapsed_ms"] / max(3, args.steps // 4),
             "kernel": ("k_traverse_f64_wide<NORM,LNL>" if m.nstates == 20 and m.ncat <= 4
+                       else "k_traverse_f64_cat (SAFE walk) + k_traverse_f64 epilogue" if m.nstates > 20
                        else f"k_traverse_f64<{m.nstates},NORM,LNL>"),
             "hbm_frac": b64 / r64["kern_avg_s"] / 1e9 / peaks["hbm_gbs"],
             "fp64_tflops": f64 / r64["kern_avg_s"] / 1e12, "fp64_peak_tflops": fp64_peak,
