@@ -355,7 +355,10 @@ static int create_engine(const iqgpu_config *cfg_in, void *dev_mem, size_t dev_b
     CKE(halloc(e, &e->h_asc, 3 * kMaxStates * 8));
     // setter staging: the largest single setter payload (pattern weights, or
     // the model arrays) per half
-    e->stage_cap = (size_t)std::max<long long>(2 * e->Ppad * 8, (n + 2 * n * n + 2 * C + (S + 2) * n) * 8 + 1024);
+    // (+ the FP32 arrays the mixed setters build: U^-1 padded, its hi/lo split, the tip vectors' hi/lo)
+    e->stage_cap = (size_t)std::max<long long>(2 * e->Ppad * 8, (n + 2 * n * n + 2 * C + (S + 2) * n) * 8 + 1024 +
+                                                                    (2 * n * n + n * (n + 3) + 2 * (S + 1) * n) * 4 +
+                                                                    4 * 256);
     CKE(halloc(e, &e->h_stage[0], (long long)e->stage_cap));
     CKE(halloc(e, &e->h_stage[1], (long long)e->stage_cap));
     CKE(cudaEventCreateWithFlags(&e->stage_ev[0], cudaEventDisableTiming));
@@ -390,14 +393,6 @@ int iqgpu_get_config(const iqgpu_engine *e, iqgpu_config *out) {
 
 // FP64 values as FP32 pairs hi = fl(v), lo = fl(v - hi) ([hi x count][lo x count]),
 // the split the double-float precompute multiplies with
-static cudaError_t upload_hilo(float *dst, const double *v, size_t count, cudaStream_t st) {
-    std::vector<float> hl(2 * count);
-    for (size_t i = 0; i < count; i++) {
-        hl[i] = (float)v[i];
-        hl[count + i] = (float)(v[i] - (double)hl[i]);
-    }
-    return cudaMemcpyAsync(dst, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice, st);
-}
 
 static void check_unit_tips(iqgpu_engine *e) {
     e->unit_tips = e->have_model && e->have_tips;
@@ -440,6 +435,38 @@ static cudaError_t stage_copy(iqgpu_engine *e, void *dst, const void *src, size_
     e->stage_used = off + bytes;
     return cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, e->st);
 }
+// An array built on the host (FP32 conversions of the caller's data) goes
+// out from the staging half too: page-locked, so the copy is queued without
+// the wait a pageable copy would take.
+static float *stage_floats(iqgpu_engine *e, size_t count) {
+    const size_t off = (e->stage_used + 255) & ~(size_t)255;
+    if (off + count * 4 > e->stage_cap) return nullptr;
+    e->stage_used = off + count * 4;
+    return reinterpret_cast<float *>(e->h_stage[e->stage_cur] + off);
+}
+static cudaError_t stage_send(iqgpu_engine *e, float *dst, const std::vector<float> &tmp, float *h, size_t count) {
+    if (!h) {  // beyond the half: in stream order from the temporary, which must outlive the copy
+        cudaError_t err = cudaMemcpyAsync(dst, tmp.data(), count * 4, cudaMemcpyHostToDevice, e->st);
+        return err != cudaSuccess ? err : cudaStreamSynchronize(e->st);
+    }
+    return cudaMemcpyAsync(dst, h, count * 4, cudaMemcpyHostToDevice, e->st);
+}
+// hi = (float)v, lo = (float)(v - hi): the double-float operand of the mixed precompute
+static cudaError_t upload_hilo(iqgpu_engine *e, float *dst, const double *v, size_t count) {
+    std::vector<float> tmp;
+    float *h = stage_floats(e, 2 * count);
+    if (!h) {
+        tmp.resize(2 * count);
+        h = nullptr;
+    }
+    float *o = h ? h : tmp.data();
+    for (size_t i = 0; i < count; i++) {
+        o[i] = (float)v[i];
+        o[count + i] = (float)(v[i] - (double)o[i]);
+    }
+    return stage_send(e, dst, tmp, h, 2 * count);
+}
+
 static cudaError_t stage_end(iqgpu_engine *e) {
     cudaError_t err = cudaEventRecord(e->stage_ev[e->stage_cur], e->st);
     if (err == cudaSuccess && e->stage_direct) err = cudaEventSynchronize(e->stage_ev[e->stage_cur]);
@@ -457,21 +484,25 @@ int iqgpu_set_model(iqgpu_engine *e, const double *eval, const double *evec, con
     CK(stage_copy(e, e->d_inv, inv_evec, n * n * 8));
     CK(stage_copy(e, e->d_rates, rates, C * 8));
     CK(stage_copy(e, e->d_props, props, C * 8));
+    if (is_mixed(&e->cfg)) {
+        // FP32 copy of U^-1, rows padded to npad, after the op matrix blocks
+        const size_t cnt = (size_t)n * e->npad;
+        std::vector<float> tmp;
+        float *h = stage_floats(e, cnt);
+        if (!h) tmp.resize(cnt);
+        float *o = h ? h : tmp.data();
+        for (size_t i = 0; i < n; i++)
+            for (size_t j = 0; j < (size_t)e->npad; j++) o[i * e->npad + j] = j < n ? (float)inv_evec[i * n + j] : 0.f;
+        float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
+        CK(stage_send(e, dst, tmp, h, cnt));
+        if (e->d_ivhl) CK(upload_hilo(e, e->d_ivhl, inv_evec, n * n));
+    }
     CK(stage_end(e));
     std::memcpy(e->h_eval, eval, n * 8);
     std::memcpy(e->h_rates, rates, C * 8);
     std::memcpy(e->h_props, props, C * 8);
     std::memcpy(e->h_evec, evec, n * n * 8);
     std::memcpy(e->h_inv, inv_evec, n * n * 8);
-    if (is_mixed(&e->cfg)) {
-        // FP32 copy of U^-1, rows padded to npad, after the op matrix blocks
-        std::vector<float> inv32((size_t)n * e->npad, 0.f);
-        for (size_t i = 0; i < n; i++)
-            for (size_t j = 0; j < n; j++) inv32[i * e->npad + j] = (float)inv_evec[i * n + j];
-        float *dst = e->d_opmats32 + (long long)(e->cfg.max_ops + 1) * e->op_stride32;
-        CK(cudaMemcpyAsync(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice, e->st));
-        if (e->d_ivhl) CK(upload_hilo(e->d_ivhl, inv_evec, n * n, e->st));
-    }
     e->have_model = true;
     e->theta_valid = false;
     if (e->nonrev) {  // back to a reversible model: its tip vectors must be set again
@@ -517,8 +548,10 @@ int iqgpu_set_mixture(iqgpu_engine *e, int32_t nmix, const double *eval, const d
         CK(cudaMemcpy(dst, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice));
     }
     if (mixed && e->d_ivhl) {
-        for (size_t m = 0; m < K; m++) CK(upload_hilo(e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n, e->st));
-        CK(upload_hilo(e->d_tiphl, tip_lh, S1 * K * n, e->st));
+        CK(stage_begin(e));
+        for (size_t m = 0; m < K; m++) CK(upload_hilo(e, e->d_ivhl + m * 2 * n * n, inv_evec + m * n * n, n * n));
+        CK(upload_hilo(e, e->d_tiphl, tip_lh, S1 * K * n));
+        CK(stage_end(e));
     }
     // leaf-table shortcut: every class's unambiguous tip vectors are columns of its U^-1
     bool unit = true;
@@ -600,8 +633,8 @@ int iqgpu_set_tip_partials(iqgpu_engine *e, const double *tip_lh) {
     CK(cudaSetDevice(e->dev));
     CK(stage_begin(e));
     CK(stage_copy(e, e->d_tip, tip_lh, (size_t)(e->S + 1) * e->n * 8));
+    if (e->d_tiphl) CK(upload_hilo(e, e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n));
     CK(stage_end(e));
-    if (e->d_tiphl) CK(upload_hilo(e->d_tiphl, tip_lh, (size_t)(e->S + 1) * e->n, e->st));
     std::memcpy(e->h_tipv, tip_lh, (size_t)e->n * e->n * 8);
     e->have_tips = true;
     check_unit_tips(e);
