@@ -1309,7 +1309,7 @@ static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
     size_t smem = (REG ? 0 : (size_t)kMaxStates * tpb * sizeof(double)) +
                   (EPI == EPI_LNL ? (size_t)kMaxCat * kMaxStates * sizeof(double) : 0);
     auto kern = k_traverse_f64<NT, SAFE, EPI>;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {  // static arrays count against the 48 KB default too
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "traverse_f64 smem attribute");
     }
@@ -1337,10 +1337,9 @@ template <bool SAFE, int EPI>
 static int launch_wide_t(iqgpu_engine *e, const TravParams &P) {
     const size_t smem = ((size_t)2 * e->C * kWideN * kWideP + (size_t)3 * e->C * kWideN * kWideN) * sizeof(double);
     auto kern = k_traverse_f64_wide<SAFE, EPI>;
-    if (smem > 48 * 1024) {
-        cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (err != cudaSuccess) return cuda_fail(err, "traverse_f64_wide smem attribute");
-    }
+    // (always: with its static arrays even 2 categories pass the 48 KB default)
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_f64_wide smem attribute");
     kern<<<(unsigned)(e->Ppad / kWideP), kWideN * kWideP, smem, e->st>>>(P);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "traverse_f64_wide");

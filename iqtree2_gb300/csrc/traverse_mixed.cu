@@ -751,7 +751,7 @@ static int launch_mix_t(iqgpu_engine *e, const MixParams &P) {
     // an epilogue-only launch stages no P(t): no dynamic shared memory, full occupancy
     const size_t smem = P.nops > 0 ? nbuf * pm_bytes : 0;
     auto kern = k_traverse_mixed<NQ, EPI>;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {  // static arrays count against the 48 KB default too
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "traverse_mixed smem attribute");
     }
@@ -768,7 +768,8 @@ static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
     const size_t smem = P.nops > 0 ? (size_t)2 * 2 * e->C * e->n * e->npad * 4 : 0;  // double-buffered P(t) of one op
     auto kern = k_chain_mixed<NQ, EPI>;
     cudaError_t err = cudaSuccess;
-    if (smem > 48 * 1024) err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 0)  // static arrays count against the 48 KB default too
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return cuda_fail(err, "chain_mixed smem attribute");
     int sms = 1, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
@@ -790,7 +791,7 @@ static int launch_levels_t(iqgpu_engine *e, const MixParams &P, int l0 = 0) {
     const int grid = (int)(e->Ppad / TP);
     const size_t smem = (size_t)2 * e->C * e->n * e->npad * 4;
     auto kern = k_level_mixed<NQ>;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {  // static arrays count against the 48 KB default too
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return cuda_fail(err, "level_mixed smem attribute");
     }

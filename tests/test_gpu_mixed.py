@@ -123,3 +123,30 @@ def test_mixed_full_size_configs(oracle_mod, kind):
     err = rel(lg, lo)
     print(f"{kind}: mixed lnL {lg:.6f} oracle {lo:.6f} rel err {err:.2e}")
     assert err < LNL_RTOL
+
+
+@pytest.mark.parametrize("kind,ncat,schedule", [("codon", 3, 1), ("protein", 7, 0), ("protein", 7, 1),
+                                                ("protein", 8, 0), ("codon", 1, 0)])
+def test_mixed_category_counts_and_shared_memory(oracle_mod, kind, ncat, schedule):
+    """Category counts whose P(t) staging sits just under the 48 KB default of
+    dynamic shared memory while the kernel's static arrays push it over
+    (codon x 3 categories on the level kernel, protein x 7 on the fused one):
+    the launchers raise the limit whenever they stage, and the lnL matches the
+    oracle."""
+    import dataclasses
+    from iqtree2_gb300 import autotune, models
+    ds = (simulate.codon_gy94_dataset(12, 300, 91) if kind == "codon" else simulate.protein_lg_dataset(16, 600, 92))
+    rates, props = models.gamma_rates_mean(0.6, ncat)
+    m = dataclasses.replace(ds.model, rates=np.asarray(rates, np.float64), props=np.asarray(props, np.float64))
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots, precision=engine.F32,
+                        max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    autotune.apply(eng, (32, schedule, 0, 0))
+    leaf, nb = 0, topo.adj[0][0][0]
+    lg = eng.compute_likelihood(topo.branch_ops(nb, leaf), topo.ref(leaf, nb), topo.ref(nb, leaf),
+                                topo.edge_len(leaf, nb))
+    lo = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    assert rel(lg, lo) < LNL_RTOL, (lg, lo)
