@@ -334,3 +334,33 @@ def test_bf16_schedules_agree(oracle_mod, kind):
         err = rel(v, want)
         print(f"{kind}: bf16 lnL rel err {err:.2e}")
         assert err < BF16_LNL_RTOL
+
+
+@pytest.mark.parametrize("kind,ncat", [("protein", 1), ("protein", 3), ("protein", 8), ("codon", 1), ("codon", 3)])
+def test_tc_category_counts_every_schedule(oracle_mod, kind, ncat):
+    """Odd and single category counts on every tensor-core candidate (the
+    accumulators alternate by category parity; category-split items with one
+    category; the dataflow schedules): lnL within 1e-6 of the FP64 oracle,
+    and every codon candidate bit-identical (every op on the tensor cores)."""
+    import dataclasses
+    from iqtree2_gb300 import models
+    ds = (simulate.protein_lg_dataset(30, 900, 93) if kind == "protein" else simulate.codon_gy94_dataset(14, 400, 94))
+    rates, props = models.gamma_rates_mean(0.6, ncat)
+    m = dataclasses.replace(ds.model, rates=np.asarray(rates, np.float64), props=np.asarray(props, np.float64))
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                        precision=engine.TF32X3, max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    got = {}
+    for cand in autotune.candidates(eng):
+        autotune.apply(eng, cand)
+        got[cand] = eng.compute_likelihood(ops, a, b, length)
+        assert rel(got[cand], want) < LNL_RTOL, (cand, got[cand], want)
+    if kind == "codon":
+        assert len(set(got.values())) == 1, got
