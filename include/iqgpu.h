@@ -325,8 +325,11 @@ int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 int iqgpu_set_stages(iqgpu_engine *e, int32_t stages);
 /* K pieces per copied stage of the tensor-core traversal: 0/1 = a stage
  * carries a category's whole K; 2 = halves (61-state models: half the shared
- * memory per stage, two CTAs per SM instead of one). Ignored where K does not
- * split evenly. Chosen by the autotuner; results do not depend on it. */
+ * memory per stage, two CTAs per SM instead of one); 4 = quarters with one
+ * accumulator buffer per CTA (61-state models on schedule 6: a quarter of the
+ * shared memory per stage and half the tensor memory, four CTAs per SM).
+ * Ignored where K does not split evenly. Chosen by the autotuner; results do
+ * not depend on it. */
 int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces);
 int iqgpu_get_timing(iqgpu_engine *e, double *total_ms, int64_t *launches);
 /* Failure detection (no counterpart in the reference, whose kernels cannot

@@ -36,6 +36,8 @@ def candidates(eng):
         if npad <= 32:  # category-split narrow levels on the tensor cores
             out += [(0, 5, st, 1) for st in (2, 3)]
         out += [(0, 6, st, kp) for st in (2, 3) for kp in pieces]  # dataflow, category-split items
+        if npad > 32 and npad % 16 == 0:  # ... with K in quarters and one accumulator buffer
+            out += [(0, 6, st, 4) for st in (2, 3)]
         out += [(0, 7, 2, kp) for kp in pieces]  # dataflow, whole (op, tile) items
         if npad == 20 and getattr(eng, "precision", 0) == 2:  # split TF32
             out.append((0, 4, 0, 0))

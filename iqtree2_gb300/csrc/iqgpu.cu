@@ -1386,8 +1386,8 @@ int iqgpu_set_stages(iqgpu_engine *e, int32_t stages) {
 }
 
 int iqgpu_set_kpieces(iqgpu_engine *e, int32_t pieces) {
-    if (!e || pieces < 0 || pieces > 2) {
-        set_error("pieces must be 0, 1 or 2");
+    if (!e || pieces < 0 || pieces > 4 || pieces == 3) {
+        set_error("pieces must be 0, 1, 2 or 4");
         return IQGPU_ERR_ARG;
     }
     e->tc_kpieces = pieces;

@@ -457,8 +457,10 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 //    once the workers have read out the category that last used the same
 //    accumulator buffer (epi_done counter, release/acquire in shared memory).
 // Categories are numbered g = item * CI + c over the CTA's items (CI = ncat
-// categories per item, or 1 for category-split items); buffer g & 1 holds
-// category g. Workers synchronise among themselves only with a 128-thread
+// categories per item, or 1 for category-split items); buffer g % NACC holds
+// category g (NACC = 2; NACC = 1 halves the tensor memory of a CTA, for
+// category-split items only, which read out each item before the next one's
+// MMAs start). Workers synchronise among themselves only with a 128-thread
 // named barrier per category epilogue. Every wait is bounded; a wait that
 // gives up raises the shared abort flag and the status word.
 // csplit: items are (tile, op, category) triples (narrow levels: ncat times
@@ -480,11 +482,14 @@ __global__ void __launch_bounds__(kTcRows, 1) k_traverse_tc(const __grid_constan
 // the residency; the waits are bounded all the same.
 constexpr int kFlowFifo = 8;  // item ids between the issuer and the workers
 
-template <int NP, int NSTAGE, bool BF, bool CSPLIT, bool FLOW = false>
+template <int NP, int NSTAGE, bool BF, bool CSPLIT, bool FLOW = false, int NACC = 2>
 __global__ void __launch_bounds__(kTcRows + 32, 4)
     k_traverse_tc_ws(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl,
                      float *__restrict__ cmax_out, unsigned *__restrict__ pair_cnt,
                      unsigned *__restrict__ flow_done, unsigned *__restrict__ ticket, const unsigned epoch) {
+    static_assert(NACC == 2 || (NACC == 1 && CSPLIT),
+                  "one accumulator buffer needs category-split items: a whole item converts category g's "
+                  "stages before reading out g - 1, which a single buffer would stall");
     constexpr bool csplit = CSPLIT;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad, kq = T.kq;
@@ -537,7 +542,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
         fence_mbar_init();
     }
     if (warp == 0) {
-        tmem_alloc(smem_u32(&tmem_base_s), 4 * NP);
+        tmem_alloc(smem_u32(&tmem_base_s), NACC * 2 * NP);
         tmem_relinquish();
     }
     fence_proxy_async_smem();
@@ -647,12 +652,12 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     const int g = mi * CI + (csplit ? 0 : c);
                     const bool first = sk == 0, last = sk == per * ksplit - 1;
                     if (mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
-                        (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
+                        (!first || g < NACC || ld_acquire_cta(&epi_done) >= (unsigned)(g - NACC + 1))) {
                         tc_fence_after();
-                        const unsigned d = tmem + (unsigned)((g & 1) * 2 * NP + side * NP);
+                        const unsigned d = tmem + (unsigned)((g % NACC) * 2 * NP + side * NP);
                         tc_stage_mmas<NP, BF>(T, d, slot_at(s), kh);
                         mma_commit(&mmab[s]);
-                        if (last) mma_commit(&ebar[g & 1]);
+                        if (last) mma_commit(&ebar[g % NACC]);
                         mdone++;
                         if (++ms >= tc_nstages(mit, C, ksplit)) {
                             mi++;
@@ -725,12 +730,12 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     const int g = mi * CI + (csplit ? 0 : c);
                     const bool first = sk == 0, last = sk == per * ksplit - 1;
                     if (mdone < issued && mbar_test(&conv[s], (unsigned)((mdone / NSTAGE) & 1)) &&
-                        (!first || g < 2 || ld_acquire_cta(&epi_done) >= (unsigned)(g - 1))) {
+                        (!first || g < NACC || ld_acquire_cta(&epi_done) >= (unsigned)(g - NACC + 1))) {
                         tc_fence_after();
-                        const unsigned d = tmem + (unsigned)((g & 1) * 2 * NP + side * NP);
+                        const unsigned d = tmem + (unsigned)((g % NACC) * 2 * NP + side * NP);
                         tc_stage_mmas<NP, BF>(T, d, slot_at(s), kh);
                         mma_commit(&mmab[s]);
-                        if (last) mma_commit(&ebar[g & 1]);
+                        if (last) mma_commit(&ebar[g % NACC]);
                         mdone++;
                         ms++;
                         skip(mi, ms, mit);
@@ -757,7 +762,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
         // ---------------- workers ----------------
         const int r = tid;
         const unsigned lane_off = (unsigned)(warp * 32) << 16;
-        int consumed = 0, ecount0 = 0, ecount1 = 0;
+        int consumed = 0, ecount[2] = {0, 0};  // commits made to ebar[0], ebar[1]
         bool abort = false;
         auto epilogue = [&](const TcItem &it, int c, int g, float *dad, long long p, const float *TL, int sl, int sr,
                             float &cmax) -> bool {
@@ -766,12 +771,12 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
             const float *tr = it.rint ? nullptr : TL + (it.lch ? -TB : TB) + (long long)sr * C * npad + c * npad;
             bool ok = !*(volatile unsigned *)&abort_flag;
             if (per > 0 && ok) {
-                const int ec = (g & 1) ? ecount1 : ecount0;
-                ok = mbar_wait(&ebar[g & 1], (unsigned)((ec - 1) & 1), kWaitPolls);
+                const int ec = ecount[g % NACC];
+                ok = mbar_wait(&ebar[g % NACC], (unsigned)((ec - 1) & 1), kWaitPolls);
             }
             if (bar_or_part(kTcRows, !ok)) return false;  // uniform stop for every worker
             if (per > 0) tc_fence_after();
-            const unsigned dL = tmem + lane_off + (unsigned)((g & 1) * 2 * NP), dR = dL + NP;
+            const unsigned dL = tmem + lane_off + (unsigned)((g % NACC) * 2 * NP), dR = dL + NP;
             float *out = dad + (p >> 3) * (8LL * C * npad) + (p & 7) * 4 + (long long)c * kq * 32;
             for (int q = 0; q < kq; q++) {
                 float lv[4], rv[4];
@@ -794,7 +799,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                 }
                 *reinterpret_cast<float4 *>(out + q * 32) = make_float4(o[0], o[1], o[2], o[3]);
             }
-            // every worker has read its row of buffer g & 1: the issuer may reuse it
+            // every worker has read its row of buffer g % NACC: the issuer may reuse it
             tc_fence_before();
             bar_sync_part(kTcRows);
             if (r == 0) st_release_cta(&epi_done, (unsigned)(g + 1));
@@ -861,10 +866,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
                     consumed++;
                 }
                 if (abort) break;
-                if (per > 0) {  // category g's last stage commits ebar[g & 1]
-                    if (g & 1) ecount1++;
-                    else ecount0++;
-                }
+                if (per > 0) ecount[g % NACC]++;  // category g's last stage commits ebar[g % NACC]
                 if (cc > 0 && !epilogue(it, c - 1, g - 1, dad, p, TL, sl, sr, cmax)) { abort = true; break; }
             }
             if (abort) break;
@@ -947,7 +949,7 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 4 * NP);
+    if (warp == 0) tmem_dealloc(tmem, NACC * 2 * NP);
 }
 
 // ---------------------------------------------------------------------------
@@ -1333,7 +1335,8 @@ int tc_kp(int npad) { return (npad + 7) / 8 * 8; }
 // (two 61-state CTAs per SM instead of one) at twice the stages per op; needs
 // npad > 32 and a multiple of 16.
 int tc_ksplit(const iqgpu_engine *e) {
-    return (e->tc_kpieces == 2 && e->npad > 32 && e->npad % 16 == 0) ? 2 : 1;
+    if (e->npad <= 32 || e->npad % 16 != 0) return 1;
+    return e->tc_kpieces == 4 ? 4 : e->tc_kpieces == 2 ? 2 : 1;
 }
 
 int launch_tc_prep(iqgpu_engine *e, int nops) {
@@ -1422,7 +1425,7 @@ static size_t tc_smem_bytes(const TcParams &T, int nstage) {
     return (size_t)nstage * T.slot_bytes + 128;  // + alignment spare
 }
 
-template <int NP, int NSTAGE, bool BF>
+template <int NP, int NSTAGE, bool BF, int NACC = 2>
 static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     int rc = tc_tensor_map(e);
     if (rc) return rc;
@@ -1432,7 +1435,7 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     auto kern = k_traverse_tc<NP, NSTAGE, BF>;
     auto kern_ws = k_traverse_tc_ws<NP, NSTAGE, BF, false>;
     auto kern_ws_cs = k_traverse_tc_ws<NP, NSTAGE, BF, true>;
-    auto kern_flow = k_traverse_tc_ws<NP, NSTAGE, BF, true, true>;
+    auto kern_flow = k_traverse_tc_ws<NP, NSTAGE, BF, true, true, NACC>;
     auto kern_flow_whole = k_traverse_tc_ws<NP, NSTAGE, BF, false, true>;
     const bool split_ok = NP == 64 || e->tc_split;  // 61 states always; fewer states with schedule 5
     const bool ws = e->level_sync && (e->tc_ws || e->tc_tm);  // warp-specialised level kernel
@@ -1466,12 +1469,13 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
     cudaFuncAttributes fa;
     size_t stat = 0;
     int regs = 0;
-    if ((ws ? cudaFuncGetAttributes(&fa, kern_ws) : cudaFuncGetAttributes(&fa, kern)) == cudaSuccess) {
+    if ((NACC == 1 ? cudaFuncGetAttributes(&fa, kern_flow)
+                   : ws ? cudaFuncGetAttributes(&fa, kern_ws) : cudaFuncGetAttributes(&fa, kern)) == cudaSuccess) {
         stat = fa.sharedSizeBytes;
         regs = fa.numRegs;
     }
     const size_t per_cta = smem + stat + (size_t)reserve;
-    int per_sm = (int)std::min<size_t>(512 / (4 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
+    int per_sm = (int)std::min<size_t>(512 / (NACC * 2 * NP), per_cta ? (size_t)smem_sm / per_cta : 1);
     if (regs > 0) {  // and by the register file (allocated per warp in units of 256)
         const int per_warp = ((regs * 32 + 255) / 256) * 256;
         per_sm = std::min(per_sm, 65536 / (per_warp * (nthr / 32)));
@@ -1547,6 +1551,10 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
             }
             return IQGPU_OK;
         }
+    }
+    if constexpr (NACC == 1) {  // the level kernels keep two accumulator buffers
+        set_error("one accumulator buffer (four K pieces) runs on the dataflow schedule only");
+        return IQGPU_ERR_STATE;
     }
     int lt = e->nlevels;
     if (NP == 32)
@@ -1644,6 +1652,16 @@ static int launch_tc_tm(iqgpu_engine *e, const MixParams &M, int *rest) {
 
 template <int NP, bool BF>
 static int launch_tc_depth(iqgpu_engine *e, const MixParams &M, int depth, int *rest) {
+    if constexpr (NP == 64 && !BF) {
+        // four K pieces with one accumulator buffer: the category-split dataflow schedule only
+        if (e->tc_flow && tc_ksplit(e) == 4) {
+            switch (depth) {
+            case 2: return launch_tc_t<NP, 2, BF, 1>(e, M, rest);
+            case 3: return launch_tc_t<NP, 3, BF, 1>(e, M, rest);
+            default: return launch_tc_t<NP, 4, BF, 1>(e, M, rest);
+            }
+        }
+    }
     switch (depth) {
     case 2: return launch_tc_t<NP, 2, BF>(e, M, rest);
     case 3: return launch_tc_t<NP, 3, BF>(e, M, rest);

@@ -200,7 +200,7 @@ def test_tc_dataflow_schedule(oracle_mod, kind):
     want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
     eng = _engine(ds, topo)
     res = {}
-    for cand in [(0, 5, 2, 1), (0, 6, 2, 1), (0, 6, 3, 1), (0, 7, 2, 1)]:
+    for cand in [(0, 5, 2, 1), (0, 6, 2, 1), (0, 6, 3, 1), (0, 7, 2, 1)] + ([(0, 6, 2, 4)] if kind == "codon" else []):
         autotune.apply(eng, cand)
         l0 = eng.launches()
         lnl = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
@@ -211,7 +211,7 @@ def test_tc_dataflow_schedule(oracle_mod, kind):
     print({c: (v[0], v[1]) for c, v in res.items()}, "oracle", want)
     ref = res[(0, 5, 2, 1)]
     if kind == "codon":  # every op on the tensor cores in every schedule: same per-item arithmetic
-        for cand in [(0, 6, 2, 1), (0, 6, 3, 1), (0, 7, 2, 1)]:
+        for cand in [(0, 6, 2, 1), (0, 6, 3, 1), (0, 7, 2, 1), (0, 6, 2, 4)]:
             assert res[cand][0] == ref[0], cand
             for (p1, e1), (p2, e2) in zip(res[cand][2], ref[2]):
                 np.testing.assert_array_equal(p1, p2)
