@@ -210,12 +210,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _number(v):
+    """A peak given as a number, or as {"value": number, ...}."""
+    if isinstance(v, dict):
+        v = v.get("value", v.get("gbs", v.get("tflops")))
+    return float(v) if isinstance(v, (int, float)) and v > 0 else None
+
+
 def measured_peaks():
+    """The measured copy bandwidth (hbm_gbs) and bf16 GEMM rate of this machine's
+    GPUs from MEASURED_PEAKS.json, else the fallback figures."""
     try:
         with open(PEAKS_PATH) as f:
-            return json.load(f), "measured"
+            d = json.load(f)
     except (OSError, ValueError):
-        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+        d = None
+    if isinstance(d, dict) and _number(d.get("hbm_gbs")):
+        out = dict(d)
+        out["hbm_gbs"] = _number(d["hbm_gbs"])
+        out["bf16_tflops"] = _number(d.get("bf16_tflops")) or 1900.0
+        return out, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
 def fp64_peak_tflops(device=0):
