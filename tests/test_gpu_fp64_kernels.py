@@ -32,20 +32,22 @@ def _with_ncat(model, ncat, alpha=0.6):
     return dataclasses.replace(model, rates=np.asarray(rates, np.float64), props=np.asarray(props, np.float64))
 
 
-def _check(oracle_mod, ds, model, safe, partial_tol=1e-10):
+def _check(oracle_mod, ds, model, safe, partial_tol=1e-10, invar=None):
     topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
     eng = engine.Engine(ds.nptn, model.nstates, model.ncat, ds.ntaxa, model.state_unknown, topo.nslots,
                         safe=safe, max_ops=2 * topo.nslots, flags=engine.FLAG_SAFE_AS_GIVEN)
     eng.set_model(model)
-    eng.set_patterns(ds.freq)
+    eng.set_patterns(ds.freq, invar)
     eng.set_tip_states(ds.patterns)
     eng.compute_partials(topo.all_partials_ops())
-    orc = oracle_mod.OracleTree(model, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe)
+    orc = oracle_mod.OracleTree(model, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe, invar=invar)
     scaled = 0
     for (u, v), slot in topo.slot.items():
         gp, gs = eng.partial(slot)
         op, os_ = orc.partial(u, v)
         np.testing.assert_array_equal(gs, os_)
+        if invar is not None:  # a pattern with an invariant-site term is never rescaled
+            assert not gs[np.asarray(invar)[:len(gs)] > 0].any(), (u, v)
         scaled += int(gs.sum())
         scale = np.maximum(np.abs(op).max(axis=1, keepdims=True), 1e-300)
         assert np.max(np.abs(gp - op) / scale) < partial_tol, (u, v)
@@ -57,7 +59,8 @@ def _check(oracle_mod, ds, model, safe, partial_tol=1e-10):
     n1, n2 = next((int(u), int(v)) for (u, v) in ds.edges if min(int(u), int(v)) >= ds.ntaxa)
     ops = topo.branch_ops(n2, n1)
     df, ddf = eng.likelihood_derv(ops, topo.ref(n1, n2), topo.ref(n2, n1), 0.07)
-    odf, oddf = oracle_mod.OracleTree(model, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe).derv(n1, n2, 0.07)
+    odf, oddf = oracle_mod.OracleTree(model, ds.patterns, ds.freq, ds.edges, ds.lengths, safe=safe,
+                                      invar=invar).derv(n1, n2, 0.07)
     assert abs(df - odf) <= 1e-9 * max(1.0, abs(odf)) and abs(ddf - oddf) <= 1e-9 * max(1.0, abs(oddf))
     return scaled
 
@@ -88,3 +91,16 @@ def test_category_kernel_counts(oracle_mod, ncat):
     ds = simulate.codon_gy94_dataset(60, 300, 83, mean_bl=0.5)
     scaled = _check(oracle_mod, ds, _with_ncat(ds.model, ncat), True, partial_tol=1e-6)
     assert scaled > 0
+
+
+def test_category_kernel_invariant_sites(oracle_mod):
+    """Codon +I+G4 in SAFE on the per-category kernel: a pattern with an
+    invariant-site term is never rescaled (the reference's condition
+    lh_max < 2^-256 && ptn_invar == 0), while the others' counts grow; every
+    count identical to the oracle, partials, lnL and derivatives as above."""
+    ds = simulate.codon_gy94_dataset(60, 300, 84, mean_bl=0.5)
+    r, p = models.gamma_invar_rates(0.5, 0.3, 4)
+    m = dataclasses.replace(ds.model, rates=np.asarray(r, np.float64), props=np.asarray(p, np.float64))
+    inv = models.invariant_site_lh(ds.patterns, m.pi, 0.3, m.nstates)
+    assert (inv > 0).sum() > 0
+    assert _check(oracle_mod, ds, m, True, partial_tol=1e-6, invar=inv) > 0
