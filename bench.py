@@ -89,6 +89,8 @@ def kernel_name(use_tc, n, tile, bf16=False):
         depth = next((int(t[1:]) for t in tile.split("/") if t.startswith("s")), 2)
         if "/level-tm" in tile and not bf16:
             return "k_traverse_tc_tm"
+        if "/level-ring" in tile and not bf16:
+            return "k_traverse_tc_ring"
         np_ = 64 if n > 32 else 32
         bf = 'true' if bf16 else 'false'
         if "/flow-tcw" in tile:  # dataflow, whole (op, tile) items

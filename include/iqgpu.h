@@ -314,8 +314,12 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * issued once the items writing its children are done (bounded waits; the
  * level form of 5 when the traversal has more (op, tile) pairs than the
  * engine's pair counters; other kernels run as 3); 7 = as 6 with whole
- * (tile, op) items (every category of the pair in one item). Results do not
- * depend on it. */
+ * (tile, op) items (every category of the pair in one item); 8 = as 1 on the
+ * deep-ring tensor-core kernel (20-state models in IQGPU_TF32X3: one CTA per
+ * SM, a ring of six (tile, op, category) stages landed by TMA, operand A
+ * split into TF32 hi/lo in tensor memory; the one-op levels near the root on
+ * the CUDA-core tail; others run as 3); 9 = as 8 with every level on the
+ * tensor cores. Results do not depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots

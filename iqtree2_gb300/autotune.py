@@ -28,7 +28,10 @@ def candidates(eng):
     category-split items on the narrow levels (up to 32 padded states),
     6 = dataflow on the tensor cores (one launch of category-split items,
     each waiting for the items writing its children), 7 = as 6 with whole
-    (op, tile) items."""
+    (op, tile) items, 8 = level-synchronous on the deep-ring kernel (20 states,
+    split TF32: one CTA per SM, six categories in flight, operand A in tensor
+    memory; one-op levels on the CUDA-core tail), 9 = as 8 with every level on
+    the tensor cores."""
     if getattr(eng, "tensor_cores", False):  # one CTA = 128 patterns (the MMA's M)
         npad = (eng.nstates + 3) // 4 * 4
         pieces = (1, 2) if (npad > 32 and npad % 16 == 0) else (1,)
@@ -41,6 +44,7 @@ def candidates(eng):
         out += [(0, 7, 2, kp) for kp in pieces]  # dataflow, whole (op, tile) items
         if npad == 20 and getattr(eng, "precision", 0) == 2:  # split TF32
             out.append((0, 4, 0, 0))
+            out += [(0, 8, 0, 0), (0, 9, 0, 0)]  # deep ring, one CTA per SM
         return out
     out = ([(1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (2, 1, 0, 0)]
            if eng.nstates == 4 and eng.ncat <= 4 else [])
@@ -54,7 +58,9 @@ def candidates(eng):
 
 def label(cand):
     tile, sched, stages, kp = cand
-    return (f"{tile}/{('fused', 'level', 'flow', 'level-ws', 'level-tm', 'level-wsc', 'flow-tc', 'flow-tcw')[sched]}" +
+    names = ('fused', 'level', 'flow', 'level-ws', 'level-tm', 'level-wsc', 'flow-tc', 'flow-tcw', 'level-ring',
+             'level-ring-all')
+    return (f"{tile}/{names[sched]}" +
             (f"/s{stages}" if stages else "") +
             (f"/k{kp}" if kp else ""))
 

@@ -1359,7 +1359,7 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta) {
 }
 
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
-    if (!e || schedule < 0 || schedule > 7) { set_error("schedule must be 0 .. 7"); return IQGPU_ERR_ARG; }
+    if (!e || schedule < 0 || schedule > 9) { set_error("schedule must be 0 .. 9"); return IQGPU_ERR_ARG; }
     e->level_sync = schedule == 1 || schedule >= 3;
     e->flow = schedule == 2;
     e->tc_ws = schedule == 3 || schedule >= 5;
@@ -1367,6 +1367,8 @@ int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule) {
     e->tc_split = schedule == 5 || schedule == 6;
     e->tc_flow = schedule == 6;
     e->tc_flow_whole = schedule == 7;
+    e->tc_ring = schedule == 8 || schedule == 9;
+    e->tc_ring_all = schedule == 9;
     return IQGPU_OK;
 }
 

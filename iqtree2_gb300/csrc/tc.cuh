@@ -151,6 +151,44 @@ __device__ __forceinline__ void tmem_ld20(unsigned taddr, float (&v)[20]) {
     for (int i = 0; i < 20; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 12 consecutive columns (x8 + x4) from each of two addresses, one wait.
+__device__ __forceinline__ void tmem_ld12x2(unsigned ta, unsigned tb, float (&a)[12], float (&b)[12]) {
+    unsigned r[24];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%24];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8, %9, %10, %11}, [%25];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%12, %13, %14, %15, %16, %17, %18, %19}, [%26];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20, %21, %22, %23}, [%27];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+        : "r"(ta), "r"(ta + 8u), "r"(tb), "r"(tb + 8u)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[12 + i]);
+    }
+}
+// 8 consecutive columns from each of two addresses, one wait.
+__device__ __forceinline__ void tmem_ld8x2(unsigned ta, unsigned tb, float (&a)[8], float (&b)[8]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%16];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%17];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(ta), "r"(tb)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[8 + i]);
+    }
+}
+
 // ---- registers -> TMEM (32x32b: this thread's lane, 8 consecutive columns) ----
 __device__ __forceinline__ void tmem_st8(unsigned taddr, const float *v) {
     asm volatile(

@@ -1288,6 +1288,420 @@ __global__ void __launch_bounds__(kTcRows + 32, 2) k_traverse_tc_tm(const TcPara
     if (warp == 0) tmem_dealloc(tmem, kTmCols);
 }
 
+// ---------------------------------------------------------------------------
+// Deep-ring level kernel (schedules 8 and 9; 20 states, split TF32)
+// ---------------------------------------------------------------------------
+// The kernels above hold a shared-memory slot from its copy until its MMAs
+// complete and fit two slots per CTA, four CTAs per SM: about eight child
+// slices in flight per SM, too few to cover HBM latency at full bandwidth.
+// Here one CTA per SM owns the whole shared memory as a ring of kRgNS stages;
+// a stage is one (item, category): both children's A slices and both sides'
+// B = P_c(t) hi/lo, landed by TMA (32 KB), so six categories (about 120 KB of
+// partials) are in flight per SM. Four roles run side by side on different
+// stages:
+//  * converter warps 0-7: warps 0-3 take the left child's rows of a stage and
+//    warps 4-7 the right child's, each thread reading its pattern row from the
+//    slice once, splitting it into TF32 hi/lo in registers and writing both
+//    into one of kRgNA A buffers in tensor memory with tcgen05.st (A never goes
+//    back to shared memory); for an item with one tip child (always on the
+//    left after the swap), warps 0-3 write the tip's leaf-table rows into the
+//    left accumulator columns instead, which its MMAs leave alone;
+//  * a copy warp (16, lane 0) keeps the copies kRgNS stages ahead; MMA warps
+//    17 and 18 (lane 0, even and odd stages) run a stage's MMAs (A from
+//    tensor memory, B from the slot; the same three
+//    passes in the same order as the other split-TF32 kernels, so results are
+//    bit-identical) into one of kRgNACC accumulator buffers once the stage is
+//    converted and the buffer's previous stage has been read out; their
+//    completion frees the slot and the A buffer. (Measured with clock
+//    stamps per stage: one thread issuing both the copies and the MMAs took
+//    about 2,300 cycles per stage, one thread issuing the MMAs alone about
+//    1,700, the 18 MMAs of a stage taking some 800 cycles to issue; with two
+//    accumulator buffers an epilogue's pause at an item's end stalled the MMAs
+//    two stages later. Separate rings for A (freed on conversion) and B
+//    were slower: the copy queue then held far-ahead A slices in front of the
+//    B operands the next MMAs needed.)
+//  * epilogue warps 8-15: warps 8-11 form the products of states 0-11 of their
+//    rows, warps 12-15 of states 12-19; at an item's end the two halves of a
+//    row exchange their maxima through shared memory and each rescales its
+//    own states; items of two tips are computed here from the leaf tables.
+// Warps w, w + 4, w + 8 and w + 12 share tensor-memory lanes 32 (w % 4) ...
+// Tensor memory (512 columns): accumulators D[a][side] at a * 64 + side * 32
+// (a < kRgNACC); A buffer b, side s: hi at kRgAcol + b * 96 + s * 48, lo 24
+// columns further.
+// A global load issued where it stands in the program (volatile: the compiler
+// neither sinks it to its first use nor merges it).
+__device__ __forceinline__ int ld_issue_s32(const int32_t *p) {
+    int v;
+    asm volatile("ld.global.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+constexpr int kRgConv = 256;                // converter threads (warps 0-7)
+constexpr int kRgEpi = 256;                 // epilogue threads (warps 8-15)
+constexpr int kRgMma = 2;                   // MMA-issuing warps
+constexpr int kRgThreads = kRgConv + kRgEpi + 32 * (1 + kRgMma);  // + a copy warp and the MMA warps
+constexpr int kRgNS = 6;                    // shared-memory stages
+constexpr int kRgNA = 2;                    // A buffers in tensor memory
+constexpr int kRgNACC = 4;                  // accumulator buffers in tensor memory
+constexpr unsigned kRgAcol = kRgNACC * 64;  // first column of the A buffers
+constexpr int kRgA = 16 * kTmKQ * 128;      // one side's A slice as copied (10,240 B)
+constexpr int kRgB = 2 * 32 * kTmKP * 4;    // one side's B, hi and lo (6,144 B)
+constexpr int kRgSlot = 2 * kRgA + 2 * kRgB;
+static_assert(kRgAcol + kRgNA * 96 <= 512, "tensor memory of the ring kernel");
+
+__global__ void __launch_bounds__(kRgThreads, 1)
+    k_traverse_tc_ring(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl) {
+    constexpr int KQ = kTmKQ, KP = kTmKP, NP = 32, KSTEPS = KP / 8;
+    const MixParams &P = T.M;
+    const int C = P.ncat, n = P.n, npad = P.npad;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const long long ld = P.ldp;
+    const int total = T.ntiles * nl;
+    const int nitems =
+        (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const long long PM = (long long)C * n * npad;
+    const long long TB = (long long)(P.state_unknown + 1) * C * npad;
+
+    extern __shared__ __align__(128) unsigned char tc_smem_raw[];
+    // full: a stage landed; mmab: its MMAs complete (slot free); conv: A buffer
+    // written by the converters; adone: the A buffer's MMAs complete; ebar: an
+    // accumulator buffer holds its stage's products; efree: read out again
+    __shared__ unsigned long long full[kRgNS], mmab[kRgNS], conv[kRgNA], adone[kRgNA], ebar[kRgNACC], efree[kRgNACC];
+    __shared__ unsigned tmem_base_s, abort_flag;
+    __shared__ int4 opc[kTcOpCache];
+    __shared__ float rmax[2][2][kTcRows];  // [item parity][half][row]: maxima of the two halves of a row
+    unsigned char *const ring = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
+
+    for (int i = tid; i < nl && i < kTcOpCache; i += blockDim.x) {
+        const OpDev op = P.ops[op0 + i];
+        opc[i] = make_int4(op.dad_slot, op.child[0], op.child[1], 0);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kRgNS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&mmab[s], 1);
+        }
+        for (int b = 0; b < kRgNA; b++) {
+            mbar_init(&conv[b], kRgConv);
+            mbar_init(&adone[b], 1);
+        }
+        for (int a = 0; a < kRgNACC; a++) {
+            mbar_init(&ebar[a], 1);
+            mbar_init(&efree[a], kRgEpi);
+        }
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(&tmem_base_s), 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = tmem_base_s;
+    const unsigned lane_off = (unsigned)((warp & 3) * 32) << 16;
+    const int r = (warp & 3) * 32 + (tid & 31);  // pattern row of the tile = tensor-memory lane
+
+    // (item, category) cursors over the stages: items of two tips have none
+    auto skip_tips = [&](int &j, int &c, TcItem &it) {
+        while (j < nitems && !(it.lint || it.rint)) {
+            j++;
+            c = 0;
+            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+        }
+    };
+    auto advance = [&](int &j, int &c, TcItem &it) {
+        if (++c == C) {
+            c = 0;
+            j++;
+            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+        }
+        skip_tips(j, c, it);
+    };
+
+    constexpr int kWarpCopy = (kRgConv + kRgEpi) / 32, kWarpM = kWarpCopy + 1;
+    if (warp == kWarpCopy) {
+        // ---------------- copies (lane 0) ----------------
+        // A wait that gives up raises the abort flag and the status word; every
+        // role then skips its remaining waits and runs to its end.
+        if ((tid & 31) == 0 && nitems > 0) {
+            int bj = 0, bc = 0, issued = 0;
+            TcItem bit = tc_item(T, 0, false, op0, opc);
+            skip_tips(bj, bc, bit);
+            for (; bj < nitems; issued++) {
+                const int s = issued % kRgNS;
+                if (issued >= kRgNS) {  // the slot's previous stage is out of the tensor cores
+                    if (*(volatile unsigned *)&abort_flag ||
+                        !mbar_wait(&mmab[s], (unsigned)((issued / kRgNS - 1) & 1), kWaitPolls)) {
+                        atomicExch(&abort_flag, 1u);
+                        atomicExch(P.status, kStatusTimeout);
+                        break;
+                    }
+                }
+                unsigned char *slot = ring + s * kRgSlot;
+                mbar_expect_tx(&full[s], (unsigned)(kRgA + kRgB) * ((unsigned)bit.lint + (unsigned)bit.rint));
+                for (int side = 0; side < 2; side++) {
+                    if (!(side == 0 ? bit.lint : bit.rint)) continue;
+                    const int child = side == 0 ? bit.lref : bit.rref;
+                    tma_load_3d(slot + side * kRgA, &tmA, 0, bc * KQ, child * T.groups_per_slot + bit.tile * 16,
+                                &full[s]);
+                    const int ch = side == 0 ? bit.lch : 1 - bit.lch;
+                    tma_load_1d(slot + 2 * kRgA + side * kRgB,
+                                T.tcb + (long long)bit.k * T.tcb_stride + (long long)(ch * C + bc) * T.b_stage,
+                                (unsigned)kRgB, &full[s]);
+                }
+                advance(bj, bc, bit);
+            }
+            // the last copies have landed before the shared memory is released
+            for (int i = issued > kRgNS ? issued - kRgNS : 0; i < issued; i++)
+                mbar_wait(&full[i % kRgNS], (unsigned)((i / kRgNS) & 1), kWaitPolls);
+        }
+        __syncwarp();
+    } else if (warp >= kWarpM) {
+        // ---------------- MMAs (lane 0 of kRgMma warps, stages round-robin) ----------------
+        // Each barrier still sees its commits in stage order: a stage's gates
+        // (conv, efree) complete only after the previous stage using the same A
+        // buffer or accumulator buffer has completed.
+        const int mw = warp - kWarpM;
+        if ((tid & 31) == 0 && nitems > 0) {
+            const uint32_t idesc = idesc_tf32(kTcRows, NP);
+            const unsigned b_sbo = (unsigned)(KP / 4 * 128);
+            int mj = 0, mc = 0, mdone = 0;
+            TcItem mit = tc_item(T, 0, false, op0, opc);
+            skip_tips(mj, mc, mit);
+            for (int i = 0; i < mw && mj < nitems; i++, mdone++) advance(mj, mc, mit);
+            for (; mj < nitems; mdone += kRgMma) {
+                const int b = mdone % kRgNA, a = mdone % kRgNACC, s = mdone % kRgNS;
+                // A converted (the stage landed before that), and the accumulator buffer read out
+                if (*(volatile unsigned *)&abort_flag) break;
+                if (!mbar_wait(&conv[b], (unsigned)((mdone / kRgNA) & 1), kWaitPolls) ||
+                    (mdone >= kRgNACC &&
+                     !mbar_wait(&efree[a], (unsigned)((mdone / kRgNACC - 1) & 1), kWaitPolls))) {
+                    atomicExch(&abort_flag, 1u);
+                    atomicExch(P.status, kStatusTimeout);
+                    break;
+                }
+                tc_fence_after();
+                const unsigned ub = smem_u32(ring + s * kRgSlot + 2 * kRgA);
+                for (int side = 0; side < 2; side++) {
+                    if (!(side == 0 ? mit.lint : mit.rint)) continue;
+                    const unsigned d = tmem + (unsigned)(a * 2 * NP + side * NP);
+                    const unsigned ah = tmem + kRgAcol + (unsigned)(b * 96 + side * 48), al = ah + (unsigned)KP;
+                    const unsigned bh = ub + (unsigned)(side * kRgB), bl = bh + (unsigned)(kRgB / 2);
+#pragma unroll
+                    for (int ks = 0; ks < KSTEPS; ks++) {
+                        const uint64_t dbh = smem_desc(bh + ks * 256, 128, b_sbo);
+                        const uint64_t dbl = smem_desc(bl + ks * 256, 128, b_sbo);
+                        mma_tf32_ts(d, al + 8 * ks, dbh, idesc, ks > 0);
+                        mma_tf32_ts(d, ah + 8 * ks, dbl, idesc, true);
+                        mma_tf32_ts(d, ah + 8 * ks, dbh, idesc, true);
+                    }
+                }
+                mma_commit(&mmab[s]);
+                mma_commit(&adone[b]);
+                mma_commit(&ebar[a]);
+                for (int i = 0; i < kRgMma && mj < nitems; i++) advance(mj, mc, mit);
+            }
+            // this thread's MMAs are complete before the tensor memory is released
+            const int last = mdone - kRgMma;
+            if (last >= 0) mbar_wait(&mmab[last % kRgNS], (unsigned)((last / kRgNS) & 1), kWaitPolls);
+        }
+        __syncwarp();
+    } else if (warp < kRgConv / 32) {
+        // ---------------- converters ----------------
+        // A wait that gives up raises the abort flag; every later wait is then
+        // skipped (the data is garbage, the status reports the timeout), so
+        // every role runs to its end without blocking. For an item with one
+        // tip child (always on the left after the swap), warps 0-3 write the
+        // tip's leaf-table rows of the stage's category into the left
+        // accumulator columns (which its MMAs leave alone) once the epilogue
+        // has read that buffer's previous stage: the epilogue then reads both
+        // sides from tensor memory and loads nothing per stage.
+        const int side = warp >> 2;
+        int j = 0, c = 0;
+        TcItem it = tc_item(T, 0, false, op0, opc);
+        if (nitems > 0) skip_tips(j, c, it);
+        int tsl = 0, tj = -1;  // this row's tip state, for item tj
+        for (int m = 0; j < nitems; m++) {
+            const int s = m % kRgNS, b = m % kRgNA, a = m % kRgNACC;
+            const bool tipside = side == 0 && !it.lint;
+            const bool mine = side == 0 ? it.lint : it.rint;  // this side has an A slice
+            float tv[4 * KQ];
+            if (tipside) {
+                if (tj != j) {
+                    tsl = P.states[(long long)(-1 - it.lref) * ld + (long long)it.tile * kTcRows + r];
+                    tj = j;
+                }
+                const float *tl = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0) +
+                                  (long long)tsl * C * npad + c * npad;
+#pragma unroll
+                for (int q = 0; q < KQ; q++) {
+                    const float4 t4 = ld4(tl + 4 * q);
+                    tv[4 * q] = t4.x; tv[4 * q + 1] = t4.y; tv[4 * q + 2] = t4.z; tv[4 * q + 3] = t4.w;
+                }
+            }
+            // every converter waits for the A buffer's previous stage (its MMAs imply
+            // that stage's conv phase is complete, so arrivals never run a phase ahead)
+            bool ok = *(volatile unsigned *)&abort_flag == 0;
+            if (ok && mine) ok = mbar_wait(&full[s], (unsigned)((m / kRgNS) & 1), kWaitPolls);
+            if (ok && m >= kRgNA) ok = mbar_wait(&adone[b], (unsigned)((m / kRgNA - 1) & 1), kWaitPolls);
+            if (ok && tipside && m >= kRgNACC)
+                ok = mbar_wait(&efree[a], (unsigned)((m / kRgNACC - 1) & 1), kWaitPolls);
+            ok = __all_sync(0xffffffffu, ok);  // tcgen05.st is warp-collective
+            if (!ok) atomicExch(&abort_flag, 1u);
+            if (ok && tipside) {
+                tc_fence_after();
+                const unsigned ad = tmem + lane_off + (unsigned)(a * 2 * NP);
+                float z[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) z[i] = i < 4 * KQ - 16 ? tv[16 + i] : 0.f;
+                tmem_st8(ad, &tv[0]);
+                tmem_st8(ad + 8, &tv[8]);
+                tmem_st8(ad + 16, z);
+                tmem_st_wait();
+            } else if (ok && mine) {
+                tc_fence_after();
+                const float *ar = reinterpret_cast<const float *>(ring + s * kRgSlot + side * kRgA) +
+                                  (r >> 3) * KQ * 32 + (r & 7) * 4;
+                const unsigned ad = tmem + lane_off + kRgAcol + (unsigned)(b * 96 + side * 48);
+#pragma unroll
+                for (int t = 0; t < KSTEPS; t++) {  // K step t: states 8t .. 8t + 7 (zero beyond the 20)
+                    float h[8], l[8];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int q = 2 * t + u;
+                        const float4 v = q < KQ ? *reinterpret_cast<const float4 *>(ar + q * 32)
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                        const float xv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            h[4 * u + i] = tf32_hi(xv[i]);
+                            l[4 * u + i] = xv[i] - h[4 * u + i];
+                        }
+                    }
+                    tmem_st8(ad + 8 * t, h);
+                    tmem_st8(ad + KP + 8 * t, l);
+                }
+                tmem_st_wait();
+            }
+            tc_fence_before();
+            mbar_arrive(&conv[b]);
+            advance(j, c, it);
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        // Both sides of a staged item come from tensor memory (a tip's rows
+        // were written there by the converters); the children's exponents are
+        // loaded one item ahead. Items of two tips use the leaf tables.
+        const int half = (warp - kRgConv / 32) >> 2;
+        const int q0 = half ? 3 : 0, nq = half ? KQ - 3 : 3;  // this thread's 4-state chunks
+        // (volatile loads: issued here, not sunk to their first use an item later)
+        auto expo_in = [&](const TcItem &x, long long px, int &e_l, int &e_r) {
+            e_l = (x.lint && half == 0) ? ld_issue_s32(P.expo + (long long)x.lref * ld + px) : 0;
+            e_r = (x.rint && half == 0) ? ld_issue_s32(P.expo + (long long)x.rref * ld + px) : 0;
+        };
+        int m = 0;  // stages read out
+        TcItem it = tc_item(T, 0, false, op0, opc);
+        long long p = (long long)it.tile * kTcRows + r;
+        int e_l = 0, e_r = 0;
+        if (nitems > 0) expo_in(it, p, e_l, e_r);
+        for (int j = 0; j < nitems; j++) {
+            TcItem nit = it;  // the next item's exponents, in flight while this one is read out
+            long long np_ = p;
+            int nel = 0, ner = 0;
+            if (j + 1 < nitems) {
+                nit = tc_item(T, j + 1, false, op0, opc);
+                np_ = (long long)nit.tile * kTcRows + r;
+                expo_in(nit, np_, nel, ner);
+            }
+            float *row = P.part + (long long)it.dad * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
+            const bool staged = it.lint || it.rint;
+            const float *TL = P.opmats + (long long)it.k * P.op_stride + 2 * PM + (it.lch ? TB : 0);
+            const int sl = staged ? 0 : P.states[(long long)(-1 - it.lref) * ld + p];
+            const int sr = staged ? 0 : P.states[(long long)(-1 - it.rref) * ld + p];
+            float cmax = 0.f;
+            for (int c = 0; c < C; c++) {
+                float lv[12], rv[12];
+                if (staged) {
+                    const int a = m % kRgNACC;
+                    if (!*(volatile unsigned *)&abort_flag &&
+                        !mbar_wait(&ebar[a], (unsigned)((m / kRgNACC) & 1), kWaitPolls))
+                        atomicExch(&abort_flag, 1u);
+                    __syncwarp();  // tcgen05.ld is warp-collective
+                    tc_fence_after();
+                    const unsigned dL = tmem + lane_off + (unsigned)(a * 2 * NP + 4 * q0), dR = dL + NP;
+                    if (half == 0) {
+                        tmem_ld12x2(dL, dR, lv, rv);
+                    } else {
+                        float l8[8], r8[8];
+                        tmem_ld8x2(dL, dR, l8, r8);
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            lv[i] = l8[i];
+                            rv[i] = r8[i];
+                        }
+                    }
+                    tc_fence_before();
+                    mbar_arrive(&efree[a]);  // this thread's reads of buffer a are done
+                    m++;
+                } else {  // two tips
+                    const float *tl = TL + (long long)sl * C * npad + c * npad + 4 * q0;
+                    const float *tr = TL + (it.lch ? -TB : TB) + (long long)sr * C * npad + c * npad + 4 * q0;
+#pragma unroll
+                    for (int q = 0; q < 3; q++)
+                        if (q < nq) {
+                            const float4 a4 = ld4(tl + 4 * q), b4 = ld4(tr + 4 * q);
+                            lv[4 * q] = a4.x; lv[4 * q + 1] = a4.y; lv[4 * q + 2] = a4.z; lv[4 * q + 3] = a4.w;
+                            rv[4 * q] = b4.x; rv[4 * q + 1] = b4.y; rv[4 * q + 2] = b4.z; rv[4 * q + 3] = b4.w;
+                        }
+                }
+                float *out = row + (long long)c * KQ * 32 + q0 * 32;
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+                    if (q < nq) {
+                        float o[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            o[i] = (4 * (q0 + q) + i < n) ? lv[4 * q + i] * rv[4 * q + i] : 0.f;
+                            cmax = fmaxf(cmax, o[i]);
+                        }
+                        *reinterpret_cast<float4 *>(out + q * 32) = make_float4(o[0], o[1], o[2], o[3]);
+                    }
+            }
+            // the row maximum over both halves (one vote per item: the epilogue warps stop together),
+            // the exact power-of-two rescale and the exponent
+            rmax[j & 1][half][r] = cmax;
+            if (bar_or_part(kRgEpi, *(volatile unsigned *)&abort_flag != 0)) break;
+            const float mx = fmaxf(rmax[j & 1][0][r], rmax[j & 1][1][r]);
+            int sh = 0;
+            if (mx < kMixThreshold && mx > 0.f) {
+                int ex;
+                frexpf(mx, &ex);
+                sh = 1 - ex;
+                const float mul = __int_as_float((127 + sh) << 23);
+                for (int cc = 0; cc < C; cc++)
+                    for (int q = 0; q < nq; q++) {
+                        float4 *v4 = reinterpret_cast<float4 *>(row + (long long)cc * KQ * 32 + (q0 + q) * 32);
+                        float4 v = *v4;
+                        v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
+                        *v4 = v;
+                    }
+            }
+            if (half == 0) P.expo[(long long)it.dad * ld + p] = e_l + e_r - sh;
+            it = nit;
+            p = np_;
+            e_l = nel;
+            e_r = ner;
+        }
+        if (*(volatile unsigned *)&abort_flag && tid == kRgConv) atomicExch(P.status, kStatusTimeout);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 // B operands: per op, child, category and K piece kh: hi and lo of
 // P_c(t)[x][y] for y in piece kh, in [x/8][y'/4][x%8][y'%4] order (y' = y - kh
 // KS), zero outside x < n, y < n.
@@ -1650,6 +2064,49 @@ static int launch_tc_tm(iqgpu_engine *e, const MixParams &M, int *rest) {
     return IQGPU_OK;
 }
 
+// Level schedule on k_traverse_tc_ring: one CTA per SM (its shared memory
+// and its 512 tensor-memory columns); schedule 8 leaves the levels from the
+// first one with fewer than three (tile, op) pairs per SM (the one-op levels
+// near the root) to the CUDA-core tail, schedule 9 runs every level here.
+static int launch_tc_ring(iqgpu_engine *e, const MixParams &M, int *rest) {
+    int rc = tc_tensor_map(e);
+    if (rc) return rc;
+    const TcParams T = tc_params(e, M, 32, false);
+    const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
+    const size_t smem = (size_t)kRgNS * kRgSlot + 128;
+    cudaError_t err = cudaFuncSetAttribute(k_traverse_tc_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_traverse_tc_ring, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring smem attribute");
+    int sms = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
+    const long long resident = sms;
+    int lt = e->nlevels;
+    if (!e->tc_ring_all)
+        for (int l = 0; l < e->nlevels; l++)
+            if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < 3 * resident) {
+                lt = l;
+                break;
+            }
+    *rest = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
+    for (int l = 0; l < lt; l++) {
+        const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
+        if (nl <= 0) continue;
+        if (level_all_tiptip(e, op0, nl)) {
+            rc = launch_tiptip_level(e, M, op0, nl);
+            if (rc) return rc;
+            continue;
+        }
+        const long long items = (long long)T.ntiles * nl;
+        const int grid = (int)std::min<long long>(items, resident);
+        k_traverse_tc_ring<<<grid, kRgThreads, smem, e->st>>>(tm, T, op0, nl);
+        e->launches++;
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring level");
+    }
+    return IQGPU_OK;
+}
+
 template <int NP, bool BF>
 static int launch_tc_depth(iqgpu_engine *e, const MixParams &M, int depth, int *rest) {
     if constexpr (NP == 64 && !BF) {
@@ -1691,6 +2148,8 @@ int launch_traverse_tc(iqgpu_engine *e, const MixParams &M, int *rest) {
     if (M.nops <= 0) return IQGPU_OK;
     const int depth = tc_depth(e);
     const bool BF = e->cfg.precision == IQGPU_BF16;
+    if (e->level_sync && e->tc_ring && !BF && e->npad == 4 * kTmKQ && tc_ksplit(e) == 1)
+        return launch_tc_ring(e, M, rest);
     if (e->level_sync && e->tc_tm && !BF && e->npad == 4 * kTmKQ && tc_ksplit(e) == 1)
         return launch_tc_tm(e, M, rest);
     if (tc_np(e->npad) == 64)

@@ -350,7 +350,10 @@ class Engine:
     def set_schedule(self, schedule):
         """0 = fused, 1 = level-synchronous, 2 = dataflow (4-state kernel),
         3 = level-synchronous on the warp-specialised tensor-core kernel,
-        4 = level-synchronous with operand A in tensor memory (20 states)."""
+        4 = level-synchronous with operand A in tensor memory (20 states),
+        5 = as 3 with category-split narrow levels, 6 / 7 = dataflow on the
+        tensor cores (category-split / whole items), 8 / 9 = level-synchronous
+        on the deep-ring kernel (20 states; 9 with the one-op levels too)."""
         _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
 
     def launches(self):

@@ -146,7 +146,9 @@ def test_tc_level_kernels_protein(oracle_mod):
     tensor memory), bit-identical; the A-in-tensor-memory kernel
     deterministic; schedule 5 runs the narrow levels as category-split items
     (bit-identical partials on the levels every schedule puts on the tensor
-    cores)."""
+    cores); schedules 8 and 9 run the deep-ring kernel (one CTA per SM, eight
+    worker warps splitting each row's states between two warps), bit-identical
+    on those levels and deterministic."""
     ds = simulate.protein_lg_dataset(100, 20000, 35)
     topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
     leaf, nb = 0, topo.adj[0][0][0]
@@ -159,7 +161,8 @@ def test_tc_level_kernels_protein(oracle_mod):
     assert len(check) >= 20
     eng = _engine(ds, topo)
     got, launches, parts = {}, {}, {}
-    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0), (0, 5, 2, 1), (0, 6, 2, 1), (0, 7, 2, 1)]:
+    for cand in [(0, 0, 2, 1), (0, 1, 2, 1), (0, 3, 2, 1), (0, 4, 0, 0), (0, 5, 2, 1), (0, 6, 2, 1), (0, 7, 2, 1),
+                 (0, 8, 0, 0), (0, 9, 0, 0)]:
         autotune.apply(eng, cand)
         l0 = eng.launches()
         got[cand] = eng.compute_likelihood(ops, a, b, length)
@@ -174,9 +177,11 @@ def test_tc_level_kernels_protein(oracle_mod):
             np.testing.assert_array_equal(x, y, err_msg=str(cand))
     base = got[(0, 1, 2, 1)]
     assert all(rel(v, base) < 3e-7 for v in got.values()), got
-    autotune.apply(eng, (0, 4, 0, 0))
-    again = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
-    assert again == [got[(0, 4, 0, 0)]] * 3
+    for cand in [(0, 4, 0, 0), (0, 8, 0, 0), (0, 9, 0, 0)]:
+        autotune.apply(eng, cand)
+        again = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
+        assert again == [got[cand]] * 3, cand
+    assert launches[(0, 8, 0, 0)] < launches[(0, 9, 0, 0)]  # the one-op levels: one tail launch against one each
 
 
 @pytest.mark.parametrize("kind", ["codon", "protein"])
