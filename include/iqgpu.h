@@ -318,8 +318,9 @@ int iqgpu_set_tile(iqgpu_engine *e, int32_t patterns_per_cta);
  * deep-ring tensor-core kernel (20-state models in IQGPU_TF32X3: one CTA per
  * SM, a ring of six (tile, op, category) stages landed by TMA, operand A
  * split into TF32 hi/lo in tensor memory; the one-op levels near the root on
- * the CUDA-core tail; others run as 3); 9 = as 8 with every level on the
- * tensor cores. Results do not depend on it. */
+ * the CUDA-core tail; others run as 3); 9 = as 8, with those one-op levels
+ * in one more launch of the same kernel, each CTA taking its pattern tiles
+ * through all of them in level order. Results do not depend on it. */
 int iqgpu_set_schedule(iqgpu_engine *e, int32_t schedule);
 /* Copy depth of the tensor-core traversal (precision IQGPU_TF32X3 / BF16):
  * how many child slices per CTA may be in flight as TMA copies (landing slots

@@ -30,8 +30,9 @@ def candidates(eng):
     each waiting for the items writing its children), 7 = as 6 with whole
     (op, tile) items, 8 = level-synchronous on the deep-ring kernel (20 states,
     split TF32: one CTA per SM, six categories in flight, operand A in tensor
-    memory; one-op levels on the CUDA-core tail), 9 = as 8 with every level on
-    the tensor cores."""
+    memory; one-op levels on the CUDA-core tail), 9 = as 8 with the one-op
+    levels in one launch of the same kernel, each CTA taking its tiles through
+    all of them."""
     if getattr(eng, "tensor_cores", False):  # one CTA = 128 patterns (the MMA's M)
         npad = (eng.nstates + 3) // 4 * 4
         pieces = (1, 2) if (npad > 32 and npad % 16 == 0) else (1,)

@@ -162,7 +162,7 @@ struct iqgpu_engine {
     bool tc_flow;             // dataflow schedule on the warp-specialised tensor-core kernel (schedule 6)
     bool tc_flow_whole;       // as tc_flow, with whole (op, tile) items (schedule 7)
     bool tc_ring;             // level schedule on the deep-ring kernel (20 states, split TF32; schedules 8, 9)
-    bool tc_ring_all;         // ... with the one-op levels on it too (schedule 9)
+    bool tc_ring_all;         // ... with the one-op levels on it too, per tile in one launch (schedule 9)
     bool has_multi;           // the uploaded op list holds multifurcating records (IQGPU_OP_MORE)
     int sms;                  // multiprocessors of the engine's device
     float *d_ivhl, *d_tiphl;  // mixed, 16+ states: U^-1 and the eigen-space tip vectors as FP32 hi/lo pairs

@@ -103,6 +103,26 @@ struct MixBufParams {
 
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
+// Exact power-of-two rescale of a pattern's own stores: n 16-byte chunks at
+// base + chunk(i) floats. The loads go out eight at a time before their
+// stores, so re-reading the row costs one memory latency per eight chunks
+// (one load after another's store paid a full round trip per chunk).
+template <class Chunk>
+__device__ __forceinline__ void rescale_chunks(float *base, int n, float mul, Chunk chunk) {
+    for (int i0 = 0; i0 < n; i0 += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (i0 + u < n) v[u] = *reinterpret_cast<const float4 *>(base + chunk(i0 + u));
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (i0 + u < n) {
+                v[u].x *= mul; v[u].y *= mul; v[u].z *= mul; v[u].w *= mul;
+                *reinterpret_cast<float4 *>(base + chunk(i0 + u)) = v[u];
+            }
+    }
+}
+
 // Per-pattern sums over the B = ncat * n eigen-space entries of theta (FP32 in
 // memory, row stride ld): s_j = sum_k w_j[k] theta[k] for NW weight rows held
 // as FP32 pairs (w = hi + lo, from the FP64 values). Double-float arithmetic:

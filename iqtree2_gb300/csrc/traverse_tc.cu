@@ -91,8 +91,11 @@ constexpr int kTcOpCache = 128;  // ops whose (dad, child0, child1) are staged i
 // grid, tiles of the same op adjacent (their B operands share L2 lines).
 // Category-split (csplit): (tile, op, category) triples, the categories of a
 // pair on adjacent CTAs; the last of them to finish applies the rescale.
+// Per tile (ntl > 0): this CTA's ntl tiles blockIdx.x + t * gridDim.x, each
+// through every op of the launch, ops in level order and the tiles of an op
+// adjacent (item j = (op, tile t) with t = j % ntl).
 __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, int op0, const int4 *opc,
-                                          bool csplit = false, int flow_id = -1) {
+                                          bool csplit = false, int flow_id = -1, int ntl = 0) {
     const MixParams &P = T.M;
     TcItem it;
     it.cat = -1;
@@ -108,6 +111,12 @@ __device__ __forceinline__ TcItem tc_item(const TcParams &T, int j, bool fused, 
     } else if (fused) {
         it.k = j;
         it.tile = blockIdx.x;
+    } else if (ntl > 0) {
+        it.tile = (int)blockIdx.x + (j % ntl) * (int)gridDim.x;
+        it.k = op0 + j / ntl;
+        const OpDev &od = P.ops[it.k];
+        it.prod0 = od.prod0;
+        it.prod1 = od.prod1;
     } else {
         int i = blockIdx.x + j * gridDim.x;
         if (csplit) {
@@ -1349,16 +1358,24 @@ constexpr int kRgB = 2 * 32 * kTmKP * 4;    // one side's B, hi and lo (6,144 B)
 constexpr int kRgSlot = 2 * kRgA + 2 * kRgB;
 static_assert(kRgAcol + kRgNA * 96 <= 512, "tensor memory of the ring kernel");
 
+template <bool PER_TILE>
 __global__ void __launch_bounds__(kRgThreads, 1)
     k_traverse_tc_ring(const __grid_constant__ CUtensorMap tmA, const TcParams T, const int op0, const int nl) {
+    constexpr bool per_tile = PER_TILE;
     constexpr int KQ = kTmKQ, KP = kTmKP, NP = 32, KSTEPS = KP / 8;
     const MixParams &P = T.M;
     const int C = P.ncat, n = P.n, npad = P.npad;
     const int tid = threadIdx.x, warp = tid >> 5;
     const long long ld = P.ldp;
     const int total = T.ntiles * nl;
-    const int nitems =
-        (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    // per tile: this CTA's tiles through every op of the launch (a child written
+    // in this launch comes from an earlier item of the same CTA)
+    const int ntl = !per_tile ? 0
+                    : (int)blockIdx.x < T.ntiles ? (T.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                                                 : 0;
+    const int nitems = per_tile ? ntl * nl
+                       : (int)blockIdx.x < total ? (total - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                                                 : 0;
     const long long PM = (long long)C * n * npad;
     const long long TB = (long long)(P.state_unknown + 1) * C * npad;
 
@@ -1367,7 +1384,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
     // written by the converters; adone: the A buffer's MMAs complete; ebar: an
     // accumulator buffer holds its stage's products; efree: read out again
     __shared__ unsigned long long full[kRgNS], mmab[kRgNS], conv[kRgNA], adone[kRgNA], ebar[kRgNACC], efree[kRgNACC];
-    __shared__ unsigned tmem_base_s, abort_flag;
+    __shared__ unsigned tmem_base_s, abort_flag, fin_cnt;  // fin_cnt: items written out (per tile)
     __shared__ int4 opc[kTcOpCache];
     __shared__ float rmax[2][2][kTcRows];  // [item parity][half][row]: maxima of the two halves of a row
     unsigned char *const ring = tc_smem_raw + ((128u - (smem_u32(tc_smem_raw) & 127u)) & 127u);
@@ -1390,6 +1407,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
             mbar_init(&efree[a], kRgEpi);
         }
         abort_flag = 0;
+        fin_cnt = 0;
         fence_mbar_init();
     }
     if (warp == 0) {
@@ -1408,18 +1426,26 @@ __global__ void __launch_bounds__(kRgThreads, 1)
         while (j < nitems && !(it.lint || it.rint)) {
             j++;
             c = 0;
-            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+            if (j < nitems) it = tc_item(T, j, false, op0, opc, false, -1, ntl);
         }
     };
     auto advance = [&](int &j, int &c, TcItem &it) {
         if (++c == C) {
             c = 0;
             j++;
-            if (j < nitems) it = tc_item(T, j, false, op0, opc);
+            if (j < nitems) it = tc_item(T, j, false, op0, opc, false, -1, ntl);
         }
         skip_tips(j, c, it);
     };
 
+    // per tile: the item of this CTA that writes the child on `side`, or -1
+    auto producer = [&](const TcItem &x, int j, int side) -> int {
+        if (!PER_TILE || !(side == 0 ? x.lint : x.rint)) return -1;
+        const int ch = side == 0 ? x.lch : 1 - x.lch;
+        const int prod = ch == 0 ? x.prod0 : x.prod1;
+        return prod >= op0 + P.op_base ? (prod - P.op_base - op0) * ntl + j % ntl : -1;
+    };
+    auto chained = [&](const TcItem &x, int side) { return producer(x, 0, side) >= 0; };
     constexpr int kWarpCopy = (kRgConv + kRgEpi) / 32, kWarpM = kWarpCopy + 1;
     if (warp == kWarpCopy) {
         // ---------------- copies (lane 0) ----------------
@@ -1427,7 +1453,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
         // role then skips its remaining waits and runs to its end.
         if ((tid & 31) == 0 && nitems > 0) {
             int bj = 0, bc = 0, issued = 0;
-            TcItem bit = tc_item(T, 0, false, op0, opc);
+            TcItem bit = tc_item(T, 0, false, op0, opc, false, -1, ntl);
             skip_tips(bj, bc, bit);
             for (; bj < nitems; issued++) {
                 const int s = issued % kRgNS;
@@ -1440,12 +1466,17 @@ __global__ void __launch_bounds__(kRgThreads, 1)
                     }
                 }
                 unsigned char *slot = ring + s * kRgSlot;
-                mbar_expect_tx(&full[s], (unsigned)(kRgA + kRgB) * ((unsigned)bit.lint + (unsigned)bit.rint));
+                // per tile, a child written by an earlier item of this CTA is read by the
+                // converters from global memory, not copied
+                const bool chl = chained(bit, 0), chr = chained(bit, 1);
+                mbar_expect_tx(&full[s], (unsigned)kRgB * ((unsigned)bit.lint + (unsigned)bit.rint) +
+                                             (unsigned)kRgA * ((unsigned)(bit.lint && !chl) + (unsigned)(bit.rint && !chr)));
                 for (int side = 0; side < 2; side++) {
                     if (!(side == 0 ? bit.lint : bit.rint)) continue;
                     const int child = side == 0 ? bit.lref : bit.rref;
-                    tma_load_3d(slot + side * kRgA, &tmA, 0, bc * KQ, child * T.groups_per_slot + bit.tile * 16,
-                                &full[s]);
+                    if (!(side == 0 ? chl : chr))
+                        tma_load_3d(slot + side * kRgA, &tmA, 0, bc * KQ, child * T.groups_per_slot + bit.tile * 16,
+                                    &full[s]);
                     const int ch = side == 0 ? bit.lch : 1 - bit.lch;
                     tma_load_1d(slot + 2 * kRgA + side * kRgB,
                                 T.tcb + (long long)bit.k * T.tcb_stride + (long long)(ch * C + bc) * T.b_stage,
@@ -1468,7 +1499,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
             const uint32_t idesc = idesc_tf32(kTcRows, NP);
             const unsigned b_sbo = (unsigned)(KP / 4 * 128);
             int mj = 0, mc = 0, mdone = 0;
-            TcItem mit = tc_item(T, 0, false, op0, opc);
+            TcItem mit = tc_item(T, 0, false, op0, opc, false, -1, ntl);
             skip_tips(mj, mc, mit);
             for (int i = 0; i < mw && mj < nitems; i++, mdone++) advance(mj, mc, mit);
             for (; mj < nitems; mdone += kRgMma) {
@@ -1520,7 +1551,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
         // sides from tensor memory and loads nothing per stage.
         const int side = warp >> 2;
         int j = 0, c = 0;
-        TcItem it = tc_item(T, 0, false, op0, opc);
+        TcItem it = tc_item(T, 0, false, op0, opc, false, -1, ntl);
         if (nitems > 0) skip_tips(j, c, it);
         int tsl = 0, tj = -1;  // this row's tip state, for item tj
         for (int m = 0; j < nitems; m++) {
@@ -1543,8 +1574,19 @@ __global__ void __launch_bounds__(kRgThreads, 1)
             }
             // every converter waits for the A buffer's previous stage (its MMAs imply
             // that stage's conv phase is complete, so arrivals never run a phase ahead)
+            const int jp = producer(it, j, side);  // per tile: an earlier item writes this child
             bool ok = *(volatile unsigned *)&abort_flag == 0;
-            if (ok && mine) ok = mbar_wait(&full[s], (unsigned)((m / kRgNS) & 1), kWaitPolls);
+            if (ok && mine && jp < 0) ok = mbar_wait(&full[s], (unsigned)((m / kRgNS) & 1), kWaitPolls);
+            if (ok && jp >= 0) {  // written out (the epilogue's release after its barrier)
+                unsigned polls = 0;
+                while ((int)ld_acquire_cta(&fin_cnt) <= jp) {
+                    if (*(volatile unsigned *)&abort_flag || ++polls >= kWaitPolls / 8) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
             if (ok && m >= kRgNA) ok = mbar_wait(&adone[b], (unsigned)((m / kRgNA - 1) & 1), kWaitPolls);
             if (ok && tipside && m >= kRgNACC)
                 ok = mbar_wait(&efree[a], (unsigned)((m / kRgNACC - 1) & 1), kWaitPolls);
@@ -1562,8 +1604,11 @@ __global__ void __launch_bounds__(kRgThreads, 1)
                 tmem_st_wait();
             } else if (ok && mine) {
                 tc_fence_after();
-                const float *ar = reinterpret_cast<const float *>(ring + s * kRgSlot + side * kRgA) +
-                                  (r >> 3) * KQ * 32 + (r & 7) * 4;
+                const long long pr = (long long)it.tile * kTcRows + r;
+                const float *ar = jp >= 0 ? P.part + (long long)(side == 0 ? it.lref : it.rref) * P.slot_floats +
+                                                (pr >> 3) * (8LL * C * npad) + (pr & 7) * 4 + (long long)c * KQ * 32
+                                          : reinterpret_cast<const float *>(ring + s * kRgSlot + side * kRgA) +
+                                                (r >> 3) * KQ * 32 + (r & 7) * 4;
                 const unsigned ad = tmem + lane_off + kRgAcol + (unsigned)(b * 96 + side * 48);
 #pragma unroll
                 for (int t = 0; t < KSTEPS; t++) {  // K step t: states 8t .. 8t + 7 (zero beyond the 20)
@@ -1571,8 +1616,9 @@ __global__ void __launch_bounds__(kRgThreads, 1)
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
                         const int q = 2 * t + u;
-                        const float4 v = q < KQ ? *reinterpret_cast<const float4 *>(ar + q * 32)
-                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                        const float4 v = q >= KQ ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                         : jp >= 0 ? __ldcg(reinterpret_cast<const float4 *>(ar + q * 32))
+                                                   : *reinterpret_cast<const float4 *>(ar + q * 32);
                         const float xv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
                         for (int i = 0; i < 4; i++) {
@@ -1602,18 +1648,20 @@ __global__ void __launch_bounds__(kRgThreads, 1)
             e_r = (x.rint && half == 0) ? ld_issue_s32(P.expo + (long long)x.rref * ld + px) : 0;
         };
         int m = 0;  // stages read out
-        TcItem it = tc_item(T, 0, false, op0, opc);
+        TcItem it = tc_item(T, 0, false, op0, opc, false, -1, ntl);
         long long p = (long long)it.tile * kTcRows + r;
         int e_l = 0, e_r = 0;
         if (nitems > 0) expo_in(it, p, e_l, e_r);
         for (int j = 0; j < nitems; j++) {
-            TcItem nit = it;  // the next item's exponents, in flight while this one is read out
+            // the next item's exponents, in flight while this one is read out (per tile: a
+            // child may be the item just finished, so they are loaded as the item starts)
+            TcItem nit = it;
             long long np_ = p;
             int nel = 0, ner = 0;
             if (j + 1 < nitems) {
-                nit = tc_item(T, j + 1, false, op0, opc);
+                nit = tc_item(T, j + 1, false, op0, opc, false, -1, ntl);
                 np_ = (long long)nit.tile * kTcRows + r;
-                expo_in(nit, np_, nel, ner);
+                if (!per_tile) expo_in(nit, np_, nel, ner);
             }
             float *row = P.part + (long long)it.dad * P.slot_floats + (p >> 3) * (8LL * C * npad) + (p & 7) * 4;
             const bool staged = it.lint || it.rint;
@@ -1680,19 +1728,22 @@ __global__ void __launch_bounds__(kRgThreads, 1)
                 frexpf(mx, &ex);
                 sh = 1 - ex;
                 const float mul = __int_as_float((127 + sh) << 23);
-                for (int cc = 0; cc < C; cc++)
-                    for (int q = 0; q < nq; q++) {
-                        float4 *v4 = reinterpret_cast<float4 *>(row + (long long)cc * KQ * 32 + (q0 + q) * 32);
-                        float4 v = *v4;
-                        v.x *= mul; v.y *= mul; v.z *= mul; v.w *= mul;
-                        *v4 = v;
-                    }
+                // this thread's chunks q0 .. q0 + nq - 1 of every category
+                rescale_chunks(row, C * nq, mul, [&](int i) { return ((i / nq) * KQ + q0 + i % nq) * 32; });
             }
             if (half == 0) P.expo[(long long)it.dad * ld + p] = e_l + e_r - sh;
+            if (per_tile) {  // the item is written out: later items of this CTA may read it
+                bar_sync_part(kRgEpi);
+                if (tid == kRgConv) st_release_cta(&fin_cnt, (unsigned)(j + 1));
+            }
             it = nit;
             p = np_;
-            e_l = nel;
-            e_r = ner;
+            if (per_tile) {
+                if (j + 1 < nitems) expo_in(it, p, e_l, e_r);
+            } else {
+                e_l = nel;
+                e_r = ner;
+            }
         }
         if (*(volatile unsigned *)&abort_flag && tid == kRgConv) atomicExch(P.status, kStatusTimeout);
     }
@@ -2065,30 +2116,33 @@ static int launch_tc_tm(iqgpu_engine *e, const MixParams &M, int *rest) {
 }
 
 // Level schedule on k_traverse_tc_ring: one CTA per SM (its shared memory
-// and its 512 tensor-memory columns); schedule 8 leaves the levels from the
-// first one with fewer than three (tile, op) pairs per SM (the one-op levels
-// near the root) to the CUDA-core tail, schedule 9 runs every level here.
+// and its 512 tensor-memory columns). From the first level with fewer than
+// three (tile, op) pairs per SM (the one-op levels near the root), schedule 8
+// leaves the ops to the CUDA-core tail and schedule 9 runs them in one more
+// launch per tile: each CTA takes its tiles through all of those ops in level
+// order, waiting only for its own earlier items, with no launch per level.
 static int launch_tc_ring(iqgpu_engine *e, const MixParams &M, int *rest) {
     int rc = tc_tensor_map(e);
     if (rc) return rc;
     const TcParams T = tc_params(e, M, 32, false);
     const CUtensorMap &tm = *reinterpret_cast<const CUtensorMap *>(e->tc_tmap);
     const size_t smem = (size_t)kRgNS * kRgSlot + 128;
-    cudaError_t err = cudaFuncSetAttribute(k_traverse_tc_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err == cudaSuccess)
-        err = cudaFuncSetAttribute(k_traverse_tc_ring, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaError_t err = cudaSuccess;
+    for (auto kern : {k_traverse_tc_ring<false>, k_traverse_tc_ring<true>}) {
+        if (err == cudaSuccess) err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err == cudaSuccess) err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
     if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring smem attribute");
     int sms = 1;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->dev) != cudaSuccess || sms < 1) sms = 1;
     const long long resident = sms;
     int lt = e->nlevels;
-    if (!e->tc_ring_all)
-        for (int l = 0; l < e->nlevels; l++)
-            if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < 3 * resident) {
-                lt = l;
-                break;
-            }
-    *rest = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
+    for (int l = 0; l < e->nlevels; l++)
+        if ((long long)(e->level_off[l + 1] - e->level_off[l]) * T.ntiles < 3 * resident) {
+            lt = l;
+            break;
+        }
+    const int tail0 = e->nlevels > 0 ? (lt < e->nlevels ? e->level_off[lt] : M.nops) : M.nops;
     for (int l = 0; l < lt; l++) {
         const int op0 = e->level_off[l], nl = e->level_off[l + 1] - op0;
         if (nl <= 0) continue;
@@ -2099,10 +2153,19 @@ static int launch_tc_ring(iqgpu_engine *e, const MixParams &M, int *rest) {
         }
         const long long items = (long long)T.ntiles * nl;
         const int grid = (int)std::min<long long>(items, resident);
-        k_traverse_tc_ring<<<grid, kRgThreads, smem, e->st>>>(tm, T, op0, nl);
+        k_traverse_tc_ring<false><<<grid, kRgThreads, smem, e->st>>>(tm, T, op0, nl);
         e->launches++;
         err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring level");
+    }
+    *rest = tail0;
+    if (e->tc_ring_all && tail0 < M.nops) {
+        const int grid = (int)std::min<long long>(T.ntiles, resident);
+        k_traverse_tc_ring<true><<<grid, kRgThreads, smem, e->st>>>(tm, T, tail0, M.nops - tail0);
+        e->launches++;
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring per tile");
+        *rest = M.nops;
     }
     return IQGPU_OK;
 }

@@ -353,7 +353,8 @@ class Engine:
         4 = level-synchronous with operand A in tensor memory (20 states),
         5 = as 3 with category-split narrow levels, 6 / 7 = dataflow on the
         tensor cores (category-split / whole items), 8 / 9 = level-synchronous
-        on the deep-ring kernel (20 states; 9 with the one-op levels too)."""
+        on the deep-ring kernel (20 states; 9 with the one-op levels in one
+        launch per pattern tile)."""
         _check(lib().iqgpu_set_schedule(self.h, int(schedule)))
 
     def launches(self):

@@ -148,7 +148,10 @@ def test_tc_level_kernels_protein(oracle_mod):
     (bit-identical partials on the levels every schedule puts on the tensor
     cores); schedules 8 and 9 run the deep-ring kernel (one CTA per SM, eight
     worker warps splitting each row's states between two warps), bit-identical
-    on those levels and deterministic."""
+    on those levels and deterministic; schedule 9 runs the one-op levels in
+    one launch of it per pattern tile (each CTA waiting only on its own
+    earlier items), on a tree and on a small alignment where every op goes
+    there."""
     ds = simulate.protein_lg_dataset(100, 20000, 35)
     topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
     leaf, nb = 0, topo.adj[0][0][0]
@@ -181,7 +184,7 @@ def test_tc_level_kernels_protein(oracle_mod):
         autotune.apply(eng, cand)
         again = [eng.compute_likelihood(ops, a, b, length) for _ in range(3)]
         assert again == [got[cand]] * 3, cand
-    assert launches[(0, 8, 0, 0)] < launches[(0, 9, 0, 0)]  # the one-op levels: one tail launch against one each
+    assert launches[(0, 9, 0, 0)] == launches[(0, 8, 0, 0)] + 1  # one per-tile launch beside the CUDA-core epilogue
 
 
 @pytest.mark.parametrize("kind", ["codon", "protein"])
