@@ -372,3 +372,40 @@ def test_tc_category_counts_every_schedule(oracle_mod, kind, ncat):
         assert rel(got[cand], want) < LNL_RTOL, (cand, got[cand], want)
     if kind == "codon":
         assert len(set(got.values())) == 1, got
+
+
+@pytest.mark.parametrize("ncat", [1, 3, 6])
+def test_ring_kernel_category_counts(oracle_mod, ncat):
+    """The deep-ring kernel (schedules 8 and 9) with 1, 3 and 6 categories on
+    an alignment wide enough for its level launches (100 taxa x 20,000 sites):
+    partials of levels 1-3 bit-identical to the level-synchronous kernel (same
+    three MMA passes, same products and rescale), lnL within 1e-6 of the FP64
+    oracle."""
+    import dataclasses
+    from iqtree2_gb300 import models
+    ds = simulate.protein_lg_dataset(100, 20000, 95)
+    rates, props = models.gamma_rates_mean(0.6, ncat)
+    m = dataclasses.replace(ds.model, rates=np.asarray(rates, np.float64), props=np.asarray(props, np.float64))
+    topo = Topology(ds.edges, ds.lengths, ds.ntaxa)
+    eng = engine.Engine(ds.nptn, m.nstates, m.ncat, ds.ntaxa, m.state_unknown, topo.nslots,
+                        precision=engine.TF32X3, max_ops=topo.nslots)
+    eng.set_model(m)
+    eng.set_patterns(ds.freq)
+    eng.set_tip_states(ds.patterns)
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops_l = topo.branch_ops(nb, leaf)
+    ops = engine.Engine.ops_array(ops_l)
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(m, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    lv = _levels(ops_l)
+    check = [op[0] for op, l in zip(ops_l, lv) if 1 <= l <= 3]
+    assert len(check) >= 20
+    parts = {}
+    for cand in [(0, 1, 2, 1), (0, 8, 0, 0), (0, 9, 0, 0)]:
+        autotune.apply(eng, cand)
+        lnl = eng.compute_likelihood(ops, a, b, length)
+        assert rel(lnl, want) < LNL_RTOL, (cand, lnl, want)
+        parts[cand] = [eng.partial(sl)[0].copy() for sl in check]
+    for cand in [(0, 8, 0, 0), (0, 9, 0, 0)]:
+        for x, y in zip(parts[cand], parts[(0, 1, 2, 1)]):
+            np.testing.assert_array_equal(x, y, err_msg=str(cand))
