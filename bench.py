@@ -57,7 +57,7 @@ PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # the workload's own size, from the captures summarised in profiles/ (the bench
 # does not run ncu itself); None where no capture was made.
 TRAFFIC_BYTES = {
-    "protein": (2583.1e6, "profiles/k_traverse_tc_ws_protein100x50k.md"),
+    "protein": (2581.7e6, "profiles/k_traverse_tc_ring_protein100x50k.md"),  # the tuned deep-ring schedule
     "dna-large": (2219.6e6, "profiles/k_level_dna_dna200x100k.md"),
     "codon": (438.3e6, "profiles/k_traverse_tc_ws_flow_codon40x10k.md"),  # the tuned dataflow schedule
 }
