@@ -409,3 +409,39 @@ def test_ring_kernel_category_counts(oracle_mod, ncat):
     for cand in [(0, 8, 0, 0), (0, 9, 0, 0)]:
         for x, y in zip(parts[cand], parts[(0, 1, 2, 1)]):
             np.testing.assert_array_equal(x, y, err_msg=str(cand))
+
+
+def test_ring_per_tile_several_tiles_per_cta(oracle_mod):
+    """Schedule 9's per-tile launch with more pattern tiles than SMs (about
+    200 tiles: some CTAs take two through the one-op levels, each waiting on
+    its own earlier items for the chained child): lnL within 3e-7 of schedule 8
+    (the same levels on the CUDA-core tail) and within 1e-6 of the FP64
+    oracle; then the tree driver on schedule 9 after a branch-length change,
+    so the per-tile launch also meets children written by earlier
+    traversals."""
+    ds = simulate.protein_lg_dataset(100, 30000, 96)
+    topo = Topology(ds.edges, ds.lengths, ds.patterns.shape[0])
+    assert ds.nptn > 128 * 152  # more tiles than CTAs
+    leaf, nb = 0, topo.adj[0][0][0]
+    ops = engine.Engine.ops_array(topo.branch_ops(nb, leaf))
+    a, b, length = topo.ref(leaf, nb), topo.ref(nb, leaf), topo.edge_len(leaf, nb)
+    want = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths).lnl_branch(nb, leaf)
+    eng = _engine(ds, topo)
+    got = {}
+    for cand in [(0, 8, 0, 0), (0, 9, 0, 0)]:
+        autotune.apply(eng, cand)
+        got[cand] = [eng.compute_likelihood(ops, a, b, length) for _ in range(2)]
+        assert got[cand][0] == got[cand][1], cand  # deterministic
+        assert rel(got[cand][0], want) < LNL_RTOL, (cand, got[cand][0], want)
+    assert rel(got[(0, 9, 0, 0)][0], got[(0, 8, 0, 0)][0]) < 3e-7
+    t = engine.GpuTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths, precision=engine.TF32X3)
+    autotune.apply(t.engine, (0, 9, 0, 0))
+    o = oracle_mod.OracleTree(ds.model, ds.patterns, ds.freq, ds.edges, ds.lengths)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
+    lens = ds.lengths.copy()
+    internal = [i for i, (u, v) in enumerate(ds.edges) if min(u, v) >= ds.ntaxa]
+    for i in internal[::5]:
+        lens[i] *= 1.3
+    t.set_lengths(lens)
+    o.set_lengths(lens)
+    assert rel(t.compute_likelihood(), o.compute_likelihood()) < LNL_RTOL
