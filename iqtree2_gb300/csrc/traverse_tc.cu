@@ -1443,7 +1443,7 @@ __global__ void __launch_bounds__(kRgThreads, 1)
         if (!PER_TILE || !(side == 0 ? x.lint : x.rint)) return -1;
         const int ch = side == 0 ? x.lch : 1 - x.lch;
         const int prod = ch == 0 ? x.prod0 : x.prod1;
-        return prod >= op0 + P.op_base ? (prod - P.op_base - op0) * ntl + j % ntl : -1;
+        return prod >= op0 + P.op_base ? (prod - P.op_base - op0) * ntl + (ntl > 0 ? j % ntl : 0) : -1;
     };
     auto chained = [&](const TcItem &x, int side) { return producer(x, 0, side) >= 0; };
     constexpr int kWarpCopy = (kRgConv + kRgEpi) / 32, kWarpM = kWarpCopy + 1;
