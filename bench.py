@@ -499,6 +499,8 @@ def branch_optimisation_dna16(args):
         return (time.perf_counter() - t0) / reps, lnl
 
     g_s, g_lnl = timed(t)
+    t.set_device_newton(2)
+    b_s, _ = timed(t)
     t.set_device_newton(False)
     h_s, _ = timed(t)
     t.set_device_newton(True)
@@ -509,15 +511,17 @@ def branch_optimisation_dna16(args):
     gpu_updates = t.num_updates() - upd0
     t.close()
     return {"workload": "DNA GTR+G4 16 taxa x 1000 sites: lnL + optimizeAllBranches (all-branch Newton-Raphson)",
-            "gpu_fp64_ms": g_s * 1e3, "gpu_fp64_host_newton_ms": h_s * 1e3, "cpu_oracle_1core_ms": c_s * 1e3,
+            "gpu_fp64_ms": g_s * 1e3, "gpu_fp64_branch_newton_ms": b_s * 1e3, "gpu_fp64_host_newton_ms": h_s * 1e3,
+            "cpu_oracle_1core_ms": c_s * 1e3,
             "speedup": c_s / g_s,
             "optimisations_per_s": 1.0 / g_s, "pattern_node_updates_per_run": gpu_updates,
             "lnl": {"gpu_fp64": g_lnl, "cpu": c_lnl, "rel_err": abs(g_lnl - c_lnl) / abs(c_lnl)},
             "note": "GPU: host drivers (csrc/tree.cpp) over the FP64 kernels (the lane kernel for this short "
-                    "4-state alignment), minimizeNewton as one thread-block-cluster kernel per branch "
-                    "(iqgpu_newton_branch; gpu_fp64_host_newton_ms: the host loop, one launch and read-back per "
-                    "derivative); CPU: the C restatement of the same drivers and kernels, one thread (the "
-                    "alignment has ~600 patterns)"}
+                    "4-state alignment), minimizeNewton as one thread-block-cluster kernel per branch, each "
+                    "optimizeAllBranches pass enqueued whole with the lengths in device memory and one host wait "
+                    "per pass (gpu_fp64_branch_newton_ms: one host wait per branch, iqgpu_newton_branch; "
+                    "gpu_fp64_host_newton_ms: the host loop, one launch and read-back per derivative); CPU: the C "
+                    "restatement of the same drivers and kernels, one thread (the alignment has ~600 patterns)"}
 
 
 def run_ours(args):

@@ -499,7 +499,12 @@ int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl);
 int iqgpu_tree_num_updates(iqgpu_tree *t, int64_t *updates);
 /* Where optimizeOneBranch runs minimizeNewton: on the device through
  * iqgpu_newton_branch (on = 1, the default; engines it does not serve keep the
- * host loop) or on the host, one iqgpu_likelihood_derv per step (on = 0). */
+ * host loop) or on the host, one iqgpu_likelihood_derv per step (on = 0).
+ * With on = 1 iqgpu_tree_optimize_all_branches runs each pass over the
+ * branches on the device with one host wait per pass, where the engine is not
+ * in a caller's region and every directed internal partial has a slot of its
+ * own (a pass that meets the 0.95 max_bl comparison or an error is taken again
+ * branch by branch); on = 2 keeps one host wait per branch. */
 int iqgpu_tree_set_device_newton(iqgpu_tree *t, int32_t on);
 
 /* ---- partitions: one graph launch over several engines ------------------- */

@@ -191,6 +191,13 @@ struct iqgpu_engine {
     double timing_ms;
     long long timing_launches;
     long long launches;       // kernel launches this engine has issued (throughput accounting)
+    // device-resident branch-optimisation pass (allocated on first use): every
+    // branch's op records, the edge each record's lengths come from, the
+    // branch lengths the Newton solves update, and the per-branch results
+    iqg::OpDev *d_pass_ops;
+    int32_t *d_pass_edge;
+    double *d_pass_len, *d_pass_res, *h_pass_res;
+    long long pass_ops_cap, pass_edge_cap, pass_len_cap, pass_res_cap;
 };
 
 namespace iqg {
@@ -198,11 +205,14 @@ void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
 // FP64 kernel launchers (kernels_f64.cu)
-int launch_partial_info_f64(iqgpu_engine *e, int nops);
+// src/edge/len: the records of one branch of a device optimisation pass,
+// staged into the engine's op list with their lengths from device memory
+int launch_partial_info_f64(iqgpu_engine *e, int nops, const OpDev *src = nullptr, const int32_t *edge = nullptr,
+                            const double *len = nullptr);
 int launch_traverse_f64(iqgpu_engine *e, int nops, int epi, int32_t a, int32_t b, double len);
 int launch_derv_f64(iqgpu_engine *e, double len);
 int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, double xacc, int max_steps,
-                      double *out_dev);
+                      double *out_dev, const double *xg_dev = nullptr, double *len_out = nullptr);
 int launch_from_buffer_f64(iqgpu_engine *e, double len);
 
 // mixed-precision launchers (kernels_mixed.cu); op index nops holds the

@@ -174,13 +174,14 @@ static void free_engine(iqgpu_engine *e) {
                         e->d_theta, e->d_bscale, e->d_plh, e->d_red_partials, e->d_ticket, e->d_red_out,
                         e->d_part32, e->d_exp, e->d_theta32, e->d_pi, e->d_opmats32, e->d_tcb,
                         e->d_flow_done, e->d_asc, e->d_cmax, e->d_ivhl, e->d_tiphl, e->d_pair_cnt,
-                        e->d_nr, e->d_nrmats};
+                        e->d_nr, e->d_nrmats, e->d_pass_ops, e->d_pass_edge, e->d_pass_len, e->d_pass_res};
     if (e->d_asc_holder) cudaFree(e->d_asc_holder);  // cudaMalloc'd even in a region engine
     if (!e->arena_base) {
         for (void *p : dev_ptrs)
             if (p) cudaFree(p);
         if (e->h_ops) cudaFreeHost(e->h_ops);
         if (e->h_red_out) cudaFreeHost(e->h_red_out);
+        if (e->h_pass_res) cudaFreeHost(e->h_pass_res);
         for (char *h : e->h_stage)
             if (h) cudaFreeHost(h);
         if (e->h_asc) cudaFreeHost(e->h_asc);
@@ -720,16 +721,8 @@ static int check_ref(iqgpu_engine *e, int32_t r) {
 // The mixed path evaluates a branch with FP32 transition matrices, so a
 // branch evaluation appends one entry (index nops) whose child 0 is the far
 // end b of the branch with the branch length.
-static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch = false, int32_t b = 0,
-                      double len = 0.0, bool stage_only = false) {
-    if (nops < 0 || nops > e->cfg.max_ops || (nops > 0 && !ops)) {
-        set_error("traversal length out of range");
-        return IQGPU_ERR_ARG;
-    }
-    const bool extra = branch && is_mixed(&e->cfg);
-    if (nops == 0 && !extra) return IQGPU_OK;
-    // the previous upload must have left the staging buffer
-    CK(cudaStreamSynchronize(e->st));
+// The checks every op list passes before it reaches the device.
+static int check_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops) {
     bool in_group = false;  // inside the records of a multifurcating node
     for (int k = 0; k < nops; k++) {
         const iqgpu_op &o = ops[k];
@@ -765,6 +758,21 @@ static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool b
         set_error("the last traversal entry is flagged IQGPU_OP_MORE");
         return IQGPU_ERR_ARG;
     }
+    return IQGPU_OK;
+}
+
+static int upload_ops(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, bool branch = false, int32_t b = 0,
+                      double len = 0.0, bool stage_only = false) {
+    if (nops < 0 || nops > e->cfg.max_ops || (nops > 0 && !ops)) {
+        set_error("traversal length out of range");
+        return IQGPU_ERR_ARG;
+    }
+    const bool extra = branch && is_mixed(&e->cfg);
+    if (nops == 0 && !extra) return IQGPU_OK;
+    // the previous upload must have left the staging buffer
+    CK(cudaStreamSynchronize(e->st));
+    int rc = check_ops(e, ops, nops);
+    if (rc) return rc;
     e->has_multi = false;
     for (int k = 0; k < nops && !e->has_multi; k++) e->has_multi = (ops[k].flags & IQGPU_OP_MORE) != 0;
     // Mixed engines take the ops in tree-level order (a valid post-order: every
@@ -1192,6 +1200,131 @@ int iqgpu_newton_branch(iqgpu_engine *e, const iqgpu_op *ops, int32_t nops, int3
     default: set_error("Maximum number of iterations exceeded in minimizeNewton"); return IQGPU_ERR_NEWTON;
     }
 }
+
+}  // extern "C"
+
+namespace iqg {
+// engines whose tree driver runs whole optimisation passes on the device
+bool pass_served(const iqgpu_engine *e) { return newton_on_device(e) && !e->arena_base; }
+
+template <class T>
+static cudaError_t grow_dev(T **p, long long &cap, long long need) {
+    if (need <= cap) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    const long long n = std::max(need, 64LL);
+    cudaError_t err = cudaMalloc(p, (size_t)n * sizeof(T));
+    if (err == cudaSuccess) cap = n;
+    return err;
+}
+
+// One optimizeAllBranches pass (tree/phylotree.cpp:2698-2774) with every
+// branch's minimizeNewton (utils/optimization.cpp:422-499) on the device and
+// one host wait for the whole pass. Branch j rebuilds its stale partials,
+// ops[off[j], off[j+1]), with each record's lengths read from the pass's
+// device copy of the branch lengths (edges[2k], edges[2k+1]: the edge of
+// each child, -1 for none), forms theta on refs ab[2j] (internal) and
+// ab[2j+1], and k_newton_f64 solves it from the length of edge bedge[j],
+// writing the optimum back there before the next branch's records are staged.
+// res[4j..4j+3] = {optimum, status + 16 * steps, d2l, last evaluated length}
+// as iqgpu_newton_branch reports them; a branch whose solve failed keeps its
+// length, and the caller decides what to keep.
+int run_pass(iqgpu_engine *e, const iqgpu_op *ops, const int32_t *edges, const int32_t *off, const int32_t *ab,
+             const int32_t *bedge, int nb, const double *lengths, int nedge, double x1, double x2, double xacc,
+             int max_steps, double *res) {
+    int rc = ready(e);
+    if (rc) return rc;
+    if (!pass_served(e)) {
+        set_error("device optimisation pass: engines served by iqgpu_newton_branch, not in a caller's region");
+        return IQGPU_ERR_ARG;
+    }
+    if (nb <= 0 || nedge <= 0 || !edges || !off || !ab || !bedge || !lengths || !res || off[0] != 0) {
+        set_error("bad optimisation pass");
+        return IQGPU_ERR_ARG;
+    }
+    if (!std::isfinite(x1) || !std::isfinite(x2) || !std::isfinite(xacc) || x1 < 0.0) {
+        set_error("bad Newton-Raphson bounds");
+        return IQGPU_ERR_ARG;
+    }
+    for (int j = 0; j < nb; j++) {
+        const int n = off[j + 1] - off[j];
+        if (n < 0 || n > e->cfg.max_ops || (n > 0 && !ops)) {
+            set_error("traversal length out of range");
+            return IQGPU_ERR_ARG;
+        }
+        if ((rc = check_ops(e, ops + off[j], n))) return rc;
+        const int a = ab[2 * j], b = ab[2 * j + 1];
+        if (a < 0 || check_ref(e, a) || check_ref(e, b) || a == b || bedge[j] < 0 || bedge[j] >= nedge) {
+            set_error("bad branch " + std::to_string(j));
+            return IQGPU_ERR_ARG;
+        }
+    }
+    const int total = off[nb];
+    for (int k = 0; k < 2 * total; k++)
+        if (edges[k] < -1 || edges[k] >= nedge) {
+            set_error("bad edge of traversal entry " + std::to_string(k / 2));
+            return IQGPU_ERR_ARG;
+        }
+    for (int k = 0; k < nedge; k++)
+        if (!(lengths[k] >= 0.0) || !std::isfinite(lengths[k])) {
+            set_error("bad branch length");
+            return IQGPU_ERR_ARG;
+        }
+    CK(cudaSetDevice(e->dev));
+    e->theta_valid = false;
+    CK(grow_dev(&e->d_pass_ops, e->pass_ops_cap, std::max(total, 1)));
+    CK(grow_dev(&e->d_pass_edge, e->pass_edge_cap, 2LL * std::max(total, 1)));
+    CK(grow_dev(&e->d_pass_len, e->pass_len_cap, nedge));
+    if (e->pass_res_cap < 4LL * nb) {
+        CK(cudaStreamSynchronize(e->st));  // the previous pass's read-back has landed
+        if (e->h_pass_res) cudaFreeHost(e->h_pass_res);
+        e->h_pass_res = nullptr;
+        CK(grow_dev(&e->d_pass_res, e->pass_res_cap, 4LL * nb));
+        CK(cudaMallocHost(&e->h_pass_res, (size_t)e->pass_res_cap * sizeof(double)));
+    }
+    // each branch's records index their matrices from 0, as one uploaded list
+    std::vector<OpDev> h((size_t)std::max(total, 1));
+    for (int j = 0; j < nb; j++)
+        for (int k = off[j]; k < off[j + 1]; k++) {
+            const iqgpu_op &o = ops[k];
+            OpDev &d = h[k];
+            d.dad_slot = o.dad_slot;
+            d.child[0] = o.child[0];
+            d.child[1] = o.child[1];
+            d.prod0 = d.prod1 = -1;
+            d.len[0] = d.len[1] = 0.0;  // staged from the pass's lengths
+            d.mat_off = (long long)(k - off[j]) * e->op_stride;
+            d.flags = o.flags;
+        }
+    // pageable sources: each copy has read its source when the call returns
+    CK(cudaMemcpyAsync(e->d_pass_ops, h.data(), sizeof(OpDev) * total, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_pass_edge, edges, sizeof(int32_t) * 2 * total, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_pass_len, lengths, sizeof(double) * nedge, cudaMemcpyHostToDevice, e->st));
+    for (int j = 0; j < nb; j++) {
+        const int n = off[j + 1] - off[j];
+        const int a = ab[2 * j], b = ab[2 * j + 1];
+        e->has_multi = false;
+        for (int k = off[j]; k < off[j + 1] && !e->has_multi; k++) e->has_multi = (ops[k].flags & IQGPU_OP_MORE) != 0;
+        if (n > 0 && (rc = launch_partial_info_f64(e, n, e->d_pass_ops + off[j], e->d_pass_edge + 2 * off[j],
+                                                   e->d_pass_len)))
+            return rc;
+        if ((rc = traverse(e, n, EPI_THETA, a, b, 0.0))) return rc;
+        double *len = e->d_pass_len + bedge[j];
+        if ((rc = launch_newton_f64(e, x1, 0.0, x2, xacc, max_steps, e->d_pass_res + 4 * j, len, len))) return rc;
+    }
+    e->theta_valid = true;
+    e->theta_a = ab[2 * nb - 2];
+    e->theta_b = ab[2 * nb - 1];
+    CK(cudaMemcpyAsync(e->h_pass_res, e->d_pass_res, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    if ((rc = settle_timing(e))) return rc;
+    std::memcpy(res, e->h_pass_res, sizeof(double) * 4 * nb);
+    return IQGPU_OK;
+}
+}  // namespace iqg
+
+extern "C" {
 
 int iqgpu_lnl_from_buffer(iqgpu_engine *e, double len, double *lnl) {
     int rc = ready(e);

@@ -23,12 +23,27 @@ namespace iqg {
 // ---------------------------------------------------------------------------
 // Mixtures: category c takes its class's eigen system (m = c / cpc) and the
 // class's eigen-space tip vectors tip_lh[s][m] (tree/phylokernelnew.h:908-918).
-__global__ void k_partial_info_f64(const OpDev *__restrict__ ops, double *__restrict__ opmats,
+// With `pass` set, record k comes from pass.src with its lengths read from
+// pass.len (by pass.edge), and is written to ops for the traversal after it.
+struct PassStage {
+    const OpDev *src;
+    const int32_t *edge;
+    const double *len;
+};
+__global__ void k_partial_info_f64(OpDev *__restrict__ ops, double *__restrict__ opmats,
                                    const double *__restrict__ evec, const double *__restrict__ eval,
                                    const double *__restrict__ rates, const double *__restrict__ tip_lh,
-                                   int n, int C, int S, int nmix, int cpc) {
+                                   int n, int C, int S, int nmix, int cpc, const PassStage pass) {
     const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
-    const OpDev op = ops[k];
+    OpDev op;
+    if (pass.src) {
+        op = pass.src[k];
+        op.len[0] = pass.edge[2 * k] >= 0 ? pass.len[pass.edge[2 * k]] : 0.0;
+        op.len[1] = pass.edge[2 * k + 1] >= 0 ? pass.len[pass.edge[2 * k + 1]] : 0.0;
+        if (ch == 0 && z == 0 && threadIdx.x == 0) ops[k] = op;
+    } else {
+        op = ops[k];
+    }
     const int ref = op.child[ch];
     if (ref == IQGPU_NO_CHILD) return;  // odd child count of a multifurcating node
     const double len = op.len[ch];
@@ -1063,8 +1078,10 @@ __global__ void __launch_bounds__(kTPB) k_derv_f64(const BufParams P) {
 // 1 non-finite NORM derivative, 2 the reference's "Wrong computeFuncDerv",
 // 3 too many iterations.
 // ---------------------------------------------------------------------------
-constexpr int kNewtonThreads = 256;
-constexpr int kNewtonMaxCluster = 8;
+constexpr int kNewtonThreads = 256;    // largest CTA (sizes the warp-sum array)
+constexpr int kNewtonMaxCluster = 16;  // a non-portable cluster size; 8 where 16 cannot be placed
+constexpr int kNewtonBlock = 128;       // threads per CTA
+constexpr size_t kNewtonCacheBytes = 160 * 1024;  // dynamic shared memory for a CTA's theta rows
 
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -1077,14 +1094,17 @@ __device__ __forceinline__ double2 ld_dsmem_f64x2(const double2 *local, unsigned
     return v;
 }
 
+// cache (optional): this CTA's theta rows [B][chunk], then its patterns'
+// frequencies and invariant-site terms [chunk] each, loaded once per solve
+// scof, sprop: lambda_i r_c and the category weights, read once per solve
 __device__ void newton_derv(const BufParams &P, double len, double *v0, double *v1, double *v2, double *red,
-                            double2 *part, int step, unsigned rank, unsigned nrank, bool safe, double *f, double *df) {
+                            double2 *part, int step, unsigned rank, unsigned nrank, bool safe, double *f, double *df,
+                            const double *cache, const double *scof, const double *sprop, long long chunk) {
     const int n = P.n, C = P.ncat, B = n * C, tid = threadIdx.x;
     __syncthreads();  // this CTA's readers of v0..v2 and red for the previous step are done
     for (int t = tid; t < B; t += blockDim.x) {
-        const int c = t / n, i = t % n;
-        const double cof = P.eval[(c / P.cpc) * n + i] * P.rates[c];
-        const double val = exp(cof * len) * P.props[c];
+        const double cof = scof[t];
+        const double val = exp(cof * len) * sprop[t / n];
         const double val1 = cof * val;
         v0[t] = val;
         v1[t] = val1;
@@ -1092,30 +1112,31 @@ __device__ void newton_derv(const BufParams &P, double len, double *v0, double *
     }
     __syncthreads();
     double s1 = 0.0, s2 = 0.0;
-    // contiguous chunks of whole warps per CTA, so every CTA of the cluster has patterns
-    const long long chunk = (((long long)P.nptn + nrank - 1) / nrank + 31) / 32 * 32;
+    // CTA `rank` takes the contiguous patterns [rank * chunk, (rank + 1) * chunk)
     const long long p_end = min((long long)P.nptn, (long long)(rank + 1) * chunk);
-    for (long long p = rank * chunk + tid; p < p_end; p += blockDim.x) {
-        const double *th = P.theta + p;
+    const long long p0 = rank * chunk;
+    const long long ldt = cache ? chunk : P.ldp;
+    for (long long p = p0 + tid; p < p_end; p += blockDim.x) {
+        const double *th = cache ? cache + (p - p0) : P.theta + p;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
         int k = 0;
         for (; k + 1 < B; k += 2) {
-            const double t0 = th[(long long)k * P.ldp], t1 = th[(long long)(k + 1) * P.ldp];
+            const double t0 = th[(long long)k * ldt], t1 = th[(long long)(k + 1) * ldt];
             a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
             b0 = fma(v0[k + 1], t1, b0); b1 = fma(v1[k + 1], t1, b1); b2 = fma(v2[k + 1], t1, b2);
         }
         if (k < B) {
-            const double t0 = th[(long long)k * P.ldp];
+            const double t0 = th[(long long)k * ldt];
             a0 = fma(v0[k], t0, a0); a1 = fma(v1[k], t0, a1); a2 = fma(v2[k], t0, a2);
         }
         if (P.tail_dup) {
-            const double t0 = th[(long long)(B - 1) * P.ldp];
+            const double t0 = th[(long long)(B - 1) * ldt];
             a0 = fma(v0[B - 1], t0, a0); a1 = fma(v1[B - 1], t0, a1); a2 = fma(v2[B - 1], t0, a2);
         }
-        const double lh = fabs(a0 + b0) + P.invar[p];
+        const double lh = fabs(a0 + b0) + (cache ? cache[(B + 1) * chunk + (p - p0)] : P.invar[p]);
         const double inv = 1.0 / lh;
         const double df_frac = (a1 + b1) * inv, ddf_frac = (a2 + b2) * inv;
-        const double fq = P.freq[p];
+        const double fq = cache ? cache[B * chunk + (p - p0)] : P.freq[p];
         const double tmp1 = df_frac * fq, tmp2 = ddf_frac * fq;
         s1 += tmp1;
         s2 += fma(-tmp1, df_frac, tmp2);
@@ -1142,20 +1163,30 @@ __device__ void newton_derv(const BufParams &P, double len, double *v0, double *
     // publishes part[step & 1] of every CTA; part[(step + 1) & 1] is rewritten
     // only after the next barrier, which every CTA reaches after reading this one
     cluster_sync_all();
+    double2 v[kNewtonMaxCluster];  // every CTA's sums requested at once, then added in rank order
+#pragma unroll
+    for (unsigned q = 0; q < kNewtonMaxCluster; q++)
+        if (q < nrank) v[q] = ld_dsmem_f64x2(part + (step & 1), q);
     double t1 = 0.0, t2 = 0.0;
-    for (unsigned q = 0; q < nrank; q++) {
-        const double2 v = ld_dsmem_f64x2(part + (step & 1), q);
-        t1 += v.x;
-        t2 += v.y;
-    }
+#pragma unroll
+    for (unsigned q = 0; q < kNewtonMaxCluster; q++)
+        if (q < nrank) {
+            t1 += v[q].x;
+            t2 += v[q].y;
+        }
     if (!isfinite(t1) && safe) t1 = t2 = 0.0;  // tree/phylokernelnew.h:2629-2632
     *f = -t1;  // computeFuncDerv returns the negated sums
     *df = -t2;
 }
 
+// xg_dev (optional) holds the start length in device memory; len_out
+// (optional) takes the optimum when the solve succeeded (status 0)
 __global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParams P, double x1, double xguess,
                                                                 double x2, double xacc, int max_steps, int safe,
-                                                                double *out) {
+                                                                double *out, const double *xg_dev,
+                                                                double *len_out, int cached, long long chunk) {
+    extern __shared__ double newton_cache[];
+    __shared__ double scof[kMaxCat * kMaxStates], sprop[kMaxCat];
     __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
     __shared__ double red[2 * (kNewtonThreads / 32)];
     __shared__ double2 part[2];
@@ -1164,11 +1195,28 @@ __global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParam
     asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(nrank));
     double f, df, dx, temp, xh, xl, rts, rts_old, xlast;
     int status = 0, steps = 0, step = 0;
-    rts = xguess;
+    for (int t = threadIdx.x; t < P.n * P.ncat; t += blockDim.x) {
+        const int c = t / P.n, i = t % P.n;
+        scof[t] = P.eval[(c / P.cpc) * P.n + i] * P.rates[c];
+        if (i == 0) sprop[c] = P.props[c];
+    }
+    const double *cache = nullptr;
+    if (cached) {  // this CTA's patterns, as newton_derv splits them, read once for every step
+        const int B = P.n * P.ncat;
+        const long long p0 = rank * chunk;
+        for (long long i = threadIdx.x; i < (B + 2) * chunk; i += blockDim.x) {
+            const long long k = i / chunk, p = p0 + i % chunk;
+            double v = 0.0;
+            if (p < P.nptn) v = k < B ? P.theta[k * P.ldp + p] : (k == B ? P.freq[p] : P.invar[p]);
+            newton_cache[i] = v;
+        }
+        cache = newton_cache;  // newton_derv's first barrier orders these stores before the reads
+    }
+    rts = xg_dev ? *xg_dev : xguess;
     if (rts < x1) rts = x1;
     if (rts > x2) rts = x2;
     xlast = rts;
-    newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df);
+    newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df, cache, scof, sprop, chunk);
     if (!isfinite(f)) status = safe ? 2 : 1;
     else if (!isfinite(df)) status = 2;
     else if (!(df >= 0.0 && fabs(f) < xacc)) {
@@ -1190,7 +1238,7 @@ __global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParam
             }
             if (fabs(dx) < xacc || (j == max_steps)) { rts = rts_old; status = 0; break; }
             xlast = rts;
-            newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df);
+            newton_derv(P, rts, v0, v1, v2, red, part, step++, rank, nrank, safe != 0, &f, &df, cache, scof, sprop, chunk);
             if (!isfinite(f)) { status = safe ? 2 : 1; break; }
             if (!isfinite(df)) { status = 2; break; }
             if (df > 0.0 && fabs(f) < xacc) { status = 0; break; }
@@ -1203,6 +1251,8 @@ __global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParam
         out[1] = (double)(status + 16 * steps);
         out[2] = df;  // d2l: minimizeNewton leaves it at the latest df
         out[3] = xlast;
+        // every CTA read *xg_dev before its first cluster barrier, which this one passed
+        if (len_out && status == 0) *len_out = rts;
     }
     cluster_sync_all();  // no CTA leaves while another may still read its shared memory
 }
@@ -1278,7 +1328,7 @@ static TravParams trav_params(iqgpu_engine *e, int nops) {
     return P;
 }
 
-int launch_partial_info_f64(iqgpu_engine *e, int nops) {
+int launch_partial_info_f64(iqgpu_engine *e, int nops, const OpDev *src, const int32_t *edge, const double *len) {
     if (nops <= 0) return IQGPU_OK;
     if (e->nonrev) {
         const size_t smem = ((size_t)e->n * e->n + 2 * e->n) * 8;
@@ -1289,7 +1339,8 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops) {
     }
     dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
     k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
-                                                 e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc);
+                                                 e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc,
+                                                 PassStage{src, edge, len});
     e->launches++;
     return cuda_fail(cudaGetLastError(), "partial_info_f64");
 }
@@ -1431,13 +1482,43 @@ static BufParams buf_params(iqgpu_engine *e, double len) {
 }
 
 int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, double xacc, int max_steps,
-                      double *out_dev) {
-    // one cluster, one CTA per 32 patterns up to 8 (the portable cluster size)
-    const int q = (int)std::min<long long>(kNewtonMaxCluster, std::max<long long>(1, (e->P + 31) / 32));
+                      double *out_dev, const double *xg_dev, double *len_out) {
+    // Per SM GB300 issues only a few FP64 FMAs per clock, so the solve spreads
+    // the patterns over one cluster of up to 16 CTAs (one per 32 patterns),
+    // each a contiguous chunk, with the CTA's theta rows, frequencies and
+    // invariant terms in shared memory when they fit.
+    static int cluster_max[64] = {};  // per device: 16 or 8, once probed
+    const int dv = e->dev >= 0 && e->dev < 64 ? e->dev : 0;
+    if (!cluster_max[dv]) {
+        cudaError_t err = cudaFuncSetAttribute(k_newton_f64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kNewtonCacheBytes);
+        if (err != cudaSuccess) return cuda_fail(err, "newton_f64 smem attribute");
+        cluster_max[dv] = 8;
+        if (cudaFuncSetAttribute(k_newton_f64, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t probe = {};
+            probe.gridDim = dim3(kNewtonMaxCluster);
+            probe.blockDim = dim3(kNewtonBlock);
+            probe.dynamicSmemBytes = kNewtonCacheBytes;
+            cudaLaunchAttribute pa[1];
+            pa[0].id = cudaLaunchAttributeClusterDimension;
+            pa[0].val.clusterDim.x = kNewtonMaxCluster;
+            pa[0].val.clusterDim.y = 1;
+            pa[0].val.clusterDim.z = 1;
+            probe.attrs = pa;
+            probe.numAttrs = 1;
+            int nc = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc, k_newton_f64, &probe) == cudaSuccess && nc >= 1)
+                cluster_max[dv] = kNewtonMaxCluster;
+        }
+        cudaGetLastError();  // a refused probe leaves no error behind
+    }
+    const int q = (int)std::min<long long>(cluster_max[dv], std::max<long long>(1, (e->P + 31) / 32));
+    const long long chunk = (e->P + q - 1) / q;
+    const size_t cache_bytes = (size_t)(e->n * e->C + 2) * chunk * sizeof(double);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)q);
-    cfg.blockDim = dim3(kNewtonThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.blockDim = dim3(kNewtonBlock);
+    cfg.dynamicSmemBytes = cache_bytes <= kNewtonCacheBytes ? cache_bytes : 0;
     cfg.stream = e->st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1448,7 +1529,9 @@ int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, doub
     cfg.numAttrs = 1;
     const BufParams P = buf_params(e, 0.0);
     const int safe = e->cfg.safe ? 1 : 0;
-    cudaError_t err = cudaLaunchKernelEx(&cfg, k_newton_f64, P, x1, xguess, x2, xacc, max_steps, safe, out_dev);
+    const int cached = cfg.dynamicSmemBytes > 0 ? 1 : 0;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, k_newton_f64, P, x1, xguess, x2, xacc, max_steps, safe, out_dev, xg_dev,
+                                         len_out, cached, chunk);
     e->launches++;
     if (err != cudaSuccess) return cuda_fail(err, "newton_f64");
     return cuda_fail(cudaGetLastError(), "newton_f64");

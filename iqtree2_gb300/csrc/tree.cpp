@@ -27,6 +27,10 @@
 namespace iqg {
 void set_error(const std::string &msg);
 bool newton_on_device(const iqgpu_engine *e);
+bool pass_served(const iqgpu_engine *e);
+int run_pass(iqgpu_engine *e, const iqgpu_op *ops, const int32_t *edges, const int32_t *off, const int32_t *ab,
+             const int32_t *bedge, int nb, const double *lengths, int nedge, double x1, double x2, double xacc,
+             int max_steps, double *res);
 }
 
 // largest node degree (a multifurcating node of degree d has d - 1 children)
@@ -42,11 +46,14 @@ struct iqgpu_tree {
     std::vector<double> len;
     std::vector<int> height;
     std::vector<iqgpu_op> ops;         // records not yet executed
+    std::vector<int32_t> op_edge;      // [2 per record]: the edge of each child's length (-1: none)
     int64_t nupdates = 0;
     double min_bl = 1e-6, max_bl = 10.0;
     int cur1 = -1, cur2 = -1;  // current_it: cur1 -> cur2
     bool theta_computed = false;
-    bool device_newton = true;  // minimizeNewton through iqgpu_newton_branch where the engine serves it
+    // minimizeNewton through iqgpu_newton_branch where the engine serves it:
+    // 1 whole passes of optimizeAllBranches on the device, 2 one branch at a time
+    int device_newton = 1;
     int last_rc = IQGPU_OK;
 
     // HBM slots. A tree may have more directed internal partials than its
@@ -118,6 +125,7 @@ struct iqgpu_tree {
     }
     void settled(int rc) {  // the evaluation launch executed the pending records (or failed)
         ops.clear();
+        op_edge.clear();
         std::fill(pending.begin(), pending.end(), 0);
         if (rc) std::fill(computed.begin(), computed.end(), 0);  // nothing of a failed launch is valid
     }
@@ -166,6 +174,8 @@ struct iqgpu_tree {
             op.len[1] = i + 1 < k ? len[edge[node * kMaxDeg + kid_q[i + 1]]] : 0.0;
             op.flags = i + 2 < k ? IQGPU_OP_MORE : 0;
             ops.push_back(op);
+            op_edge.push_back(edge[node * kMaxDeg + kid_q[i]]);
+            op_edge.push_back(i + 1 < k ? edge[node * kMaxDeg + kid_q[i + 1]] : -1);
         }
         for (int i = 0; i < k; i++)
             if (refs[i] >= 0) {
@@ -319,6 +329,81 @@ int minimize_newton_device(iqgpu_tree *t, double x1, double xguess, double x2, d
     return IQGPU_OK;
 }
 
+// One pass of optimizeAllBranches (tree/phylotree.cpp:2698-2774) on the
+// device: the pass's op lists are built here first, as the branch-by-branch
+// driver builds them when every branch's length changes (each branch then
+// clears the partials behind it, tree/phylotree.cpp:2635-2640), and
+// iqg::run_pass rebuilds, forms theta and solves branch after branch with the
+// lengths kept on the device. Recomputing a partial whose branch kept its
+// length gives the same values, so the pass matches the branch-by-branch
+// driver's results. It stands when every solve returned an optimum below
+// 0.95 max_bl; otherwise (the reference's lnL comparison at the bound, or an
+// error) the lengths go back to the pass's start, every partial is marked
+// stale and *done is false, for the branch-by-branch driver to take the pass.
+// Served when every directed internal partial has its own slot (no eviction).
+int device_pass(iqgpu_tree *t, const std::vector<int> &n1, const std::vector<int> &n2, int max_nr_step,
+                bool *done) {
+    *done = false;
+    const std::vector<double> saved = t->len;
+    std::vector<iqgpu_op> ops;
+    std::vector<int32_t> edges, off{0}, ab, bedge;
+    for (size_t j = 0; j < n1.size(); j++) {
+        int node = n2[j], dad = n1[j];
+        if (t->leaf(node)) std::swap(node, dad);
+        int a, b;
+        int rc = t->collect(node, dad, &a, &b);
+        if (rc) {
+            t->settled(rc);
+            t->unpin(a);
+            t->unpin(b);
+            return rc;
+        }
+        ops.insert(ops.end(), t->ops.begin(), t->ops.end());
+        edges.insert(edges.end(), t->op_edge.begin(), t->op_edge.end());
+        off.push_back((int32_t)ops.size());
+        t->nupdates += (int64_t)t->ops.size() * nptn_of(t);
+        t->settled(IQGPU_OK);
+        t->unpin(a);
+        t->unpin(b);
+        if (a < 0) std::swap(a, b);
+        ab.push_back(a);
+        ab.push_back(b);
+        bedge.push_back(t->edge[n1[j] * kMaxDeg + t->idx(n1[j], n2[j])]);
+        t->clear_reverse(n1[j], n2[j]);
+        t->clear_reverse(n2[j], n1[j]);
+    }
+    std::vector<double> res(4 * n1.size());
+    int rc = iqg::run_pass(t->e, ops.data(), edges.data(), off.data(), ab.data(), bedge.data(), (int)n1.size(),
+                           t->len.data(), t->nedge, t->min_bl, t->max_bl, t->min_bl, max_nr_step, res.data());
+    if (rc) {
+        t->settled(rc);
+        return rc;
+    }
+    bool ok = true;
+    for (size_t j = 0; j < n1.size() && ok; j++) {
+        ok = ((int)res[4 * j + 1] & 15) == 0 && !(res[4 * j] > t->max_bl * 0.95);
+        t->len[bedge[j]] = res[4 * j];
+    }
+    if (!ok) {
+        t->len = saved;
+        std::fill(t->computed.begin(), t->computed.end(), 0);
+        t->theta_computed = false;
+        return IQGPU_OK;
+    }
+    t->cur1 = n1.back();
+    t->cur2 = n2.back();
+    t->theta_computed = true;
+    *done = true;
+    return IQGPU_OK;
+}
+
+// every directed partial of an internal node has a slot of its own
+bool slots_for_all(const iqgpu_tree *t) {
+    long long need = 0;
+    for (int u = t->ntaxa; u < t->nnode; u++) need += t->deg[u];
+    return need <= t->nslots;
+}
+
 }  // namespace
 
 extern "C" {
@@ -464,9 +549,12 @@ int iqgpu_tree_optimize_all_branches(iqgpu_tree *t, int32_t iterations, double t
     int rc = lnl_branch(t, n2[0], n1[0], &tree_lh);
     if (rc) return rc;
     std::vector<double> saved;
+    const bool on_device = t->device_newton == 1 && iqg::pass_served(t->e) && slots_for_all(t) && !n1.empty();
     for (int it = 0; it < iterations; it++) {
         saved = t->len;
-        for (size_t j = 0; j < n1.size(); j++)
+        bool done = false;
+        if (on_device && (rc = device_pass(t, n1, n2, max_nr_step, &done))) return rc;
+        for (size_t j = 0; j < n1.size() && !done; j++)
             if ((rc = iqgpu_tree_optimize_one_branch(t, n1[j], n2[j], max_nr_step))) return rc;
         double new_lh;
         if ((rc = from_buffer(t, &new_lh))) return rc;
@@ -511,7 +599,7 @@ int iqgpu_tree_set_bounds(iqgpu_tree *t, double min_bl, double max_bl) {
 
 int iqgpu_tree_set_device_newton(iqgpu_tree *t, int32_t on) {
     if (!t) { iqg::set_error("null argument"); return IQGPU_ERR_ARG; }
-    t->device_newton = on != 0;
+    t->device_newton = on < 0 || on > 2 ? 1 : on;
     return IQGPU_OK;
 }
 

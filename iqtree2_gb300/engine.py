@@ -515,7 +515,10 @@ class GpuTree:
         _check(lib().iqgpu_tree_set_bounds(self.h, min_bl, max_bl))
 
     def set_device_newton(self, on):
-        _check(lib().iqgpu_tree_set_device_newton(self.h, int(bool(on))))
+        """False: minimizeNewton on the host; True (1): on the device, whole
+        optimizeAllBranches passes at once where served; 2: on the device,
+        one branch at a time."""
+        _check(lib().iqgpu_tree_set_device_newton(self.h, 2 if on == 2 else int(bool(on))))
 
     def num_updates(self):
         out = ct.c_int64()

@@ -179,3 +179,72 @@ def test_iteration_limit_and_refusals():
     with pytest.raises(engine.EngineError) as ei:
         em.newton_branch(ops, a, b, 1e-6, 0.3, 10.0, 1e-6, 100)
     assert ei.value.code == ARG
+
+
+def _optimise(g_or_ds, mode, safe=False, bounds=None, slots=None, max_nr_step=100):
+    t = engine.GpuTree(g_or_ds.model, g_or_ds.patterns, g_or_ds.freq, g_or_ds.edges, g_or_ds.lengths, safe=safe,
+                       flags=engine.FLAG_SAFE_AS_GIVEN, slots=slots)
+    t.set_device_newton(mode)
+    if bounds:
+        t.set_bounds(*bounds)
+    lnl = t.optimize_all_branches(max_nr_step=max_nr_step)
+    out = (lnl, t.lengths(), t.compute_likelihood(), t.num_updates())
+    t.close()
+    return out
+
+
+@pytest.mark.parametrize("name,safe", [("example", False), ("prot_M126_27_269", False), ("underflow150", True)])
+def test_device_pass_matches_branch_by_branch(oracle_mod, name, safe):
+    """optimizeAllBranches with each pass on the device (one host wait per
+    pass, lengths kept in device memory between the branches' solves) runs the
+    same kernels on the same inputs as the branch-by-branch device driver: the
+    same lnL, lengths and tree lnL afterwards, bit for bit, and the oracle's
+    lnL within 1e-9."""
+    g = load_ref_golden(name)
+    (lp, Lp, cp, up), (lb, Lb, cb, ub) = _optimise(g, 1, safe), _optimise(g, 2, safe)
+    assert lp == lb and cp == cb
+    np.testing.assert_array_equal(Lp, Lb)
+    assert up >= ub  # a branch that kept its length may leave partials the pass recomputes
+    o = oracle_mod.OracleTree(g.model, g.patterns, g.freq, g.edges, g.lengths, safe=safe)
+    assert rel(lp, o.optimize_all_branches()) < 1e-9
+
+
+def test_device_pass_short_alignment():
+    """DNA GTR+G4 16 taxa x 1,000 sites, the CPU-runnable configuration: the
+    pass and the branch-by-branch driver agree bit for bit."""
+    ds = simulate.dna_gtr_dataset(16, 1000, 1, mean_bl=0.1, alpha=0.5)
+    (lp, Lp, cp, _), (lb, Lb, cb, _) = _optimise(ds, 1), _optimise(ds, 2)
+    assert lp == lb and cp == cb
+    np.testing.assert_array_equal(Lp, Lb)
+
+
+def test_device_pass_taken_again_at_the_bound():
+    """With max_bl low enough that optima land above 0.95 max_bl (where the
+    reference compares the lnL at the bound with the one at the old length),
+    or with no Newton step allowed (the solve fails), the pass goes back to
+    its start and runs branch by branch: the same results, or the same error,
+    as that driver."""
+    g = load_ref_golden("example")
+    assert g.lengths.max() > 0.02
+    for kw in (dict(bounds=(1e-6, 0.02)), dict(max_nr_step=0)):
+        try:
+            ref = _optimise(g, 2, **kw)
+        except engine.EngineError as err:
+            with pytest.raises(engine.EngineError) as ei:
+                _optimise(g, 1, **kw)
+            assert ei.value.code == err.code
+            continue
+        lp, Lp, cp, _ = _optimise(g, 1, **kw)
+        assert lp == ref[0] and cp == ref[2]
+        np.testing.assert_array_equal(Lp, ref[1])
+
+
+def test_device_pass_not_taken_without_a_slot_per_partial():
+    """Fewer slots than directed internal partials (slots recycled, the
+    reference's LM_MEM_SAVE): the branch-by-branch driver runs, results as
+    with a slot per partial."""
+    g = load_ref_golden("example")
+    full = _optimise(g, 1)
+    few = _optimise(g, 1, slots=max(6, 3 * (g.ntaxa - 2) // 2))
+    assert rel(few[0], full[0]) < 1e-12
+    np.testing.assert_allclose(few[1], full[1], atol=1e-12)
