@@ -670,6 +670,8 @@ __global__ void __launch_bounds__(512) k_level_mixed(const MixParams P, const in
 // computes this case from the same lookup tables).
 template <int PPT>
 __global__ void __launch_bounds__(128) k_tiptip_level(const MixParams P, const int op0) {
+    pdl_wait();  // the leaf tables come from the kernels before
+    pdl_trigger();
     const int C = P.ncat, n = P.n, npad = P.npad, kq = npad >> 2;
     const long long ld = P.ldp;
     const int k = op0 + blockIdx.y;
@@ -723,12 +725,13 @@ bool level_all_tiptip(const iqgpu_engine *e, int op0, int nl) {
 int launch_tiptip_level(iqgpu_engine *e, const MixParams &P, int op0, int nl) {
     for (int c0 = 0; c0 < nl; c0 += 65535) {
         const int cnt = std::min(65535, nl - c0);
-        if (e->npad == 4)
-            k_tiptip_level<4><<<dim3((unsigned)((e->Ppad + 511) / 512), cnt), 128, 0, e->st>>>(P, op0 + c0);
-        else
-            k_tiptip_level<1><<<dim3((unsigned)(e->Ppad / 128), cnt), 128, 0, e->st>>>(P, op0 + c0);
+        cudaError_t err =
+            e->npad == 4
+                ? pdl_launch(k_tiptip_level<4>, dim3((unsigned)((e->Ppad + 511) / 512), cnt), dim3(128), 0, e->st, P,
+                             op0 + c0)
+                : pdl_launch(k_tiptip_level<1>, dim3((unsigned)(e->Ppad / 128), cnt), dim3(128), 0, e->st, P, op0 + c0);
         e->launches++;
-        cudaError_t err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "tiptip_level");
     }
     return IQGPU_OK;
@@ -779,6 +782,8 @@ static int launch_chain_t(iqgpu_engine *e, const MixParams &P) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 64, smem) == cudaSuccess &&
         e->Ppad / 32 <= (long long)per_sm * sms)
         tb = 64;
+    // an ordinary launch: as a dependent of the last tensor-core level its CTAs
+    // would sit beside that level's CTAs until it ends, and measured slower
     kern<<<(unsigned)(e->Ppad / (tb / 2)), tb, smem, e->st>>>(P);
     e->launches++;
     return cuda_fail(cudaGetLastError(), "chain_mixed");

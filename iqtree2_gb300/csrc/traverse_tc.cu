@@ -1417,6 +1417,12 @@ __global__ void __launch_bounds__(kRgThreads, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    // Launched as a programmatic dependent of the previous level: everything
+    // above (the op records, uploaded before any level, barriers, tensor
+    // memory) overlaps that level's last items; its outputs are read only
+    // after this wait, and the next level may be scheduled from here on.
+    pdl_wait();
+    pdl_trigger();
     const unsigned tmem = tmem_base_s;
     const unsigned lane_off = (unsigned)((warp & 3) * 32) << 16;
     const int r = (warp & 3) * 32 + (tid & 31);  // pattern row of the tile = tensor-memory lane
@@ -1758,6 +1764,8 @@ __global__ void __launch_bounds__(kRgThreads, 1)
 // KS), zero outside x < n, y < n.
 __global__ void k_tc_prep_b(const float *opmats, long long op_stride, float *tcb, long long tcb_stride, int n,
                             int npad, int C, int NP, int KP, int ksplit) {
+    pdl_wait();  // the P(t) matrices come from the kernel before
+    pdl_trigger();
     const int k = blockIdx.x, ch = blockIdx.y / C, c = blockIdx.y % C;
     const int KS = KP / ksplit;
     const float *Pm = opmats + (long long)k * op_stride + (long long)ch * C * n * npad + (long long)c * n * npad;
@@ -1815,9 +1823,10 @@ int launch_tc_prep(iqgpu_engine *e, int nops) {
         return cuda_fail(cudaGetLastError(), "tc_prep_b16");
     }
     const int NP = tc_np(e->npad), KP = tc_kp(e->npad);
-    k_tc_prep_b<<<dim3(nops, 2 * e->C), 256, 0, e->st>>>(e->d_opmats32, e->op_stride32, e->d_tcb, e->tcb_stride,
-                                                           e->n, e->npad, e->C, NP, KP, tc_ksplit(e));
+    cudaError_t err = pdl_launch(k_tc_prep_b, dim3(nops, 2 * e->C), dim3(256), 0, e->st, (const float *)e->d_opmats32,
+                                 e->op_stride32, e->d_tcb, e->tcb_stride, e->n, e->npad, e->C, NP, KP, tc_ksplit(e));
     e->launches++;
+    if (err != cudaSuccess) return cuda_fail(err, "tc_prep_b");
     return cuda_fail(cudaGetLastError(), "tc_prep_b");
 }
 
@@ -2153,9 +2162,9 @@ static int launch_tc_ring(iqgpu_engine *e, const MixParams &M, int *rest) {
         }
         const long long items = (long long)T.ntiles * nl;
         const int grid = (int)std::min<long long>(items, resident);
-        k_traverse_tc_ring<false><<<grid, kRgThreads, smem, e->st>>>(tm, T, op0, nl);
+        err = pdl_launch(k_traverse_tc_ring<false>, dim3((unsigned)grid), dim3(kRgThreads), smem, e->st, tm, T, op0, nl);
         e->launches++;
-        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc_ring level");
     }
     *rest = tail0;
