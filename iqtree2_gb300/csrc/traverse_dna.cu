@@ -386,6 +386,8 @@ struct LevelOps {
 // PPT patterns per thread: CTA (x, y) covers patterns 128 PPT x .. 128 PPT (x + 1) - 1.
 template <int PPT>
 __global__ void __launch_bounds__(kDnaTile) k_level_dna(const MixParams P, const int op0, const LevelOps L) {
+    pdl_wait();  // the children come from the levels before
+    pdl_trigger();
     const int3 o = L.op[blockIdx.y];
     dna_op<PPT>(P, op0 + blockIdx.y, blockIdx.x, o.x, o.y, o.z);
 }
@@ -471,9 +473,9 @@ static int launch_levels_dna_t(iqgpu_engine *e, MixParams P, int epi) {
                 const OpDev &d = e->h_ops[op0 + c0 + i];
                 L.op[i] = make_int3(d.dad_slot, d.child[0], d.child[1]);
             }
-            k_level_dna<PPT><<<dim3(grid, cnt), kDnaTile, 0, e->st>>>(P, op0 + c0, L);
+            cudaError_t err = pdl_launch(k_level_dna<PPT>, dim3(grid, cnt), dim3(kDnaTile), 0, e->st, P, op0 + c0, L);
             e->launches++;
-            cudaError_t err = cudaGetLastError();
+            if (err == cudaSuccess) err = cudaGetLastError();
             if (err != cudaSuccess) return cuda_fail(err, "level_dna");
         }
     }
