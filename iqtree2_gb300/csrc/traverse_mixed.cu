@@ -628,6 +628,8 @@ __global__ void __launch_bounds__(512) k_traverse_mixed(const MixParams P, const
 // level-synchronous schedule: CTA (x, y) computes op op0+y for pattern tile x
 template <int NQ>
 __global__ void __launch_bounds__(512) k_level_mixed(const MixParams P, const int TP, const int op0) {
+    pdl_wait();  // the children come from the levels before
+    pdl_trigger();
     const int C = P.ncat, npad = P.npad;
     const int nq = NQ ? NQ : npad >> 2;
     const int c = threadIdx.x / TP;
@@ -808,9 +810,9 @@ static int launch_levels_t(iqgpu_engine *e, const MixParams &P, int l0 = 0) {
             if (rc) return rc;
             continue;
         }
-        kern<<<dim3(grid, nl), TP * e->C, smem, e->st>>>(P, TP, op0);
+        cudaError_t err = pdl_launch(kern, dim3(grid, nl), dim3(TP * e->C), smem, e->st, P, TP, op0);
         e->launches++;
-        cudaError_t err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "level_mixed");
     }
     return IQGPU_OK;
