@@ -59,8 +59,17 @@ PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_BYTES = {
     "protein": (2581.7e6, "profiles/k_traverse_tc_ring_protein100x50k.md"),  # the tuned deep-ring schedule
     "dna-large": (2219.6e6, "profiles/k_level_dna_dna200x100k.md"),
-    "codon": (438.3e6, "profiles/k_traverse_tc_ws_flow_codon40x10k.md"),  # the tuned dataflow schedule
+    "codon": (438.3e6, "profiles/k_traverse_tc_ws_flow_codon40x10k.md"),  # the dataflow schedule
 }
+# schedules the autotuner may pick instead, with their own captures
+TRAFFIC_BY_SCHEDULE = {
+    ("codon", "0/level-ws/s2/k2"): (418.7e6, "profiles/k_traverse_tc_ws_codon40x10k.md"),
+}
+
+
+def traffic_of(key, tile):
+    """DRAM bytes per evaluation of the schedule that ran, from its ncu summary."""
+    return TRAFFIC_BY_SCHEDULE.get((key, str(tile)), TRAFFIC_BYTES.get(key, (None, None)))
 
 
 def dataset(w=None):
@@ -453,8 +462,8 @@ def extra_workload(key, args, stream, local, peaks, peak_src, fp64_peak):
         "ms_per_step": r["elapsed_ms"] / steps, "dtype": "tf32x3" if use_tc else "f32", "tile": tile,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peak_src,
-                     "traffic": TRAFFIC_BYTES.get(key, (None, None))[0],
-                     "traffic_source": TRAFFIC_BYTES.get(key, (None, None))[1],
+                     "traffic": traffic_of(key, tile)[0],
+                     "traffic_source": traffic_of(key, tile)[1],
                      "kernel": kernel_name(use_tc, m.nstates, tile), "algorithmic_bytes_per_launch": bmx,
                      "kernel_ms": r["kern_avg_s"] * 1e3, "fp32_tflops": fmx / r["kern_avg_s"] / 1e12},
         "e2e": {"value": upd / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 32},
@@ -615,8 +624,8 @@ def run_ours(args):
                 "rel_err": abs(r["lnl"] - r64["lnl"]) / abs(r64["lnl"]) if r64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": TRAFFIC_BYTES.get(args.workload, (None, None))[0],
-                     "traffic_source": TRAFFIC_BYTES.get(args.workload, (None, None))[1], "peak_source": peak_src,
+                     "traffic": traffic_of(args.workload, tile)[0],
+                     "traffic_source": traffic_of(args.workload, tile)[1], "peak_source": peak_src,
                      "kernel": kernel_name(use_tc, m.nstates, tile), "algorithmic_bytes_per_launch": bmx,
                      "fp32_tflops": fmx / r["kern_avg_s"] / 1e12, "flops_per_launch": fmx,
                      "kernel_ms": r["kern_avg_s"] * 1e3},

@@ -558,6 +558,10 @@ __global__ void __launch_bounds__(kTcRows + 32, 4)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    // a level launched as a programmatic dependent of the one before reads its
+    // outputs only after this wait (the op records were uploaded before both)
+    pdl_wait();
+    pdl_trigger();
     const unsigned tmem = tmem_base_s;
 
     // producers' flags of an item, polled once each (issuer) or waited for (workers)
@@ -2059,13 +2063,15 @@ static int launch_tc_t(iqgpu_engine *e, const MixParams &M, int *rest) {
                         (size_t)nl * e->C * (size_t)e->Ppad * sizeof(float) <= e->cmax_bytes;
         const int grid = (int)std::min<long long>(items * (cs ? e->C : 1), resident);
         if (ws && cs)
-            kern_ws_cs<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt, nullptr, nullptr, 1u);
+            err = pdl_launch(kern_ws_cs, dim3((unsigned)grid), dim3(nthr), smem, e->st, tm, T, op0, nl, e->d_cmax,
+                             e->d_pair_cnt, (unsigned *)nullptr, (unsigned *)nullptr, 1u);
         else if (ws)
-            kern_ws<<<grid, nthr, smem, e->st>>>(tm, T, op0, nl, e->d_cmax, e->d_pair_cnt, nullptr, nullptr, 1u);
+            err = pdl_launch(kern_ws, dim3((unsigned)grid), dim3(nthr), smem, e->st, tm, T, op0, nl, e->d_cmax,
+                             e->d_pair_cnt, (unsigned *)nullptr, (unsigned *)nullptr, 1u);
         else
             kern<<<grid, kTcRows, smem, e->st>>>(tm, T, op0, nl, 0);
         e->launches++;
-        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaGetLastError();
         if (err != cudaSuccess) return cuda_fail(err, "traverse_tc level");
     }
     return IQGPU_OK;
