@@ -34,6 +34,8 @@ __global__ void k_partial_info_f64(OpDev *__restrict__ ops, double *__restrict__
                                    const double *__restrict__ evec, const double *__restrict__ eval,
                                    const double *__restrict__ rates, const double *__restrict__ tip_lh,
                                    int n, int C, int S, int nmix, int cpc, const PassStage pass) {
+    pdl_wait();  // a pass's lengths come from the solve before
+    pdl_trigger();
     const int k = blockIdx.x, ch = blockIdx.y, z = blockIdx.z, Z = gridDim.z;
     OpDev op;
     if (pass.src) {
@@ -529,6 +531,8 @@ __global__ void __launch_bounds__(kTPB) k_traverse_f64(const TravParams P) {
 // ---------------------------------------------------------------------------
 template <bool SAFE, int EPI, int G>
 __global__ void __launch_bounds__(128) k_traverse_f64_lanes(const TravParams P) {
+    pdl_wait();  // P(t) and the children come from the kernels before
+    pdl_trigger();
     constexpr int n = 4;
     static_assert(G >= 4 && G <= 32 && (G & (G - 1)) == 0, "lanes per pattern");
     __shared__ double sval[kMaxCat * kMaxStates];
@@ -1185,6 +1189,8 @@ __global__ void __launch_bounds__(kNewtonThreads, 1) k_newton_f64(const BufParam
                                                                 double x2, double xacc, int max_steps, int safe,
                                                                 double *out, const double *xg_dev,
                                                                 double *len_out, int cached, long long chunk) {
+    pdl_wait();  // theta and the start length come from the kernels before
+    pdl_trigger();
     extern __shared__ double newton_cache[];
     __shared__ double scof[kMaxCat * kMaxStates], sprop[kMaxCat];
     __shared__ double v0[kMaxCat * kMaxStates], v1[kMaxCat * kMaxStates], v2[kMaxCat * kMaxStates];
@@ -1338,10 +1344,12 @@ int launch_partial_info_f64(iqgpu_engine *e, int nops, const OpDev *src, const i
         return cuda_fail(cudaGetLastError(), "partial_info_nonrev64");
     }
     dim3 grid(nops, 2, e->n > 20 ? 16 : 2);
-    k_partial_info_f64<<<grid, 256, 0, e->st>>>(e->d_ops, e->d_opmats, e->d_evec, e->d_eval, e->d_rates,
-                                                 e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc,
-                                                 PassStage{src, edge, len});
+    cudaError_t err = pdl_launch(k_partial_info_f64, grid, dim3(256), 0, e->st, e->d_ops, e->d_opmats,
+                                 (const double *)e->d_evec, (const double *)e->d_eval, (const double *)e->d_rates,
+                                 (const double *)e->d_tip, e->n, e->C, e->S, e->nmix, e->cpc,
+                                 PassStage{src, edge, len});
     e->launches++;
+    if (err != cudaSuccess) return cuda_fail(err, "partial_info_f64");
     return cuda_fail(cudaGetLastError(), "partial_info_f64");
 }
 
@@ -1372,8 +1380,10 @@ static int launch_trav_t(iqgpu_engine *e, const TravParams &P) {
 // 4-state models on short alignments: the lane kernel (see above)
 template <bool SAFE, int EPI, int G>
 static int launch_lanes_t(iqgpu_engine *e, const TravParams &P) {
-    k_traverse_f64_lanes<SAFE, EPI, G><<<(unsigned)(e->Ppad * G / 128), 128, 0, e->st>>>(P);
+    cudaError_t err =
+        pdl_launch(k_traverse_f64_lanes<SAFE, EPI, G>, dim3((unsigned)(e->Ppad * G / 128)), dim3(128), 0, e->st, P);
     e->launches++;
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_f64_lanes");
     return cuda_fail(cudaGetLastError(), "traverse_f64_lanes");
 }
 
@@ -1520,13 +1530,15 @@ int launch_newton_f64(iqgpu_engine *e, double x1, double xguess, double x2, doub
     cfg.blockDim = dim3(kNewtonBlock);
     cfg.dynamicSmemBytes = cache_bytes <= kNewtonCacheBytes ? cache_bytes : 0;
     cfg.stream = e->st;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)q;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // a dependent launch (pdl_wait)
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     const BufParams P = buf_params(e, 0.0);
     const int safe = e->cfg.safe ? 1 : 0;
     const int cached = cfg.dynamicSmemBytes > 0 ? 1 : 0;

@@ -16,29 +16,6 @@
 
 namespace iqg {
 
-// Programmatic dependent launch: a kernel started by pdl_launch may be
-// scheduled while the previous kernel of its stream is still running, and
-// calls pdl_wait() before it reads anything that kernel (or one before it)
-// writes; pdl_trigger() lets the next such kernel be scheduled. Both are
-// no-ops for a kernel launched the ordinary way.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-template <typename... K, typename... A>
-static cudaError_t pdl_launch(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, static_cast<A &&>(args)...);
-}
-
 constexpr float kMixThreshold = 9.094947017729282e-13f;  // 2^-40
 constexpr double kLn2 = 0.6931471805599453094172321;
 constexpr int kMixTile = 128;  // patterns per CTA; the CTA has kMixTile * ncat threads
