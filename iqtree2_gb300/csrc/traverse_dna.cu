@@ -39,6 +39,8 @@ constexpr int kDnaAhead = 4;  // ops whose other child is in flight ahead of the
 
 template <int EPI>
 __global__ void __launch_bounds__(kDnaTile, 5) k_traverse_dna(const MixParams P) {
+    pdl_wait();  // the levels before wrote its first children
+    pdl_trigger();
     constexpr int n = 4, npad = 4;
     const int C = P.ncat, S = P.state_unknown;
     const long long p = (long long)blockIdx.x * kDnaTile + threadIdx.x;
@@ -522,11 +524,13 @@ int launch_flow_dna(iqgpu_engine *e, const MixParams &P) {
 int launch_traverse_dna(iqgpu_engine *e, const MixParams &P, int epi) {
     const int grid = (int)(e->Ppad / kDnaTile);
     e->launches++;
+    cudaError_t err = cudaSuccess;
     switch (epi) {
-    case EPI_NONE: k_traverse_dna<EPI_NONE><<<grid, kDnaTile, 0, e->st>>>(P); break;
-    case EPI_LNL: k_traverse_dna<EPI_LNL><<<grid, kDnaTile, 0, e->st>>>(P); break;
-    default: k_traverse_dna<EPI_THETA><<<grid, kDnaTile, 0, e->st>>>(P); break;
+    case EPI_NONE: err = pdl_launch(k_traverse_dna<EPI_NONE>, dim3(grid), dim3(kDnaTile), 0, e->st, P); break;
+    case EPI_LNL: err = pdl_launch(k_traverse_dna<EPI_LNL>, dim3(grid), dim3(kDnaTile), 0, e->st, P); break;
+    default: err = pdl_launch(k_traverse_dna<EPI_THETA>, dim3(grid), dim3(kDnaTile), 0, e->st, P); break;
     }
+    if (err != cudaSuccess) return cuda_fail(err, "traverse_dna");
     return cuda_fail(cudaGetLastError(), "traverse_dna");
 }
 
